@@ -1,0 +1,354 @@
+"""Mesh containers and structured mesh generators.
+
+The reference builds meshes through gmsh (``EasyFEA/FEM/_mesher.py``) and stores
+them as ``Mesh`` objects holding one ``_GroupElem`` per element type
+(``EasyFEA/FEM/_mesh.py:46-91``, ``EasyFEA/FEM/_group_elem.py:2225-2355``).  gmsh
+is not part of this library: meshes are given as ``coord`` / ``connect`` arrays,
+or produced by the organised (structured) generators below, which reproduce the
+node and element orderings of the reference's organised meshes:
+
+* QUAD4 / QUAD9 / TRI3 rectangles: node id ``j*(nx+1)+i``; counter-clockwise
+  elements; SEG2 boundary groups on the four edges.
+* HEXA8 boxes: node id ``(k*(ny+1)+j)*(nx+1)+i``; local node order of
+  ``EasyFEA/FEM/Elems/_hexa.py:14-60``; QUAD4 boundary faces on the six faces.
+
+Everything here is host-side numpy (set-up work done once per mesh); device
+copies are made by the simulations that use the mesh.
+"""
+
+from __future__ import annotations
+
+from enum import Enum
+from typing import Callable, Optional
+
+import numpy as np
+
+
+class ElemType(str, Enum):
+    """Element types handled by the GPU path (names of ``EasyFEA/FEM/_utils.py:9-34``)."""
+
+    SEG2 = "SEG2"
+    TRI3 = "TRI3"
+    QUAD4 = "QUAD4"
+    QUAD9 = "QUAD9"
+    HEXA8 = "HEXA8"
+
+
+class MatrixType(str, Enum):
+    """Quadrature families (``EasyFEA/FEM/_utils.py:79-88``)."""
+
+    rigi = "rigi"
+    mass = "mass"
+
+
+# (nPe, topological dim, C-ABI element code)
+ELEM_INFO = {
+    ElemType.SEG2: (2, 1, 0),
+    ElemType.TRI3: (3, 2, 1),
+    ElemType.QUAD4: (4, 2, 2),
+    ElemType.QUAD9: (9, 2, 3),
+    ElemType.HEXA8: (8, 3, 4),
+}
+
+# Gauss points per (element, matrixType), as chosen by
+# EasyFEA/FEM/_gauss.py:364-480 (TRI3 rigi 1 / mass 3, QUAD4 4, QUAD9 9,
+# HEXA8 8, SEG2 rigi 1 / mass 2).
+NPG = {
+    (ElemType.SEG2, MatrixType.rigi): 1,
+    (ElemType.SEG2, MatrixType.mass): 2,
+    (ElemType.TRI3, MatrixType.rigi): 1,
+    (ElemType.TRI3, MatrixType.mass): 3,
+    (ElemType.QUAD4, MatrixType.rigi): 4,
+    (ElemType.QUAD4, MatrixType.mass): 4,
+    (ElemType.QUAD9, MatrixType.rigi): 9,
+    (ElemType.QUAD9, MatrixType.mass): 9,
+    (ElemType.HEXA8, MatrixType.rigi): 8,
+    (ElemType.HEXA8, MatrixType.mass): 8,
+}
+
+
+class GroupElem:
+    """One element group: ``connect`` (Ne, nPe) into the shared ``coord`` (Nn, 3).
+
+    Mirrors the data half of ``_GroupElem`` (``EasyFEA/FEM/_group_elem.py``);
+    the Gauss-point arithmetic lives in the CUDA kernels.
+    """
+
+    def __init__(self, elemType: ElemType, connect: np.ndarray, coord: np.ndarray):
+        elemType = ElemType(elemType)
+        nPe, dim, code = ELEM_INFO[elemType]
+        connect = np.ascontiguousarray(connect, dtype=np.int64)
+        assert connect.ndim == 2 and connect.shape[1] == nPe, (
+            f"{elemType} connect must be (Ne, {nPe})"
+        )
+        self.elemType = elemType
+        self.nPe = nPe
+        self.dim = dim
+        self.code = code
+        self.__connect = connect
+        self.__connect.setflags(write=False)
+        self.__coord = coord
+
+    @property
+    def connect(self) -> np.ndarray:
+        return self.__connect
+
+    @property
+    def coord(self) -> np.ndarray:
+        return self.__coord
+
+    @property
+    def Ne(self) -> int:
+        return self.__connect.shape[0]
+
+    @property
+    def nodes(self) -> np.ndarray:
+        return np.unique(self.__connect)
+
+    def Get_assembly_e(self, dof_n: int) -> np.ndarray:
+        """Element DOF map ``node*dof_n + d`` (``EasyFEA/FEM/_group_elem.py:346-380``)."""
+        Ne, nPe = self.__connect.shape
+        assembly = np.empty((Ne, nPe * dof_n), dtype=np.int64)
+        for d in range(dof_n):
+            assembly[:, d::dof_n] = self.__connect * dof_n + d
+        return assembly
+
+    def Get_Elements_Nodes(self, nodes: np.ndarray, exclusively: bool = True) -> np.ndarray:
+        """Elements using the given nodes (``EasyFEA/FEM/_group_elem.py:1500-1537``).
+
+        With ``exclusively`` only elements whose every node is in ``nodes``.
+        """
+        mark = np.zeros(self.__coord.shape[0], dtype=bool)
+        nodes = np.asarray(nodes, dtype=np.int64)
+        mark[nodes[nodes < mark.size]] = True
+        hit = mark[self.__connect]
+        sel = hit.all(axis=1) if exclusively else hit.any(axis=1)
+        return np.nonzero(sel)[0]
+
+
+class Mesh:
+    """A set of element groups sharing one coordinate array (``EasyFEA/FEM/_mesh.py:46-191``)."""
+
+    def __init__(self, dict_groupElem: dict):
+        assert len(dict_groupElem) > 0, "dict_groupElem is empty."
+        coords = {id(g.coord) for g in dict_groupElem.values()}
+        assert len(coords) == 1, "All element groups must share the same coordinates."
+        self.__dict = dict(dict_groupElem)
+        first = next(iter(self.__dict.values()))
+        self.__coord = first.coord
+        self.__dim = max(g.dim for g in self.__dict.values())
+        used = np.zeros(self.Nn, dtype=bool)
+        for g in self.__dict.values():
+            used[g.connect.ravel()] = True
+        self.__orphanNodes = np.nonzero(~used)[0]
+        self.__version = 0
+
+    @property
+    def dict_groupElem(self) -> dict:
+        return self.__dict
+
+    @property
+    def coord(self) -> np.ndarray:
+        return self.__coord
+
+    @property
+    def coordGlob(self) -> np.ndarray:
+        return self.__coord
+
+    @property
+    def Nn(self) -> int:
+        return self.__coord.shape[0]
+
+    @property
+    def dim(self) -> int:
+        return self.__dim
+
+    @property
+    def inDim(self) -> int:
+        """Embedding dimension deduced from the coordinates (``EasyFEA/FEM/_group_elem.py:155-175``)."""
+        if self.__dim == 3:
+            return 3
+        _, y, z = np.abs(self.__coord.T)
+        if z.size and np.max(z) > 0:
+            return 3
+        if y.size and np.max(y) > 0:
+            return 2
+        return 1
+
+    @property
+    def orphanNodes(self) -> np.ndarray:
+        return self.__orphanNodes
+
+    @property
+    def groupElem(self) -> GroupElem:
+        """The main-dimension element group."""
+        return self.Get_list_groupElem(self.__dim)[0]
+
+    @property
+    def elemType(self) -> ElemType:
+        return self.groupElem.elemType
+
+    @property
+    def Ne(self) -> int:
+        return self.groupElem.Ne
+
+    @property
+    def connect(self) -> np.ndarray:
+        return self.groupElem.connect
+
+    def Get_list_groupElem(self, dim: Optional[int] = None) -> list:
+        if dim is None:
+            dim = self.__dim
+        out = [g for g in self.__dict.values() if g.dim == dim]
+        out.reverse()
+        return out
+
+    def Nodes_Conditions(self, func: Callable) -> np.ndarray:
+        """Nodes of the main group whose coordinates satisfy ``func(x, y, z)``
+        (``EasyFEA/FEM/_mesh.py:619-644``)."""
+        nodes = self.groupElem.nodes
+        x, y, z = self.__coord[nodes].T
+        return nodes[np.asarray(func(x, y, z), dtype=bool)]
+
+    def __str__(self) -> str:
+        return f"elemType: {self.elemType.value}\nNe: {self.Ne}\nNn: {self.Nn}"
+
+
+# ---------------------------------------------------------------------------
+# organised mesh generators
+# ---------------------------------------------------------------------------
+
+
+def _grid2d(L: float, h: float, nx: int, ny: int, x0: float = 0.0, y0: float = 0.0):
+    xs = x0 + np.linspace(0.0, L, nx + 1)
+    ys = y0 + np.linspace(0.0, h, ny + 1)
+    X, Y = np.meshgrid(xs, ys)  # (ny+1, nx+1), node id j*(nx+1)+i
+    coord = np.zeros(((nx + 1) * (ny + 1), 3))
+    coord[:, 0] = X.ravel()
+    coord[:, 1] = Y.ravel()
+    return coord
+
+
+def _edges2d(nx: int, ny: int, stride: int = 1):
+    """SEG2 edges of an (nx*stride)x(ny*stride) node grid boundary, counter-clockwise."""
+    NX = nx * stride
+    nid = lambda i, j: j * (NX + 1) + i  # noqa: E731
+    segs = []
+    for i in range(NX):
+        segs.append((nid(i, 0), nid(i + 1, 0)))
+    for j in range(ny * stride):
+        segs.append((nid(NX, j), nid(NX, j + 1)))
+    for i in range(NX, 0, -1):
+        segs.append((nid(i, ny * stride), nid(i - 1, ny * stride)))
+    for j in range(ny * stride, 0, -1):
+        segs.append((nid(0, j), nid(0, j - 1)))
+    return np.asarray(segs, dtype=np.int64)
+
+
+def Mesh_Quad4_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised QUAD4 mesh of [0,L]x[0,h] with SEG2 boundary edges."""
+    coord = _grid2d(L, h, nx, ny)
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny))
+    i = i.ravel()
+    j = j.ravel()
+    n0 = j * (nx + 1) + i
+    connect = np.stack([n0, n0 + 1, n0 + nx + 2, n0 + nx + 1], axis=1)
+    groups = {
+        ElemType.SEG2: GroupElem(ElemType.SEG2, _edges2d(nx, ny), coord),
+        ElemType.QUAD4: GroupElem(ElemType.QUAD4, connect, coord),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Tri3_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised TRI3 mesh: each square split along its (i,j)-(i+1,j+1) diagonal."""
+    coord = _grid2d(L, h, nx, ny)
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny))
+    n00 = (j * (nx + 1) + i).ravel()
+    n10 = n00 + 1
+    n11 = n00 + nx + 2
+    n01 = n00 + nx + 1
+    t1 = np.stack([n00, n10, n11], axis=1)
+    t2 = np.stack([n00, n11, n01], axis=1)
+    connect = np.stack([t1, t2], axis=1).reshape(-1, 3)
+    groups = {
+        ElemType.SEG2: GroupElem(ElemType.SEG2, _edges2d(nx, ny), coord),
+        ElemType.TRI3: GroupElem(ElemType.TRI3, connect, coord),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Quad9_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised QUAD9 mesh (corner, mid-edge, centre nodes) on a (2nx+1)x(2ny+1) grid."""
+    NX, NY = 2 * nx, 2 * ny
+    coord = _grid2d(L, h, NX, NY)
+    nid = lambda i, j: j * (NX + 1) + i  # noqa: E731
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny))
+    I = 2 * I.ravel()
+    J = 2 * J.ravel()
+    connect = np.stack(
+        [
+            nid(I, J), nid(I + 2, J), nid(I + 2, J + 2), nid(I, J + 2),
+            nid(I + 1, J), nid(I + 2, J + 1), nid(I + 1, J + 2), nid(I, J + 1),
+            nid(I + 1, J + 1),
+        ],
+        axis=1,
+    )
+    # boundary: SEG2 pieces between consecutive boundary nodes
+    groups = {
+        ElemType.SEG2: GroupElem(ElemType.SEG2, _edges2d(NX, NY), coord),
+        ElemType.QUAD9: GroupElem(ElemType.QUAD9, connect, coord),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Hexa8_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised HEXA8 mesh of [0,Lx]x[0,Ly]x[0,Lz] with QUAD4 boundary faces."""
+    xs = np.linspace(0.0, Lx, nx + 1)
+    ys = np.linspace(0.0, Ly, ny + 1)
+    zs = np.linspace(0.0, Lz, nz + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    coord = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    nid = lambda i, j, k: (k * (ny + 1) + j) * (nx + 1) + i  # noqa: E731
+    K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    I, J, K = I.ravel(), J.ravel(), K.ravel()
+    connect = np.stack(
+        [
+            nid(I, J, K), nid(I + 1, J, K), nid(I + 1, J + 1, K), nid(I, J + 1, K),
+            nid(I, J, K + 1), nid(I + 1, J, K + 1), nid(I + 1, J + 1, K + 1), nid(I, J + 1, K + 1),
+        ],
+        axis=1,
+    )
+    faces = []
+    # x = 0 and x = Lx
+    b, a = np.meshgrid(np.arange(nz), np.arange(ny), indexing="ij")
+    a, b = a.ravel(), b.ravel()
+    for i in (0, nx):
+        faces.append(np.stack([nid(i, a, b), nid(i, a + 1, b), nid(i, a + 1, b + 1), nid(i, a, b + 1)], 1))
+    # y = 0 and y = Ly
+    b, a = np.meshgrid(np.arange(nz), np.arange(nx), indexing="ij")
+    a, b = a.ravel(), b.ravel()
+    for j in (0, ny):
+        faces.append(np.stack([nid(a, j, b), nid(a + 1, j, b), nid(a + 1, j, b + 1), nid(a, j, b + 1)], 1))
+    # z = 0 and z = Lz
+    b, a = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    a, b = a.ravel(), b.ravel()
+    for k in (0, nz):
+        faces.append(np.stack([nid(a, b, k), nid(a + 1, b, k), nid(a + 1, b + 1, k), nid(a, b + 1, k)], 1))
+    faces = np.concatenate(faces, 0)
+    groups = {
+        ElemType.QUAD4: GroupElem(ElemType.QUAD4, faces, coord),
+        ElemType.HEXA8: GroupElem(ElemType.HEXA8, connect, coord),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
+    elemType = ElemType(elemType)
+    if elemType == ElemType.QUAD4:
+        return Mesh_Quad4_Rect(L, h, nx, ny)
+    if elemType == ElemType.TRI3:
+        return Mesh_Tri3_Rect(L, h, nx, ny)
+    if elemType == ElemType.QUAD9:
+        return Mesh_Quad9_Rect(L, h, nx, ny)
+    raise NotImplementedError(elemType)

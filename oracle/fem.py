@@ -1,0 +1,713 @@
+"""CPU oracle for the EasyFEA finite-element hot path -- TEST INFRASTRUCTURE ONLY.
+
+A plain numpy/scipy restatement of the reference algorithms (matnoel/EasyFEA
+v3.5.1), used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU baseline
+leg of ``bench.py`` as the checker.  Nothing in the product package imports it.
+
+Parity is pinned: ``tests/golden/make_golden.py`` runs the reference itself (in
+a container where its sources are importable) and stores its outputs under
+``tests/golden/``; ``tests/test_oracle_golden.py`` checks this module against
+them.
+
+Each function cites the reference file:line it restates.  All arithmetic is
+float64, as in the reference.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as sla
+
+SQRT2 = np.sqrt(2.0)
+
+# ---------------------------------------------------------------------------
+# quadrature (EasyFEA/FEM/_gauss.py)
+# ---------------------------------------------------------------------------
+
+
+def gauss(elem: str, matrixType: str):
+    """Gauss points (nPg, dim) and weights (nPg,).
+
+    EasyFEA/FEM/_gauss.py:364-480 (Gauss_factory); triangle table :55-108,
+    quadrangle :111-138, hexahedron :201-..., SEG2 Gauss-Legendre :373-382.
+    """
+    if elem == "SEG2":
+        n = 1 if matrixType == "rigi" else 2
+        x, w = np.polynomial.legendre.leggauss(n)
+        return x.reshape(-1, 1), w
+    if elem == "TRI3":
+        if matrixType == "rigi":
+            xi, eta, w = [1 / 3], [1 / 3], [1 / 2]
+        else:
+            xi, eta, w = [1 / 6, 2 / 3, 1 / 6], [1 / 6, 1 / 6, 2 / 3], [1 / 6] * 3
+        return np.array([xi, eta]).T, np.array(w)
+    if elem == "QUAD4":
+        a = 1 / np.sqrt(3)
+        return np.array([[-a, a, a, -a], [-a, -a, a, a]]).T, np.ones(4)
+    if elem == "QUAD9":
+        a = 0.774596669241483
+        xi = [-a, a, a, -a, 0.0, a, 0.0, -a, 0.0]
+        eta = [-a, -a, a, a, -a, 0.0, a, 0.0, 0.0]
+        w = [25 / 81] * 4 + [40 / 81] * 4 + [64 / 81]
+        return np.array([xi, eta]).T, np.array(w)
+    if elem == "HEXA8":
+        a = 1 / np.sqrt(3)
+        x = [-a, -a, -a, -a, a, a, a, a]
+        y = [-a, -a, a, a, -a, -a, a, a]
+        z = [-a, a, -a, a, -a, a, -a, a]
+        return np.array([x, y, z]).T, np.ones(8)
+    raise NotImplementedError(elem)
+
+
+# ---------------------------------------------------------------------------
+# shape functions (EasyFEA/FEM/Elems/*.py)
+# ---------------------------------------------------------------------------
+
+
+def shape_N(elem: str, p: np.ndarray) -> np.ndarray:
+    """N at one point -> (nPe,).  _seg.py:55-60, _tri.py:55-60, _quad.py:55-60,
+    _quad.py:255-266 (QUAD9), _hexa.py:75-86."""
+    if elem == "SEG2":
+        (r,) = p
+        return np.array([-(r - 1) / 2, (r + 1) / 2])
+    if elem == "TRI3":
+        r, s = p
+        return np.array([-r - s + 1, r, s])
+    if elem == "QUAD4":
+        r, s = p
+        return np.array([(r - 1) * (s - 1) / 4, -(r + 1) * (s - 1) / 4,
+                         (r + 1) * (s + 1) / 4, -(r - 1) * (s + 1) / 4])
+    if elem == "QUAD9":
+        r, s = p
+        return np.array([
+            r * s * (r - 1) * (s - 1) / 4, r * s * (r + 1) * (s - 1) / 4,
+            r * s * (r + 1) * (s + 1) / 4, r * s * (r - 1) * (s + 1) / 4,
+            -s * (r - 1) * (r + 1) * (s - 1) / 2, -r * (r + 1) * (s - 1) * (s + 1) / 2,
+            -s * (r - 1) * (r + 1) * (s + 1) / 2, -r * (r - 1) * (s - 1) * (s + 1) / 2,
+            (r - 1) * (r + 1) * (s - 1) * (s + 1)])
+    if elem == "HEXA8":
+        r, s, t = p
+        return np.array([
+            -(r - 1) * (s - 1) * (t - 1) / 8, (r + 1) * (s - 1) * (t - 1) / 8,
+            -(r + 1) * (s + 1) * (t - 1) / 8, (r - 1) * (s + 1) * (t - 1) / 8,
+            (r - 1) * (s - 1) * (t + 1) / 8, -(r + 1) * (s - 1) * (t + 1) / 8,
+            (r + 1) * (s + 1) * (t + 1) / 8, -(r - 1) * (s + 1) * (t + 1) / 8])
+    raise NotImplementedError(elem)
+
+
+def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
+    """dN/dxi at one point -> (dim, nPe).  _seg.py:62-68, _tri.py:62-68,
+    _quad.py:62-70, _quad.py:268-305 (QUAD9), _hexa.py:88-130."""
+    if elem == "SEG2":
+        return np.array([[-1 / 2, 1 / 2]])
+    if elem == "TRI3":
+        return np.array([[-1.0, 1.0, 0.0], [-1.0, 0.0, 1.0]])
+    if elem == "QUAD4":
+        r, s = p
+        return np.array([[s / 4 - 1 / 4, 1 / 4 - s / 4, s / 4 + 1 / 4, -s / 4 - 1 / 4],
+                         [r / 4 - 1 / 4, -r / 4 - 1 / 4, r / 4 + 1 / 4, 1 / 4 - r / 4]])
+    if elem == "QUAD9":
+        r, s = p
+        dr = [
+            r * s * (s - 1) / 4 + s * (r - 1) * (s - 1) / 4,
+            r * s * (s - 1) / 4 + s * (r + 1) * (s - 1) / 4,
+            r * s * (s + 1) / 4 + s * (r + 1) * (s + 1) / 4,
+            r * s * (s + 1) / 4 + s * (r - 1) * (s + 1) / 4,
+            -s * (r - 1) * (s - 1) / 2 - s * (r + 1) * (s - 1) / 2,
+            -r * (s - 1) * (s + 1) / 2 - (r + 1) * (s - 1) * (s + 1) / 2,
+            -s * (r - 1) * (s + 1) / 2 - s * (r + 1) * (s + 1) / 2,
+            -r * (s - 1) * (s + 1) / 2 - (r - 1) * (s - 1) * (s + 1) / 2,
+            (r - 1) * (s - 1) * (s + 1) + (r + 1) * (s - 1) * (s + 1),
+        ]
+        ds = [
+            r * s * (r - 1) / 4 + r * (r - 1) * (s - 1) / 4,
+            r * s * (r + 1) / 4 + r * (r + 1) * (s - 1) / 4,
+            r * s * (r + 1) / 4 + r * (r + 1) * (s + 1) / 4,
+            r * s * (r - 1) / 4 + r * (r - 1) * (s + 1) / 4,
+            -s * (r - 1) * (r + 1) / 2 - (r - 1) * (r + 1) * (s - 1) / 2,
+            -r * (r + 1) * (s - 1) / 2 - r * (r + 1) * (s + 1) / 2,
+            -s * (r - 1) * (r + 1) / 2 - (r - 1) * (r + 1) * (s + 1) / 2,
+            -r * (r - 1) * (s - 1) / 2 - r * (r - 1) * (s + 1) / 2,
+            (r - 1) * (r + 1) * (s - 1) + (r - 1) * (r + 1) * (s + 1),
+        ]
+        return np.array([dr, ds])
+    if elem == "HEXA8":
+        r, s, t = p
+        return np.array([
+            [-(s - 1) * (t - 1) / 8, (s - 1) * (t - 1) / 8, -(s + 1) * (t - 1) / 8, (s + 1) * (t - 1) / 8,
+             (s - 1) * (t + 1) / 8, -(s - 1) * (t + 1) / 8, (s + 1) * (t + 1) / 8, -(s + 1) * (t + 1) / 8],
+            [-(r - 1) * (t - 1) / 8, (r + 1) * (t - 1) / 8, -(r + 1) * (t - 1) / 8, (r - 1) * (t - 1) / 8,
+             (r - 1) * (t + 1) / 8, -(r + 1) * (t + 1) / 8, (r + 1) * (t + 1) / 8, -(r - 1) * (t + 1) / 8],
+            [-(r - 1) * (s - 1) / 8, (r + 1) * (s - 1) / 8, -(r + 1) * (s + 1) / 8, (r - 1) * (s + 1) / 8,
+             (r - 1) * (s - 1) / 8, -(r + 1) * (s - 1) / 8, (r + 1) * (s + 1) / 8, -(r - 1) * (s + 1) / 8],
+        ])
+    raise NotImplementedError(elem)
+
+
+ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3}
+
+
+def N_pg(elem, matrixType):
+    """(nPg, nPe) -- _group_elem.py:990-1000 (Get_N_pg)."""
+    xg, _ = gauss(elem, matrixType)
+    return np.array([shape_N(elem, p) for p in xg])
+
+
+def dN_pg(elem, matrixType):
+    """(nPg, dim, nPe) -- _group_elem.py:1063-1081 (Get_dN_pg)."""
+    xg, _ = gauss(elem, matrixType)
+    return np.array([shape_dN(elem, p) for p in xg])
+
+
+# ---------------------------------------------------------------------------
+# element geometry (EasyFEA/FEM/_group_elem.py:833-915, _linalg.py:533-656)
+# ---------------------------------------------------------------------------
+
+
+def det(F):
+    """Closed-form determinant, _linalg.py:533-573."""
+    d = F.shape[-1]
+    if d == 1:
+        return F[..., 0, 0]
+    if d == 2:
+        return F[..., 0, 0] * F[..., 1, 1] - F[..., 1, 0] * F[..., 0, 1]
+    a = F
+    return (a[..., 0, 0] * (a[..., 1, 1] * a[..., 2, 2] - a[..., 2, 1] * a[..., 1, 2])
+            - a[..., 0, 1] * (a[..., 1, 0] * a[..., 2, 2] - a[..., 2, 0] * a[..., 1, 2])
+            + a[..., 0, 2] * (a[..., 1, 0] * a[..., 2, 1] - a[..., 2, 0] * a[..., 1, 1]))
+
+
+def inv(F):
+    """Adjugate inverse, _linalg.py:576-656."""
+    d = F.shape[-1]
+    D = det(F)
+    if d == 1:
+        return 1 / F
+    adj = np.zeros_like(F)
+    if d == 2:
+        adj[..., 0, 0] = F[..., 1, 1]
+        adj[..., 0, 1] = -F[..., 0, 1]
+        adj[..., 1, 0] = -F[..., 1, 0]
+        adj[..., 1, 1] = F[..., 0, 0]
+        return adj / D[..., None, None]
+    T = np.swapaxes(F, -1, -2)
+    a = lambda i, j: T[..., i, j]  # noqa: E731
+    adj[..., 0, 0] = a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)
+    adj[..., 0, 1] = -(a(1, 0) * a(2, 2) - a(2, 0) * a(1, 2))
+    adj[..., 0, 2] = a(1, 0) * a(2, 1) - a(2, 0) * a(1, 1)
+    adj[..., 1, 0] = -(a(0, 1) * a(2, 2) - a(2, 1) * a(0, 2))
+    adj[..., 1, 1] = a(0, 0) * a(2, 2) - a(2, 0) * a(0, 2)
+    adj[..., 1, 2] = -(a(0, 0) * a(2, 1) - a(2, 0) * a(0, 1))
+    adj[..., 2, 0] = a(0, 1) * a(1, 2) - a(1, 1) * a(0, 2)
+    adj[..., 2, 1] = -(a(0, 0) * a(1, 2) - a(1, 0) * a(0, 2))
+    adj[..., 2, 2] = a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1)
+    return adj / D[..., None, None]
+
+
+class Geometry:
+    """Per-(element, Gauss point) geometry of one group for one matrixType.
+
+    F = dN_pg @ X_e (_group_elem.py:833-869), wJ = |det F| * w (:872-900),
+    dN_e = inv(F) @ dN_pg (:903-915, :1084-1105).  Boundary groups (dim <
+    embedding dim) use the element-local frame of _group_elem.py:404-500; for
+    straight segments and flat faces |det F| equals the length / area scale
+    computed here from the tangent vectors.
+    """
+
+    def __init__(self, elem, coord, connect, matrixType):
+        self.elem = elem
+        self.dim = ELEM_DIM[elem]
+        xg, w = gauss(elem, matrixType)
+        self.w = w
+        self.N = N_pg(elem, matrixType)
+        self.dN = dN_pg(elem, matrixType)
+        X = coord[connect]  # (Ne, nPe, 3)
+        if self.dim == coord_dim(coord) or self.dim == 3:
+            Xd = X[:, :, : self.dim]
+            F = np.einsum("pdn,enk->epdk", self.dN, Xd)
+            self.F = F
+            self.detJ = np.abs(det(F))
+            self.invF = inv(F)
+            self.dNx = np.einsum("epij,pjn->epin", self.invF, self.dN)
+        else:
+            # tangent vectors dx/dxi_k (Ne, nPg, dim, 3)
+            T = np.einsum("pdn,enk->epdk", self.dN, X)
+            if self.dim == 1:
+                self.detJ = np.linalg.norm(T[:, :, 0, :], axis=-1)
+            else:
+                self.detJ = np.linalg.norm(np.cross(T[:, :, 0, :], T[:, :, 1, :]), axis=-1)
+            self.dNx = None
+        self.wJ = self.detJ * w[None, :]
+        self.X = X
+
+
+def coord_dim(coord):
+    _, y, z = np.abs(coord.T)
+    if z.size and z.max() > 0:
+        return 3
+    if y.size and y.max() > 0:
+        return 2
+    return 1
+
+
+def B_e_pg(dNx):
+    """Kelvin-Mandel strain-displacement operator, _group_elem.py:1242-1312."""
+    Ne, nPg, dim, nPe = dNx.shape
+    cM = 1 / np.sqrt(2)
+    if dim == 2:
+        B = np.zeros((Ne, nPg, 3, nPe * 2))
+        dx, dy = dNx[:, :, 0], dNx[:, :, 1]
+        B[:, :, 0, 0::2] = dx
+        B[:, :, 1, 1::2] = dy
+        B[:, :, 2, 0::2] = dy * cM
+        B[:, :, 2, 1::2] = dx * cM
+    else:
+        B = np.zeros((Ne, nPg, 6, nPe * 3))
+        dx, dy, dz = dNx[:, :, 0], dNx[:, :, 1], dNx[:, :, 2]
+        B[:, :, 0, 0::3] = dx
+        B[:, :, 1, 1::3] = dy
+        B[:, :, 2, 2::3] = dz
+        B[:, :, 3, 1::3] = dz * cM
+        B[:, :, 3, 2::3] = dy * cM
+        B[:, :, 4, 0::3] = dz * cM
+        B[:, :, 4, 2::3] = dx * cM
+        B[:, :, 5, 0::3] = dy * cM
+        B[:, :, 5, 1::3] = dx * cM
+    return B
+
+
+# ---------------------------------------------------------------------------
+# constitutive law (EasyFEA/Models/Elastic/_laws.py, Models/_utils.py)
+# ---------------------------------------------------------------------------
+
+
+def lame(E, v, dim, planeStress):
+    """lambda, mu -- Elastic/_laws.py:376-403 (plane stress lambda = E v / (1 - v^2))."""
+    E = np.asarray(E, dtype=float)
+    lmbda = E * v / ((1 + v) * (1 - 2 * v))
+    if dim == 2 and planeStress:
+        lmbda = E * v / (1 - v**2)
+    mu = E / (2 * (1 + v))
+    return lmbda, mu
+
+
+def isotropic_C(E, v, dim, planeStress=True):
+    """Kelvin-Mandel C, Elastic/_laws.py:407-482 + Models/_utils.py:111-152.
+
+    ``E`` scalar -> (3,3)/(6,6); ``E`` (Ne,) -> (Ne,3,3)/(Ne,6,6)
+    (Heterogeneous_Array, Models/_utils.py:69-108).
+    """
+    lmbda, mu = lame(E, v, dim, planeStress)
+    r2 = np.sqrt(2)
+    if dim == 2:
+        shape = np.shape(lmbda) + (3, 3)
+        c = np.zeros(shape)
+        c[..., 0, 0] = c[..., 1, 1] = lmbda + 2 * mu
+        c[..., 0, 1] = c[..., 1, 0] = lmbda
+        c[..., 2, 2] = mu
+        T = np.array([[1, 1, r2], [1, 1, r2], [r2, r2, 2]])
+    else:
+        shape = np.shape(lmbda) + (6, 6)
+        c = np.zeros(shape)
+        for i in range(3):
+            for j in range(3):
+                c[..., i, j] = lmbda
+            c[..., i, i] = lmbda + 2 * mu
+        for i in range(3, 6):
+            c[..., i, i] = mu
+        T = np.ones((6, 6))
+        T[3:, :3] = r2
+        T[:3, 3:] = r2
+        T[3:, 3:] = 2
+    return c * T
+
+
+# ---------------------------------------------------------------------------
+# element operators (EasyFEA/FEM/Operators/Bilinear.py, Linear.py)
+# ---------------------------------------------------------------------------
+
+
+def K_elastic_e(geo: Geometry, C):
+    """K_e = sum_pg wJ B^T C B -- Bilinear.py:62-79 (LinearizedElasticity).
+
+    C: (n,n), (Ne,n,n) or (Ne,nPg,n,n)."""
+    B = B_e_pg(geo.dNx)
+    left = geo.wJ[:, :, None, None] * np.swapaxes(B, -1, -2)
+    C = np.asarray(C)
+    if C.ndim == 2:
+        LC = left @ C
+    elif C.ndim == 3:
+        LC = left @ C[:, None]
+    else:
+        LC = left @ C
+    return np.einsum("epij,epjk->eik", LC, B)
+
+
+def UV_e(geo: Geometry, coef, dof_n=1):
+    """M_e = sum_pg coef wJ N^T N -- Bilinear.py:42-59 with _group_elem.py:1338-1360."""
+    N = geo.N  # (nPg, nPe)
+    nPg, nPe = N.shape
+    if dof_n == 1:
+        Nr = N[:, None, :]
+    else:
+        Nr = np.zeros((nPg, dof_n, nPe * dof_n))
+        for r in range(dof_n):
+            Nr[:, r, r::dof_n] = N
+    NtN = np.einsum("pri,prj->pij", Nr, Nr)
+    coef = np.broadcast_to(np.asarray(coef, dtype=float), geo.wJ.shape) if np.ndim(coef) != 1 \
+        else np.broadcast_to(np.asarray(coef, dtype=float)[:, None], geo.wJ.shape)
+    return np.einsum("ep,pij->eij", coef * geo.wJ, NtN)
+
+
+def GradU_A_GradV_e(geo: Geometry, A, k):
+    """D_e = sum_pg k wJ dN^T A dN -- Bilinear.py:229-249 (_group_elem.py:1363-1380)."""
+    A = np.asarray(A, dtype=float)
+    return np.einsum("ep,epin,ij,epjm->enm", k * geo.wJ, geo.dNx, A, geo.dNx)
+
+
+def V_e(geo: Geometry, f):
+    """F_e = sum_pg f wJ N^T -- Linear.py:18-35 (_group_elem.py:1383-1407)."""
+    return np.einsum("ep,pn->en", f * geo.wJ, geo.N)
+
+
+# ---------------------------------------------------------------------------
+# assembly (EasyFEA/Simulations/_simu.py:989-1102)
+# ---------------------------------------------------------------------------
+
+
+def assembly_e(connect, dof_n):
+    """_group_elem.py:346-380."""
+    Ne, nPe = connect.shape
+    a = np.empty((Ne, nPe * dof_n), dtype=np.int64)
+    for d in range(dof_n):
+        a[:, d::dof_n] = connect * dof_n + d
+    return a
+
+
+def csr_map(connect, dof_n, Ndof):
+    """(inv, indices, indptr, nnz) -- _simu.py:1062-1102 (__Get_csr_map).
+
+    rows/cols from _group_elem.py:382-402 (row-major (i, j) over local DOFs);
+    scipy builds the canonical pattern, searchsorted maps each element entry."""
+    a = assembly_e(connect, dof_n)
+    Ne, nd = a.shape
+    rows = np.repeat(a, nd).reshape(Ne, nd * nd).ravel()
+    cols = np.repeat(a, nd, axis=0).reshape(Ne, nd * nd).ravel()
+    M = sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(Ndof, Ndof))
+    M.sort_indices()
+    canon = np.repeat(np.arange(Ndof), np.diff(M.indptr)) * Ndof + M.indices
+    invmap = np.searchsorted(canon, rows.astype(np.int64) * Ndof + cols).astype(np.int32)
+    return invmap, M.indices, M.indptr, M.nnz
+
+
+def assemble_csr(K_e, invmap, indices, indptr, nnz, Ndof):
+    """np.bincount scatter, _simu.py:1044-1058."""
+    data = np.bincount(invmap, weights=K_e.ravel(), minlength=nnz)
+    A = sp.csr_matrix((data, indices, indptr), shape=(Ndof, Ndof))
+    A.has_canonical_format = True
+    return A
+
+
+def assemble_vec(F_e, connect, dof_n, Ndof):
+    """Vector assembly (isMatrix False), _simu.py:1086-1090 + :1044-1058."""
+    a = assembly_e(connect, dof_n).ravel()
+    return np.bincount(a, weights=np.asarray(F_e).ravel(), minlength=Ndof)
+
+
+# ---------------------------------------------------------------------------
+# boundary conditions (EasyFEA/Simulations/_simu.py:2400-2842)
+# ---------------------------------------------------------------------------
+
+UNKNOWNS = {1: ["d"], 2: ["x", "y"], 3: ["x", "y", "z"]}
+
+
+def dofs_nodes(nodes, unknowns, available):
+    """node * dof_n + index(unknown) -- FEM/_boundary_conditions.py:160-205."""
+    nodes = np.asarray(nodes, dtype=np.int64)
+    dof_n = len(available)
+    out = np.zeros((nodes.size, len(unknowns)), dtype=np.int64)
+    for i, u in enumerate(unknowns):
+        out[:, i] = nodes * dof_n + available.index(u)
+    return out.ravel()
+
+
+def surf_load(elem, coord, connect, nodes, values, unknowns, available, thickness=1.0):
+    """Neumann nodal loads -- _simu.py:2770-2842 (__Bc_Integration_Dim) with the
+    2D thickness factor of :2572-2630.  Constant ``values`` only.
+
+    Returns (dofs, dofsValues) in the COO form the reference appends."""
+    mark = np.zeros(coord.shape[0], dtype=bool)
+    mark[np.asarray(nodes)] = True
+    sel = np.nonzero(mark[connect].all(axis=1))[0]
+    if sel.size == 0:
+        return np.zeros(0, np.int64), np.zeros(0)
+    con = connect[sel]
+    geo = Geometry(elem, coord, con, "mass")
+    Ne, nPe = con.shape
+    vals = np.zeros((Ne * nPe, len(unknowns)))
+    dofs = np.zeros((Ne * nPe, len(unknowns)), dtype=np.int64)
+    for u, name in enumerate(unknowns):
+        ev = np.full(geo.wJ.shape, float(values[u]))
+        ve = np.einsum("ep,ep,pn->epn", geo.wJ, ev, geo.N)
+        vals[:, u] = ve.sum(1).ravel()
+        dofs[:, u] = dofs_nodes(con.ravel(), [name], available)
+    return dofs.ravel(), vals.ravel() * thickness
+
+
+def solve_r1(A, b, known, known_values, orphan_dofs=()):
+    """Dirichlet elimination + direct solve -- Solvers.py:502-553 (__Solver_1),
+    _simu.py:1916-1968 (orphan diagonal fix), :2295-2316 (known/unknown sets),
+    Solvers.py:361-362 (scipy spsolve)."""
+    Ndof = A.shape[0]
+    known = np.asarray(known, dtype=np.int64)
+    x = sp.csr_matrix((np.asarray(known_values, float), (known, np.zeros_like(known))),
+                      shape=(Ndof, 1)).toarray().ravel()
+    if len(orphan_dofs):
+        diag = np.zeros(Ndof)
+        diag[np.asarray(orphan_dofs)] = 1.0
+        A = A + sp.diags(diag, format="csr")
+    mask = np.ones(Ndof, dtype=bool)
+    mask[known] = False
+    dk = np.nonzero(~mask)[0]
+    du = np.nonzero(mask)[0]
+    Ai = A[du, :].tocsc()
+    Aii = Ai[:, du]
+    Aic = Ai[:, dk]
+    bi = b[du] - Aic @ x[dk]
+    xi = sla.spsolve(Aii, bi)
+    x[du] = xi
+    return x
+
+
+# ---------------------------------------------------------------------------
+# phase-field split (EasyFEA/Models/_phasefield.py)
+# ---------------------------------------------------------------------------
+
+
+def vec_to_mat(v):
+    """Project_vector_to_matrix, Models/_utils.py:155-188 (coef sqrt 2)."""
+    n = v.shape[-1]
+    dim = 2 if n == 3 else 3
+    M = np.zeros(v.shape[:-1] + (dim, dim))
+    for d in range(dim):
+        M[..., d, d] = v[..., d]
+    if dim == 2:
+        M[..., 0, 1] = M[..., 1, 0] = v[..., 2] / SQRT2
+    else:
+        M[..., 1, 2] = M[..., 2, 1] = v[..., 3] / SQRT2
+        M[..., 0, 2] = M[..., 2, 0] = v[..., 4] / SQRT2
+        M[..., 0, 1] = M[..., 1, 0] = v[..., 5] / SQRT2
+    return M
+
+
+def mat_to_vec(M):
+    """Project_matrix_to_vector, Models/_utils.py:191-222."""
+    dim = M.shape[-1]
+    if dim == 2:
+        return np.stack([M[..., 0, 0], M[..., 1, 1], M[..., 0, 1] * SQRT2], -1)
+    return np.stack([M[..., 0, 0], M[..., 1, 1], M[..., 2, 2],
+                     M[..., 1, 2] * SQRT2, M[..., 0, 2] * SQRT2, M[..., 0, 1] * SQRT2], -1)
+
+
+def eigen_projectors(eps, clamp=False):
+    """Eigenvalues and eigenprojectors of the strain -- Models/_phasefield.py:751-1041.
+
+    2D closed form :777-807; 3D Q.-C. He closed form with the Lode-angle cases
+    :809-948 and the Frobenius normalisation of M1, M3 at :944-948.
+
+    The reference evaluates ``arccos`` of an argument that rounding can push just
+    past +-1 at repeated eigenvalues, which yields NaN there.  ``clamp=False``
+    reproduces that; ``clamp=True`` clips the argument to [-1, 1] (the GPU kernels'
+    behaviour), selecting the repeated-eigenvalue branch instead."""
+    M = vec_to_mat(eps)
+    dim = M.shape[-1]
+    I = np.zeros_like(M)
+    for d in range(dim):
+        I[..., d, d] = 1
+    shp = eps.shape[:-1]
+    if dim == 2:
+        D = det(M)
+        tr = M[..., 0, 0] + M[..., 1, 1]
+        delta = tr**2 - 4 * D
+        vals = np.zeros(shp + (2,))
+        vals[..., 0] = (tr - np.sqrt(delta)) / 2
+        vals[..., 1] = (tr + np.sqrt(delta)) / 2
+        v1mv2 = vals[..., 0] - vals[..., 1]
+        diff = vals[..., 0] != vals[..., 1]
+        M1 = np.zeros_like(M)
+        M1[..., 0, 0] = 1
+        if diff.any():
+            v = v1mv2.copy()
+            v[v == 0] = 1
+            m1 = (M - vals[..., 1][..., None, None] * I) / v[..., None, None]
+            M1[diff] = m1[diff]
+        M2 = I - M1
+        return vals, [M1, M2]
+    I1 = M[..., 0, 0] + M[..., 1, 1] + M[..., 2, 2]
+    MM = M @ M
+    I2 = 0.5 * (I1**2 - (MM[..., 0, 0] + MM[..., 1, 1] + MM[..., 2, 2]))
+    I3 = det(M)
+    g = I1**2 - 3 * I2
+    sg = np.sqrt(g)
+    gnz = g != 0
+    arg = 0.5 * (2 * I1**3 - 9 * I1 * I2 + 27 * I3)
+    arg = np.divide(arg, g ** (3 / 2), out=arg, where=gnz)
+    if clamp:
+        arg = np.clip(arg, -1.0, 1.0)
+    with np.errstate(invalid="ignore"):
+        theta = np.arccos(arg) / 3
+    v1 = I1 / 3
+    v2 = I1 / 3
+    v3 = I1 / 3
+    M1 = np.zeros_like(M)
+    M1[..., 0, 0] = 1
+    M3 = np.zeros_like(M)
+    M3[..., 2, 2] = 1
+    Irg = ((I1 - sg) / 3)[..., None, None] * I
+    c2 = gnz & (theta == np.pi / 3)
+    c3 = gnz & (theta == 0)
+    c1 = gnz & (theta != 0) & (theta != np.pi / 3)
+    c1 = c1 & ~c2 & ~c3
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        gm = g ** (-1 / 2)
+    old = np.seterr(invalid="ignore", divide="ignore")
+    if c2.any():
+        v1 = np.where(c2, v1 - 2 / 3 * sg, v1)
+        v2 = np.where(c2, v2 + 1 / 3 * sg, v2)
+        v3 = np.where(c2, v3 + 1 / 3 * sg, v3)
+        m1 = gm[..., None, None] * (Irg - M)
+        M1 = np.where(c2[..., None, None], m1, M1)
+        M3 = np.where(c2[..., None, None], 0.5 * (I - M1), M3)
+    if c3.any():
+        v1 = np.where(c3, v1 - 1 / 3 * sg, v1)
+        v2 = np.where(c3, v2 - 1 / 3 * sg, v2)
+        v3 = np.where(c3, v3 + 2 / 3 * sg, v3)
+        m3 = gm[..., None, None] * (M - Irg)
+        M3 = np.where(c3[..., None, None], m3, M3)
+        M1 = np.where(c3[..., None, None], 0.5 * (I - M3), M1)
+    if c1.any():
+        v1 = np.where(c1, v1 + 2 / 3 * (sg * np.cos(2 * np.pi / 3 + theta)), v1)
+        v2 = np.where(c1, v2 + 2 / 3 * (sg * np.cos(2 * np.pi / 3 - theta)), v2)
+        v3 = np.where(c1, v3 + 2 / 3 * (sg * np.cos(theta)), v3)
+        E3 = np.eye(3)
+        a = v1[..., None, None]
+        b = v2[..., None, None]
+        c = v3[..., None, None]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m1 = (M - b * E3) @ (M - c * E3) / ((a - b) * (a - c))
+            m3 = (M - a * E3) @ (M - b * E3) / ((c - a) * (c - b))
+        M1 = np.where(c1[..., None, None], m1, M1)
+        M3 = np.where(c1[..., None, None], m3, M3)
+    np.seterr(**old)
+    vals = np.stack([v1, v2, v3], -1)
+    M1 = M1 / np.linalg.norm(M1, axis=(-2, -1))[..., None, None]
+    M3 = M3 / np.linalg.norm(M3, axis=(-2, -1))[..., None, None]
+    M2 = I - (M1 + M3)
+    return vals, [M1, M2, M3]
+
+
+def spectral_projectors(eps, clamp=False):
+    """projP, projM -- Models/_phasefield.py:1043-1243 (__Spectral_Decomposition)."""
+    vals, Ms = eigen_projectors(eps, clamp)
+    dim = Ms[0].shape[-1]
+    valp = (vals + np.abs(vals)) / 2
+    dvalp = np.heaviside(vals, 0.5)
+    if dim == 2:
+        m1 = mat_to_vec(Ms[0])
+        m2 = mat_to_vec(Ms[1])
+        v = vals[..., 0] - vals[..., 1]
+        v = np.where(v == 0, 1, v)
+        BetaP = (valp[..., 0] - valp[..., 1]) / v
+        gp = dvalp - BetaP[..., None]
+        projP = (BetaP[..., None, None] * np.eye(3)
+                 + gp[..., 0, None, None] * np.einsum("...i,...j->...ij", m1, m1)
+                 + gp[..., 1, None, None] * np.einsum("...i,...j->...ij", m2, m2))
+        return projP, np.eye(3) - projP
+    M1, M2, M3 = Ms
+    ms = [mat_to_vec(Mi) for Mi in Ms]
+    th = dvalp / 2
+    d12 = vals[..., 0] - vals[..., 1]
+    d13 = vals[..., 0] - vals[..., 2]
+    d23 = vals[..., 1] - vals[..., 2]
+    d12 = np.where(d12 == 0, 1, d12)
+    d13 = np.where(d13 == 0, 1, d13)
+    d23 = np.where(d23 == 0, 1, d23)
+    th = np.stack([(valp[..., 0] - valp[..., 1]) / (2 * d12),
+                   (valp[..., 0] - valp[..., 2]) / (2 * d13),
+                   (valp[..., 1] - valp[..., 2]) / (2 * d23)], -1)
+    diag = sum(dvalp[..., k, None, None] * np.einsum("...i,...j->...ij", ms[k], ms[k]) for k in range(3))
+    rI = np.array([0, 1, 2, 1, 0, 0])
+    rJ = np.array([0, 1, 2, 2, 2, 1])
+    scale = np.ones((6, 6))
+    scale[3:, :3] = SQRT2
+    scale[:3, 3:] = SQRT2
+    scale[3:, 3:] = 2.0
+    G = 0
+    for t, (A, B) in enumerate([(M1, M2), (M1, M3), (M2, M3)]):
+        A_ik = A[..., rI[:, None], rI[None, :]]
+        A_il = A[..., rI[:, None], rJ[None, :]]
+        A_jl = A[..., rJ[:, None], rJ[None, :]]
+        B_ik = B[..., rI[:, None], rI[None, :]]
+        B_il = B[..., rI[:, None], rJ[None, :]]
+        B_jl = B[..., rJ[:, None], rJ[None, :]]
+        Gab = (A_ik * B_jl + A_il * np.swapaxes(B_il, -1, -2)
+               + B_ik * A_jl + B_il * np.swapaxes(A_il, -1, -2)) * scale
+        G = G + th[..., t, None, None] * Gab
+    projP = diag + G
+    return projP, np.eye(6) - projP
+
+
+def IxI(dim):
+    I = np.array([1.0, 1.0, 0.0]) if dim == 2 else np.array([1.0, 1, 1, 0, 0, 0])
+    return np.outer(I, I)
+
+
+def split_C(eps, split, lmbda, mu, dim, C=None, clamp=False):
+    """cP, cM -- Models/_phasefield.py:396-571 (Calc_C, Bourdin :433-449,
+    Amor :451-483, Rp/Rm :485-501, Miehe :503-540).
+
+    ``lmbda``/``mu`` scalars or (Ne,) arrays; eps (Ne, nPg, 3|6)."""
+    Ne, nPg = eps.shape[:2]
+    lm = np.broadcast_to(np.asarray(lmbda, float).reshape(-1, 1) if np.ndim(lmbda) else lmbda, (Ne, nPg))
+    mm = np.broadcast_to(np.asarray(mu, float).reshape(-1, 1) if np.ndim(mu) else mu, (Ne, nPg))
+    n = 3 if dim == 2 else 6
+    II = IxI(dim)
+    if split == "Bourdin":
+        Cf = np.broadcast_to(C, (Ne, nPg, n, n)) if np.ndim(C) == 2 else np.broadcast_to(C[:, None], (Ne, nPg, n, n))
+        return np.array(Cf), np.zeros((Ne, nPg, n, n))
+    tr = eps[..., 0] + eps[..., 1] + (eps[..., 2] if dim == 3 else 0)
+    Rp = (1 + np.sign(tr)) / 2
+    Rm = (1 + np.sign(-tr)) / 2
+    if split == "Amor":
+        bulk = lm + 2 * mm / dim
+        cP = bulk[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * (np.eye(n) - II / dim)
+        cM = bulk[..., None, None] * (Rm[..., None, None] * II)
+        return cP, cM
+    if split == "Miehe":
+        projP, projM = spectral_projectors(eps, clamp)
+        cP = lm[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * projP
+        cM = lm[..., None, None] * (Rm[..., None, None] * II) + 2 * mm[..., None, None] * projM
+        return cP, cM
+    raise NotImplementedError(split)
+
+
+def psi_split(eps, cP, cM):
+    """psi+- = 1/2 eps . (c+- eps) -- Models/_phasefield.py:335-394."""
+    sP = np.einsum("epij,epj->epi", cP, eps)
+    sM = np.einsum("epij,epj->epi", cM, eps)
+    return np.sum(0.5 * eps * sP, -1), np.sum(0.5 * eps * sM, -1)
+
+
+def pf_r_f_k(psiP, regu, Gc, l0):
+    """Models/_phasefield.py:237-293."""
+    if regu == "AT1":
+        k = 3 / 4 * Gc * l0
+        r = 2 * psiP
+        f = 2 * psiP - (3 * Gc) / (8 * l0)
+        f = (f + np.abs(f)) / 2
+    else:
+        k = Gc * l0
+        r = 2 * psiP + Gc / l0
+        f = 2 * psiP
+    return r, f, k

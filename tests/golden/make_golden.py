@@ -1,0 +1,236 @@
+"""Generate the golden fixtures of ``tests/golden/`` by running the reference itself.
+
+Run in a container where matnoel/EasyFEA's sources are importable::
+
+    python tests/golden/make_golden.py [/root/reference]
+
+gmsh (imported unconditionally by EasyFEA/FEM/_mesher.py:13) is replaced by an
+empty stub module; meshes come from ``easyfea_gb300.mesh``'s organised
+generators and are handed to the reference through
+``GroupElemFactory.Create`` + ``Mesh`` (EasyFEA/FEM/_group_elem.py:2330-2355,
+EasyFEA/FEM/_mesh.py:46-91).  The solver is pinned to ``scipy`` (SuperLU).
+
+Each case is written as one compressed ``.npz`` holding its inputs (mesh
+arrays, material, boundary conditions) and the reference's outputs.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from easyfea_gb300 import mesh as gmesh  # noqa: E402
+
+
+def load_reference(path):
+    sys.modules.setdefault("gmsh", types.ModuleType("gmsh"))
+    sys.path.insert(0, path)
+    import EasyFEA  # noqa: F401
+    from EasyFEA import Models, Simulations
+    from EasyFEA.FEM._group_elem import GroupElemFactory
+    from EasyFEA.FEM._mesh import Mesh
+    from EasyFEA.FEM._utils import ElemType
+    from EasyFEA.Simulations.Solvers import SolverType
+    return types.SimpleNamespace(Models=Models, Simulations=Simulations, GEF=GroupElemFactory,
+                                 Mesh=Mesh, ElemType=ElemType, SolverType=SolverType)
+
+
+def to_ref_mesh(R, m: gmesh.Mesh):
+    groups = {}
+    for g in m.dict_groupElem.values():
+        et = getattr(R.ElemType, g.elemType.value)
+        groups[et] = R.GEF.Create(et, np.array(g.connect, dtype=np.int64), m.coord.copy())
+    return R.Mesh(groups)
+
+
+def mesh_arrays(m: gmesh.Mesh):
+    g = m.groupElem
+    b = m.Get_list_groupElem(m.dim - 1)[0]
+    return dict(elem=g.elemType.value, coord=m.coord, connect=g.connect,
+                belem=b.elemType.value, bconnect=b.connect)
+
+
+def csr_parts(prefix, A):
+    A = A.tocsr()
+    A.sort_indices()
+    return {f"{prefix}_data": A.data, f"{prefix}_indices": A.indices.astype(np.int32),
+            f"{prefix}_indptr": A.indptr.astype(np.int64)}
+
+
+def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out):
+    dim = m.dim
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=thickness)
+    simu = R.Simulations.Elastic(rm, mat)
+    simu.solver = R.SolverType.scipy
+    L = m.coord[:, 0].max()
+    left = rm.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = rm.Nodes_Conditions(lambda x, y, z: x == L)
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    simu.add_dirichlet(left, [0.0] * dim, unk)
+    simu.add_surfLoad(right, [loadval], [loaddir])
+    u = simu.Solve()
+    K, C, M, F = simu.Get_K_C_M_F()
+    b = np.asarray(simu._Solver_Apply_Neumann(simu.problemType).todense()).ravel()
+    d = dict(mesh_arrays(m), E=np.asarray(E, float), v=v, planeStress=planeStress,
+             thickness=thickness, loadval=loadval, loaddir=loaddir, u=u, b=b,
+             left=left, right=right)
+    d.update(csr_parts("K", K))
+    d.update(csr_parts("M", M))
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **d)
+    print(name, "Ndof", u.size, "nnz", K.nnz, "|u|max", np.abs(u).max())
+
+
+def split_case(R, out, seed=0):
+    """cP, cM, psi+, psi- of the reference's PhaseField.Calc_C on seeded strains
+    plus the degenerate cases of Models/_phasefield.py:793-805 and :861-906."""
+    from EasyFEA.FEM._linalg import FeArray
+    rng = np.random.default_rng(seed)
+    res = {}
+    for dim in (2, 3):
+        n = 3 if dim == 2 else 6
+        eps = rng.standard_normal((48, n)) * 1e-3
+        special = [np.zeros(n)]
+        e = np.zeros(n); e[0] = 1e-3; special.append(e)           # uniaxial
+        e = np.zeros(n); e[:dim] = 1e-3; special.append(e)        # hydrostatic
+        e = np.zeros(n); e[:dim] = -2e-3; special.append(e)
+        e = np.zeros(n); e[0] = 1e-3; e[1] = 1e-3; special.append(e)  # two equal
+        e = np.zeros(n); e[0] = -1e-3; e[1] = 2e-3; special.append(e)
+        if dim == 3:
+            e = np.zeros(n); e[0] = 1e-3; e[1] = 2e-3; e[2] = 2e-3; special.append(e)
+            e = np.zeros(n); e[0] = 1e-3; e[1] = 1e-3; e[2] = 3e-3; special.append(e)
+            e = np.zeros(n); e[5] = 1e-3; special.append(e)        # pure shear
+        eps = np.concatenate([eps, np.array(special)], 0)[:, None, :]  # (Ne, 1, n)
+        for planeStress in ((True, False) if dim == 2 else (False,)):
+            mat = R.Models.Elastic.Isotropic(dim, E=210000.0, v=0.3, planeStress=planeStress)
+            for split in ("Bourdin", "Amor", "Miehe"):
+                pfm = R.Models.PhaseField(mat, split, "AT2", 2.7, 0.01)
+                cP, cM = pfm.Calc_C(FeArray.asfearray(eps.copy()))
+                psiP, psiM = pfm.Calc_psi_e_pg(FeArray.asfearray(eps.copy()))
+                key = f"d{dim}_ps{int(planeStress)}_{split}"
+                res[key + "_cP"] = np.asarray(cP)
+                res[key + "_cM"] = np.asarray(cM)
+                res[key + "_psiP"] = np.asarray(psiP)
+                res[key + "_psiM"] = np.asarray(psiM)
+        res[f"d{dim}_eps"] = eps
+    np.savez_compressed(os.path.join(out, "split.npz"), **res)
+    print("split", len(res))
+
+
+def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, tol=1e-3, maxIter=100):
+    dim = m.dim
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, split, regu, Gc, l0)
+    simu = R.Simulations.PhaseField(rm, pfm)
+    simu.solver = R.SolverType.scipy
+    H = m.coord[:, 1].max()
+    bottom = rm.Nodes_Conditions(lambda x, y, z: y == 0)
+    top = rm.Nodes_Conditions(lambda x, y, z: y == H)
+    notch = rm.Nodes_Conditions(lambda x, y, z: (np.abs(y - H / 2) < 1e-12) & (x <= 0.5 * m.coord[:, 0].max()))
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    top_dofs = simu.Bc_dofs_nodes(top, ["y"])
+    us, ds, Hs, Fs, its = [], [], [], [], []
+    for k in range(1, steps + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(notch, [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(bottom, [0.0] * dim, unk)
+        simu.add_dirichlet(top, [0.0, k * dU] + ([0.0] if dim == 3 else []), unk)
+        u, d, conv = simu.Solve(tol, maxIter, convOption=0)
+        simu.Save_Iter()
+        f = np.sum(simu.Calc_Reaction(top_dofs, simu.ProblemTypes.elastic))
+        us.append(u.copy()); ds.append(d.copy()); Fs.append(f)
+        Hs.append(np.asarray(simu._PhaseField__psiP_e_pg).copy())
+        its.append(simu._PhaseField__Niter)
+        print(name, "step", k, "F", f, "dmax", d.max(), "Niter", its[-1])
+    Ku = simu.Get_K_C_M_F("elastic")[0]
+    Kd, _, _, Fd = simu.Get_K_C_M_F("damage")
+    res = dict(mesh_arrays(m), split=split, regu=regu, planeStress=planeStress, E=E, v=v,
+               Gc=Gc, l0=l0, dU=dU, tol=tol, maxIter=maxIter,
+               u=np.array(us), d=np.array(ds), H=np.array(Hs), F=np.array(Fs), Niter=np.array(its),
+               bottom=bottom, top=top, notch=notch, top_dofs=top_dofs,
+               Fd=np.asarray(Fd.todense()).ravel())
+    res.update(csr_parts("Ku", Ku))
+    res.update(csr_parts("Kd", Kd))
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+
+
+def pf_state_case(R, name, m, split, regu, out, seed=7):
+    """Kd, Fd, Ku of the reference at a prescribed (u, d, committed history) state:
+    pins r/f/k of both regularisations and the degraded stiffness without the
+    staggered loop (PhaseField.Get_K_C_M_F, Simulations/_phasefield.py:248-269)."""
+    dim = m.dim
+    rng = np.random.default_rng(seed)
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=210000.0, v=0.3, planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, split, regu, 2.7, 0.05)
+    simu = R.Simulations.PhaseField(rm, pfm)
+    x = m.coord
+    # smooth displacement with tension and shear, damage in (0, 1)
+    u = np.zeros((m.Nn, dim))
+    u[:, 0] = 1e-3 * np.sin(2.0 * x[:, 1]) + 2e-4 * x[:, 0]
+    u[:, 1] = 3e-3 * x[:, 1] ** 2 - 1e-3 * x[:, 0]
+    if dim == 3:
+        u[:, 2] = 5e-4 * x[:, 0] * x[:, 2]
+    u = u.ravel()
+    d = np.clip(0.5 + 0.4 * np.sin(3 * x[:, 0]) * np.cos(2 * x[:, 1]), 0, 1)
+    simu._Set_solutions(simu.ProblemTypes.elastic, u)
+    simu._Set_solutions(simu.ProblemTypes.damage, d)
+    simu.Need_Update()
+    Kd, _, _, Fd = simu.Get_K_C_M_F("damage")
+    H1 = np.asarray(simu._PhaseField__psiP_e_pg).copy()
+    Ku = simu.Get_K_C_M_F("elastic")[0]
+    res = dict(mesh_arrays(m), split=split, regu=regu, E=210000.0, v=0.3, Gc=2.7, l0=0.05,
+               u=u, d=d, H=H1, Fd=np.asarray(Fd.todense()).ravel())
+    res.update(csr_parts("Ku", Ku))
+    res.update(csr_parts("Kd", Kd))
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+    print(name, "Kd nnz", Kd.nnz, "Ku nnz", Ku.nnz)
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    R = load_reference(ref)
+    out = HERE
+    import scipy
+    np.savez(os.path.join(out, "versions.npz"), numpy=np.__version__, scipy=scipy.__version__)
+
+    elastic_case(R, "el_quad4", gmesh.Mesh_Quad4_Rect(120.0, 13.0, 24, 4), 210000.0, 0.3, True, 13.0,
+                 -800 / 13**2, "y", out)
+    elastic_case(R, "el_tri3", gmesh.Mesh_Tri3_Rect(120.0, 13.0, 12, 4), 210000.0, 0.25, False, 1.0,
+                 -10.0, "y", out)
+    elastic_case(R, "el_quad9", gmesh.Mesh_Quad9_Rect(120.0, 13.0, 6, 2), 210000.0, 0.3, True, 13.0,
+                 -800 / 13**2, "y", out)
+    elastic_case(R, "el_hexa8", gmesh.Mesh_Hexa8_Box(60.0, 10.0, 10.0, 6, 2, 2), 210000.0, 0.3, False, 1.0,
+                 -1.0, "z", out)
+    rng = np.random.default_rng(3)
+    mq = gmesh.Mesh_Quad4_Rect(120.0, 13.0, 12, 3)
+    Eh = 210000.0 * np.exp(0.3 * rng.standard_normal(mq.Ne))
+    elastic_case(R, "el_quad4_hetero", mq, Eh, 0.3, True, 13.0, -800 / 13**2, "y", out)
+    # full-size 2D cantilever: QUAD4 240x26, L=120, h=13, t=13
+    elastic_case(R, "el_cantilever_240x26", gmesh.Mesh_Quad4_Rect(120.0, 13.0, 240, 26), 210000.0, 0.3,
+                 True, 13.0, -800 / 13**2, "y", out)
+
+    split_case(R, out)
+
+    pf_case(R, "pf_tri3_miehe_at2", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16), "Miehe", "AT2", False,
+            210000.0, 0.3, 2.7, 0.1, 4, 4e-3, out)
+    pf_case(R, "pf_quad4_amor_at2", gmesh.Mesh_Quad4_Rect(1.0, 1.0, 12, 12), "Amor", "AT2", True,
+            210000.0, 0.3, 2.7, 0.1, 3, 6e-3, out)
+    for split, regu, m in (("Amor", "AT1", gmesh.Mesh_Quad4_Rect(1.0, 1.0, 10, 10)),
+                           ("Miehe", "AT1", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 10, 10)),
+                           ("Miehe", "AT2", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.5, 4, 4, 2))):
+        pf_state_case(R, f"pfsys_{m.elemType.value.lower()}_{split.lower()}_{regu.lower()}", m, split, regu, out)
+    pf_case(R, "pf_hexa8_miehe_at2", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.25, 6, 6, 1), "Miehe", "AT2", False,
+            210000.0, 0.3, 2.7, 0.2, 2, 4e-3, out)
+
+
+if __name__ == "__main__":
+    main()

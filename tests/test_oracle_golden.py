@@ -1,0 +1,147 @@
+"""The CPU oracle against fixtures produced by the reference itself (CPU only)."""
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import fem
+from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve
+
+ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_cantilever_240x26"]
+
+
+def row_scaled_err(A, B):
+    """max_ij |A_ij - B_ij| / max_j |B_ij| over rows (the K parity metric)."""
+    D = (A - B).tocsr()
+    D.eliminate_zeros()
+    Babs = abs(B).tocsr()
+    rmax = Babs.max(axis=1).toarray().ravel()
+    if D.nnz == 0:
+        return 0.0
+    dmax = abs(D).max(axis=1).toarray().ravel()
+    rmax[rmax == 0] = 1
+    return float(np.max(dmax / rmax))
+
+
+def om(g):
+    return OracleMesh(str(g["elem"]), g["coord"], g["connect"], [(str(g["belem"]), g["bconnect"])])
+
+
+def csr(g, p, n):
+    return sp.csr_matrix((g[p + "_data"], g[p + "_indices"], g[p + "_indptr"]), shape=(n, n))
+
+
+@pytest.mark.parametrize("case", ELASTIC)
+def test_elastic_oracle_matches_reference(golden, case):
+    g = golden(case)
+    m = om(g)
+    dim = m.dim
+    unk = fem.UNKNOWNS[dim]
+    dirc = [(g["left"], [0.0] * dim, unk)]
+    loads = [(g["right"], [float(g["loadval"])], [str(g["loaddir"])])]
+    E = g["E"] if g["E"].ndim else float(g["E"])
+    u, K, b = elastic_solve(m, E, float(g["v"]), bool(g["planeStress"]), float(g["thickness"]), dirc, loads)
+    Kref = csr(g, "K", u.size)
+    # pattern bit-exact, values 1e-12 row-scaled
+    assert np.array_equal(K.indptr, g["K_indptr"])
+    assert np.array_equal(K.indices, g["K_indices"])
+    assert row_scaled_err(K, Kref) <= 1e-12
+    np.testing.assert_allclose(b, g["b"], rtol=1e-12, atol=1e-12 * np.abs(g["b"]).max())
+    assert np.max(np.abs(u - g["u"])) <= 1e-9 * np.max(np.abs(g["u"]))
+
+
+def test_mass_matrix_matches_reference(golden):
+    from oracle.simulate import elastic_system
+    g = golden("el_quad4")
+    m = om(g)
+    K, M = elastic_system(m, float(g["E"]), float(g["v"]), True, float(g["thickness"]))
+    assert row_scaled_err(M, csr(g, "M", K.shape[0])) <= 1e-12
+
+
+@pytest.mark.parametrize("dim,ps", [(2, 1), (2, 0), (3, 0)])
+@pytest.mark.parametrize("split", ["Bourdin", "Amor", "Miehe"])
+def test_split_oracle_matches_reference(golden, dim, ps, split):
+    g = golden("split")
+    eps = g[f"d{dim}_eps"]
+    key = f"d{dim}_ps{ps}_{split}"
+    lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
+    C = fem.isotropic_C(210000.0, 0.3, dim, bool(ps))
+    cP, cM = fem.split_C(eps, split, lmbda, mu, dim, C)
+    psiP, psiM = fem.psi_split(eps, cP, cM)
+    refP = np.broadcast_to(g[key + "_cP"].reshape((-1,) + cP.shape[1:]) if g[key + "_cP"].size != cP.size
+                           else g[key + "_cP"].reshape(cP.shape), cP.shape)
+    refM = np.broadcast_to(g[key + "_cM"].reshape((-1,) + cM.shape[1:]) if g[key + "_cM"].size != cM.size
+                           else g[key + "_cM"].reshape(cM.shape), cM.shape)
+    nan_rows = np.isnan(refP.reshape(len(eps), -1)).any(1)
+    ok = ~nan_rows
+    # the oracle reproduces the reference's NaN at rounding-broken repeated eigenvalues
+    assert np.array_equal(np.isnan(cP.reshape(len(eps), -1)).any(1), nan_rows)
+    scale = np.abs(C).max()
+    assert np.max(np.abs(cP[ok] - refP[ok])) <= 1e-12 * scale
+    assert np.max(np.abs(cM[ok] - refM[ok])) <= 1e-12 * scale
+    gP = g[key + "_psiP"].reshape(psiP.shape)
+    gM = g[key + "_psiM"].reshape(psiM.shape)
+    ps_scale = np.abs(gP[ok]).max() + np.abs(gM[ok]).max()
+    assert np.max(np.abs(psiP[ok] - gP[ok])) <= 1e-12 * ps_scale
+    assert np.max(np.abs(psiM[ok] - gM[ok])) <= 1e-12 * ps_scale
+
+
+def test_split_clamped_fixes_reference_nan(golden):
+    """With the arccos argument clipped, the degenerate 3D cases satisfy the
+    split identities (cP + cM = C, psi+ + psi- = psi) instead of giving NaN."""
+    g = golden("split")
+    eps = g["d3_eps"]
+    lmbda, mu = fem.lame(210000.0, 0.3, 3, False)
+    C = fem.isotropic_C(210000.0, 0.3, 3, False)
+    cP, cM = fem.split_C(eps, "Miehe", lmbda, mu, 3, C, clamp=True)
+    assert not np.isnan(cP).any()
+    np.testing.assert_allclose(cP + cM, np.broadcast_to(C, cP.shape), atol=1e-9 * np.abs(C).max())
+    psiP, psiM = fem.psi_split(eps, cP, cM)
+    psi = 0.5 * np.einsum("epi,ij,epj->ep", eps, C, eps)
+    np.testing.assert_allclose(psiP + psiM, psi, rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2"])
+def test_phasefield_oracle_matches_reference(golden, case):
+    g = golden(case)
+    m = om(g)
+    dim = m.dim
+    pf = PhaseFieldOracle(m, float(g["E"]), float(g["v"]), bool(g["planeStress"]), 1.0,
+                          str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    unk = fem.UNKNOWNS[dim]
+    steps = g["u"].shape[0]
+    for k in range(1, steps + 1):
+        pf.dir_d = [(g["notch"], [1.0], ["d"])]
+        pf.dir_u = [(g["bottom"], [0.0] * dim, unk),
+                    (g["top"], [0.0, k * float(g["dU"])] + ([0.0] if dim == 3 else []), unk)]
+        u, d, conv = pf.solve(float(g["tol"]), int(g["maxIter"]), 0)
+        pf.save_iter()
+        F = np.sum(pf.reaction(g["top_dofs"]))
+        assert pf.Niter == g["Niter"][k - 1]
+        assert np.max(np.abs(d - g["d"][k - 1])) <= 1e-8
+        assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-8 * np.abs(g["u"][k - 1]).max()
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]) + 1e-9
+        np.testing.assert_allclose(pf.psiP, g["H"][k - 1], rtol=1e-7, atol=1e-12 * np.abs(g["H"][k - 1]).max())
+    # end-of-loop matrices inherit the solution-level differences (state-level
+    # fixtures below pin the operators themselves at 1e-12)
+    assert row_scaled_err(pf.Ku, csr(g, "Ku", m.Nn * dim)) <= 1e-7
+    # the reference re-assembles Kd lazily (after Save_Iter) on Get_K_C_M_F("damage")
+    Kd, Fd = pf.damage_system()
+    assert row_scaled_err(Kd, csr(g, "Kd", m.Nn)) <= 1e-7
+    np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-7, atol=1e-12 * np.abs(g["Fd"]).max())
+
+
+@pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2"])
+def test_phasefield_state_systems_match_reference(golden, case):
+    g = golden(case)
+    m = om(g)
+    pf = PhaseFieldOracle(m, float(g["E"]), float(g["v"]), False, 1.0,
+                          str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    pf.u = g["u"].copy()
+    pf.d = g["d"].copy()
+    Kd, Fd = pf.damage_system()
+    np.testing.assert_allclose(pf.psiP, g["H"], rtol=1e-10, atol=1e-12 * np.abs(g["H"]).max())
+    assert row_scaled_err(Kd, csr(g, "Kd", m.Nn)) <= 1e-12
+    np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-10, atol=1e-12 * np.abs(g["Fd"]).max())
+    Ku = pf.elastic_system()
+    assert row_scaled_err(Ku, csr(g, "Ku", m.Nn * m.dim)) <= 1e-12

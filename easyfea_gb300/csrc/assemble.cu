@@ -1,0 +1,413 @@
+// Element operators at Gauss points fused with the CSR scatter.
+//
+// One group of G = next_pow2(nPe) lanes per element; lane p owns local node p:
+// it loads that node's coordinates, contributes dN_p (x) X_p to the Jacobian
+// (reduced across the group with shuffles), computes its physical gradient
+// invF.dN_p, and accumulates the block row K_pq (q = 0..nPe-1, gradients of
+// the other nodes arrive by shuffle).  The block row is scattered into the
+// CSR values with one atomic add per entry at slot
+//   dof_n^2 node_ptr[a] + i dof_n nnb(a) + dof_n rank[e,p,q] + j.
+// Element matrices never touch global memory.
+
+#include "common.cuh"
+
+namespace gfea {
+namespace {
+
+constexpr double kInvSqrt2 = 0.70710678118654752440;
+
+template <typename T>
+__device__ __forceinline__ void atomic_add_t(T* p, T v) { atomicAdd(p, v); }
+
+// B_p^T C scaled by wJ: BtC[i][s] = wJ * sum_r B_p[r][i] C[r][s]
+// (Kelvin-Mandel B of EasyFEA/FEM/_group_elem.py:1242-1312)
+template <int D, typename R>
+__device__ __forceinline__ void btc(const R (&g)[D], const R* C, R wJ, R (&out)[D][D == 2 ? 3 : 6]) {
+  const R c = (R)kInvSqrt2;
+  if constexpr (D == 2) {
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      out[0][s] = wJ * (g[0] * C[0 * 3 + s] + c * g[1] * C[2 * 3 + s]);
+      out[1][s] = wJ * (g[1] * C[1 * 3 + s] + c * g[0] * C[2 * 3 + s]);
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+      out[0][s] = wJ * (g[0] * C[0 * 6 + s] + c * (g[2] * C[4 * 6 + s] + g[1] * C[5 * 6 + s]));
+      out[1][s] = wJ * (g[1] * C[1 * 6 + s] + c * (g[2] * C[3 * 6 + s] + g[0] * C[5 * 6 + s]));
+      out[2][s] = wJ * (g[2] * C[2 * 6 + s] + c * (g[1] * C[3 * 6 + s] + g[0] * C[4 * 6 + s]));
+    }
+  }
+}
+
+// acc[i][j] += sum_s BtC[i][s] B_q[s][j]
+template <int D, typename R>
+__device__ __forceinline__ void btcb(const R (&BtC)[D][D == 2 ? 3 : 6], const R (&h)[D], R (&acc)[D][D]) {
+  const R c = (R)kInvSqrt2;
+  if constexpr (D == 2) {
+    const R chx = c * h[0], chy = c * h[1];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      acc[i][0] += BtC[i][0] * h[0] + BtC[i][2] * chy;
+      acc[i][1] += BtC[i][1] * h[1] + BtC[i][2] * chx;
+    }
+  } else {
+    const R chx = c * h[0], chy = c * h[1], chz = c * h[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      acc[i][0] += BtC[i][0] * h[0] + BtC[i][4] * chz + BtC[i][5] * chy;
+      acc[i][1] += BtC[i][1] * h[1] + BtC[i][3] * chz + BtC[i][5] * chx;
+      acc[i][2] += BtC[i][2] * h[2] + BtC[i][3] * chy + BtC[i][4] * chx;
+    }
+  }
+}
+
+// Per-lane geometry at one Gauss point: Jacobian reduced across the group,
+// wJ and the physical gradient of this lane's shape function.
+template <int ELEM, bool MASS, int G, typename R>
+__device__ __forceinline__ R lane_geometry(const RefTables<ELEM, MASS>& ref, int g, int lane, bool node_lane,
+                                           const R (&X)[Elem<ELEM>::dim], R (&grad)[Elem<ELEM>::dim]) {
+  constexpr int D = Elem<ELEM>::dim;
+  double F[D][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const R dn = node_lane ? (R)ref.dN[g][d][lane] : (R)0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) F[d][k] = (double)group_sum<G, R>(dn * X[k]);
+  }
+  double iF[D][D];
+  const double det = det_inv<D>(F, iF);
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    double v = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) v += iF[i][d] * (node_lane ? ref.dN[g][d][lane] : 0.0);
+    grad[i] = (R)v;
+  }
+  return (R)(fabs(det) * ref.w[g]);
+}
+
+template <int ELEM, typename T, typename R, int CMODE>
+__global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__ coord,
+                                                      const int32_t* __restrict__ connect, int64_t Ne,
+                                                      const int32_t* __restrict__ node_ptr,
+                                                      const uint8_t* __restrict__ rank,
+                                                      const double* __restrict__ Cglob, double factor,
+                                                      T* __restrict__ vals) {
+  using E = Elem<ELEM>;
+  constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value, NS = D == 2 ? 3 : 6;
+  constexpr int EPW = 32 / G;  // elements per warp
+  __shared__ RefTables<ELEM, false> ref;
+  __shared__ R Csh[NS * NS];
+  ref.fill();
+  if (CMODE == 0)
+    for (int i = threadIdx.x; i < NS * NS; i += blockDim.x) Csh[i] = (R)Cglob[i];
+  __syncthreads();
+
+  const int lane = threadIdx.x % G;
+  const int sub = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool node_lane = lane < nPe;
+
+  for (int64_t e0 = warp * EPW; e0 < Ne; e0 += nwarp * EPW) {
+    const int64_t e = e0 + sub;
+    const bool valid = e < Ne;
+    const int64_t ec = valid ? e : Ne - 1;
+    const bool act = valid && node_lane;
+    const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
+    R X[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) X[k] = node_lane ? (R)coord[(int64_t)a * 3 + k] : (R)0;
+    R Cl[NS * NS];
+    const R* C = Csh;
+    if (CMODE == 1) {
+#pragma unroll
+      for (int i = 0; i < NS * NS; ++i) Cl[i] = (R)__ldg(Cglob + ec * NS * NS + i);
+      C = Cl;
+    }
+    R acc[nPe][D][D];
+#pragma unroll
+    for (int q = 0; q < nPe; ++q)
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) acc[q][i][j] = 0;
+
+    for (int g = 0; g < RefTables<ELEM, false>::nPg; ++g) {
+      R grad[D];
+      const R wJ = lane_geometry<ELEM, false, G, R>(ref, g, lane, node_lane, X, grad);
+      R BtC[D][NS];
+      btc<D, R>(grad, C, wJ, BtC);
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) {
+        R h[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) h[k] = group_bcast<G, R>(grad[k], q);
+        btcb<D, R>(BtC, h, acc[q]);
+      }
+    }
+    if (act) {
+      const int32_t p0 = node_ptr[a];
+      const int32_t nb = node_ptr[a + 1] - p0;
+      const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        T* row = vals + (int64_t)D * D * p0 + (int64_t)i * D * nb;
+#pragma unroll
+        for (int q = 0; q < nPe; ++q) {
+          const int r = rk[q];
+#pragma unroll
+          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + D * r + j, (T)(factor * (double)acc[q][i][j]));
+        }
+      }
+    }
+  }
+}
+
+template <int ELEM, typename T, typename R>
+__global__ void __launch_bounds__(128) mass_kernel(const double* __restrict__ coord,
+                                                   const int32_t* __restrict__ connect, int64_t Ne,
+                                                   const int32_t* __restrict__ node_ptr,
+                                                   const uint8_t* __restrict__ rank, int dof_n, double rho,
+                                                   double factor, T* __restrict__ vals) {
+  using E = Elem<ELEM>;
+  constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value;
+  constexpr int EPW = 32 / G;
+  __shared__ RefTables<ELEM, true> ref;
+  ref.fill();
+  __syncthreads();
+  const int lane = threadIdx.x % G;
+  const int sub = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool node_lane = lane < nPe;
+  for (int64_t e0 = warp * EPW; e0 < Ne; e0 += nwarp * EPW) {
+    const int64_t e = e0 + sub;
+    const bool valid = e < Ne;
+    const int64_t ec = valid ? e : Ne - 1;
+    const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
+    R X[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) X[k] = node_lane ? (R)coord[(int64_t)a * 3 + k] : (R)0;
+    R acc[nPe];
+#pragma unroll
+    for (int q = 0; q < nPe; ++q) acc[q] = 0;
+    for (int g = 0; g < RefTables<ELEM, true>::nPg; ++g) {
+      R grad[D];
+      const R wJ = lane_geometry<ELEM, true, G, R>(ref, g, lane, node_lane, X, grad);
+      const R np = node_lane ? (R)ref.N[g][lane] : (R)0;
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) acc[q] += wJ * np * (R)ref.N[g][q];
+    }
+    if (valid && node_lane) {
+      const int32_t p0 = node_ptr[a];
+      const int32_t nb = node_ptr[a + 1] - p0;
+      const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
+      for (int i = 0; i < dof_n; ++i) {
+        T* row = vals + (int64_t)dof_n * dof_n * p0 + (int64_t)i * dof_n * nb;
+#pragma unroll
+        for (int q = 0; q < nPe; ++q) atomic_add_t<T>(row + dof_n * rk[q] + i, (T)(factor * rho * (double)acc[q]));
+      }
+    }
+  }
+}
+
+// Boundary (line / face) integration of constant tractions.
+template <int BELEM>
+__global__ void surface_load_kernel(const double* __restrict__ coord, const int32_t* __restrict__ bconnect,
+                                    int64_t Nbe, const uint8_t* __restrict__ mask, int dof_n, int nu,
+                                    int4 uidx, double4 uval, double factor, double* __restrict__ b) {
+  using E = Elem<BELEM>;
+  constexpr int nPe = E::nPe, BD = E::dim;
+  __shared__ RefTables<BELEM, true> ref;
+  ref.fill();
+  __syncthreads();
+  const int ui[4] = {uidx.x, uidx.y, uidx.z, uidx.w};
+  const double uv[4] = {uval.x, uval.y, uval.z, uval.w};
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < Nbe; e += (int64_t)gridDim.x * blockDim.x) {
+    int32_t nd[nPe];
+    bool all = true;
+    for (int p = 0; p < nPe; ++p) {
+      nd[p] = bconnect[e * nPe + p];
+      all = all && mask[nd[p]];
+    }
+    if (!all) continue;
+    double Nw[nPe];
+    for (int p = 0; p < nPe; ++p) Nw[p] = 0;
+    for (int g = 0; g < RefTables<BELEM, true>::nPg; ++g) {
+      double T[BD][3];
+      for (int d = 0; d < BD; ++d)
+        for (int k = 0; k < 3; ++k) {
+          double s = 0;
+          for (int n = 0; n < nPe; ++n) s += ref.dN[g][d][n] * coord[(int64_t)nd[n] * 3 + k];
+          T[d][k] = s;
+        }
+      double J;
+      if (BD == 1) {
+        J = sqrt(T[0][0] * T[0][0] + T[0][1] * T[0][1] + T[0][2] * T[0][2]);
+      } else {
+        const double cx = T[0][1] * T[BD - 1][2] - T[0][2] * T[BD - 1][1];
+        const double cy = T[0][2] * T[BD - 1][0] - T[0][0] * T[BD - 1][2];
+        const double cz = T[0][0] * T[BD - 1][1] - T[0][1] * T[BD - 1][0];
+        J = sqrt(cx * cx + cy * cy + cz * cz);
+      }
+      const double wJ = J * ref.w[g];
+      for (int p = 0; p < nPe; ++p) Nw[p] += wJ * ref.N[g][p];
+    }
+    for (int u = 0; u < nu; ++u)
+      for (int p = 0; p < nPe; ++p) atomicAdd(&b[(int64_t)nd[p] * dof_n + ui[u]], factor * uv[u] * Nw[p]);
+  }
+}
+
+template <int ELEM, typename T, typename R>
+int launch_elastic(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                   const uint8_t* rank, const double* C, int cpe, double factor, T* vals, cudaStream_t s) {
+  constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
+  const int64_t warps = ceil_div(Ne, 32 / G);
+  int blocks = grid_for(warps * 32, 128);
+  if (blocks > kSMs * 64) blocks = kSMs * 64;
+  if (cpe)
+    elastic_kernel<ELEM, T, R, 1><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
+  else
+    elastic_kernel<ELEM, T, R, 0><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <int ELEM, typename T, typename R>
+int launch_mass(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                const uint8_t* rank, int dof_n, double rho, double factor, T* vals, cudaStream_t s) {
+  constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
+  const int64_t warps = ceil_div(Ne, 32 / G);
+  int blocks = grid_for(warps * 32, 128);
+  if (blocks > kSMs * 64) blocks = kSMs * 64;
+  mass_kernel<ELEM, T, R><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, dof_n, rho, factor, vals);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+int elem_nPe(int elem) {
+  switch (elem) {
+    case GFEA_SEG2: return 2;
+    case GFEA_TRI3: return 3;
+    case GFEA_QUAD4: return 4;
+    case GFEA_QUAD9: return 9;
+    case GFEA_HEXA8: return 8;
+    default: return -1;
+  }
+}
+
+int elem_dim(int elem) {
+  switch (elem) {
+    case GFEA_SEG2: return 1;
+    case GFEA_HEXA8: return 3;
+    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: return 2;
+    default: return -1;
+  }
+}
+
+}  // namespace
+}  // namespace gfea
+
+using namespace gfea;
+
+extern "C" int gfea_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                                     const int32_t* node_ptr, const uint8_t* rank, const double* C,
+                                     int c_per_elem, double factor, int value_type, void* values,
+                                     int64_t n_values, int accumulate, void* stream) {
+  if (!coord || !connect || !node_ptr || !rank || !C || !values || n_elems < 0) return GFEA_ERR_ARG;
+  const int d = elem_dim(elem);
+  if (d < 2) return GFEA_ERR_ARG;
+  if (n_elems == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!accumulate && n_values > 0)
+    GFEA_CUDA_TRY(cudaMemsetAsync(values, 0, (value_type == GFEA_F64 ? 8 : 4) * (size_t)n_values, s));
+  if (value_type == GFEA_F64) {
+    auto* v = static_cast<double*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_elastic<GFEA_TRI3, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_QUAD4: return launch_elastic<GFEA_QUAD4, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_QUAD9: return launch_elastic<GFEA_QUAD9, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_HEXA8: return launch_elastic<GFEA_HEXA8, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  } else if (value_type == GFEA_F32) {
+    auto* v = static_cast<float*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_elastic<GFEA_TRI3, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_QUAD4: return launch_elastic<GFEA_QUAD4, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_QUAD9: return launch_elastic<GFEA_QUAD9, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      case GFEA_HEXA8: return launch_elastic<GFEA_HEXA8, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  }
+  return GFEA_ERR_ARG;
+}
+
+extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                                  const int32_t* node_ptr, const uint8_t* rank, int dof_n, double rho,
+                                  double factor, int value_type, void* values, int64_t n_values,
+                                  int accumulate, void* stream) {
+  if (!coord || !connect || !node_ptr || !rank || !values || n_elems < 0 || dof_n < 1 || dof_n > 3) return GFEA_ERR_ARG;
+  if (n_elems == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!accumulate && n_values > 0)
+    GFEA_CUDA_TRY(cudaMemsetAsync(values, 0, (value_type == GFEA_F64 ? 8 : 4) * (size_t)n_values, s));
+  if (value_type == GFEA_F64) {
+    auto* v = static_cast<double*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_mass<GFEA_TRI3, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD4: return launch_mass<GFEA_QUAD4, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  } else if (value_type == GFEA_F32) {
+    auto* v = static_cast<float*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_mass<GFEA_TRI3, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD4: return launch_mass<GFEA_QUAD4, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  }
+  return GFEA_ERR_ARG;
+}
+
+extern "C" int gfea_surface_load(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                                 const uint8_t* node_mask, int dof_n, int n_unknowns,
+                                 const int32_t* unknown_idx_host, const double* values_host, double factor,
+                                 double* b, void* stream) {
+  if (!coord || !bconnect || !node_mask || !b || n_belems < 0 || n_unknowns < 1 || n_unknowns > 4 ||
+      !unknown_idx_host || !values_host)
+    return GFEA_ERR_ARG;
+  if (n_belems == 0) return GFEA_OK;
+  int ui[4] = {0, 0, 0, 0};
+  double uv[4] = {0, 0, 0, 0};
+  for (int u = 0; u < n_unknowns; ++u) {
+    if (unknown_idx_host[u] < 0 || unknown_idx_host[u] >= dof_n) return GFEA_ERR_ARG;
+    ui[u] = unknown_idx_host[u];
+    uv[u] = values_host[u];
+  }
+  const int4 uidx = make_int4(ui[0], ui[1], ui[2], ui[3]);
+  const double4 uval = make_double4(uv[0], uv[1], uv[2], uv[3]);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int blocks = grid_for(n_belems, 128);
+  switch (belem) {
+    case GFEA_SEG2:
+      surface_load_kernel<GFEA_SEG2><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    case GFEA_QUAD4:
+      surface_load_kernel<GFEA_QUAD4><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    case GFEA_TRI3:
+      surface_load_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    default:
+      return GFEA_ERR_ARG;
+  }
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}

@@ -1,0 +1,274 @@
+// Internal helpers shared by the gfea kernels: element reference data,
+// lane-group reductions and status plumbing.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gfea.h"
+
+#define GFEA_CUDA_TRY(expr)                        \
+  do {                                             \
+    cudaError_t _e = (expr);                       \
+    if (_e != cudaSuccess) return GFEA_ERR_CUDA;   \
+  } while (0)
+
+#define GFEA_LAUNCH_CHECK() GFEA_CUDA_TRY(cudaGetLastError())
+
+namespace gfea {
+
+constexpr int kSMs = 152;  // GB300 streaming multiprocessors (two dies x 76)
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// Element reference data.  Gauss tables follow EasyFEA/FEM/_gauss.py:364-480
+// and the shape functions EasyFEA/FEM/Elems/{_seg,_tri,_quad,_hexa}.py; they
+// are evaluated on the device into shared memory by each kernel's prologue.
+// ---------------------------------------------------------------------------
+
+template <int ELEM> struct Elem;
+
+template <> struct Elem<GFEA_SEG2> {
+  static constexpr int nPe = 2, dim = 1, nPg_rigi = 1, nPg_mass = 2;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (!mass) { xi[0] = 0.0; *w = 2.0; return; }
+    const double a = 1.0 / sqrt(3.0);
+    xi[0] = g == 0 ? -a : a;
+    *w = 1.0;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0];
+    return n == 0 ? -(r - 1) / 2 : (r + 1) / 2;
+  }
+  __device__ static double dN(const double*, int, int n) { return n == 0 ? -0.5 : 0.5; }
+};
+
+template <> struct Elem<GFEA_TRI3> {
+  static constexpr int nPe = 3, dim = 2, nPg_rigi = 1, nPg_mass = 3;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (!mass) { xi[0] = 1.0 / 3; xi[1] = 1.0 / 3; *w = 0.5; return; }
+    const double xs[3] = {1.0 / 6, 2.0 / 3, 1.0 / 6};
+    const double ys[3] = {1.0 / 6, 1.0 / 6, 2.0 / 3};
+    xi[0] = xs[g]; xi[1] = ys[g]; *w = 1.0 / 6;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1];
+    return n == 0 ? -r - s + 1 : (n == 1 ? r : s);
+  }
+  __device__ static double dN(const double*, int d, int n) {
+    if (n == 0) return -1.0;
+    return (n == 1) == (d == 0) ? 1.0 : 0.0;
+  }
+};
+
+template <> struct Elem<GFEA_QUAD4> {
+  static constexpr int nPe = 4, dim = 2, nPg_rigi = 4, nPg_mass = 4;
+  __device__ static void gauss(bool, int g, double* xi, double* w) {
+    const double a = 1.0 / sqrt(3.0);
+    const double xs[4] = {-a, a, a, -a};
+    const double ys[4] = {-a, -a, a, a};
+    xi[0] = xs[g]; xi[1] = ys[g]; *w = 1.0;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1];
+    switch (n) {
+      case 0: return (r - 1) * (s - 1) / 4;
+      case 1: return -(r + 1) * (s - 1) / 4;
+      case 2: return (r + 1) * (s + 1) / 4;
+      default: return -(r - 1) * (s + 1) / 4;
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1];
+    if (d == 0) {
+      switch (n) {
+        case 0: return s / 4 - 1.0 / 4;
+        case 1: return 1.0 / 4 - s / 4;
+        case 2: return s / 4 + 1.0 / 4;
+        default: return -s / 4 - 1.0 / 4;
+      }
+    }
+    switch (n) {
+      case 0: return r / 4 - 1.0 / 4;
+      case 1: return -r / 4 - 1.0 / 4;
+      case 2: return r / 4 + 1.0 / 4;
+      default: return 1.0 / 4 - r / 4;
+    }
+  }
+};
+
+template <> struct Elem<GFEA_QUAD9> {
+  static constexpr int nPe = 9, dim = 2, nPg_rigi = 9, nPg_mass = 9;
+  __device__ static void gauss(bool, int g, double* xi, double* w) {
+    const double a = 0.774596669241483;  // literal of EasyFEA/FEM/_gauss.py:125
+    const double xs[9] = {-a, a, a, -a, 0.0, a, 0.0, -a, 0.0};
+    const double ys[9] = {-a, -a, a, a, -a, 0.0, a, 0.0, 0.0};
+    xi[0] = xs[g]; xi[1] = ys[g];
+    *w = g < 4 ? 25.0 / 81 : (g < 8 ? 40.0 / 81 : 64.0 / 81);
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1];
+    switch (n) {
+      case 0: return r * s * (r - 1) * (s - 1) / 4;
+      case 1: return r * s * (r + 1) * (s - 1) / 4;
+      case 2: return r * s * (r + 1) * (s + 1) / 4;
+      case 3: return r * s * (r - 1) * (s + 1) / 4;
+      case 4: return -s * (r - 1) * (r + 1) * (s - 1) / 2;
+      case 5: return -r * (r + 1) * (s - 1) * (s + 1) / 2;
+      case 6: return -s * (r - 1) * (r + 1) * (s + 1) / 2;
+      case 7: return -r * (r - 1) * (s - 1) * (s + 1) / 2;
+      default: return (r - 1) * (r + 1) * (s - 1) * (s + 1);
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1];
+    if (d == 0) {
+      switch (n) {
+        case 0: return r * s * (s - 1) / 4 + s * (r - 1) * (s - 1) / 4;
+        case 1: return r * s * (s - 1) / 4 + s * (r + 1) * (s - 1) / 4;
+        case 2: return r * s * (s + 1) / 4 + s * (r + 1) * (s + 1) / 4;
+        case 3: return r * s * (s + 1) / 4 + s * (r - 1) * (s + 1) / 4;
+        case 4: return -s * (r - 1) * (s - 1) / 2 - s * (r + 1) * (s - 1) / 2;
+        case 5: return -r * (s - 1) * (s + 1) / 2 - (r + 1) * (s - 1) * (s + 1) / 2;
+        case 6: return -s * (r - 1) * (s + 1) / 2 - s * (r + 1) * (s + 1) / 2;
+        case 7: return -r * (s - 1) * (s + 1) / 2 - (r - 1) * (s - 1) * (s + 1) / 2;
+        default: return (r - 1) * (s - 1) * (s + 1) + (r + 1) * (s - 1) * (s + 1);
+      }
+    }
+    switch (n) {
+      case 0: return r * s * (r - 1) / 4 + r * (r - 1) * (s - 1) / 4;
+      case 1: return r * s * (r + 1) / 4 + r * (r + 1) * (s - 1) / 4;
+      case 2: return r * s * (r + 1) / 4 + r * (r + 1) * (s + 1) / 4;
+      case 3: return r * s * (r - 1) / 4 + r * (r - 1) * (s + 1) / 4;
+      case 4: return -s * (r - 1) * (r + 1) / 2 - (r - 1) * (r + 1) * (s - 1) / 2;
+      case 5: return -r * (r + 1) * (s - 1) / 2 - r * (r + 1) * (s + 1) / 2;
+      case 6: return -s * (r - 1) * (r + 1) / 2 - (r - 1) * (r + 1) * (s + 1) / 2;
+      case 7: return -r * (r - 1) * (s - 1) / 2 - r * (r - 1) * (s + 1) / 2;
+      default: return (r - 1) * (r + 1) * (s - 1) + (r - 1) * (r + 1) * (s + 1);
+    }
+  }
+};
+
+template <> struct Elem<GFEA_HEXA8> {
+  static constexpr int nPe = 8, dim = 3, nPg_rigi = 8, nPg_mass = 8;
+  __device__ static void gauss(bool, int g, double* xi, double* w) {
+    const double a = 1.0 / sqrt(3.0);
+    // x = [-a]*4 + [a]*4, y = [-a,-a,a,a]*2, z = [-a,a]*4 (EasyFEA/FEM/_gauss.py:207-212)
+    xi[0] = g < 4 ? -a : a;
+    xi[1] = (g & 2) ? a : -a;
+    xi[2] = (g & 1) ? a : -a;
+    *w = 1.0;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1], t = p[2];
+    switch (n) {
+      case 0: return -(r - 1) * (s - 1) * (t - 1) / 8;
+      case 1: return (r + 1) * (s - 1) * (t - 1) / 8;
+      case 2: return -(r + 1) * (s + 1) * (t - 1) / 8;
+      case 3: return (r - 1) * (s + 1) * (t - 1) / 8;
+      case 4: return (r - 1) * (s - 1) * (t + 1) / 8;
+      case 5: return -(r + 1) * (s - 1) * (t + 1) / 8;
+      case 6: return (r + 1) * (s + 1) * (t + 1) / 8;
+      default: return -(r - 1) * (s + 1) * (t + 1) / 8;
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1], t = p[2];
+    // node signs (sr, ss, st) of the reference element corners
+    const double sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+    const double ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+    const double st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    const double a = sr[n], b = ss[n], c = st[n];
+    // N_n = (1 + a r)(1 + b s)(1 + c t) / 8
+    if (d == 0) return a * (1 + b * s) * (1 + c * t) / 8;
+    if (d == 1) return b * (1 + a * r) * (1 + c * t) / 8;
+    return c * (1 + a * r) * (1 + b * s) / 8;
+  }
+};
+
+// Shared-memory reference tables of one element type and Gauss family.
+template <int ELEM, bool MASS>
+struct RefTables {
+  using E = Elem<ELEM>;
+  static constexpr int nPg = MASS ? E::nPg_mass : E::nPg_rigi;
+  double w[nPg];
+  double N[nPg][E::nPe];
+  double dN[nPg][E::dim][E::nPe];
+
+  __device__ void fill() {
+    for (int i = threadIdx.x; i < nPg * E::nPe; i += blockDim.x) {
+      const int g = i / E::nPe, n = i % E::nPe;
+      double xi[3], wg;
+      E::gauss(MASS, g, xi, &wg);
+      N[g][n] = E::N(xi, n);
+      for (int d = 0; d < E::dim; ++d) dN[g][d][n] = E::dN(xi, d, n);
+      if (n == 0) w[g] = wg;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Lane groups: G consecutive lanes of a warp cooperate on one element/node.
+// ---------------------------------------------------------------------------
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+  return v;
+}
+
+template <int G, typename T>
+__device__ __forceinline__ T group_bcast(T v, int src) {
+  return __shfl_sync(0xffffffffu, v, src, G);
+}
+
+template <int n> struct NextPow2 {
+  static constexpr int value = n <= 1 ? 1 : (n <= 2 ? 2 : (n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : 32))));
+};
+
+// ---------------------------------------------------------------------------
+// Jacobian helpers (closed forms of EasyFEA/FEM/_linalg.py:533-656)
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ double det_inv(const double (&F)[D][D], double (&iF)[D][D]) {
+  if constexpr (D == 1) {
+    iF[0][0] = 1.0 / F[0][0];
+    return F[0][0];
+  } else if constexpr (D == 2) {
+    const double det = F[0][0] * F[1][1] - F[1][0] * F[0][1];
+    const double id = 1.0 / det;
+    iF[0][0] = id * F[1][1];
+    iF[0][1] = id * -F[0][1];
+    iF[1][0] = id * -F[1][0];
+    iF[1][1] = id * F[0][0];
+    return det;
+  } else {
+    const double a11 = F[0][0], a12 = F[0][1], a13 = F[0][2];
+    const double a21 = F[1][0], a22 = F[1][1], a23 = F[1][2];
+    const double a31 = F[2][0], a32 = F[2][1], a33 = F[2][2];
+    const double det = a11 * ((a22 * a33) - (a32 * a23)) - a12 * ((a21 * a33) - (a31 * a23)) +
+                       a13 * ((a21 * a32) - (a31 * a22));
+    const double id = 1.0 / det;
+    iF[0][0] = id * (a22 * a33 - a32 * a23);
+    iF[0][1] = id * -(a12 * a33 - a32 * a13);
+    iF[0][2] = id * (a12 * a23 - a22 * a13);
+    iF[1][0] = id * -(a21 * a33 - a31 * a23);
+    iF[1][1] = id * (a11 * a33 - a31 * a13);
+    iF[1][2] = id * -(a11 * a23 - a21 * a13);
+    iF[2][0] = id * (a21 * a32 - a31 * a22);
+    iF[2][1] = id * -(a11 * a32 - a31 * a12);
+    iF[2][2] = id * (a11 * a22 - a21 * a12);
+    return det;
+  }
+}
+
+// Launch configuration helpers.
+inline int grid_for(int64_t n_items, int per_block) {
+  int64_t g = ceil_div(n_items, per_block);
+  if (g < 1) g = 1;
+  if (g > (int64_t)1 << 30) g = (int64_t)1 << 30;
+  return (int)g;
+}
+
+}  // namespace gfea

@@ -1,0 +1,598 @@
+// Phase-field kernels: strain-energy split, History field, damage system and
+// degraded displacement stiffness, each fused with its CSR scatter.
+//
+// The split restates Models.PhaseField.Calc_C (EasyFEA/Models/_phasefield.py:
+// 396-571) in FP64 registers: Bourdin, Amor (:451-483) and Miehe with the
+// closed-form eigenprojectors of :751-1041 (2D :777-807, 3D Q.-C. He form with
+// the Lode-angle cases :809-948) and the projector assembly of :1043-1243.
+// Two deliberate differences from the reference, both at points where it
+// returns NaN: the 3D arccos argument is clipped to [-1, 1] and the 2D
+// discriminant / 3D invariant g to >= 0 (rounding can push them past the
+// bound at repeated eigenvalues).
+
+#include <math.h>
+
+#include "common.cuh"
+
+namespace gfea {
+namespace {
+
+constexpr double kSqrt2 = 1.41421356237309504880;
+
+struct PF {
+  int split, regu, dim;
+  double lambda, mu, Gc, l0, thickness, k_res;
+  double A[9];
+  double C[36];
+};
+
+__device__ __forceinline__ double heav(double v) { return v > 0 ? 1.0 : (v == 0 ? 0.5 : 0.0); }
+__device__ __forceinline__ double sgn(double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); }
+
+// c = gP * cP + cM  (n x n, row-major); gP = 1 gives cP + cM.
+// With want_parts, cP and cM are also returned separately.
+template <int D>
+__device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
+  constexpr int n = D == 2 ? 3 : 6;
+  const double tr = D == 2 ? eps[0] + eps[1] : eps[0] + eps[1] + eps[2];
+  const double Rp = (1 + sgn(tr)) / 2, Rm = (1 + sgn(-tr)) / 2;
+  auto IxI = [](int i, int j) { return (i < D && j < D) ? 1.0 : 0.0; };
+  if (P.split == GFEA_SPLIT_BOURDIN) {
+    for (int i = 0; i < n * n; ++i) {
+      c[i] = gP * P.C[i];
+      if (cPo) cPo[i] = P.C[i];
+      if (cMo) cMo[i] = 0.0;
+    }
+    return;
+  }
+  if (P.split == GFEA_SPLIT_AMOR) {
+    const double bulk = P.lambda + 2 * P.mu / D;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        const double cp = bulk * (Rp * IxI(i, j)) + 2 * P.mu * ((i == j ? 1.0 : 0.0) - 1.0 / D * IxI(i, j));
+        const double cm = bulk * (Rm * IxI(i, j));
+        c[i * n + j] = gP * cp + cm;
+        if (cPo) cPo[i * n + j] = cp;
+        if (cMo) cMo[i * n + j] = cm;
+      }
+    return;
+  }
+  // Miehe: projP from the eigen decomposition of the strain tensor
+  double projP[n * n];
+  if constexpr (D == 2) {
+    const double M00 = eps[0], M11 = eps[1], M01 = eps[2] / kSqrt2;
+    const double det = M00 * M11 - M01 * M01;
+    const double trM = M00 + M11;
+    double delta = trM * trM - 4 * det;
+    if (delta < 0) delta = 0;
+    const double sd = sqrt(delta);
+    const double v1 = (trM - sd) / 2, v2 = (trM + sd) / 2;
+    double A00 = 1, A11 = 0, A01 = 0;  // M1
+    if (v1 != v2) {
+      const double dv = v1 - v2;
+      A00 = (M00 - v2) / dv;
+      A11 = (M11 - v2) / dv;
+      A01 = M01 / dv;
+    }
+    const double m1[3] = {A00, A11, A01 * kSqrt2};
+    const double m2[3] = {1 - A00, 1 - A11, -A01 * kSqrt2};
+    const double vp1 = (v1 + fabs(v1)) / 2, vp2 = (v2 + fabs(v2)) / 2;
+    double d12 = v1 - v2;
+    if (d12 == 0) d12 = 1;
+    const double beta = (vp1 - vp2) / d12;
+    const double g1 = heav(v1) - beta, g2 = heav(v2) - beta;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        projP[i * 3 + j] = (i == j ? beta : 0.0) + g1 * m1[i] * m1[j] + g2 * m2[i] * m2[j];
+  } else {
+    double M[3][3];
+    M[0][0] = eps[0]; M[1][1] = eps[1]; M[2][2] = eps[2];
+    M[1][2] = M[2][1] = eps[3] / kSqrt2;
+    M[0][2] = M[2][0] = eps[4] / kSqrt2;
+    M[0][1] = M[1][0] = eps[5] / kSqrt2;
+    const double I1 = M[0][0] + M[1][1] + M[2][2];
+    double trMM = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) trMM += M[i][k] * M[k][i];
+    const double I2 = 0.5 * (I1 * I1 - trMM);
+    const double I3 = M[0][0] * ((M[1][1] * M[2][2]) - (M[2][1] * M[1][2])) -
+                      M[0][1] * ((M[1][0] * M[2][2]) - (M[2][0] * M[1][2])) +
+                      M[0][2] * ((M[1][0] * M[2][1]) - (M[2][0] * M[1][1]));
+    double g = I1 * I1 - 3 * I2;
+    if (g < 0) g = 0;
+    const double sg = sqrt(g);
+    double arg = 0.5 * (2 * I1 * I1 * I1 - 9 * I1 * I2 + 27 * I3);
+    if (g != 0) arg = arg / pow(g, 1.5);
+    if (arg > 1) arg = 1;
+    if (arg < -1) arg = -1;
+    double v[3] = {I1 / 3, I1 / 3, I1 / 3};
+    double M1[3][3] = {{1, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double M3[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+    if (g != 0) {
+      const double irg = (I1 - sg) / 3;
+      const double gm = 1.0 / sqrt(g);
+      if (arg == -1) {  // theta = pi/3: e1 < e2 = e3
+        v[0] += -2.0 / 3 * sg; v[1] += 1.0 / 3 * sg; v[2] += 1.0 / 3 * sg;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            M1[i][j] = gm * ((i == j ? irg : 0.0) - M[i][j]);
+          }
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) M3[i][j] = 0.5 * ((i == j ? 1.0 : 0.0) - M1[i][j]);
+      } else if (arg == 1) {  // theta = 0: e1 = e2 < e3
+        v[0] += -1.0 / 3 * sg; v[1] += -1.0 / 3 * sg; v[2] += 2.0 / 3 * sg;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) M3[i][j] = gm * (M[i][j] - (i == j ? irg : 0.0));
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) M1[i][j] = 0.5 * ((i == j ? 1.0 : 0.0) - M3[i][j]);
+      } else {
+        const double theta = acos(arg) / 3;
+        const double twopi3 = 2 * M_PI / 3;
+        v[0] += 2.0 / 3 * (sg * cos(twopi3 + theta));
+        v[1] += 2.0 / 3 * (sg * cos(twopi3 - theta));
+        v[2] += 2.0 / 3 * (sg * cos(theta));
+        double P2[3][3], P3[3][3], Q1[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            P2[i][j] = M[i][j] - (i == j ? v[1] : 0.0);
+            P3[i][j] = M[i][j] - (i == j ? v[2] : 0.0);
+            Q1[i][j] = M[i][j] - (i == j ? v[0] : 0.0);
+          }
+        const double den1 = (v[0] - v[1]) * (v[0] - v[2]);
+        const double den3 = (v[2] - v[0]) * (v[2] - v[1]);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double a = 0, b = 0;
+            for (int k = 0; k < 3; ++k) {
+              a += P2[i][k] * P3[k][j];
+              b += Q1[i][k] * P2[k][j];
+            }
+            M1[i][j] = a / den1;
+            M3[i][j] = b / den3;
+          }
+      }
+    }
+    double n1 = 0, n3 = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        n1 += M1[i][j] * M1[i][j];
+        n3 += M3[i][j] * M3[i][j];
+      }
+    n1 = sqrt(n1);
+    n3 = sqrt(n3);
+    double Ms[3][3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Ms[0][i][j] = M1[i][j] / n1;
+        Ms[2][i][j] = M3[i][j] / n3;
+        Ms[1][i][j] = (i == j ? 1.0 : 0.0) - (Ms[0][i][j] + Ms[2][i][j]);
+      }
+    double vp[3], dv[3], mv[3][6];
+    for (int k = 0; k < 3; ++k) {
+      vp[k] = (v[k] + fabs(v[k])) / 2;
+      dv[k] = heav(v[k]);
+      mv[k][0] = Ms[k][0][0]; mv[k][1] = Ms[k][1][1]; mv[k][2] = Ms[k][2][2];
+      mv[k][3] = Ms[k][1][2] * kSqrt2; mv[k][4] = Ms[k][0][2] * kSqrt2; mv[k][5] = Ms[k][0][1] * kSqrt2;
+    }
+    double d12 = v[0] - v[1], d13 = v[0] - v[2], d23 = v[1] - v[2];
+    if (d12 == 0) d12 = 1;
+    if (d13 == 0) d13 = 1;
+    if (d23 == 0) d23 = 1;
+    const double th[3] = {(vp[0] - vp[1]) / (2 * d12), (vp[0] - vp[2]) / (2 * d13), (vp[1] - vp[2]) / (2 * d23)};
+    const int rI[6] = {0, 1, 2, 1, 0, 0};
+    const int rJ[6] = {0, 1, 2, 2, 2, 1};
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    for (int I = 0; I < 6; ++I)
+      for (int K = 0; K < 6; ++K) {
+        double s = 0;
+        for (int k = 0; k < 3; ++k) s += dv[k] * mv[k][I] * mv[k][K];
+        const double sc = (I < 3) == (K < 3) ? (I < 3 ? 1.0 : 2.0) : kSqrt2;
+        const int iI = rI[I], jI = rJ[I], iK = rI[K], jK = rJ[K];
+        double gs = 0;
+        for (int t = 0; t < 3; ++t) {
+          const double (&A)[3][3] = Ms[pa[t]];
+          const double (&B)[3][3] = Ms[pb[t]];
+          const double G = (A[iI][iK] * B[jI][jK] + A[iI][jK] * B[iK][jI] + B[iI][iK] * A[jI][jK] +
+                            B[iI][jK] * A[iK][jI]) * sc;
+          gs += th[t] * G;
+        }
+        projP[I * 6 + K] = s + gs;
+      }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double pp = projP[i * n + j];
+      const double pm = (i == j ? 1.0 : 0.0) - pp;
+      const double cp = P.lambda * (Rp * IxI(i, j)) + 2 * P.mu * pp;
+      const double cm = P.lambda * (Rm * IxI(i, j)) + 2 * P.mu * pm;
+      c[i * n + j] = gP * cp + cm;
+      if (cPo) cPo[i * n + j] = cp;
+      if (cMo) cMo[i * n + j] = cm;
+    }
+}
+
+template <int D>
+__device__ double psi_plus(const PF& P, const double* eps) {
+  constexpr int n = D == 2 ? 3 : 6;
+  double c[n * n], cP[n * n];
+  split_c<D>(P, eps, 1.0, c, cP, nullptr);
+  double s = 0;
+  for (int i = 0; i < n; ++i) {
+    double sig = 0;
+    for (int j = 0; j < n; ++j) sig += cP[i * n + j] * eps[j];
+    s += 0.5 * eps[i] * sig;
+  }
+  return s;
+}
+
+// strain contribution B_p u_p of one node (KM), dim D
+template <int D>
+__device__ __forceinline__ void node_strain(const double (&g)[D], const double (&u)[D], double* e) {
+  const double c = 1.0 / kSqrt2;
+  if constexpr (D == 2) {
+    e[0] = g[0] * u[0];
+    e[1] = g[1] * u[1];
+    e[2] = c * g[1] * u[0] + c * g[0] * u[1];
+  } else {
+    e[0] = g[0] * u[0];
+    e[1] = g[1] * u[1];
+    e[2] = g[2] * u[2];
+    e[3] = c * g[2] * u[1] + c * g[1] * u[2];
+    e[4] = c * g[2] * u[0] + c * g[0] * u[2];
+    e[5] = c * g[1] * u[0] + c * g[0] * u[1];
+  }
+}
+
+template <int ELEM, bool MASS, int G>
+__device__ __forceinline__ double lane_geo(const RefTables<ELEM, MASS>& ref, int g, int lane, bool node_lane,
+                                           const double (&X)[Elem<ELEM>::dim], double (&grad)[Elem<ELEM>::dim]) {
+  constexpr int D = Elem<ELEM>::dim;
+  double F[D][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double dn = node_lane ? ref.dN[g][d][lane] : 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) F[d][k] = group_sum<G, double>(dn * X[k]);
+  }
+  double iF[D][D];
+  const double det = det_inv<D>(F, iF);
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    double v = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) v += iF[i][d] * (node_lane ? ref.dN[g][d][lane] : 0.0);
+    grad[i] = v;
+  }
+  return fabs(det) * ref.w[g];
+}
+
+template <int ELEM, int G>
+__device__ __forceinline__ void group_strain(const double (&grad)[Elem<ELEM>::dim], const double (&u)[Elem<ELEM>::dim],
+                                             bool node_lane, double* eps) {
+  constexpr int D = Elem<ELEM>::dim, n = D == 2 ? 3 : 6;
+  double e[n];
+  node_strain<D>(grad, u, e);
+#pragma unroll
+  for (int i = 0; i < n; ++i) eps[i] = group_sum<G, double>(node_lane ? e[i] : 0.0);
+}
+
+template <int ELEM>
+__global__ void __launch_bounds__(128) damage_kernel(const double* __restrict__ coord, const int32_t* __restrict__ connect,
+                                                     int64_t Ne, const int32_t* __restrict__ node_ptr,
+                                                     const uint8_t* __restrict__ rank, const double* __restrict__ u,
+                                                     PF P, const double* __restrict__ H_old, double* __restrict__ H_new,
+                                                     double* __restrict__ Kd, double* __restrict__ Fd) {
+  using E = Elem<ELEM>;
+  constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value, EPW = 32 / G;
+  constexpr int nPgM = E::nPg_mass;
+  __shared__ RefTables<ELEM, true> refm;
+  __shared__ RefTables<ELEM, false> refr;
+  refm.fill();
+  refr.fill();
+  __syncthreads();
+  const int lane = threadIdx.x % G;
+  const int sub = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool node_lane = lane < nPe;
+  const double k = P.regu == GFEA_AT1 ? 3.0 / 4 * P.Gc * P.l0 : P.Gc * P.l0;
+  for (int64_t e0 = warp * EPW; e0 < Ne; e0 += nwarp * EPW) {
+    const int64_t e = e0 + sub;
+    const bool valid = e < Ne;
+    const int64_t ec = valid ? e : Ne - 1;
+    const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
+    double X[D], ul[D];
+#pragma unroll
+    for (int kk = 0; kk < D; ++kk) {
+      X[kk] = node_lane ? coord[(int64_t)a * 3 + kk] : 0.0;
+      ul[kk] = node_lane ? u[(int64_t)a * D + kk] : 0.0;
+    }
+    double acc[nPe], fp = 0;
+#pragma unroll
+    for (int q = 0; q < nPe; ++q) acc[q] = 0;
+    for (int g = 0; g < nPgM; ++g) {
+      double grad[D];
+      const double wJ = lane_geo<ELEM, true, G>(refm, g, lane, node_lane, X, grad);
+      double eps[D == 2 ? 3 : 6];
+      group_strain<ELEM, G>(grad, ul, node_lane, eps);
+      double psi = psi_plus<D>(P, eps);
+      if (H_old) {
+        const double ho = H_old[ec * nPgM + g];
+        if (psi - ho < 0) psi = ho;
+      }
+      if (valid && lane == 0) H_new[ec * nPgM + g] = psi;
+      double r, f;
+      if (P.regu == GFEA_AT1) {
+        r = 2 * psi;
+        f = 2 * psi - (3 * P.Gc) / (8 * P.l0);
+        f = (f + fabs(f)) / 2;
+      } else {
+        r = 2 * psi + P.Gc / P.l0;
+        f = 2 * psi;
+      }
+      const double np = node_lane ? refm.N[g][lane] : 0.0;
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) acc[q] += r * wJ * np * refm.N[g][q];
+      fp += f * wJ * np;
+    }
+    for (int g = 0; g < RefTables<ELEM, false>::nPg; ++g) {
+      double grad[D];
+      const double wJ = lane_geo<ELEM, false, G>(refr, g, lane, node_lane, X, grad);
+      double Ag[D];
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        Ag[i] = 0;
+#pragma unroll
+        for (int j = 0; j < D; ++j) Ag[i] += P.A[i * D + j] * grad[j];
+      }
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) {
+        double s = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) s += group_bcast<G, double>(grad[i], q) * Ag[i];
+        acc[q] += k * wJ * s;
+      }
+    }
+    if (valid && node_lane) {
+      const int32_t p0 = node_ptr[a];
+      const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) atomicAdd(Kd + p0 + rk[q], P.thickness * acc[q]);
+      atomicAdd(Fd + a, P.thickness * fp);
+    }
+  }
+}
+
+template <int ELEM, typename T>
+__global__ void __launch_bounds__(128) pf_elastic_kernel(const double* __restrict__ coord,
+                                                         const int32_t* __restrict__ connect, int64_t Ne,
+                                                         const int32_t* __restrict__ node_ptr,
+                                                         const uint8_t* __restrict__ rank, const double* __restrict__ u,
+                                                         const double* __restrict__ dmg, PF P, T* __restrict__ vals) {
+  using E = Elem<ELEM>;
+  constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value, EPW = 32 / G, NS = D == 2 ? 3 : 6;
+  __shared__ RefTables<ELEM, false> ref;
+  ref.fill();
+  __syncthreads();
+  const int lane = threadIdx.x % G;
+  const int sub = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool node_lane = lane < nPe;
+  const double cK = 1.0 / kSqrt2;
+  for (int64_t e0 = warp * EPW; e0 < Ne; e0 += nwarp * EPW) {
+    const int64_t e = e0 + sub;
+    const bool valid = e < Ne;
+    const int64_t ec = valid ? e : Ne - 1;
+    const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
+    double X[D], ul[D];
+#pragma unroll
+    for (int kk = 0; kk < D; ++kk) {
+      X[kk] = node_lane ? coord[(int64_t)a * 3 + kk] : 0.0;
+      ul[kk] = node_lane ? u[(int64_t)a * D + kk] : 0.0;
+    }
+    const double dl = node_lane ? dmg[a] : 0.0;
+    double acc[nPe][D][D];
+#pragma unroll
+    for (int q = 0; q < nPe; ++q)
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) acc[q][i][j] = 0;
+    for (int g = 0; g < RefTables<ELEM, false>::nPg; ++g) {
+      double grad[D];
+      const double wJ = lane_geo<ELEM, false, G>(ref, g, lane, node_lane, X, grad);
+      double eps[NS];
+      group_strain<ELEM, G>(grad, ul, node_lane, eps);
+      const double dpg = group_sum<G, double>(node_lane ? ref.N[g][lane] * dl : 0.0);
+      const double gd = (1 - dpg) * (1 - dpg) + P.k_res;
+      double c[NS * NS];
+      split_c<D>(P, eps, gd, c, nullptr, nullptr);
+      // BtC and accumulation as in the elastic kernel (KM B of _group_elem.py:1242-1312)
+      double BtC[D][NS];
+      if constexpr (D == 2) {
+        for (int s = 0; s < 3; ++s) {
+          BtC[0][s] = wJ * (grad[0] * c[0 * 3 + s] + cK * grad[1] * c[2 * 3 + s]);
+          BtC[1][s] = wJ * (grad[1] * c[1 * 3 + s] + cK * grad[0] * c[2 * 3 + s]);
+        }
+      } else {
+        for (int s = 0; s < 6; ++s) {
+          BtC[0][s] = wJ * (grad[0] * c[0 * 6 + s] + cK * (grad[2] * c[4 * 6 + s] + grad[1] * c[5 * 6 + s]));
+          BtC[1][s] = wJ * (grad[1] * c[1 * 6 + s] + cK * (grad[2] * c[3 * 6 + s] + grad[0] * c[5 * 6 + s]));
+          BtC[2][s] = wJ * (grad[2] * c[2 * 6 + s] + cK * (grad[1] * c[3 * 6 + s] + grad[0] * c[4 * 6 + s]));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < nPe; ++q) {
+        double h[D];
+#pragma unroll
+        for (int kk = 0; kk < D; ++kk) h[kk] = group_bcast<G, double>(grad[kk], q);
+        if constexpr (D == 2) {
+          const double chx = cK * h[0], chy = cK * h[1];
+          for (int i = 0; i < 2; ++i) {
+            acc[q][i][0] += BtC[i][0] * h[0] + BtC[i][2] * chy;
+            acc[q][i][1] += BtC[i][1] * h[1] + BtC[i][2] * chx;
+          }
+        } else {
+          const double chx = cK * h[0], chy = cK * h[1], chz = cK * h[2];
+          for (int i = 0; i < 3; ++i) {
+            acc[q][i][0] += BtC[i][0] * h[0] + BtC[i][4] * chz + BtC[i][5] * chy;
+            acc[q][i][1] += BtC[i][1] * h[1] + BtC[i][3] * chz + BtC[i][5] * chx;
+            acc[q][i][2] += BtC[i][2] * h[2] + BtC[i][3] * chy + BtC[i][4] * chx;
+          }
+        }
+      }
+    }
+    if (valid && node_lane) {
+      const int32_t p0 = node_ptr[a];
+      const int32_t nb = node_ptr[a + 1] - p0;
+      const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        T* row = vals + (int64_t)D * D * p0 + (int64_t)i * D * nb;
+#pragma unroll
+        for (int q = 0; q < nPe; ++q) {
+          const int r = rk[q];
+#pragma unroll
+          for (int j = 0; j < D; ++j) atomicAdd(row + D * r + j, (T)(P.thickness * acc[q][i][j]));
+        }
+      }
+    }
+  }
+}
+
+template <int D>
+__global__ void split_kernel(const double* __restrict__ eps, int64_t n, PF P, double* cP, double* cM, double* psiP,
+                             double* psiM) {
+  constexpr int ns = D == 2 ? 3 : 6;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double e[ns], c[ns * ns], p[ns * ns], m[ns * ns];
+    for (int k = 0; k < ns; ++k) e[k] = eps[i * ns + k];
+    split_c<D>(P, e, 1.0, c, p, m);
+    double sp = 0, sm = 0;
+    for (int a = 0; a < ns; ++a) {
+      double tp = 0, tm = 0;
+      for (int b = 0; b < ns; ++b) {
+        tp += p[a * ns + b] * e[b];
+        tm += m[a * ns + b] * e[b];
+      }
+      sp += 0.5 * e[a] * tp;
+      sm += 0.5 * e[a] * tm;
+    }
+    if (cP) for (int k = 0; k < ns * ns; ++k) cP[i * ns * ns + k] = p[k];
+    if (cM) for (int k = 0; k < ns * ns; ++k) cM[i * ns * ns + k] = m[k];
+    if (psiP) psiP[i] = sp;
+    if (psiM) psiM[i] = sm;
+  }
+}
+
+int to_pf(const gfea_pf_params* p, PF* o) {
+  if (!p || p->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
+  if (p->dim != 2 && p->dim != 3) return GFEA_ERR_ARG;
+  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_MIEHE) return GFEA_ERR_ARG;
+  if (p->regularization != GFEA_AT1 && p->regularization != GFEA_AT2) return GFEA_ERR_ARG;
+  o->split = p->split;
+  o->regu = p->regularization;
+  o->dim = p->dim;
+  o->lambda = p->lambda_;
+  o->mu = p->mu;
+  o->Gc = p->Gc;
+  o->l0 = p->l0;
+  o->thickness = p->thickness;
+  o->k_res = p->k_res;
+  for (int i = 0; i < 9; ++i) o->A[i] = p->A[i];
+  for (int i = 0; i < 36; ++i) o->C[i] = p->C[i];
+  return GFEA_OK;
+}
+
+template <int ELEM>
+int launch_damage(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                  const uint8_t* rank, const double* u, const PF& P, const double* H_old, double* H_new, double* Kd,
+                  double* Fd, cudaStream_t s) {
+  constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
+  int blocks = grid_for(ceil_div(Ne, 32 / G) * 32, 128);
+  if (blocks > kSMs * 64) blocks = kSMs * 64;
+  damage_kernel<ELEM><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, P, H_old, H_new, Kd, Fd);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <int ELEM, typename T>
+int launch_pfel(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr, const uint8_t* rank,
+                const double* u, const double* d, const PF& P, T* vals, cudaStream_t s) {
+  constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
+  int blocks = grid_for(ceil_div(Ne, 32 / G) * 32, 128);
+  if (blocks > kSMs * 64) blocks = kSMs * 64;
+  pf_elastic_kernel<ELEM, T><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, d, P, vals);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+}  // namespace
+}  // namespace gfea
+
+using namespace gfea;
+
+extern "C" int gfea_pf_damage(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                              const int32_t* node_ptr, const uint8_t* rank, const double* u,
+                              const gfea_pf_params* params_host, const double* H_old, double* H_new,
+                              double* Kd_values, double* Fd, void* stream) {
+  PF P;
+  if (to_pf(params_host, &P)) return GFEA_ERR_ARG;
+  if (!coord || !connect || !node_ptr || !rank || !u || !H_new || !Kd_values || !Fd || n_elems < 0) return GFEA_ERR_ARG;
+  if (n_elems == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (elem) {
+    case GFEA_TRI3: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_TRI3>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_QUAD4: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD4>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_QUAD9: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD9>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_HEXA8: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_HEXA8>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    default: return GFEA_ERR_ARG;
+  }
+}
+
+extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                               const int32_t* node_ptr, const uint8_t* rank, const double* u, const double* d,
+                               const gfea_pf_params* params_host, int value_type, void* values, void* stream) {
+  PF P;
+  if (to_pf(params_host, &P)) return GFEA_ERR_ARG;
+  if (!coord || !connect || !node_ptr || !rank || !u || !d || !values || n_elems < 0) return GFEA_ERR_ARG;
+  if (n_elems == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (value_type == GFEA_F64) {
+    auto* v = static_cast<double*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_pfel<GFEA_TRI3, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD4: return launch_pfel<GFEA_QUAD4, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  } else if (value_type == GFEA_F32) {
+    auto* v = static_cast<float*>(values);
+    switch (elem) {
+      case GFEA_TRI3: return launch_pfel<GFEA_TRI3, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD4: return launch_pfel<GFEA_QUAD4, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      default: return GFEA_ERR_ARG;
+    }
+  }
+  return GFEA_ERR_ARG;
+}
+
+extern "C" int gfea_pf_split(const double* eps, int64_t n_points, const gfea_pf_params* params_host, double* cP,
+                             double* cM, double* psiP, double* psiM, void* stream) {
+  PF P;
+  if (to_pf(params_host, &P)) return GFEA_ERR_ARG;
+  if (!eps || n_points < 0) return GFEA_ERR_ARG;
+  if (n_points == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int blocks = grid_for(n_points, 128);
+  if (P.dim == 2)
+    split_kernel<2><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
+  else
+    split_kernel<3><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}

@@ -1,0 +1,765 @@
+// Sparse SPD solve: node-block CSR SpMV, nodal block-Jacobi and PCG.
+//
+// The CSR values keep the reference's scalar CSR layout, but their column
+// structure is read from the node graph: a node's dof_n rows share one sorted
+// neighbour list, so the SpMV reads 4 bytes of index per dof_n^2 values
+// instead of 4 per value.  G lanes of a warp serve one node; within a row
+// lane t reads value t, t+G, ... so every load instruction is contiguous.
+//
+// Dirichlet DOFs are eliminated as in Solvers.__Solver_1 (EasyFEA/Simulations/
+// Solvers.py:502-553) but without extracting A_ii: PCG runs on the masked
+// operator P A P + (I - P) (P = diag(unknown)); search directions vanish on
+// known DOFs, so the product is a plain SpMV with known rows zeroed.
+//
+// One PCG iteration is two kernels:
+//   dir_spmv : p' = z + beta p  (own rows), Ap' (gathered z + beta p), p'.Ap'
+//   update   : x += alpha p', r -= alpha Ap', z = D^-1 r, r.z, r.r
+// Reductions are per-block partials summed in a fixed order by the last block
+// to finish (atomic ticket, no spinning), which also derives the scalar
+// recurrences (alpha, beta, convergence) on the device.  Kernels return early
+// once the device flag 'done' is set, so a host loop (or a captured graph) may
+// run more iterations than needed at no cost.
+
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace gfea {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxBlocks = kSMs * 8;
+
+struct Scal {
+  double rz, rr, pap, alpha, beta, bb, tol2, rr_true;
+  int32_t done, iters, status, max_iters;
+  uint32_t ticket1, ticket2, ticket3, pad;
+};
+
+template <typename T>
+struct SysT {
+  int64_t Nn;
+  const int32_t* node_ptr;
+  const int32_t* nbr;
+  const T* vals;
+  const uint8_t* known;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  // warp then block reduction with a fixed tree (deterministic)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0;
+  if (w == 0) {
+    t = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+// Publish NV block partials; returns true in the last block, where out[] holds
+// the fixed-order totals (valid in every thread of that block).
+template <int NV>
+__device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* ticket, double (&out)[NV]) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) s[k] = block_sum(v[k], sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = s[k];
+    __threadfence();
+    const uint32_t t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double a = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) a += ((volatile double*)partials)[k * gridDim.x + i];
+    out[k] = block_sum(a, sh);
+    if (threadIdx.x == 0) sh[31] = out[k];
+    __syncthreads();
+    out[k] = sh[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// node-row products
+// ---------------------------------------------------------------------------
+
+// acc[i] = sum over row (a,i) of vals * xf(col); reduced across the G lanes.
+template <int D, int G, typename T, typename A, typename XF>
+__device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S, XF xf, A (&acc)[D]) {
+  const int32_t p0 = S.node_ptr[a];
+  const int32_t W = D * (S.node_ptr[a + 1] - p0);
+  const T* base = S.vals + (int64_t)D * D * p0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) acc[i] = 0;
+  for (int32_t t = lane; t < W; t += G) {
+    const int32_t k = t / D, j = t - k * D;
+    const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
+    const A xv = xf(col);
+#pragma unroll
+    for (int i = 0; i < D; ++i) acc[i] += (A)__ldg(base + (int64_t)i * W + t) * xv;
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) acc[i] = group_sum<G, A>(acc[i]);
+}
+
+// y = A x (unmasked)
+template <int D, int G, typename T>
+__global__ void __launch_bounds__(kThreads) spmv_kernel(SysT<T> S, const T* __restrict__ x, T* __restrict__ y) {
+  const int lane = threadIdx.x % G;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t Nn = S.Nn;
+  for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
+    const int64_t a = a0 + (grp % (32 / G));
+    const int64_t ac = a < Nn ? a : Nn - 1;
+    T acc[D];
+    node_rows<D, G, T, T>(ac, lane, S, [&](int64_t c) { return x[c]; }, acc);
+    if (a < Nn && lane < D) {
+      T v = acc[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) if (lane == i) v = acc[i];
+      y[a * D + lane] = v;
+    }
+  }
+}
+
+// r = P (b - A x), rc = P (b - A x_c) (x_c: x on known columns only);
+// partials r.r and rc.rc.  Used for the PCG start and the FP64 refinement.
+template <int D, int G, typename T>
+__global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double* __restrict__ b,
+                                                         const double* __restrict__ x, double* __restrict__ r,
+                                                         double* partials, Scal* sc, int mode) {
+  // mode 0: PCG start (sets bb, rr); mode 1: refinement residual (sets rr_true, keeps bb unless zero)
+  const int lane = threadIdx.x % G;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t Nn = S.Nn;
+  double v[2] = {0, 0};
+  for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
+    const int64_t a = a0 + (grp % (32 / G));
+    const int64_t ac = a < Nn ? a : Nn - 1;
+    double all[D], kn[D];
+    node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return x[c]; }, all);
+    node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return S.known[c] ? x[c] : 0.0; }, kn);
+    if (a < Nn && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        const int64_t dof = a * D + i;
+        const bool unk = !S.known[dof];
+        const double ri = unk ? b[dof] - all[i] : 0.0;
+        const double rci = unk ? b[dof] - kn[i] : 0.0;
+        r[dof] = ri;
+        v[0] += ri * ri;
+        v[1] += rci * rci;
+      }
+    }
+  }
+  double out[2];
+  if (reduce_last<2>(v, partials, &sc->ticket3, out) && threadIdx.x == 0) {
+    if (mode == 0) {
+      sc->rr = out[0];
+      sc->bb = out[1];
+    } else {
+      sc->rr_true = out[0];
+      if (sc->bb == 0) sc->bb = out[1];
+    }
+  }
+}
+
+// Block-Jacobi: invert the (masked) dof_n x dof_n diagonal block of each node.
+template <int D, typename T>
+__global__ void bjacobi_kernel(SysT<T> S, T* __restrict__ dinv, int32_t* flag) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < S.Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p0 = S.node_ptr[a], p1 = S.node_ptr[a + 1];
+    int lo = p0, hi = p1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (S.nbr[mid] < a) lo = mid + 1; else hi = mid;
+    }
+    const bool has = lo < p1 && S.nbr[lo] == a;
+    const int32_t W = D * (p1 - p0);
+    const int k = lo - p0;
+    double M[D][D];
+    bool kn[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) kn[i] = S.known[a * D + i] != 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        double v = has ? (double)S.vals[(int64_t)D * D * p0 + (int64_t)i * W + D * k + j] : 0.0;
+        if (kn[i] || kn[j]) v = (i == j) ? 1.0 : 0.0;
+        M[i][j] = v;
+      }
+    double iM[D][D];
+    const double det = det_inv<D>(M, iM);
+    bool bad = !(fabs(det) > 0) || !isfinite(det);
+    if (bad) {
+      atomicOr(flag, 1);
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) iM[i][j] = (i == j) ? 1.0 : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) dinv[a * D * D + i * D + j] = (T)iM[i][j];
+  }
+}
+
+// z = D^-1 r (+ optional x/r update), partial r.z and r.r; last block derives
+// beta and the convergence state.
+template <int D, typename T>
+__global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint8_t* __restrict__ known,
+                                                          const T* __restrict__ dinv, T* __restrict__ x,
+                                                          T* __restrict__ r, T* __restrict__ z,
+                                                          const T* __restrict__ p, const T* __restrict__ Ap,
+                                                          double* partials, Scal* sc, int init) {
+  if (!init && sc->done) return;
+  const double alpha = init ? 0.0 : sc->alpha;
+  double v[2] = {0, 0};
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    T rl[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      const int64_t dof = a * D + i;
+      T ri = r[dof];
+      if (!init) {
+        x[dof] += (T)alpha * p[dof];
+        ri -= (T)alpha * Ap[dof];
+        r[dof] = ri;
+      }
+      rl[i] = ri;
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      T zi = 0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) zi += dinv[a * D * D + i * D + j] * rl[j];
+      if (known[a * D + i]) zi = 0;
+      z[a * D + i] = zi;
+      v[0] += (double)rl[i] * (double)zi;
+      v[1] += (double)rl[i] * (double)rl[i];
+    }
+  }
+  double out[2];
+  if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
+    const double rz_new = out[0], rr = out[1];
+    sc->beta = init ? 0.0 : rz_new / sc->rz;
+    sc->rz = rz_new;
+    sc->rr = rr;
+    if (init) return;  // convergence of the start is judged by init_scal_kernel
+    sc->iters += 1;
+    if (!isfinite(rr) || !isfinite(rz_new)) {
+      sc->status = GFEA_ERR_NAN;
+      sc->done = 1;
+    } else if (rr <= sc->tol2) {
+      sc->status = GFEA_OK;
+      sc->done = 1;
+    } else if (sc->iters >= sc->max_iters) {
+      sc->status = GFEA_ERR_NOT_CONVERGED;
+      sc->done = 1;
+    }
+  }
+}
+
+// p' = z + beta p (own rows), Ap' = masked A p'; partial p'.Ap'; last block sets alpha.
+template <int D, int G, typename T>
+__global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* __restrict__ z,
+                                                            const T* __restrict__ p_old, T* __restrict__ p_new,
+                                                            T* __restrict__ Ap, double* partials, Scal* sc) {
+  if (sc->done) return;
+  const T beta = (T)sc->beta;
+  const int lane = threadIdx.x % G;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t Nn = S.Nn;
+  double v[1] = {0};
+  for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
+    const int64_t a = a0 + (grp % (32 / G));
+    const int64_t ac = a < Nn ? a : Nn - 1;
+    T acc[D];
+    node_rows<D, G, T, T>(ac, lane, S, [&](int64_t c) { return z[c] + beta * p_old[c]; }, acc);
+    if (a < Nn && lane < D) {
+      T av = acc[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) if (lane == i) av = acc[i];
+      const int64_t dof = a * D + lane;
+      const T pn = z[dof] + beta * p_old[dof];
+      if (S.known[dof]) av = 0;
+      p_new[dof] = pn;
+      Ap[dof] = av;
+      v[0] += (double)pn * (double)av;
+    }
+  }
+  double out[1];
+  if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
+    sc->pap = out[0];
+    if (!(out[0] > 0) || !isfinite(out[0])) {
+      sc->status = isfinite(out[0]) ? GFEA_ERR_BREAKDOWN : GFEA_ERR_NAN;
+      sc->done = 1;
+    } else {
+      sc->alpha = sc->rz / out[0];
+    }
+  }
+}
+
+template <typename T>
+__global__ void cast_kernel(const double* __restrict__ s, T* __restrict__ d, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = (T)s[i];
+}
+
+template <typename T>
+__global__ void add_correction_kernel(double* __restrict__ x, const T* __restrict__ dx, const uint8_t* known, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!known[i]) x[i] += (double)dx[i];
+}
+
+__global__ void zero_unknown_kernel(double* __restrict__ x, const uint8_t* known, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!known[i]) x[i] = 0.0;
+}
+
+// Runs after the start's update (rz, rr known): sets the stopping threshold,
+// relative to bb (rel_to_rr = 0) or to the starting rr (rel_to_rr = 1).
+__global__ void init_scal_kernel(Scal* sc, double tol2_rel, int max_iters, int rel_to_rr) {
+  const double ref = rel_to_rr ? sc->rr : sc->bb;
+  sc->tol2 = tol2_rel * ref;
+  sc->iters = 0;
+  sc->status = GFEA_OK;
+  sc->max_iters = max_iters;
+  sc->beta = 0;
+  sc->done = !isfinite(sc->rr) ? 1 : (sc->rr <= sc->tol2 ? 1 : 0);
+  if (!isfinite(sc->rr)) sc->status = GFEA_ERR_NAN;
+}
+
+// reaction / energy
+template <int D, int G>
+__global__ void __launch_bounds__(kThreads) reaction_kernel(SysT<double> S, const double* __restrict__ x,
+                                                            double* __restrict__ Ax, double* partials, Scal* sc) {
+  const int lane = threadIdx.x % G;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t Nn = S.Nn;
+  double v[1] = {0};
+  for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
+    const int64_t a = a0 + (grp % (32 / G));
+    const int64_t ac = a < Nn ? a : Nn - 1;
+    double acc[D];
+    node_rows<D, G, double, double>(ac, lane, S, [&](int64_t c) { return x[c]; }, acc);
+    if (a < Nn && lane < D) {
+      double av = acc[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) if (lane == i) av = acc[i];
+      Ax[a * D + lane] = av;
+      v[0] += 0.5 * x[a * D + lane] * av;
+    }
+  }
+  double out[1];
+  if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) sc->rr_true = out[0];
+}
+
+__global__ void gather_sum_kernel(const double* __restrict__ Ax, const int64_t* __restrict__ dofs, int64_t n,
+                                  double* partials, Scal* sc) {
+  double v[1] = {0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[0] += Ax[dofs[i]];
+  double out[1];
+  if (reduce_last<1>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) sc->pap = out[0];
+}
+
+__global__ void max_abs_diff_kernel(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                                    unsigned long long* out) {
+  double m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = fabs(a[i] - b[i]);
+    m = fmax(m, isnan(d) ? INFINITY : d);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // non-negative doubles order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+int pick_lanes(const gfea_system* s, int requested) {
+  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
+  const double W = s->n_nodes > 0 ? (double)s->dof_n * (double)s->n_pairs / (double)s->n_nodes : 1.0;
+  if (W <= 10) return 4;
+  if (W <= 24) return 8;
+  if (W <= 56) return 16;
+  return 32;
+}
+
+int grid_nodes(int64_t Nn, int G) {
+  const int64_t groups_per_block = kThreads / G;
+  int64_t g = ceil_div(Nn, groups_per_block);
+  if (g > kMaxBlocks) g = kMaxBlocks;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+int grid_elems(int64_t n) {
+  int64_t g = ceil_div(n, kThreads);
+  if (g > kMaxBlocks) g = kMaxBlocks;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+struct PcgWork {
+  void* r; void* z; void* pa; void* pb; void* Ap; void* dinv; void* x32;  // T-typed
+  double* r64;
+  double* partials;
+  Scal* sc;
+  int32_t* flag;
+};
+
+template <typename T>
+size_t pcg_layout(int64_t Nn, int D, bool mixed, PcgWork* w, char* base) {
+  size_t off = 0;
+  const int64_t N = Nn * D;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  PcgWork t;
+  if (!w) w = &t;
+  w->r = take(sizeof(T) * N);
+  w->z = take(sizeof(T) * N);
+  w->pa = take(sizeof(T) * N);
+  w->pb = take(sizeof(T) * N);
+  w->Ap = take(sizeof(T) * N);
+  w->dinv = take(sizeof(T) * N * D);
+  w->x32 = mixed ? take(sizeof(T) * N) : nullptr;
+  w->r64 = mixed ? reinterpret_cast<double*>(take(sizeof(double) * N)) : nullptr;
+  w->partials = reinterpret_cast<double*>(take(sizeof(double) * 4 * kMaxBlocks));
+  w->sc = reinterpret_cast<Scal*>(take(sizeof(Scal)));
+  w->flag = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * 4));
+  return off;
+}
+
+template <typename T>
+SysT<T> sys_t(const gfea_system* s);
+template <>
+SysT<double> sys_t<double>(const gfea_system* s) {
+  return SysT<double>{s->n_nodes, s->node_ptr, s->nbr, s->vals64, s->known};
+}
+template <>
+SysT<float> sys_t<float>(const gfea_system* s) {
+  return SysT<float>{s->n_nodes, s->node_ptr, s->nbr, s->vals32, s->known};
+}
+
+// Launch helpers dispatching (D, G).
+#define GFEA_DG_SWITCH(D, G, CALL)                                   \
+  switch (D * 100 + G) {                                             \
+    case 104: { constexpr int DD = 1, GG = 4; CALL; } break;          \
+    case 108: { constexpr int DD = 1, GG = 8; CALL; } break;          \
+    case 116: { constexpr int DD = 1, GG = 16; CALL; } break;         \
+    case 132: { constexpr int DD = 1, GG = 32; CALL; } break;         \
+    case 204: { constexpr int DD = 2, GG = 4; CALL; } break;          \
+    case 208: { constexpr int DD = 2, GG = 8; CALL; } break;          \
+    case 216: { constexpr int DD = 2, GG = 16; CALL; } break;         \
+    case 232: { constexpr int DD = 2, GG = 32; CALL; } break;         \
+    case 304: { constexpr int DD = 3, GG = 4; CALL; } break;          \
+    case 308: { constexpr int DD = 3, GG = 8; CALL; } break;          \
+    case 316: { constexpr int DD = 3, GG = 16; CALL; } break;         \
+    case 332: { constexpr int DD = 3, GG = 32; CALL; } break;         \
+    default: return GFEA_ERR_ARG;                                    \
+  }
+
+#define GFEA_D_SWITCH(D, CALL)                         \
+  switch (D) {                                         \
+    case 1: { constexpr int DD = 1; CALL; } break;     \
+    case 2: { constexpr int DD = 2; CALL; } break;     \
+    case 3: { constexpr int DD = 3; CALL; } break;     \
+    default: return GFEA_ERR_ARG;                      \
+  }
+
+template <typename T>
+int launch_resid(const gfea_system* s, int G, const double* b, const double* x, double* r, PcgWork& w, int mode,
+                 cudaStream_t st) {
+  const SysT<T> S = sys_t<T>(s);
+  const int grid = grid_nodes(s->n_nodes, G);
+  GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, b, x, r, w.partials, w.sc, mode)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <typename T>
+int launch_bjacobi(const gfea_system* s, PcgWork& w, cudaStream_t st) {
+  const SysT<T> S = sys_t<T>(s);
+  GFEA_D_SWITCH(s->dof_n, (bjacobi_kernel<DD, T><<<grid_elems(s->n_nodes), kThreads, 0, st>>>(S, (T*)w.dinv, w.flag)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <typename T>
+int launch_update(const gfea_system* s, PcgWork& w, T* x, T* p, int init, cudaStream_t st) {
+  const int grid = grid_elems(s->n_nodes);
+  GFEA_D_SWITCH(s->dof_n, (update_kernel<DD, T><<<grid, kThreads, 0, st>>>(s->n_nodes, s->known, (const T*)w.dinv, x,
+                                                                            (T*)w.r, (T*)w.z, p, (const T*)w.Ap,
+                                                                            w.partials + 2 * kMaxBlocks, w.sc, init)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <typename T>
+int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new, cudaStream_t st) {
+  const SysT<T> S = sys_t<T>(s);
+  const int grid = grid_nodes(s->n_nodes, G);
+  GFEA_DG_SWITCH(s->dof_n, G, (dir_spmv_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, (const T*)w.z, p_old, p_new, (T*)w.Ap,
+                                                                                      w.partials, w.sc)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+// Runs PCG iterations until the device flags done; checks every 'check' iterations.
+template <typename T>
+int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* host_sc, cudaStream_t st) {
+  T* pa = (T*)w.pa;
+  T* pb = (T*)w.pb;
+  for (;;) {
+    for (int it = 0; it < check; ++it) {
+      int e = launch_dir<T>(s, G, w, pa, pb, st);
+      if (e) return e;
+      e = launch_update<T>(s, w, x, pb, 0, st);
+      if (e) return e;
+      T* t = pa; pa = pb; pb = t;
+    }
+    GFEA_CUDA_TRY(cudaMemcpyAsync(host_sc, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    if (host_sc->done) break;
+  }
+  return GFEA_OK;
+}
+
+}  // namespace
+}  // namespace gfea
+
+using namespace gfea;
+
+extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, void* y, void* stream) {
+  if (!s || s->version != GFEA_ABI_VERSION || !x || !y || s->n_nodes <= 0) return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int G = pick_lanes(s, 0);
+  const int grid = grid_nodes(s->n_nodes, G);
+  if (value_type == GFEA_F64) {
+    if (!s->vals64) return GFEA_ERR_ARG;
+    const SysT<double> S = sys_t<double>(s);
+    GFEA_DG_SWITCH(s->dof_n, G, (spmv_kernel<DD, GG, double><<<grid, kThreads, 0, st>>>(S, (const double*)x, (double*)y)));
+  } else if (value_type == GFEA_F32) {
+    if (!s->vals32) return GFEA_ERR_ARG;
+    const SysT<float> S = sys_t<float>(s);
+    GFEA_DG_SWITCH(s->dof_n, G, (spmv_kernel<DD, GG, float><<<grid, kThreads, 0, st>>>(S, (const float*)x, (float*)y)));
+  } else {
+    return GFEA_ERR_ARG;
+  }
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+extern "C" int gfea_pcg_workspace_size(const gfea_system* s, const gfea_pcg_opts* o, size_t* bytes) {
+  if (!s || !o || !bytes || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3) return GFEA_ERR_ARG;
+  if (o->precision == GFEA_F64)
+    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, false, nullptr, nullptr);
+  else
+    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, true, nullptr, nullptr);
+  return GFEA_OK;
+}
+
+extern "C" int gfea_pcg_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
+                              size_t work_bytes, gfea_pcg_result* res, void* stream) {
+  if (!s || !o || !b || !x || !work || !res) return GFEA_ERR_ARG;
+  if (s->version != GFEA_ABI_VERSION || o->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
+  if (s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3 || !s->node_ptr || !s->nbr || !s->known || !s->vals64)
+    return GFEA_ERR_ARG;
+  if (o->max_iters < 1 || !(o->rtol > 0)) return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int G = pick_lanes(s, o->lanes);
+  const int64_t N = s->n_nodes * s->dof_n;
+  const int check = o->check_every > 0 ? o->check_every : 32;
+  res->status = GFEA_OK;
+  res->iterations = 0;
+  res->refinements = 0;
+  res->rel_residual = 0;
+  Scal hs;
+
+  if (o->precision == GFEA_F64) {
+    PcgWork w;
+    if (pcg_layout<double>(s->n_nodes, s->dof_n, false, &w, static_cast<char*>(work)) > work_bytes)
+      return GFEA_ERR_WORKSPACE;
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(double) * N, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(double) * N, st));
+    int e = launch_bjacobi<double>(s, w, st);
+    if (e) return e;
+    e = launch_resid<double>(s, G, b, x, (double*)w.r, w, 0, st);
+    if (e) return e;
+    e = launch_update<double>(s, w, x, (double*)w.pa, 1, st);
+    if (e) return e;
+    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, o->rtol * o->rtol, o->max_iters, 0);
+    GFEA_LAUNCH_CHECK();
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    int32_t flag = 0;
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
+    if (hs.bb == 0) {
+      zero_unknown_kernel<<<grid_elems(N), kThreads, 0, st>>>(x, s->known, N);
+      GFEA_LAUNCH_CHECK();
+      GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+      return GFEA_OK;
+    }
+    if (!hs.done) {
+      e = pcg_loop<double>(s, G, w, x, check, &hs, st);
+      if (e) return e;
+    }
+    res->iterations = hs.iters;
+    res->status = hs.status;
+    // true residual
+    e = launch_resid<double>(s, G, b, x, (double*)w.r, w, 1, st);
+    if (e) return e;
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    res->rel_residual = sqrt(hs.rr_true / hs.bb);
+    return res->status;
+  }
+
+  if (o->precision != GFEA_F32 || !s->vals32) return GFEA_ERR_ARG;
+  // FP32 inner PCG with FP64 iterative refinement.
+  PcgWork w;
+  if (pcg_layout<float>(s->n_nodes, s->dof_n, true, &w, static_cast<char*>(work)) > work_bytes) return GFEA_ERR_WORKSPACE;
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
+  int e = launch_bjacobi<float>(s, w, st);
+  if (e) return e;
+  // FP64 residual of the starting point (sets bb and rr_true)
+  e = launch_resid<double>(s, G, b, x, w.r64, w, 0, st);
+  if (e) return e;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+  int32_t flag = 0;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
+  const double bb = hs.bb;
+  if (bb == 0) {
+    zero_unknown_kernel<<<grid_elems(N), kThreads, 0, st>>>(x, s->known, N);
+    GFEA_LAUNCH_CHECK();
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    return GFEA_OK;
+  }
+  double rr = hs.rr;
+  int total = 0;
+  const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+  const int max_ref = o->max_refine > 0 ? o->max_refine : 20;
+  res->status = GFEA_ERR_NOT_CONVERGED;
+  for (int k = 0; k < max_ref; ++k) {
+    res->refinements = k + 1;
+    res->rel_residual = sqrt(rr / bb);
+    if (rr <= o->rtol * o->rtol * bb) { res->status = GFEA_OK; break; }
+    if (total >= o->max_iters) break;
+    // inner solve A32 d = r64 (d = 0 start, known DOFs 0)
+    cast_kernel<float><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (float*)w.r, N);
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.x32, 0, sizeof(float) * N, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(float) * N, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(float) * N, st));
+    e = launch_update<float>(s, w, (float*)w.x32, (float*)w.pa, 1, st);  // z, rz, rr of r
+    if (e) return e;
+    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, inner * inner, o->max_iters - total, 1);
+    GFEA_LAUNCH_CHECK();
+    e = pcg_loop<float>(s, G, w, (float*)w.x32, check, &hs, st);
+    if (e) return e;
+    total += hs.iters;
+    if (hs.status == GFEA_ERR_NAN || hs.status == GFEA_ERR_BREAKDOWN) { res->status = hs.status; break; }
+    add_correction_kernel<float><<<grid_elems(N), kThreads, 0, st>>>(x, (const float*)w.x32, s->known, N);
+    GFEA_LAUNCH_CHECK();
+    e = launch_resid<double>(s, G, b, x, w.r64, w, 1, st);
+    if (e) return e;
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    rr = hs.rr_true;
+  }
+  res->iterations = total;
+  res->rel_residual = sqrt(rr / bb);
+  if (res->status != GFEA_OK && rr <= o->rtol * o->rtol * bb) res->status = GFEA_OK;
+  return res->status;
+}
+
+extern "C" size_t gfea_reduce_workspace_size(void) { return sizeof(double) * 4 * kMaxBlocks + 256; }
+
+extern "C" int gfea_reaction_energy(const gfea_system* s, const double* x, const int64_t* dofs, int64_t n_dofs,
+                                    double* Ax, double* out_host, void* work, void* stream) {
+  if (!s || !x || !Ax || !out_host || !work || s->n_nodes <= 0 || !s->vals64) return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* partials = static_cast<double*>(work);
+  Scal* sc = reinterpret_cast<Scal*>(partials + 4 * kMaxBlocks);
+  GFEA_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(Scal), st));
+  const int G = pick_lanes(s, 0);
+  const SysT<double> S = sys_t<double>(s);
+  const int grid = grid_nodes(s->n_nodes, G);
+  GFEA_DG_SWITCH(s->dof_n, G, (reaction_kernel<DD, GG><<<grid, kThreads, 0, st>>>(S, x, Ax, partials, sc)));
+  GFEA_LAUNCH_CHECK();
+  if (n_dofs > 0 && dofs) {
+    gather_sum_kernel<<<grid_elems(n_dofs), kThreads, 0, st>>>(Ax, dofs, n_dofs, partials + 2 * kMaxBlocks, sc);
+    GFEA_LAUNCH_CHECK();
+  }
+  Scal hs;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  out_host[0] = (n_dofs > 0 && dofs) ? hs.pap : 0.0;
+  out_host[1] = hs.rr_true;
+  return GFEA_OK;
+}
+
+extern "C" int gfea_max_abs_diff(const double* a, const double* b, int64_t n, double* out_host, void* work,
+                                 void* stream) {
+  if (!a || !b || !out_host || !work || n < 0) return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto* o = static_cast<unsigned long long*>(work);
+  GFEA_CUDA_TRY(cudaMemsetAsync(o, 0, sizeof(unsigned long long), st));
+  if (n > 0) {
+    max_abs_diff_kernel<<<grid_elems(n), kThreads, 0, st>>>(a, b, n, o);
+    GFEA_LAUNCH_CHECK();
+  }
+  unsigned long long h = 0;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&h, o, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  double v;
+  memcpy(&v, &h, sizeof(v));
+  *out_host = v;
+  return GFEA_OK;
+}
+
+extern "C" int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void* stream) {
+  if (!src || !dst || n < 0) return GFEA_ERR_ARG;
+  if (n == 0) return GFEA_OK;
+  cast_kernel<float><<<grid_elems(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, n);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}

@@ -1,0 +1,646 @@
+"""Simulations mirroring EasyFEA's ``Simulations.Elastic`` / ``Simulations.PhaseField``.
+
+Same user-facing calls as the reference -- ``add_dirichlet``, ``add_surfLoad``,
+``add_lineLoad``, ``add_neumann``, ``Bc_Init``, ``Solve``, ``Save_Iter``,
+``Get_K_C_M_F``, ``Calc_Reaction``, ``Need_Update`` -- with the assembly and
+the solve running on the GPU (libgb300fea.so).  Boundary-condition bookkeeping
+is host code, as in the reference (EasyFEA/Simulations/_simu.py:2400-3050).
+
+Differences from the reference that a user sees:
+  * the linear solve is block-Jacobi PCG (FP64, or FP32 with FP64 refinement
+    when ``precision = "mixed"``) to relative residual ``rtol`` instead of
+    SuperLU; ``last_solve`` reports iterations and the final residual;
+  * state stays on the device between calls; ``Solve`` returns host copies.
+"""
+
+from __future__ import annotations
+
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import CsrOperator, DeviceMesh, max_abs_diff, pcg, reaction_energy
+from .mesh import Mesh
+from .models import Elastic as ElasticModels
+from .models import PhaseField as PhaseFieldModel
+from .models import _Elastic
+
+
+def _dev():
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+class _BC:
+    def __init__(self, problemType, nodes, dofs, values, unknowns, description):
+        self.problemType = problemType
+        self.nodes = nodes
+        self.dofs = dofs
+        self.values = values
+        self.unknowns = unknowns
+        self.description = description
+
+
+class _Simu:
+    """Shared machinery (EasyFEA/Simulations/_simu.py)."""
+
+    def __init__(self, mesh: Mesh, model, verbosity: bool = False):
+        assert isinstance(mesh, Mesh), "mesh must be an easyfea_gb300 Mesh"
+        self.mesh = mesh
+        self.model = model
+        self._verbosity = verbosity
+        self.rho = 1.0
+        self.precision = "fp64"
+        self.rtol = 1e-12
+        self.max_iters = 200000
+        self.last_solve = None
+        self._dmesh: Optional[DeviceMesh] = None
+        self._results: list = []
+        model._Add_observer(self)
+        self.Bc_Init()
+        self.Need_Update()
+
+    # ---- infrastructure ------------------------------------------------------
+    @property
+    def dmesh(self) -> DeviceMesh:
+        if self._dmesh is None:
+            self._dmesh = DeviceMesh(self.mesh)
+        return self._dmesh
+
+    @property
+    def dim(self) -> int:
+        return self.mesh.dim
+
+    def _Update(self, observable) -> None:
+        self.Need_Update()
+
+    def Need_Update(self, value: bool = True) -> None:
+        self._needUpdate = value
+
+    @property
+    def needUpdate(self) -> bool:
+        return self._needUpdate
+
+    def Get_problemTypes(self) -> list:
+        return [self.problemType]
+
+    def _check_pt(self, problemType):
+        if problemType is None:
+            problemType = self.problemType
+        problemType = str(getattr(problemType, "value", problemType))
+        assert problemType in self.Get_problemTypes(), f"unknown problemType {problemType}"
+        return problemType
+
+    def Ndof(self, problemType=None) -> int:
+        return self.mesh.Nn * self.Get_dof_n(problemType)
+
+    # ---- boundary conditions (EasyFEA/Simulations/_simu.py:2190-2842) --------
+    def Bc_Init(self) -> None:
+        self._dirichlet = {pt: [] for pt in self.Get_problemTypes()}
+        self._neumann = {pt: [] for pt in self.Get_problemTypes()}
+        self._b_neu = {pt: None for pt in self.Get_problemTypes()}
+
+    def Bc_dofs_nodes(self, nodes, unknowns, problemType=None) -> np.ndarray:
+        problemType = self._check_pt(problemType)
+        nodes = np.asarray(nodes, dtype=np.int64)
+        avail = self.Get_unknowns(problemType)
+        dofs = np.zeros((nodes.size, len(unknowns)), dtype=np.int64)
+        for i, u in enumerate(unknowns):
+            assert u in avail, f"unknown {u} not in {avail}"
+            dofs[:, i] = nodes * len(avail) + avail.index(u)
+        return dofs.ravel()
+
+    @staticmethod
+    def _check_inputs(nodes, values, unknowns) -> bool:
+        if len(nodes) == 0 or len(values) == 0:
+            return False
+        assert len(values) == len(unknowns), f"len(values)={len(values)} must equal len(unknowns)={len(unknowns)}."
+        return True
+
+    def _eval_nodes(self, nodes, value):
+        coord = self.mesh.coord[nodes]
+        if callable(value):
+            return np.asarray(value(coord[:, 0], coord[:, 1], coord[:, 2]), dtype=float) * np.ones(len(nodes))
+        return np.broadcast_to(np.asarray(value, dtype=float), (len(nodes),)).copy()
+
+    def add_dirichlet(self, nodes, values: list, unknowns: list, problemType=None, description="") -> None:
+        """Imposed values; duplicate DOFs add up (EasyFEA/Simulations/_simu.py:2400-2469, :3013-3040)."""
+        if not self._check_inputs(nodes, values, unknowns):
+            return
+        problemType = self._check_pt(problemType)
+        nodes = np.asarray(nodes, dtype=np.int64)
+        vals = np.zeros((nodes.size, len(unknowns)))
+        for d in range(len(unknowns)):
+            vals[:, d] = self._eval_nodes(nodes, values[d])
+        dofs = self.Bc_dofs_nodes(nodes, unknowns, problemType)
+        self._dirichlet[problemType].append(_BC(problemType, nodes, dofs, vals.ravel(), unknowns, description))
+
+    def _neumann_vec(self, problemType) -> torch.Tensor:
+        if self._b_neu[problemType] is None:
+            self._b_neu[problemType] = torch.zeros(self.Ndof(problemType), dtype=torch.float64, device=_dev())
+        return self._b_neu[problemType]
+
+    def add_neumann(self, nodes, values: list, unknowns: list, problemType=None, description="") -> None:
+        """Point loads split evenly over the nodes (EasyFEA/Simulations/_simu.py:2743-2768)."""
+        if not self._check_inputs(nodes, values, unknowns):
+            return
+        problemType = self._check_pt(problemType)
+        nodes = np.asarray(nodes, dtype=np.int64)
+        vals = np.zeros((nodes.size, len(unknowns)))
+        for i in range(len(unknowns)):
+            vals[:, i] = self._eval_nodes(nodes, values[i]) / len(nodes)
+        dofs = self.Bc_dofs_nodes(nodes, unknowns, problemType)
+        b = self._neumann_vec(problemType)
+        b.index_add_(0, torch.as_tensor(dofs, device=_dev()), torch.as_tensor(vals.ravel(), device=_dev()))
+        self._neumann[problemType].append(_BC(problemType, nodes, dofs, vals.ravel(), unknowns, description))
+
+    def _integrate_load(self, nodes, values, unknowns, problemType, factor, bdim):
+        problemType = self._check_pt(problemType)
+        for v in values:
+            if callable(v) or np.ndim(v) > 0:
+                raise NotImplementedError("surface / line loads take constant values on the GPU path")
+        L = _lib.load()
+        avail = self.Get_unknowns(problemType)
+        uidx = (ctypes_int32 * len(unknowns))(*[avail.index(u) for u in unknowns])
+        uval = (ctypes_double * len(unknowns))(*[float(v) for v in values])
+        mask = torch.zeros(self.mesh.Nn, dtype=torch.uint8, device=_dev())
+        mask[torch.as_tensor(np.asarray(nodes, dtype=np.int64), device=_dev())] = 1
+        b = self._neumann_vec(problemType)
+        groups = [g for g in self.dmesh.boundary if g.dim == bdim]
+        if bdim == self.dim:
+            groups = [self.dmesh.main]
+        for g in groups:
+            _lib.check(L.gfea_surface_load(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect), g.Ne,
+                                           _lib.ptr(mask), len(avail), len(unknowns), uidx, uval, float(factor),
+                                           _lib.ptr(b), _lib.stream()), "surface load")
+        self._neumann[problemType].append(_BC(problemType, np.asarray(nodes), None, np.asarray(values, float),
+                                              unknowns, "load"))
+
+    def add_surfLoad(self, nodes, values: list, unknowns: list, problemType=None, description="") -> None:
+        """Surface load: lines x thickness in 2D, faces in 3D (EasyFEA/Simulations/_simu.py:2572-2630)."""
+        if not self._check_inputs(nodes, values, unknowns):
+            return
+        if self.dim == 2:
+            self._integrate_load(nodes, values, unknowns, problemType, self.model_thickness, 1)
+        else:
+            self._integrate_load(nodes, values, unknowns, problemType, 1.0, 2)
+
+    def add_lineLoad(self, nodes, values: list, unknowns: list, problemType=None, description="") -> None:
+        """Line load (EasyFEA/Simulations/_simu.py:2530-2570), no thickness factor."""
+        if not self._check_inputs(nodes, values, unknowns):
+            return
+        self._integrate_load(nodes, values, unknowns, problemType, 1.0, 1)
+
+    def Bc_dofs_known_unknown(self, problemType=None):
+        problemType = self._check_pt(problemType)
+        n = self.Ndof(problemType)
+        mask = np.ones(n, dtype=bool)
+        for bc in self._dirichlet[problemType]:
+            mask[bc.dofs] = False
+        return np.nonzero(~mask)[0], np.nonzero(mask)[0]
+
+    def _dirichlet_state(self, problemType, b: torch.Tensor):
+        """(known mask uint8, x with known values) on the device.
+
+        Known values add up on duplicate DOFs (COO sum, _simu.py:1962-1966).
+        Orphan-node DOFs get x = b there, which is what the reference's unit
+        diagonal (_simu.py:1936-1946) produces."""
+        n = self.Ndof(problemType)
+        known = np.zeros(n, dtype=np.uint8)
+        xk = np.zeros(n)
+        for bc in self._dirichlet[problemType]:
+            known[bc.dofs] = 1
+            np.add.at(xk, bc.dofs, bc.values)
+        orphans = np.asarray(self.mesh.orphanNodes, dtype=np.int64)
+        od = np.zeros(0, dtype=np.int64)
+        if orphans.size:
+            od = self.Bc_dofs_nodes(orphans, self.Get_unknowns(problemType), problemType)
+            od = od[known[od] == 0]
+            known[od] = 1
+        known_d = torch.as_tensor(known, device=_dev())
+        x = torch.as_tensor(xk, device=_dev())
+        if od.size:
+            odd = torch.as_tensor(od, device=_dev())
+            x[odd] = b[odd]
+        return known_d, x
+
+    def _solve_system(self, op: CsrOperator, b: torch.Tensor, problemType, x0: Optional[torch.Tensor] = None):
+        known, x = self._dirichlet_state(problemType, b)
+        if x0 is not None:
+            x = torch.where(known.bool(), x, x0)
+        info = pcg(op, b, x, known, rtol=self.rtol, precision="fp64" if self.precision == "fp64" else "mixed",
+                   max_iters=self.max_iters)
+        self.last_solve = info
+        return x
+
+    # ---- results -----------------------------------------------------------
+    def Save_Iter(self, iter: Optional[dict] = None) -> dict:
+        it = {} if iter is None else iter
+        self._results.append(it)
+        return it
+
+    @property
+    def results(self) -> list:
+        return self._results
+
+
+ctypes_int32 = __import__("ctypes").c_int32
+ctypes_double = __import__("ctypes").c_double
+
+
+class Elastic(_Simu):
+    """Linear elasticity (EasyFEA/Simulations/_elastic.py)."""
+
+    problemType = "elastic"
+
+    def __init__(self, mesh: Mesh, model: _Elastic, folder: str = "", verbosity: bool = False):
+        assert isinstance(model, _Elastic), "model must be an elastic model"
+        assert model.dim == mesh.dim, "the material and the mesh must have the same dimension"
+        self.__K = None
+        self.__M = None
+        self.__u = None
+        super().__init__(mesh, model, verbosity)
+
+    @property
+    def material(self):
+        return self.model
+
+    @property
+    def model_thickness(self) -> float:
+        return self.model.thickness
+
+    def Get_unknowns(self, problemType=None) -> list:
+        return ["x", "y"] if self.dim == 2 else ["x", "y", "z"]
+
+    def Get_dof_n(self, problemType=None) -> int:
+        return self.dim
+
+    def Need_Update(self, value: bool = True) -> None:
+        super().Need_Update(value)
+        if value:
+            self.__M = None
+
+    def _C_device(self):
+        C = self.material.C
+        per_elem = C.ndim == 3
+        return torch.as_tensor(np.ascontiguousarray(C, dtype=np.float64), device=_dev()), per_elem
+
+    def Assembly(self, problemType=None) -> CsrOperator:
+        """K = sum_e K_e x thickness on the device (_elastic.py:123-152, _simu.py:1104-1144)."""
+        dm = self.dmesh
+        op = self.__K if self.__K is not None else CsrOperator(dm, self.dim)
+        C, per_elem = self._C_device()
+        g = dm.main
+        factor = self.material.thickness if self.dim == 2 else 1.0
+        _lib.check(_lib.load().gfea_assemble_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                                     _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C),
+                                                     int(per_elem), factor, _lib.F64, _lib.ptr(op.vals64),
+                                                     op.nnz, 0, _lib.stream()), "assemble elastic")
+        self.__K = op
+        return op
+
+    def _mass(self) -> CsrOperator:
+        if self.__M is None:
+            dm = self.dmesh
+            op = CsrOperator(dm, self.dim)
+            g = dm.main
+            factor = self.material.thickness if self.dim == 2 else 1.0
+            _lib.check(_lib.load().gfea_assemble_mass(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                                      _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), self.dim,
+                                                      float(self.rho), factor, _lib.F64, _lib.ptr(op.vals64),
+                                                      op.nnz, 0, _lib.stream()), "assemble mass")
+            self.__M = op
+        return self.__M
+
+    @property
+    def K_device(self) -> CsrOperator:
+        if self.needUpdate or self.__K is None:
+            self.Assembly()
+            self.Need_Update(False)
+        return self.__K
+
+    def Get_K_C_M_F(self, problemType=None):
+        """Host scipy copies (K, C, M, F) with the reference's CSR layout (_simu.py:161-175)."""
+        import scipy.sparse as sp
+
+        K = self.K_device.to_scipy()
+        M = self._mass().to_scipy()
+        C = sp.csr_matrix((np.zeros(K.nnz), K.indices, K.indptr), shape=K.shape)
+        F = sp.csr_matrix((K.shape[0], 1))
+        return K, C, M, F
+
+    def Solve(self) -> np.ndarray:
+        """Solve K u = b with the Dirichlet conditions; returns u (host copy)."""
+        op = self.K_device
+        b = self._neumann_vec(self.problemType)
+        self.__u = self._solve_system(op, b, self.problemType)
+        return self.__u.cpu().numpy()
+
+    @property
+    def u_device(self) -> Optional[torch.Tensor]:
+        return self.__u
+
+    @property
+    def displacement(self) -> np.ndarray:
+        if self.__u is None:
+            return np.zeros(self.Ndof())
+        return self.__u.cpu().numpy()
+
+    def Calc_Reaction(self, dofs=None, problemType=None) -> np.ndarray:
+        """K[dofs] @ u (_simu.py:212-260)."""
+        op = self.K_device
+        u = self.__u if self.__u is not None else torch.zeros(self.Ndof(), dtype=torch.float64, device=_dev())
+        _, _, Ku = reaction_energy(op, u, None)
+        Ku = Ku.cpu().numpy()
+        return Ku if dofs is None else Ku[np.asarray(dofs)]
+
+    def Save_Iter(self, iter: Optional[dict] = None) -> dict:
+        it = {} if iter is None else iter
+        it["displacement"] = self.displacement
+        return super().Save_Iter(it)
+
+
+class PhaseField(_Simu):
+    """Staggered phase-field damage (EasyFEA/Simulations/_phasefield.py)."""
+
+    problemType = "damage"
+
+    class ProblemTypes:
+        damage = "damage"
+        elastic = "elastic"
+
+    def __init__(self, mesh: Mesh, model: PhaseFieldModel, folder: str = "", verbosity: bool = False):
+        assert isinstance(model, PhaseFieldModel), "model must be a phase field model"
+        assert model.dim == mesh.dim, "the material and the mesh must have the same dimension"
+        self.__u = None
+        self.__d = None
+        self.__Ku = None
+        self.__Kd = None
+        self.__Fd = None
+        self.__psiP = None
+        self.__psiP_old = None
+        self.__updatedDamage = False
+        self.__updatedDisplacement = False
+        self.__Niter = 0
+        self.__convIter = 0.0
+        super().__init__(mesh, model, verbosity)
+
+    @property
+    def phaseFieldModel(self) -> PhaseFieldModel:
+        return self.model
+
+    @property
+    def model_thickness(self) -> float:
+        return self.model.thickness
+
+    def Get_problemTypes(self) -> list:
+        return ["damage", "elastic"]
+
+    def Get_unknowns(self, problemType=None) -> list:
+        if self._check_pt_raw(problemType) == "damage":
+            return ["d"]
+        return ["x", "y"] if self.dim == 2 else ["x", "y", "z"]
+
+    @staticmethod
+    def _check_pt_raw(problemType):
+        return str(getattr(problemType, "value", problemType)) if problemType is not None else "damage"
+
+    def Get_dof_n(self, problemType=None) -> int:
+        return 1 if self._check_pt_raw(problemType) == "damage" else self.dim
+
+    def Bc_dofs_nodes(self, nodes, unknowns, problemType="elastic") -> np.ndarray:
+        return super().Bc_dofs_nodes(nodes, unknowns, problemType)
+
+    def add_dirichlet(self, nodes, values, unknowns, problemType="elastic", description=""):
+        return super().add_dirichlet(nodes, values, unknowns, problemType, description)
+
+    def add_neumann(self, nodes, values, unknowns, problemType="elastic", description=""):
+        return super().add_neumann(nodes, values, unknowns, problemType, description)
+
+    def add_surfLoad(self, nodes, values, unknowns, problemType="elastic", description=""):
+        return super().add_surfLoad(nodes, values, unknowns, problemType, description)
+
+    def add_lineLoad(self, nodes, values, unknowns, problemType="elastic", description=""):
+        return super().add_lineLoad(nodes, values, unknowns, problemType, description)
+
+    def Need_Update(self, value: bool = True) -> None:
+        super().Need_Update(value)
+        self.__updatedDamage = not value
+        self.__updatedDisplacement = not value
+
+    # ---- state ---------------------------------------------------------------
+    def _state(self):
+        if self.__u is None:
+            self.__u = torch.zeros(self.mesh.Nn * self.dim, dtype=torch.float64, device=_dev())
+            self.__d = torch.zeros(self.mesh.Nn, dtype=torch.float64, device=_dev())
+        return self.__u, self.__d
+
+    @property
+    def displacement(self) -> np.ndarray:
+        return self._state()[0].cpu().numpy()
+
+    @property
+    def damage(self) -> np.ndarray:
+        return self._state()[1].cpu().numpy()
+
+    @property
+    def u_device(self) -> torch.Tensor:
+        return self._state()[0]
+
+    @property
+    def d_device(self) -> torch.Tensor:
+        return self._state()[1]
+
+    @property
+    def psiP_device(self) -> Optional[torch.Tensor]:
+        return self.__psiP
+
+    def _params(self) -> _lib.PfParams:
+        m = self.phaseFieldModel
+        mat = m.material
+        p = _lib.PfParams()
+        p.version = _lib.ABI_VERSION
+        p.split = _lib.SPLIT_CODE[m.split]
+        p.regularization = _lib.REGU_CODE[m.regularization]
+        p.dim = self.dim
+        p.lambda_ = float(mat.get_lambda())
+        p.mu = float(mat.get_mu())
+        p.Gc = m.Gc
+        p.l0 = m.l0
+        p.thickness = m.thickness if self.dim == 2 else 1.0
+        A = np.asarray(m.A, dtype=float).reshape(self.dim, self.dim)
+        for i in range(self.dim * self.dim):
+            p.A[i] = A.ravel()[i]
+        C = mat.C.ravel()
+        for i in range(C.size):
+            p.C[i] = C[i]
+        p.k_res = 1e-12
+        return p
+
+    # ---- assembly ----------------------------------------------------------
+    def _assemble_damage(self):
+        """Kd, Fd and psi+ with the History max (_phasefield.py:494-573)."""
+        dm = self.dmesh
+        u, _ = self._state()
+        g = dm.main
+        from .mesh import NPG, MatrixType
+
+        nPg = NPG[(g.elemType, MatrixType.mass)]
+        if self.__Kd is None:
+            self.__Kd = CsrOperator(dm, 1)
+            self.__Fd = torch.zeros(self.mesh.Nn, dtype=torch.float64, device=_dev())
+            self.__psiP = torch.zeros(g.Ne * nPg, dtype=torch.float64, device=_dev())
+        self.__Kd.vals64.zero_()
+        self.__Fd.zero_()
+        p = self._params()
+        H_old = self.__psiP_old
+        _lib.check(_lib.load().gfea_pf_damage(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                              _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(u),
+                                              __import__("ctypes").byref(p), _lib.ptr(H_old),
+                                              _lib.ptr(self.__psiP), _lib.ptr(self.__Kd.vals64),
+                                              _lib.ptr(self.__Fd), _lib.stream()), "phase-field damage")
+        self.__updatedDamage = True
+
+    def _assemble_elastic(self):
+        """Degraded stiffness g(d) cP + cM (_phasefield.py:444-482)."""
+        dm = self.dmesh
+        u, d = self._state()
+        g = dm.main
+        if self.__Ku is None:
+            self.__Ku = CsrOperator(dm, self.dim)
+        self.__Ku.vals64.zero_()
+        p = self._params()
+        _lib.check(_lib.load().gfea_pf_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                               _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(u), _lib.ptr(d),
+                                               __import__("ctypes").byref(p), _lib.F64,
+                                               _lib.ptr(self.__Ku.vals64), _lib.stream()), "phase-field elastic")
+        self.__updatedDisplacement = True
+
+    def Get_K_C_M_F(self, problemType=None):
+        import scipy.sparse as sp
+
+        pt = self._check_pt_raw(problemType) if problemType is not None else "elastic"
+        if pt == "elastic":
+            if not self.__updatedDisplacement or self.__Ku is None:
+                self._assemble_elastic()
+            K = self.__Ku.to_scipy()
+            return K, sp.csr_matrix(K.shape), sp.csr_matrix(K.shape), sp.csr_matrix((K.shape[0], 1))
+        if not self.__updatedDamage or self.__Kd is None:
+            self._assemble_damage()
+        K = self.__Kd.to_scipy()
+        F = sp.csr_matrix(self.__Fd.cpu().numpy().reshape(-1, 1))
+        return K, sp.csr_matrix(K.shape), sp.csr_matrix(K.shape), F
+
+    # ---- staggered scheme (_phasefield.py:303-432) ----------------------------
+    def _energy(self, op, x, dofs=None):
+        return reaction_energy(op, x, None)[1]
+
+    def Solve(self, tolConv: float = 1.0, maxIter: int = 500, convOption: int = 2):
+        assert 0 < tolConv <= 1, "tolConv must be between 0 and 1."
+        assert maxIter > 1, "Must be > 1."
+        assert convOption in (0, 1, 2, 3), "convOption must be 0, 1, 2 or 3"
+        u, d = self._state()
+        old_damage = d.clone()
+        Niter = 0
+        converged = False
+        convIter = 0.0
+        fu = self._neumann_vec("elastic")
+        while not converged and Niter < maxIter:
+            Niter += 1
+            d_n = d.clone()
+            u_n = u.clone()
+            if convOption in (1, 2):
+                E_n = self._psi_crack()
+                if convOption == 2:
+                    E_n += self._psi_elas() - self._psi_ext(fu)
+            # damage
+            self._assemble_damage()
+            bd = self.__Fd + self._neumann_vec("damage")
+            d_new = self._solve_system(self.__Kd, bd, "damage", x0=d)
+            d.copy_(d_new)
+            self.__updatedDisplacement = False
+            # displacement
+            self._assemble_elastic()
+            u_new = self._solve_system(self.__Ku, fu, "elastic", x0=u)
+            u.copy_(u_new)
+            self.__updatedDamage = False
+            if convOption == 0:
+                convIter = max_abs_diff(d, d_n)
+            elif convOption in (1, 2):
+                E_np1 = self._psi_crack()
+                if convOption == 2:
+                    E_np1 += self._psi_elas() - self._psi_ext(fu)
+                convIter = abs(E_n - E_np1) if E_np1 == 0 else abs((E_n - E_np1) / E_np1)
+            else:
+                diffU = (u - u_n).abs()
+                nz = u != 0
+                diffU[nz] = diffU[nz] / u[nz].abs()
+                diffD = (d - d_n).abs()
+                nz = d != 0
+                diffD[nz] = diffD[nz] / d[nz].abs()
+                convU = float(diffU.sum())
+                convD = float(diffD.sum())
+                convIter = max(convD, convU)
+            dmax = float(d.max())
+            if tolConv == 1 or dmax == 0:
+                converged = True
+            elif convOption == 3:
+                converged = (convD <= tolConv) and (convU <= tolConv * 0.999)
+            else:
+                converged = convIter <= tolConv
+        if self.phaseFieldModel.solver == "HistoryDamage":
+            torch.maximum(d, old_damage, out=d)
+        self.__Niter = Niter
+        self.__convIter = convIter
+        return u.cpu().numpy(), d.cpu().numpy(), converged
+
+    def _psi_crack(self) -> float:
+        if not self.__updatedDamage or self.__Kd is None:
+            self._assemble_damage()
+        return self._energy(self.__Kd, self._state()[1])
+
+    def _psi_elas(self) -> float:
+        if not self.__updatedDisplacement or self.__Ku is None:
+            self._assemble_elastic()
+        return self._energy(self.__Ku, self._state()[0])
+
+    def _psi_ext(self, fu: torch.Tensor) -> float:
+        return float(torch.dot(self._state()[0], fu))
+
+    @property
+    def Niter(self) -> int:
+        return self.__Niter
+
+    def Save_Iter(self, iter: Optional[dict] = None) -> dict:
+        """Commit the History field (_phasefield.py:613-630) and store u, d."""
+        it = {} if iter is None else iter
+        it["Niter"] = self.__Niter
+        it["convIter"] = self.__convIter
+        if self.phaseFieldModel.solver == "History" and self.__psiP is not None:
+            if self.__psiP_old is None:
+                self.__psiP_old = self.__psiP.clone()
+            else:
+                self.__psiP_old.copy_(self.__psiP)
+        it["displacement"] = self.displacement
+        it["damage"] = self.damage
+        return super().Save_Iter(it)
+
+    def Calc_Reaction(self, dofs=None, problemType=None) -> np.ndarray:
+        """Ku[dofs] @ u on the current degraded stiffness (_simu.py:212-260)."""
+        pt = self._check_pt_raw(problemType) if problemType is not None else "damage"
+        if pt == "damage":
+            if self.__Kd is None:
+                self._assemble_damage()
+            op, x = self.__Kd, self._state()[1]
+        else:
+            if self.__Ku is None:
+                self._assemble_elastic()
+            op, x = self.__Ku, self._state()[0]
+        _, _, Ax = reaction_energy(op, x, None)
+        Ax = Ax.cpu().numpy()
+        return Ax if dofs is None else Ax[np.asarray(dofs)]
+
+    def reaction_sum(self, dofs: torch.Tensor) -> float:
+        """sum Ku[dofs] @ u reduced on the device (no host copy of the vector)."""
+        return reaction_energy(self.__Ku, self._state()[0], dofs)[0]

@@ -1,0 +1,243 @@
+/*
+ * gfea.h -- C ABI of libgb300fea.so, the GB300 (sm_103a) finite-element hot
+ * path behind easyfea_gb300's Simulations.Elastic / Simulations.PhaseField.
+ *
+ * Conventions
+ *  - extern "C", plain pointers and sizes, no C++ types across the boundary.
+ *  - Every array argument is a DEVICE pointer (caller-owned, e.g. a torch
+ *    tensor's data_ptr()) unless its name ends in _host.
+ *  - Every entry point returns an int status (GFEA_OK == 0); nothing throws.
+ *  - The library allocates no device memory: scratch comes from caller
+ *    buffers sized by the matching *_workspace_size query.
+ *  - All work is enqueued on the given stream; calls that return values to
+ *    the host (counts, PCG results) synchronise that stream.
+ *
+ * Data layout (DOF numbering node*dof_n + component, EasyFEA/FEM/_group_elem.py:346-380):
+ *  - coord   double[Nn*3]           node coordinates (x, y, z)
+ *  - connect int32[Ne*nPe]          element connectivity, reference node order
+ *  - node graph: node_ptr int32[Nn+1], nbr int32[node_ptr[Nn]] -- sorted
+ *    neighbour nodes of every node (nodes sharing an element, itself included)
+ *  - rank    uint8[Ne*nPe*nPe]      position of connect[e,q] in the neighbour
+ *    list of connect[e,p]; the CSR slot of element entry (p,i,q,j) is
+ *    indptr[dof_n*a+i] + dof_n*rank + j with a = connect[e,p]
+ *  - CSR values are laid out exactly as scipy's canonical CSR of the
+ *    reference (sorted column indices, one slot per coupled DOF pair):
+ *    row (a,i) starts at dof_n^2*node_ptr[a] + i*dof_n*nnb(a).
+ */
+#ifndef GFEA_H
+#define GFEA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFEA_ABI_VERSION 1
+
+/* status codes */
+#define GFEA_OK 0
+#define GFEA_ERR_ARG 1          /* invalid argument / size                       */
+#define GFEA_ERR_CUDA 2         /* a CUDA runtime call failed                    */
+#define GFEA_ERR_CAPACITY 3     /* a node has more neighbours than supported     */
+#define GFEA_ERR_SINGULAR 4     /* zero / singular diagonal block                */
+#define GFEA_ERR_NOT_CONVERGED 5/* PCG reached max_iters                         */
+#define GFEA_ERR_BREAKDOWN 6    /* PCG p.Ap <= 0 (matrix not SPD on unknowns)    */
+#define GFEA_ERR_NAN 7          /* non-finite value met                          */
+#define GFEA_ERR_WORKSPACE 8    /* workspace too small                           */
+
+/* element codes */
+#define GFEA_SEG2 0
+#define GFEA_TRI3 1
+#define GFEA_QUAD4 2
+#define GFEA_QUAD9 3
+#define GFEA_HEXA8 4
+
+/* value types */
+#define GFEA_F64 0
+#define GFEA_F32 1
+
+/* phase-field splits and regularisations (EasyFEA/Models/_phasefield.py:41-70) */
+#define GFEA_SPLIT_BOURDIN 0
+#define GFEA_SPLIT_AMOR 1
+#define GFEA_SPLIT_MIEHE 2
+#define GFEA_AT1 0
+#define GFEA_AT2 1
+
+const char* gfea_version(void);
+const char* gfea_status_string(int status);
+
+/* ------------------------------------------------------------------------
+ * Sparsity pattern.  Replaces _Simu.__Get_csr_map (EasyFEA/Simulations/
+ * _simu.py:1062-1102) and _GroupElem.Get_rows_e/Get_columns_e
+ * (EasyFEA/FEM/_group_elem.py:382-402): the node graph and the element slot
+ * ranks are built on the device; indptr/indices equal scipy's canonical
+ * pattern bit for bit.
+ * ---------------------------------------------------------------------- */
+int gfea_graph_workspace_size(int64_t n_nodes, int64_t n_elems, int nPe, size_t* bytes_host);
+/* pass 1: node_ptr[Nn+1] (exclusive scan of neighbour counts); also copies
+ * node_ptr[Nn] (number of node pairs) to *n_pairs_host. */
+int gfea_graph_count(const int32_t* connect, int64_t n_elems, int nPe, int64_t n_nodes,
+                     int32_t* node_ptr, int64_t* n_pairs_host, void* work, size_t work_bytes,
+                     void* stream);
+/* pass 2 (same workspace, untouched since pass 1): nbr[n_pairs], rank[Ne*nPe*nPe] */
+int gfea_graph_fill(const int32_t* connect, int64_t n_elems, int nPe, int64_t n_nodes,
+                    const int32_t* node_ptr, int32_t* nbr, uint8_t* rank, void* work,
+                    size_t work_bytes, void* stream);
+/* DOF-level CSR pattern for dof_n components per node: indptr[Nn*dof_n+1] (int64),
+ * indices[dof_n^2 * n_pairs] (int32). */
+int gfea_csr_pattern(const int32_t* node_ptr, const int32_t* nbr, int64_t n_nodes, int dof_n,
+                     int64_t* indptr, int32_t* indices, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Element operators fused with the CSR scatter.
+ * ---------------------------------------------------------------------- */
+/* K = sum_e sum_pg wJ B^T C B * factor into CSR values (rigi Gauss points).
+ * Replaces Bilinear.LinearizedElasticity (EasyFEA/FEM/Operators/Bilinear.py:62-79)
+ * with _GroupElem.Get_F_e_pg .. Get_leftDispPart_e_pg (EasyFEA/FEM/
+ * _group_elem.py:833-1333), Elastic.Construct_local_matrix_system's K part
+ * (EasyFEA/Simulations/_elastic.py:123-152) and _Simu.__Assemble_csr's
+ * bincount (EasyFEA/Simulations/_simu.py:989-1060).
+ * C: Kelvin-Mandel (3x3 in 2D, 6x6 in 3D), c_per_elem = 0 homogeneous,
+ * 1 per element (Ne x n x n, Models/_utils.py:69-108).
+ * values (value_type GFEA_F64/F32, n_values = dof_n^2 * n_pairs entries) are
+ * zeroed first unless accumulate != 0. */
+int gfea_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                          const int32_t* node_ptr, const uint8_t* rank, const double* C,
+                          int c_per_elem, double factor, int value_type, void* values,
+                          int64_t n_values, int accumulate, void* stream);
+
+/* M = sum_e sum_pg rho wJ N^T N * factor (mass Gauss points, dof_n components).
+ * Replaces Bilinear.UV (EasyFEA/FEM/Operators/Bilinear.py:42-59) as used by
+ * EasyFEA/Simulations/_elastic.py:137. */
+int gfea_assemble_mass(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                       const int32_t* node_ptr, const uint8_t* rank, int dof_n, double rho,
+                       double factor, int value_type, void* values, int64_t n_values,
+                       int accumulate, void* stream);
+
+/* Neumann surface / line loads: b[dof] += factor * value_u * sum_pg wJ N
+ * over boundary elements whose every node has node_mask set (mass Gauss
+ * points).  Replaces _Simu.__Bc_Integration_Dim (EasyFEA/Simulations/
+ * _simu.py:2770-2842) for constant values, and the COO summation of
+ * _Solver_Apply_Neumann (:1750-1756). */
+int gfea_surface_load(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                      const uint8_t* node_mask, int dof_n, int n_unknowns,
+                      const int32_t* unknown_idx_host, const double* values_host, double factor,
+                      double* b, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Phase field.
+ * ---------------------------------------------------------------------- */
+typedef struct gfea_pf_params {
+  int32_t version;       /* GFEA_ABI_VERSION */
+  int32_t split;         /* GFEA_SPLIT_* */
+  int32_t regularization;/* GFEA_AT1 / GFEA_AT2 */
+  int32_t dim;           /* 2 or 3 */
+  double lambda_, mu;    /* Lame constants (plane-stress lambda in 2D plane stress) */
+  double Gc, l0;
+  double thickness;      /* factor applied to Kd, Fd, Ku (1 in 3D) */
+  double A[9];           /* diffusion tensor, row-major dim x dim (identity by default) */
+  double C[36];          /* Kelvin-Mandel C, row-major n x n (used by the Bourdin split) */
+  double k_res;          /* residual stiffness of g(d), 1e-12 in the reference */
+} gfea_pf_params;
+
+/* Damage system at the current displacement: strain at mass Gauss points,
+ * split, psi+ with the History max against H_old (NULL = none), r/f/k,
+ * Kd = int r N^T N + int k grad N . A grad N, Fd = int f N (x thickness).
+ * Replaces PhaseField.__Construct_Damage_Matrix and __Calc_psiPlus_e_pg
+ * (EasyFEA/Simulations/_phasefield.py:494-573) with Models.PhaseField
+ * Calc_psi_e_pg / Calc_C / Get_r_e_pg / Get_f_e_pg / k
+ * (EasyFEA/Models/_phasefield.py:237-571, :751-1243).
+ * H_new (Ne x nPg_mass) receives psi+ after the max; Kd values (dof_n 1
+ * pattern) and Fd (Nn) are zeroed first. */
+int gfea_pf_damage(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                   const int32_t* node_ptr, const uint8_t* rank, const double* u,
+                   const gfea_pf_params* params_host, const double* H_old, double* H_new,
+                   double* Kd_values, double* Fd, void* stream);
+
+/* Degraded displacement stiffness: strain at rigi Gauss points, split,
+ * g = (1 - N.d)^2 + k_res, c = g cP + cM, K = int B^T c B (x thickness).
+ * Replaces PhaseField.__Construct_Elastic_Matrix (EasyFEA/Simulations/
+ * _phasefield.py:444-482) and Get_g_e_pg (EasyFEA/Models/_phasefield.py:295-317). */
+int gfea_pf_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                    const int32_t* node_ptr, const uint8_t* rank, const double* u, const double* d,
+                    const gfea_pf_params* params_host, int value_type, void* values, void* stream);
+
+/* psi+ / psi- and cP / cM of given strains (Ne*nPg rows of n KM components):
+ * Models.PhaseField.Calc_C + Calc_psi_e_pg (EasyFEA/Models/_phasefield.py:335-571).
+ * Any of cP, cM, psiP, psiM may be NULL. */
+int gfea_pf_split(const double* eps, int64_t n_points, const gfea_pf_params* params_host,
+                  double* cP, double* cM, double* psiP, double* psiM, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Sparse SPD solve.  Replaces Solvers.__Solver_1 (EasyFEA/Simulations/
+ * Solvers.py:502-553: Dirichlet elimination) and _Solve_Axb's spsolve
+ * (Solvers.py:361-362) by block-Jacobi PCG on the masked operator
+ * P A P + (I - P), P = diag(unknown), which equals the reference's reduced
+ * system A_ii x_i = b_i - A_ic x_c.
+ * ---------------------------------------------------------------------- */
+typedef struct gfea_system {
+  int32_t version;          /* GFEA_ABI_VERSION */
+  int32_t dof_n;            /* components per node (1, 2, 3) */
+  int64_t n_nodes;
+  int64_t n_pairs;          /* node_ptr[n_nodes] */
+  const int32_t* node_ptr;  /* node graph */
+  const int32_t* nbr;
+  const double* vals64;     /* CSR values, FP64 (may be NULL for FP32-only use) */
+  const float* vals32;      /* CSR values, FP32 (may be NULL for FP64-only use) */
+  const uint8_t* known;     /* per-DOF Dirichlet mask (1 = known) */
+} gfea_system;
+
+typedef struct gfea_pcg_opts {
+  int32_t version;          /* GFEA_ABI_VERSION */
+  int32_t precision;        /* GFEA_F64: FP64 PCG; GFEA_F32: FP32 inner PCG + FP64 refinement */
+  int32_t max_iters;        /* total PCG iteration cap */
+  int32_t check_every;      /* host convergence check period (iterations) */
+  double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)|| */
+  double inner_rtol;        /* FP32 inner solve reduction per refinement step */
+  int32_t max_refine;       /* refinement steps cap (mixed precision) */
+  int32_t lanes;            /* SpMV lanes per node (0 = automatic) */
+} gfea_pcg_opts;
+
+typedef struct gfea_pcg_result {
+  int32_t status;           /* GFEA_OK or an error code */
+  int32_t iterations;       /* PCG iterations performed (all refinement steps) */
+  int32_t refinements;      /* outer FP64 residual evaluations (mixed precision) */
+  int32_t pad;
+  double rel_residual;      /* final FP64 ||P(b - A x)|| / ||P(b - A x_c)|| */
+} gfea_pcg_result;
+
+/* y = A x (unmasked), value_type selects vals64/x,y double or vals32/x,y float. */
+int gfea_spmv(const gfea_system* sys_host, int value_type, const void* x, void* y, void* stream);
+
+int gfea_pcg_workspace_size(const gfea_system* sys_host, const gfea_pcg_opts* opts_host,
+                            size_t* bytes_host);
+
+/* x: on entry known DOFs hold their Dirichlet values and unknown DOFs the
+ * initial guess; on exit the solution.  b: full right-hand side. */
+int gfea_pcg_solve(const gfea_system* sys_host, const double* b, double* x,
+                   const gfea_pcg_opts* opts_host, void* work, size_t work_bytes,
+                   gfea_pcg_result* result_host, void* stream);
+
+/* Scratch bytes of the reductions below. */
+size_t gfea_reduce_workspace_size(void);
+
+/* Reductions for Calc_Reaction / Calc_Energy (EasyFEA/Simulations/_simu.py:177-260):
+ * Ax = A x (FP64); out_host[0] = sum_{dofs} (A x)[dof]  (dofs: n_dofs device
+ * indices); out_host[1] = 1/2 x.A x over all DOFs. */
+int gfea_reaction_energy(const gfea_system* sys_host, const double* x, const int64_t* dofs,
+                         int64_t n_dofs, double* Ax, double* out_host, void* work, void* stream);
+
+/* max_i |a_i - b_i| (PhaseField.Solve convOption 0, EasyFEA/Simulations/_phasefield.py:379) */
+int gfea_max_abs_diff(const double* a, const double* b, int64_t n, double* out_host,
+                      void* work, void* stream);
+
+/* FP64 -> FP32 copy of CSR values (mixed-precision operator) */
+int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFEA_H */

@@ -1,0 +1,73 @@
+"""Elastic assembly + solve on the GPU against the reference's outputs."""
+
+import numpy as np
+import pytest
+
+from helpers import csr, mesh_from_golden, row_scaled_err, same_pattern
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_cantilever_240x26"]
+
+
+def run_case(g, precision="fp64", rtol=1e-12):
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import simulations as Simulations
+
+    m = mesh_from_golden(g)
+    dim = m.dim
+    E = g["E"] if g["E"].ndim else float(g["E"])
+    mat = Models.Elastic.Isotropic(dim, E=E, v=float(g["v"]), planeStress=bool(g["planeStress"]),
+                                   thickness=float(g["thickness"]))
+    simu = Simulations.Elastic(m, mat)
+    simu.precision = precision
+    simu.rtol = rtol
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    simu.add_dirichlet(g["left"], [0.0] * dim, unk)
+    simu.add_surfLoad(g["right"], [float(g["loadval"])], [str(g["loaddir"])])
+    u = simu.Solve()
+    return simu, u
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_stiffness_matches_reference(golden, case):
+    g = golden(case)
+    simu, u = run_case(g)
+    n = u.size
+    K, C, M, F = simu.Get_K_C_M_F()
+    Kref = csr(g, "K", n)
+    assert same_pattern(K, Kref), "CSR pattern differs from the reference's"
+    assert row_scaled_err(K, Kref) <= 1e-12
+    assert row_scaled_err(M, csr(g, "M", n)) <= 1e-12
+    b = simu._neumann_vec("elastic").cpu().numpy()
+    np.testing.assert_allclose(b, g["b"], rtol=1e-12, atol=1e-13 * np.abs(g["b"]).max())
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_displacement_matches_reference_direct_solve(golden, case):
+    g = golden(case)
+    simu, u = run_case(g)
+    uref = g["u"]
+    err = np.max(np.abs(u - uref)) / np.max(np.abs(uref))
+    assert simu.last_solve.rel_residual <= 1e-12
+    assert err <= 1e-8, f"relative displacement error {err:.3e}"
+
+
+@pytest.mark.parametrize("case", ["el_quad4", "el_hexa8", "el_cantilever_240x26"])
+def test_mixed_precision_matches_fp64(golden, case):
+    g = golden(case)
+    simu, u = run_case(g, precision="mixed", rtol=1e-12)
+    err = np.max(np.abs(u - g["u"])) / np.max(np.abs(g["u"]))
+    assert simu.last_solve.rel_residual <= 1e-12
+    assert simu.last_solve.refinements >= 2
+    assert err <= 1e-8, f"relative displacement error {err:.3e}"
+
+
+def test_reaction_balances_load(golden):
+    """Sum of reactions at the clamp equals minus the applied load."""
+    g = golden("el_quad4")
+    simu, u = run_case(g)
+    dofs = simu.Bc_dofs_nodes(g["left"], ["y"])
+    R = np.sum(simu.Calc_Reaction(dofs))
+    total = float(g["loadval"]) * 13.0 * float(g["thickness"])
+    assert abs(R + total) <= 1e-8 * abs(total)

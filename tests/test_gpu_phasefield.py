@@ -1,0 +1,62 @@
+"""Phase-field damage system, degraded stiffness and staggered loop on the GPU
+against the reference's outputs."""
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import csr, mesh_from_golden, row_scaled_err, same_pattern
+
+pytestmark = pytest.mark.gpu
+
+
+def make_simu(g, planeStress=None):
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import simulations as Simulations
+
+    m = mesh_from_golden(g)
+    ps = bool(g["planeStress"]) if planeStress is None else planeStress
+    mat = Models.Elastic.Isotropic(m.dim, E=float(g["E"]), v=float(g["v"]), planeStress=ps, thickness=1.0)
+    pfm = Models.PhaseField(mat, str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    return m, Simulations.PhaseField(m, pfm)
+
+
+@pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2"])
+def test_state_systems_match_reference(golden, case):
+    g = golden(case)
+    m, simu = make_simu(g, planeStress=False)
+    simu.u_device.copy_(torch.as_tensor(g["u"]))
+    simu.d_device.copy_(torch.as_tensor(g["d"]))
+    Kd, _, _, Fd = simu.Get_K_C_M_F("damage")
+    Kref = csr(g, "Kd", m.Nn)
+    assert same_pattern(Kd, Kref)
+    assert row_scaled_err(Kd, Kref) <= 1e-12
+    Fd = np.asarray(Fd.todense()).ravel()
+    np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-10, atol=1e-12 * np.abs(g["Fd"]).max())
+    H = simu.psiP_device.cpu().numpy().reshape(g["H"].shape)
+    np.testing.assert_allclose(H, g["H"], rtol=1e-10, atol=1e-12 * np.abs(g["H"]).max())
+    Ku = simu.Get_K_C_M_F("elastic")[0]
+    Kuref = csr(g, "Ku", m.Nn * m.dim)
+    assert same_pattern(Ku, Kuref)
+    assert row_scaled_err(Ku, Kuref) <= 1e-12
+
+
+@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2"])
+def test_staggered_loop_matches_reference(golden, case):
+    g = golden(case)
+    m, simu = make_simu(g)
+    dim = m.dim
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    top_dofs = torch.as_tensor(g["top_dofs"], device="cuda")
+    for k in range(1, g["u"].shape[0] + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(g["notch"], [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(g["bottom"], [0.0] * dim, unk)
+        simu.add_dirichlet(g["top"], [0.0, k * float(g["dU"])] + ([0.0] if dim == 3 else []), unk)
+        u, d, conv = simu.Solve(float(g["tol"]), int(g["maxIter"]), convOption=0)
+        simu.Save_Iter()
+        F = simu.reaction_sum(top_dofs)
+        assert simu.Niter == g["Niter"][k - 1], f"step {k}: {simu.Niter} staggered iterations, reference {g['Niter'][k - 1]}"
+        assert np.max(np.abs(d - g["d"][k - 1])) <= 1e-6, f"step {k}"
+        assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-6 * np.abs(g["u"][k - 1]).max(), f"step {k}"
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"

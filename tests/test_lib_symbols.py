@@ -1,0 +1,49 @@
+"""The C-ABI library builds, loads and exports every entry point declared in
+include/gfea.h (no compute calls: runs without a GPU)."""
+
+import os
+import re
+
+from easyfea_gb300 import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names.update(re.findall(r"\b(gfea_\w+)\s*\(", src))
+    return sorted(names)
+
+
+def test_library_exports_all_declared_symbols():
+    path = _build.build()
+    lib = _lib.load(path)
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # every declared symbol has a ctypes signature and vice versa
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+def test_host_only_entry_points():
+    import ctypes
+
+    lib = _lib.load()
+    assert lib.gfea_version().startswith(b"gfea")
+    assert lib.gfea_status_string(0) == b"ok"
+    ws = ctypes.c_size_t()
+    assert lib.gfea_graph_workspace_size(100, 50, 4, ctypes.byref(ws)) == 0 and ws.value > 0
+    assert lib.gfea_graph_workspace_size(100, 50, 0, ctypes.byref(ws)) == 1  # invalid nPe
+    sysd = _lib.System(_lib.ABI_VERSION, 2, 10, 30, 0, 0, 0, 0, 0)
+    opts = _lib.PcgOpts(_lib.ABI_VERSION, _lib.F64, 100, 10, 1e-10, 1e-4, 10, 0)
+    assert lib.gfea_pcg_workspace_size(ctypes.byref(sysd), ctypes.byref(opts), ctypes.byref(ws)) == 0
+    assert ws.value > 20 * 8
+    # argument checks fail loudly before touching the device
+    res = _lib.PcgResult()
+    assert lib.gfea_pcg_solve(ctypes.byref(sysd), 0, 0, ctypes.byref(opts), 0, 0, ctypes.byref(res), 0) == 1
+    assert lib.gfea_reduce_workspace_size() > 0

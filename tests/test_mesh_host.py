@@ -1,0 +1,98 @@
+"""Mesh generators and host-side boundary-condition bookkeeping (CPU only)."""
+
+import numpy as np
+import pytest
+
+from easyfea_gb300 import mesh as gmesh
+from oracle import fem
+
+
+@pytest.mark.parametrize("make,area", [
+    (lambda: gmesh.Mesh_Quad4_Rect(120.0, 13.0, 24, 4), 120 * 13),
+    (lambda: gmesh.Mesh_Tri3_Rect(1.0, 1.0, 8, 8), 1.0),
+    (lambda: gmesh.Mesh_Quad9_Rect(3.0, 2.0, 4, 3), 6.0),
+    (lambda: gmesh.Mesh_Hexa8_Box(3.0, 2.0, 1.0, 4, 3, 2), 6.0),
+])
+def test_generators_positive_jacobian_and_measure(make, area):
+    """Sum of wJ equals the domain measure (tests/FEM/mesh_test.py:135-149 of the reference)."""
+    m = make()
+    geo = fem.Geometry(m.elemType.value, m.coord, np.asarray(m.connect), "rigi")
+    assert np.all(fem.det(geo.F) > 0), "elements must be positively oriented"
+    assert abs(geo.wJ.sum() - area) <= 1e-11 * area
+
+
+def test_boundary_groups_cover_the_boundary():
+    m = gmesh.Mesh_Quad4_Rect(2.0, 1.0, 4, 2)
+    seg = m.Get_list_groupElem(1)[0]
+    assert seg.Ne == 2 * (4 + 2)
+    h = gmesh.Mesh_Hexa8_Box(2.0, 1.0, 1.0, 4, 2, 2)
+    faces = h.Get_list_groupElem(2)[0]
+    assert faces.Ne == 2 * (4 * 2 + 4 * 2 + 2 * 2)
+    assert h.orphanNodes.size == 0
+
+
+def test_assembly_e_layout():
+    """Element DOF map node*dof_n + d (EasyFEA/FEM/_group_elem.py:346-380)."""
+    m = gmesh.Mesh_Quad4_Rect(1.0, 1.0, 2, 2)
+    a = m.groupElem.Get_assembly_e(2)
+    np.testing.assert_array_equal(a, fem.assembly_e(np.asarray(m.connect), 2))
+
+
+def test_get_elements_nodes_exclusively():
+    m = gmesh.Mesh_Quad4_Rect(2.0, 1.0, 2, 1)
+    seg = m.Get_list_groupElem(1)[0]
+    right = m.Nodes_Conditions(lambda x, y, z: x == 2.0)
+    els = seg.Get_Elements_Nodes(right)
+    assert els.size == 1
+    assert set(seg.connect[els[0]]) <= set(right)
+
+
+def test_dirichlet_bookkeeping_sums_duplicates():
+    """Duplicate Dirichlet DOFs add up (EasyFEA/Simulations/_simu.py:3013-3040)."""
+    import types
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300.simulations import Elastic
+
+    m = gmesh.Mesh_Quad4_Rect(2.0, 1.0, 2, 1)
+    mat = Models.Elastic.Isotropic(2, E=1.0, v=0.3)
+    simu = Elastic.__new__(Elastic)
+    # host bookkeeping only (no device): initialise the pieces Bc_* use
+    simu.mesh = m
+    simu._Elastic__K = None
+    simu.model = mat
+    simu.Bc_Init()
+    left = m.Nodes_Conditions(lambda x, y, z: x == 0)
+    simu.add_dirichlet(left, [1.0, 0.0], ["x", "y"])
+    simu.add_dirichlet(left, [lambda x, y, z: y], ["x"])
+    known, unknown = simu.Bc_dofs_known_unknown("elastic")
+    np.testing.assert_array_equal(known, np.sort(np.concatenate([left * 2, left * 2 + 1])))
+    xk = np.zeros(m.Nn * 2)
+    for bc in simu._dirichlet["elastic"]:
+        np.add.at(xk, bc.dofs, bc.values)
+    np.testing.assert_allclose(xk[left * 2], 1.0 + m.coord[left, 1])
+    assert isinstance(types, object)
+
+
+def test_model_observers_trigger_update():
+    from easyfea_gb300 import Models
+
+    class Obs:
+        n = 0
+
+        def _Update(self, o):
+            self.n += 1
+
+    mat = Models.Elastic.Isotropic(2, E=210000.0, v=0.3)
+    o = Obs()
+    mat._Add_observer(o)
+    mat.E = 100000.0
+    mat.v = 0.25
+    assert o.n == 2
+    pfm = Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.01)
+    o2 = Obs()
+    pfm._Add_observer(o2)
+    mat.E = 1.0
+    pfm.Gc = 1.0
+    assert o2.n == 2
+    np.testing.assert_allclose(mat.C, fem.isotropic_C(1.0, 0.25, 2, True))

@@ -67,6 +67,7 @@ class PcgResult(ctypes.Structure):
         ("refinements", c_int32),
         ("pad", c_int32),
         ("rel_residual", c_double),
+        ("floor_rel", c_double),
     ]
 
 

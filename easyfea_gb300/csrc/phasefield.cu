@@ -5,10 +5,16 @@
 // 396-571) in FP64 registers: Bourdin, Amor (:451-483) and Miehe with the
 // closed-form eigenprojectors of :751-1041 (2D :777-807, 3D Q.-C. He form with
 // the Lode-angle cases :809-948) and the projector assembly of :1043-1243.
-// Two deliberate differences from the reference, both at points where it
-// returns NaN: the 3D arccos argument is clipped to [-1, 1] and the 2D
-// discriminant / 3D invariant g to >= 0 (rounding can push them past the
-// bound at repeated eigenvalues).
+// The reference picks its repeated-eigenvalue branches with exact equality
+// tests (v1 == v2, g == 0, theta == 0 or pi/3).  Those tests depend on the
+// last bit of the computed invariants: with fused multiply-adds, or a 1-ulp
+// difference in pow, a repeated eigenvalue comes out as a gap of 1e-16 and
+// the distinct-eigenvalue formulas then divide rounding noise by rounding
+// noise (the reference itself returns NaN at some of these points, when the
+// arccos argument rounds past +-1).  Here the branches are chosen with small
+// relative tolerances instead (kEigTol*): identical to the reference wherever
+// its branch choice is exact or its formulas are well conditioned, accurate
+// in the band of eigenvalue gaps below ~1e-7 where they are not.
 
 #include <math.h>
 
@@ -18,6 +24,10 @@ namespace gfea {
 namespace {
 
 constexpr double kSqrt2 = 1.41421356237309504880;
+// repeated-eigenvalue tolerances: 2D discriminant and 3D invariant g relative to
+// the squared Frobenius norm; 3D arccos argument distance to +-1
+constexpr double kEigTolSq = 1e-14;
+constexpr double kEigTolArg = 4e-15;
 
 struct PF {
   int split, regu, dim;
@@ -26,13 +36,13 @@ struct PF {
   double C[36];
 };
 
-__device__ __forceinline__ double heav(double v) { return v > 0 ? 1.0 : (v == 0 ? 0.5 : 0.0); }
-__device__ __forceinline__ double sgn(double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); }
+__host__ __device__ __forceinline__ double heav(double v) { return v > 0 ? 1.0 : (v == 0 ? 0.5 : 0.0); }
+__host__ __device__ __forceinline__ double sgn(double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); }
 
 // c = gP * cP + cM  (n x n, row-major); gP = 1 gives cP + cM.
 // With want_parts, cP and cM are also returned separately.
 template <int D>
-__device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
+__host__ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
   constexpr int n = D == 2 ? 3 : 6;
   const double tr = D == 2 ? eps[0] + eps[1] : eps[0] + eps[1] + eps[2];
   const double Rp = (1 + sgn(tr)) / 2, Rm = (1 + sgn(-tr)) / 2;
@@ -64,11 +74,12 @@ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, do
     const double det = M00 * M11 - M01 * M01;
     const double trM = M00 + M11;
     double delta = trM * trM - 4 * det;
-    if (delta < 0) delta = 0;
+    const bool repeated = delta <= kEigTolSq * (M00 * M00 + M11 * M11 + 2 * M01 * M01);
+    if (repeated) delta = 0;
     const double sd = sqrt(delta);
     const double v1 = (trM - sd) / 2, v2 = (trM + sd) / 2;
     double A00 = 1, A11 = 0, A01 = 0;  // M1
-    if (v1 != v2) {
+    if (!repeated) {
       const double dv = v1 - v2;
       A00 = (M00 - v2) / dv;
       A11 = (M11 - v2) / dv;
@@ -99,7 +110,7 @@ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, do
                       M[0][1] * ((M[1][0] * M[2][2]) - (M[2][0] * M[1][2])) +
                       M[0][2] * ((M[1][0] * M[2][1]) - (M[2][0] * M[1][1]));
     double g = I1 * I1 - 3 * I2;
-    if (g < 0) g = 0;
+    if (g <= kEigTolSq * trMM) g = 0;  // three equal eigenvalues
     const double sg = sqrt(g);
     double arg = 0.5 * (2 * I1 * I1 * I1 - 9 * I1 * I2 + 27 * I3);
     if (g != 0) arg = arg / pow(g, 1.5);
@@ -111,7 +122,7 @@ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, do
     if (g != 0) {
       const double irg = (I1 - sg) / 3;
       const double gm = 1.0 / sqrt(g);
-      if (arg == -1) {  // theta = pi/3: e1 < e2 = e3
+      if (arg <= -1 + kEigTolArg) {  // theta = pi/3: e1 < e2 = e3
         v[0] += -2.0 / 3 * sg; v[1] += 1.0 / 3 * sg; v[2] += 1.0 / 3 * sg;
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) {
@@ -119,7 +130,7 @@ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, do
           }
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) M3[i][j] = 0.5 * ((i == j ? 1.0 : 0.0) - M1[i][j]);
-      } else if (arg == 1) {  // theta = 0: e1 = e2 < e3
+      } else if (arg >= 1 - kEigTolArg) {  // theta = 0: e1 = e2 < e3
         v[0] += -1.0 / 3 * sg; v[1] += -1.0 / 3 * sg; v[2] += 2.0 / 3 * sg;
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) M3[i][j] = gm * (M[i][j] - (i == j ? irg : 0.0));

@@ -32,7 +32,7 @@ constexpr int kThreads = 256;
 constexpr int kMaxBlocks = kSMs * 8;
 
 struct Scal {
-  double rz, rr, pap, alpha, beta, bb, tol2, rr_true;
+  double rz, rr, pap, alpha, beta, bb, tol2, rr_true, absAx;
   int32_t done, iters, status, max_iters;
   uint32_t ticket1, ticket2, ticket3, pad;
 };
@@ -100,8 +100,9 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
 // node-row products
 // ---------------------------------------------------------------------------
 
-// acc[i] = sum over row (a,i) of vals * xf(col); reduced across the G lanes.
-template <int D, int G, typename T, typename A, typename XF>
+// acc[i] = sum over row (a,i) of vals * xf(col) (|vals| * xf with ABS);
+// reduced across the G lanes.
+template <int D, int G, typename T, typename A, bool ABS = false, typename XF>
 __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S, XF xf, A (&acc)[D]) {
   const int32_t p0 = S.node_ptr[a];
   const int32_t W = D * (S.node_ptr[a + 1] - p0);
@@ -113,7 +114,10 @@ __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S,
     const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
     const A xv = xf(col);
 #pragma unroll
-    for (int i = 0; i < D; ++i) acc[i] += (A)__ldg(base + (int64_t)i * W + t) * xv;
+    for (int i = 0; i < D; ++i) {
+      const A v = (A)__ldg(base + (int64_t)i * W + t);
+      acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv;
+    }
   }
 #pragma unroll
   for (int i = 0; i < D; ++i) acc[i] = group_sum<G, A>(acc[i]);
@@ -140,24 +144,25 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SysT<T> S, const T* __re
   }
 }
 
-// r = P (b - A x), rc = P (b - A x_c) (x_c: x on known columns only);
-// partials r.r and rc.rc.  Used for the PCG start and the FP64 refinement.
+// FP64 residual of the reduced system: r = P (b - A x); partials r.r,
+// ||P (b - A x_c)||^2 (x_c: x on known columns only, the reference norm) and
+// ||P |A| |x|||^2 (scale of the rounding floor of r).
 template <int D, int G, typename T>
 __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double* __restrict__ b,
                                                          const double* __restrict__ x, double* __restrict__ r,
-                                                         double* partials, Scal* sc, int mode) {
-  // mode 0: PCG start (sets bb, rr); mode 1: refinement residual (sets rr_true, keeps bb unless zero)
+                                                         double* partials, Scal* sc) {
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
   const int64_t Nn = S.Nn;
-  double v[2] = {0, 0};
+  double v[3] = {0, 0, 0};
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    double all[D], kn[D];
+    double all[D], kn[D], ab[D];
     node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return x[c]; }, all);
     node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return S.known[c] ? x[c] : 0.0; }, kn);
+    node_rows<D, G, T, double, true>(ac, lane, S, [&](int64_t c) { return fabs(x[c]); }, ab);
     if (a < Nn && lane == 0) {
 #pragma unroll
       for (int i = 0; i < D; ++i) {
@@ -165,21 +170,19 @@ __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double
         const bool unk = !S.known[dof];
         const double ri = unk ? b[dof] - all[i] : 0.0;
         const double rci = unk ? b[dof] - kn[i] : 0.0;
+        const double ai = unk ? ab[i] + fabs(b[dof]) : 0.0;
         r[dof] = ri;
         v[0] += ri * ri;
         v[1] += rci * rci;
+        v[2] += ai * ai;
       }
     }
   }
-  double out[2];
-  if (reduce_last<2>(v, partials, &sc->ticket3, out) && threadIdx.x == 0) {
-    if (mode == 0) {
-      sc->rr = out[0];
-      sc->bb = out[1];
-    } else {
-      sc->rr_true = out[0];
-      if (sc->bb == 0) sc->bb = out[1];
-    }
+  double out[3];
+  if (reduce_last<3>(v, partials, &sc->ticket3, out) && threadIdx.x == 0) {
+    sc->rr_true = out[0];
+    sc->bb = out[1];
+    sc->absAx = out[2];
   }
 }
 
@@ -324,6 +327,7 @@ __global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* 
 
 template <typename T>
 __global__ void cast_kernel(const double* __restrict__ s, T* __restrict__ d, int64_t n) {
+  // FP64 -> T copy
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     d[i] = (T)s[i];
 }
@@ -431,15 +435,15 @@ int grid_elems(int64_t n) {
 }
 
 struct PcgWork {
-  void* r; void* z; void* pa; void* pb; void* Ap; void* dinv; void* x32;  // T-typed
-  double* r64;
+  void* r; void* z; void* pa; void* pb; void* Ap; void* dinv; void* dx;  // T-typed (inner solve)
+  double* r64;                                                         // FP64 residual
   double* partials;
   Scal* sc;
   int32_t* flag;
 };
 
 template <typename T>
-size_t pcg_layout(int64_t Nn, int D, bool mixed, PcgWork* w, char* base) {
+size_t pcg_layout(int64_t Nn, int D, PcgWork* w, char* base) {
   size_t off = 0;
   const int64_t N = Nn * D;
   auto take = [&](size_t bytes) {
@@ -455,8 +459,8 @@ size_t pcg_layout(int64_t Nn, int D, bool mixed, PcgWork* w, char* base) {
   w->pb = take(sizeof(T) * N);
   w->Ap = take(sizeof(T) * N);
   w->dinv = take(sizeof(T) * N * D);
-  w->x32 = mixed ? take(sizeof(T) * N) : nullptr;
-  w->r64 = mixed ? reinterpret_cast<double*>(take(sizeof(double) * N)) : nullptr;
+  w->dx = take(sizeof(T) * N);
+  w->r64 = reinterpret_cast<double*>(take(sizeof(double) * N));
   w->partials = reinterpret_cast<double*>(take(sizeof(double) * 4 * kMaxBlocks));
   w->sc = reinterpret_cast<Scal*>(take(sizeof(Scal)));
   w->flag = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * 4));
@@ -500,12 +504,10 @@ SysT<float> sys_t<float>(const gfea_system* s) {
     default: return GFEA_ERR_ARG;                      \
   }
 
-template <typename T>
-int launch_resid(const gfea_system* s, int G, const double* b, const double* x, double* r, PcgWork& w, int mode,
-                 cudaStream_t st) {
-  const SysT<T> S = sys_t<T>(s);
+int launch_resid(const gfea_system* s, int G, const double* b, const double* x, PcgWork& w, cudaStream_t st) {
+  const SysT<double> S = sys_t<double>(s);
   const int grid = grid_nodes(s->n_nodes, G);
-  GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, b, x, r, w.partials, w.sc, mode)));
+  GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -558,6 +560,99 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* hos
   return GFEA_OK;
 }
 
+int fetch(Scal* h, PcgWork& w, cudaStream_t st) {
+  GFEA_CUDA_TRY(cudaMemcpyAsync(h, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  return GFEA_OK;
+}
+
+// Iterative refinement around a T-precision PCG:
+//   r = P(b - A x) in FP64; stop when ||r|| <= max(rtol ||P(b - A x_c)||,
+//   floor), floor = 32 eps64 ||P(|A||x| + |b|)|| (the rounding level of an FP64
+//   residual); else solve A d = r with PCG (T values and vectors, FP64 dots),
+//   x += d, repeat.  FP64 inner solves aim at the target directly and the next
+//   residual corrects the recursive-residual drift; FP32 inner solves reduce the
+//   residual by inner_rtol per step.
+template <typename T>
+int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
+                 size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
+  PcgWork w;
+  if (pcg_layout<T>(s->n_nodes, s->dof_n, &w, static_cast<char*>(work)) > work_bytes) return GFEA_ERR_WORKSPACE;
+  const int G = pick_lanes(s, o->lanes);
+  const int64_t N = s->n_nodes * s->dof_n;
+  const int check = o->check_every > 0 ? o->check_every : 32;
+  const bool fp64 = sizeof(T) == 8;
+  const double eps64 = 2.220446049250313e-16;
+  Scal hs;
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
+  int e = launch_bjacobi<T>(s, w, st);
+  if (e) return e;
+  e = launch_resid(s, G, b, x, w, st);
+  if (e) return e;
+  int32_t flag = 0;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  e = fetch(&hs, w, st);
+  if (e) return e;
+  if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
+  const double bb = hs.bb;
+  if (!(bb == bb) || !isfinite(hs.rr_true)) { res->status = GFEA_ERR_NAN; return GFEA_ERR_NAN; }
+  if (bb == 0) {  // b_i - A_ic x_c = 0: the unknowns are zero
+    zero_unknown_kernel<<<grid_elems(N), kThreads, 0, st>>>(x, s->known, N);
+    GFEA_LAUNCH_CHECK();
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    res->status = GFEA_OK;
+    return GFEA_OK;
+  }
+  double rr = hs.rr_true, rr_prev = 0;
+  int total = 0, stall = 0;
+  const int max_ref = o->max_refine > 0 ? o->max_refine : 30;
+  const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+  res->status = GFEA_ERR_NOT_CONVERGED;
+  for (int k = 0;; ++k) {
+    const double floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;
+    const double tol2 = fmax(o->rtol * o->rtol * bb, floor2);
+    res->rel_residual = sqrt(rr / bb);
+    res->floor_rel = sqrt(floor2 / bb);
+    if (rr <= tol2) { res->status = GFEA_OK; break; }
+    if (k > 0) {
+      stall = rr > 0.25 * rr_prev ? stall + 1 : 0;
+      if (stall >= 3) break;  // refinement no longer reduces the residual
+    }
+    if (k >= max_ref || total >= o->max_iters) break;
+    res->refinements = k + 1;
+    rr_prev = rr;
+    // inner solve A d = r (d = 0 start; known DOFs stay 0)
+    double inner2 = fp64 ? fmax(0.1 * tol2 / rr, 1e-30) : fmax(inner * inner, 0.1 * tol2 / rr);
+    cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.r, N);
+    GFEA_LAUNCH_CHECK();
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(T) * N, st));
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(T) * N, st));
+    e = launch_update<T>(s, w, (T*)w.dx, (T*)w.pa, 1, st);
+    if (e) return e;
+    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, inner2, o->max_iters - total, 1);
+    GFEA_LAUNCH_CHECK();
+    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, &hs, st);
+    if (e) return e;
+    total += hs.iters;
+    if (hs.status == GFEA_ERR_NAN || hs.status == GFEA_ERR_BREAKDOWN) {
+      // breakdown after some progress: keep the correction of the completed iterations
+      if (hs.status == GFEA_ERR_NAN || hs.iters == 0) { res->status = hs.status; break; }
+    }
+    add_correction_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(x, (const T*)w.dx, s->known, N);
+    GFEA_LAUNCH_CHECK();
+    e = launch_resid(s, G, b, x, w, st);
+    if (e) return e;
+    e = fetch(&hs, w, st);
+    if (e) return e;
+    rr = hs.rr_true;
+    if (!isfinite(rr)) { res->status = GFEA_ERR_NAN; break; }
+  }
+  res->iterations = total;
+  return res->status;
+}
+
 }  // namespace
 }  // namespace gfea
 
@@ -586,9 +681,9 @@ extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, vo
 extern "C" int gfea_pcg_workspace_size(const gfea_system* s, const gfea_pcg_opts* o, size_t* bytes) {
   if (!s || !o || !bytes || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3) return GFEA_ERR_ARG;
   if (o->precision == GFEA_F64)
-    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, false, nullptr, nullptr);
+    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, nullptr, nullptr);
   else
-    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, true, nullptr, nullptr);
+    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, nullptr, nullptr);
   return GFEA_OK;
 }
 
@@ -599,116 +694,18 @@ extern "C" int gfea_pcg_solve(const gfea_system* s, const double* b, double* x, 
   if (s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3 || !s->node_ptr || !s->nbr || !s->known || !s->vals64)
     return GFEA_ERR_ARG;
   if (o->max_iters < 1 || !(o->rtol > 0)) return GFEA_ERR_ARG;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int G = pick_lanes(s, o->lanes);
-  const int64_t N = s->n_nodes * s->dof_n;
-  const int check = o->check_every > 0 ? o->check_every : 32;
   res->status = GFEA_OK;
   res->iterations = 0;
   res->refinements = 0;
   res->rel_residual = 0;
-  Scal hs;
-
-  if (o->precision == GFEA_F64) {
-    PcgWork w;
-    if (pcg_layout<double>(s->n_nodes, s->dof_n, false, &w, static_cast<char*>(work)) > work_bytes)
-      return GFEA_ERR_WORKSPACE;
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(double) * N, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(double) * N, st));
-    int e = launch_bjacobi<double>(s, w, st);
-    if (e) return e;
-    e = launch_resid<double>(s, G, b, x, (double*)w.r, w, 0, st);
-    if (e) return e;
-    e = launch_update<double>(s, w, x, (double*)w.pa, 1, st);
-    if (e) return e;
-    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, o->rtol * o->rtol, o->max_iters, 0);
-    GFEA_LAUNCH_CHECK();
-    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-    int32_t flag = 0;
-    GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
-    if (hs.bb == 0) {
-      zero_unknown_kernel<<<grid_elems(N), kThreads, 0, st>>>(x, s->known, N);
-      GFEA_LAUNCH_CHECK();
-      GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-      return GFEA_OK;
-    }
-    if (!hs.done) {
-      e = pcg_loop<double>(s, G, w, x, check, &hs, st);
-      if (e) return e;
-    }
-    res->iterations = hs.iters;
-    res->status = hs.status;
-    // true residual
-    e = launch_resid<double>(s, G, b, x, (double*)w.r, w, 1, st);
-    if (e) return e;
-    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    res->rel_residual = sqrt(hs.rr_true / hs.bb);
-    return res->status;
+  res->floor_rel = 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (o->precision == GFEA_F64) return refine_solve<double>(s, b, x, o, work, work_bytes, res, st);
+  if (o->precision == GFEA_F32) {
+    if (!s->vals32) return GFEA_ERR_ARG;
+    return refine_solve<float>(s, b, x, o, work, work_bytes, res, st);
   }
-
-  if (o->precision != GFEA_F32 || !s->vals32) return GFEA_ERR_ARG;
-  // FP32 inner PCG with FP64 iterative refinement.
-  PcgWork w;
-  if (pcg_layout<float>(s->n_nodes, s->dof_n, true, &w, static_cast<char*>(work)) > work_bytes) return GFEA_ERR_WORKSPACE;
-  GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
-  GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
-  int e = launch_bjacobi<float>(s, w, st);
-  if (e) return e;
-  // FP64 residual of the starting point (sets bb and rr_true)
-  e = launch_resid<double>(s, G, b, x, w.r64, w, 0, st);
-  if (e) return e;
-  GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-  int32_t flag = 0;
-  GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-  if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
-  const double bb = hs.bb;
-  if (bb == 0) {
-    zero_unknown_kernel<<<grid_elems(N), kThreads, 0, st>>>(x, s->known, N);
-    GFEA_LAUNCH_CHECK();
-    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    return GFEA_OK;
-  }
-  double rr = hs.rr;
-  int total = 0;
-  const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
-  const int max_ref = o->max_refine > 0 ? o->max_refine : 20;
-  res->status = GFEA_ERR_NOT_CONVERGED;
-  for (int k = 0; k < max_ref; ++k) {
-    res->refinements = k + 1;
-    res->rel_residual = sqrt(rr / bb);
-    if (rr <= o->rtol * o->rtol * bb) { res->status = GFEA_OK; break; }
-    if (total >= o->max_iters) break;
-    // inner solve A32 d = r64 (d = 0 start, known DOFs 0)
-    cast_kernel<float><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (float*)w.r, N);
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.x32, 0, sizeof(float) * N, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(float) * N, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(float) * N, st));
-    e = launch_update<float>(s, w, (float*)w.x32, (float*)w.pa, 1, st);  // z, rz, rr of r
-    if (e) return e;
-    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, inner * inner, o->max_iters - total, 1);
-    GFEA_LAUNCH_CHECK();
-    e = pcg_loop<float>(s, G, w, (float*)w.x32, check, &hs, st);
-    if (e) return e;
-    total += hs.iters;
-    if (hs.status == GFEA_ERR_NAN || hs.status == GFEA_ERR_BREAKDOWN) { res->status = hs.status; break; }
-    add_correction_kernel<float><<<grid_elems(N), kThreads, 0, st>>>(x, (const float*)w.x32, s->known, N);
-    GFEA_LAUNCH_CHECK();
-    e = launch_resid<double>(s, G, b, x, w.r64, w, 1, st);
-    if (e) return e;
-    GFEA_CUDA_TRY(cudaMemcpyAsync(&hs, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    rr = hs.rr_true;
-  }
-  res->iterations = total;
-  res->rel_residual = sqrt(rr / bb);
-  if (res->status != GFEA_OK && rr <= o->rtol * o->rtol * bb) res->status = GFEA_OK;
-  return res->status;
+  return GFEA_ERR_ARG;
 }
 
 extern "C" size_t gfea_reduce_workspace_size(void) { return sizeof(double) * 4 * kMaxBlocks + 256; }

@@ -138,6 +138,7 @@ class PcgInfo:
     iterations: int
     refinements: int
     rel_residual: float
+    floor_rel: float = 0.0
 
 
 def pcg(op: CsrOperator, b: torch.Tensor, x: torch.Tensor, known: torch.Tensor, rtol: float = 1e-12,
@@ -151,14 +152,15 @@ def pcg(op: CsrOperator, b: torch.Tensor, x: torch.Tensor, known: torch.Tensor, 
         op.ensure_f32()
     sys = op.system(known)
     opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, int(max_iters), int(check_every), float(rtol), float(inner_rtol),
-                        50, int(lanes))
+                        30, int(lanes))
     ws = ctypes.c_size_t()
     _lib.check(L.gfea_pcg_workspace_size(ctypes.byref(sys), ctypes.byref(opts), ctypes.byref(ws)), "pcg workspace")
     work = _workspace(int(ws.value))
     res = _lib.PcgResult()
     st = L.gfea_pcg_solve(ctypes.byref(sys), _lib.ptr(b), _lib.ptr(x), ctypes.byref(opts), _lib.ptr(work),
                           work.numel(), ctypes.byref(res), _lib.stream())
-    info = PcgInfo(int(res.status), int(res.iterations), int(res.refinements), float(res.rel_residual))
+    info = PcgInfo(int(res.status), int(res.iterations), int(res.refinements), float(res.rel_residual),
+                   float(res.floor_rel))
     if raise_on_fail:
         _lib.check(st, f"pcg (iterations {info.iterations}, rel residual {info.rel_residual:.3e})")
     return info

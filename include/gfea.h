@@ -194,7 +194,8 @@ typedef struct gfea_pcg_opts {
   int32_t precision;        /* GFEA_F64: FP64 PCG; GFEA_F32: FP32 inner PCG + FP64 refinement */
   int32_t max_iters;        /* total PCG iteration cap */
   int32_t check_every;      /* host convergence check period (iterations) */
-  double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)|| */
+  double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)||; the solve
+                               stops at max(rtol, rounding floor), see gfea_pcg_result */
   double inner_rtol;        /* FP32 inner solve reduction per refinement step */
   int32_t max_refine;       /* refinement steps cap (mixed precision) */
   int32_t lanes;            /* SpMV lanes per node (0 = automatic) */
@@ -203,9 +204,10 @@ typedef struct gfea_pcg_opts {
 typedef struct gfea_pcg_result {
   int32_t status;           /* GFEA_OK or an error code */
   int32_t iterations;       /* PCG iterations performed (all refinement steps) */
-  int32_t refinements;      /* outer FP64 residual evaluations (mixed precision) */
+  int32_t refinements;      /* inner PCG solves (each followed by an FP64 residual) */
   int32_t pad;
   double rel_residual;      /* final FP64 ||P(b - A x)|| / ||P(b - A x_c)|| */
+  double floor_rel;         /* rounding floor of that residual: 32 eps ||P(|A||x|+|b|)|| / ||P(b - A x_c)|| */
 } gfea_pcg_result;
 
 /* y = A x (unmasked), value_type selects vals64/x,y double or vals32/x,y float. */

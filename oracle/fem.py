@@ -510,16 +510,22 @@ def mat_to_vec(M):
                      M[..., 1, 2] * SQRT2, M[..., 0, 2] * SQRT2, M[..., 0, 1] * SQRT2], -1)
 
 
-def eigen_projectors(eps, clamp=False):
+EIG_TOL_SQ = 1e-14
+EIG_TOL_ARG = 4e-15
+
+
+def eigen_projectors(eps, robust=False):
     """Eigenvalues and eigenprojectors of the strain -- Models/_phasefield.py:751-1041.
 
     2D closed form :777-807; 3D Q.-C. He closed form with the Lode-angle cases
     :809-948 and the Frobenius normalisation of M1, M3 at :944-948.
 
-    The reference evaluates ``arccos`` of an argument that rounding can push just
-    past +-1 at repeated eigenvalues, which yields NaN there.  ``clamp=False``
-    reproduces that; ``clamp=True`` clips the argument to [-1, 1] (the GPU kernels'
-    behaviour), selecting the repeated-eigenvalue branch instead."""
+    The reference chooses its repeated-eigenvalue branches by exact equality
+    (v1 == v2, g == 0, theta == 0 or pi/3), and evaluates ``arccos`` of an
+    argument that rounding can push just past +-1 (NaN there).  ``robust=False``
+    reproduces that exactly; ``robust=True`` is the GPU kernels' rule: branches
+    chosen with the relative tolerances EIG_TOL_SQ (2D discriminant, 3D g) and
+    EIG_TOL_ARG (3D arccos argument to +-1), argument clipped to [-1, 1]."""
     M = vec_to_mat(eps)
     dim = M.shape[-1]
     I = np.zeros_like(M)
@@ -530,6 +536,9 @@ def eigen_projectors(eps, clamp=False):
         D = det(M)
         tr = M[..., 0, 0] + M[..., 1, 1]
         delta = tr**2 - 4 * D
+        if robust:
+            F2 = M[..., 0, 0] ** 2 + M[..., 1, 1] ** 2 + 2 * M[..., 0, 1] ** 2
+            delta = np.where(delta <= EIG_TOL_SQ * F2, 0.0, delta)
         vals = np.zeros(shp + (2,))
         vals[..., 0] = (tr - np.sqrt(delta)) / 2
         vals[..., 1] = (tr + np.sqrt(delta)) / 2
@@ -549,12 +558,16 @@ def eigen_projectors(eps, clamp=False):
     I2 = 0.5 * (I1**2 - (MM[..., 0, 0] + MM[..., 1, 1] + MM[..., 2, 2]))
     I3 = det(M)
     g = I1**2 - 3 * I2
+    if robust:
+        trMM = MM[..., 0, 0] + MM[..., 1, 1] + MM[..., 2, 2]
+        g = np.where(g <= EIG_TOL_SQ * trMM, 0.0, g)
     sg = np.sqrt(g)
     gnz = g != 0
     arg = 0.5 * (2 * I1**3 - 9 * I1 * I2 + 27 * I3)
     arg = np.divide(arg, g ** (3 / 2), out=arg, where=gnz)
-    if clamp:
+    if robust:
         arg = np.clip(arg, -1.0, 1.0)
+        arg = np.where(arg <= -1 + EIG_TOL_ARG, -1.0, np.where(arg >= 1 - EIG_TOL_ARG, 1.0, arg))
     with np.errstate(invalid="ignore"):
         theta = np.arccos(arg) / 3
     v1 = I1 / 3
@@ -607,9 +620,9 @@ def eigen_projectors(eps, clamp=False):
     return vals, [M1, M2, M3]
 
 
-def spectral_projectors(eps, clamp=False):
+def spectral_projectors(eps, robust=False):
     """projP, projM -- Models/_phasefield.py:1043-1243 (__Spectral_Decomposition)."""
-    vals, Ms = eigen_projectors(eps, clamp)
+    vals, Ms = eigen_projectors(eps, robust)
     dim = Ms[0].shape[-1]
     valp = (vals + np.abs(vals)) / 2
     dvalp = np.heaviside(vals, 0.5)
@@ -663,7 +676,7 @@ def IxI(dim):
     return np.outer(I, I)
 
 
-def split_C(eps, split, lmbda, mu, dim, C=None, clamp=False):
+def split_C(eps, split, lmbda, mu, dim, C=None, robust=False):
     """cP, cM -- Models/_phasefield.py:396-571 (Calc_C, Bourdin :433-449,
     Amor :451-483, Rp/Rm :485-501, Miehe :503-540).
 
@@ -685,7 +698,7 @@ def split_C(eps, split, lmbda, mu, dim, C=None, clamp=False):
         cM = bulk[..., None, None] * (Rm[..., None, None] * II)
         return cP, cM
     if split == "Miehe":
-        projP, projM = spectral_projectors(eps, clamp)
+        projP, projM = spectral_projectors(eps, robust)
         cP = lm[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * projP
         cM = lm[..., None, None] * (Rm[..., None, None] * II) + 2 * mm[..., None, None] * projM
         return cP, cM

@@ -50,9 +50,16 @@ def test_split_matches_reference(golden, dim, ps, split):
     n = cP.shape[-1]
     refP = np.broadcast_to(g[key + "_cP"].reshape(-1, n, n), cP.shape)
     refM = np.broadcast_to(g[key + "_cM"].reshape(-1, n, n), cM.shape)
-    bad = np.isnan(refP.reshape(len(cP), -1)).any(1)
-    ok = ~bad
     scale = np.abs(C).max()
+    lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
+    fP, _ = fem.split_C(eps, split, lmbda, mu, dim, C, robust=False)
+    rP, rM = fem.split_C(eps, split, lmbda, mu, dim, C, robust=True)
+    # degenerate rows: the reference returns NaN, or its exact-equality branch
+    # choice at a repeated eigenvalue differs from the tolerance rule
+    bad = np.isnan(refP.reshape(len(cP), -1)).any(1) | \
+        (np.abs(np.nan_to_num(fP, nan=1e300) - rP).reshape(len(cP), -1).max(1) > 1e-9 * scale)
+    assert bad.sum() <= 4
+    ok = ~bad
     assert np.max(np.abs(cP[ok] - refP[ok])) <= 1e-12 * scale
     assert np.max(np.abs(cM[ok] - refM[ok])) <= 1e-12 * scale
     gp = g[key + "_psiP"].reshape(-1)
@@ -61,11 +68,10 @@ def test_split_matches_reference(golden, dim, ps, split):
     assert np.max(np.abs(psiP[ok] - gp[ok])) <= 1e-12 * s
     assert np.max(np.abs(psiM[ok] - gm[ok])) <= 1e-12 * s
     if bad.any():
-        # where the reference returns NaN the kernel follows the clipped oracle
-        lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
-        oP, oM = fem.split_C(eps[bad], split, lmbda, mu, dim, C, clamp=True)
+        # degenerate rows follow the robust oracle and keep the split identities
         assert not np.isnan(cP[bad]).any()
-        np.testing.assert_allclose(cP[bad], oP.reshape(cP[bad].shape), atol=1e-9 * scale)
+        np.testing.assert_allclose(cP[bad], rP.reshape(cP.shape)[bad], atol=1e-9 * scale)
+        np.testing.assert_allclose(cM[bad], rM.reshape(cM.shape)[bad], atol=1e-9 * scale)
         np.testing.assert_allclose(cP[bad] + cM[bad], np.broadcast_to(C, cP[bad].shape), atol=1e-9 * scale)
 
 

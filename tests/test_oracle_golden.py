@@ -86,14 +86,14 @@ def test_split_oracle_matches_reference(golden, dim, ps, split):
     assert np.max(np.abs(psiM[ok] - gM[ok])) <= 1e-12 * ps_scale
 
 
-def test_split_clamped_fixes_reference_nan(golden):
+def test_split_robust_fixes_reference_nan(golden):
     """With the arccos argument clipped, the degenerate 3D cases satisfy the
     split identities (cP + cM = C, psi+ + psi- = psi) instead of giving NaN."""
     g = golden("split")
     eps = g["d3_eps"]
     lmbda, mu = fem.lame(210000.0, 0.3, 3, False)
     C = fem.isotropic_C(210000.0, 0.3, 3, False)
-    cP, cM = fem.split_C(eps, "Miehe", lmbda, mu, 3, C, clamp=True)
+    cP, cM = fem.split_C(eps, "Miehe", lmbda, mu, 3, C, robust=True)
     assert not np.isnan(cP).any()
     np.testing.assert_allclose(cP + cM, np.broadcast_to(C, cP.shape), atol=1e-9 * np.abs(C).max())
     psiP, psiM = fem.psi_split(eps, cP, cM)
@@ -145,3 +145,22 @@ def test_phasefield_state_systems_match_reference(golden, case):
     np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-10, atol=1e-12 * np.abs(g["Fd"]).max())
     Ku = pf.elastic_system()
     assert row_scaled_err(Ku, csr(g, "Ku", m.Nn * m.dim)) <= 1e-12
+
+
+def test_robust_split_differs_from_reference_only_at_degenerate_points(golden):
+    """The tolerance-based branch rule (the GPU kernels' rule) agrees with the
+    reference except at the exactly repeated eigenvalues where the reference
+    returns NaN or divides rounding noise by rounding noise."""
+    g = golden("split")
+    for dim, ps, expected in ((2, 1, []), (2, 0, []), (3, 0, [49, 52, 54, 55])):
+        eps = g[f"d{dim}_eps"]
+        lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
+        C = fem.isotropic_C(210000.0, 0.3, dim, bool(ps))
+        ref = g[f"d{dim}_ps{ps}_Miehe_cP"]
+        rP, _ = fem.split_C(eps, "Miehe", lmbda, mu, dim, C, robust=True)
+        d = np.abs(np.nan_to_num(ref, nan=1e300) - rP).reshape(len(eps), -1).max(1)
+        assert list(np.nonzero(d > 1e-12 * np.abs(C).max())[0]) == expected
+        # at those points the strain has exactly repeated eigenvalues
+        for r in expected:
+            w = np.linalg.eigvalsh(fem.vec_to_mat(eps[r, 0]))
+            assert np.min(np.abs(np.diff(w))) < 1e-12 * np.abs(w).max()

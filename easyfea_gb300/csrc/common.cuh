@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/gfea.h"
 
 #define GFEA_CUDA_TRY(expr)                        \
@@ -13,7 +15,19 @@
     if (_e != cudaSuccess) return GFEA_ERR_CUDA;   \
   } while (0)
 
-#define GFEA_LAUNCH_CHECK() GFEA_CUDA_TRY(cudaGetLastError())
+namespace gfea {
+// number of kernels this library has launched (process lifetime)
+inline std::atomic<long long>& launch_counter() {
+  static std::atomic<long long> n{0};
+  return n;
+}
+}  // namespace gfea
+
+#define GFEA_LAUNCH_CHECK()                 \
+  do {                                      \
+    gfea::launch_counter().fetch_add(1);    \
+    GFEA_CUDA_TRY(cudaGetLastError());      \
+  } while (0)
 
 namespace gfea {
 

@@ -119,7 +119,9 @@ int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, cu
   const int nb = (int)ceil_div(n, kScanTile);
   if (nb == 0) return GFEA_OK;
   scan_reduce<<<nb, kScanThreads, 0, s>>>(in, n, sums);
+  GFEA_LAUNCH_CHECK();
   scan_sums<<<1, kScanThreads, 0, s>>>(sums, nb);
+  GFEA_LAUNCH_CHECK();
   scan_apply<<<nb, kScanThreads, 0, s>>>(in, n, sums, out);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;

@@ -27,7 +27,7 @@ constexpr double kSqrt2 = 1.41421356237309504880;
 // repeated-eigenvalue tolerances: 2D discriminant and 3D invariant g relative to
 // the squared Frobenius norm; 3D arccos argument distance to +-1
 constexpr double kEigTolSq = 1e-14;
-constexpr double kEigTolArg = 4e-15;
+constexpr double kEigTolArg = 1e-12;
 
 struct PF {
   int split, regu, dim;
@@ -70,20 +70,21 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
   // Miehe: projP from the eigen decomposition of the strain tensor
   double projP[n * n];
   if constexpr (D == 2) {
+    // eigenvalues m -+ rad with m = tr/2 and rad^2 = ((M00 - M11)/2)^2 + M01^2,
+    // i.e. the reference's (tr -+ sqrt(tr^2 - 4 det))/2 without its cancellation
     const double M00 = eps[0], M11 = eps[1], M01 = eps[2] / kSqrt2;
-    const double det = M00 * M11 - M01 * M01;
     const double trM = M00 + M11;
-    double delta = trM * trM - 4 * det;
-    const bool repeated = delta <= kEigTolSq * (M00 * M00 + M11 * M11 + 2 * M01 * M01);
-    if (repeated) delta = 0;
-    const double sd = sqrt(delta);
-    const double v1 = (trM - sd) / 2, v2 = (trM + sd) / 2;
-    double A00 = 1, A11 = 0, A01 = 0;  // M1
+    const double h = (M00 - M11) / 2;
+    double rad2 = h * h + M01 * M01;
+    const bool repeated = rad2 <= 0.25 * kEigTolSq * (M00 * M00 + M11 * M11 + 2 * M01 * M01);
+    if (repeated) rad2 = 0;
+    const double rad = sqrt(rad2);
+    const double v1 = trM / 2 - rad, v2 = trM / 2 + rad;
+    double A00 = 1, A11 = 0, A01 = 0;  // M1 = (M - v2 I) / (v1 - v2)
     if (!repeated) {
-      const double dv = v1 - v2;
-      A00 = (M00 - v2) / dv;
-      A11 = (M11 - v2) / dv;
-      A01 = M01 / dv;
+      A00 = (rad - h) / (2 * rad);
+      A11 = (rad + h) / (2 * rad);
+      A01 = -M01 / (2 * rad);
     }
     const double m1[3] = {A00, A11, A01 * kSqrt2};
     const double m2[3] = {1 - A00, 1 - A11, -A01 * kSqrt2};
@@ -101,56 +102,65 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
     M[1][2] = M[2][1] = eps[3] / kSqrt2;
     M[0][2] = M[2][0] = eps[4] / kSqrt2;
     M[0][1] = M[1][0] = eps[5] / kSqrt2;
+    // Invariants of the deviator s = M - I1/3 I: g = I1^2 - 3 I2 = 3/2 tr(s^2)
+    // and 2 I1^3 - 9 I1 I2 + 27 I3 = 27 det(s), the reference's quantities
+    // without their cancellation when the eigenvalues cluster.
     const double I1 = M[0][0] + M[1][1] + M[2][2];
     double trMM = 0;
     for (int i = 0; i < 3; ++i)
       for (int k = 0; k < 3; ++k) trMM += M[i][k] * M[k][i];
-    const double I2 = 0.5 * (I1 * I1 - trMM);
-    const double I3 = M[0][0] * ((M[1][1] * M[2][2]) - (M[2][1] * M[1][2])) -
-                      M[0][1] * ((M[1][0] * M[2][2]) - (M[2][0] * M[1][2])) +
-                      M[0][2] * ((M[1][0] * M[2][1]) - (M[2][0] * M[1][1]));
-    double g = I1 * I1 - 3 * I2;
+    double S[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S[i][j] = M[i][j] - (i == j ? I1 / 3 : 0.0);
+    double trSS = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) trSS += S[i][k] * S[k][i];
+    const double detS = S[0][0] * ((S[1][1] * S[2][2]) - (S[2][1] * S[1][2])) -
+                        S[0][1] * ((S[1][0] * S[2][2]) - (S[2][0] * S[1][2])) +
+                        S[0][2] * ((S[1][0] * S[2][1]) - (S[2][0] * S[1][1]));
+    double g = 1.5 * trSS;
     if (g <= kEigTolSq * trMM) g = 0;  // three equal eigenvalues
     const double sg = sqrt(g);
-    double arg = 0.5 * (2 * I1 * I1 * I1 - 9 * I1 * I2 + 27 * I3);
-    if (g != 0) arg = arg / pow(g, 1.5);
+    double arg = 0.0;
+    if (g != 0) arg = 13.5 * detS / (g * sg);
     if (arg > 1) arg = 1;
     if (arg < -1) arg = -1;
     double v[3] = {I1 / 3, I1 / 3, I1 / 3};
     double M1[3][3] = {{1, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     double M3[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
     if (g != 0) {
-      const double irg = (I1 - sg) / 3;
-      const double gm = 1.0 / sqrt(g);
+      // M - ((I1 - sg)/3) I = S + sg/3 I
+      const double gm = 1.0 / sg;
       if (arg <= -1 + kEigTolArg) {  // theta = pi/3: e1 < e2 = e3
         v[0] += -2.0 / 3 * sg; v[1] += 1.0 / 3 * sg; v[2] += 1.0 / 3 * sg;
         for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) {
-            M1[i][j] = gm * ((i == j ? irg : 0.0) - M[i][j]);
-          }
+          for (int j = 0; j < 3; ++j) M1[i][j] = -gm * (S[i][j] + (i == j ? sg / 3 : 0.0));
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) M3[i][j] = 0.5 * ((i == j ? 1.0 : 0.0) - M1[i][j]);
       } else if (arg >= 1 - kEigTolArg) {  // theta = 0: e1 = e2 < e3
         v[0] += -1.0 / 3 * sg; v[1] += -1.0 / 3 * sg; v[2] += 2.0 / 3 * sg;
         for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) M3[i][j] = gm * (M[i][j] - (i == j ? irg : 0.0));
+          for (int j = 0; j < 3; ++j) M3[i][j] = gm * (S[i][j] + (i == j ? sg / 3 : 0.0));
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) M1[i][j] = 0.5 * ((i == j ? 1.0 : 0.0) - M3[i][j]);
       } else {
         const double theta = acos(arg) / 3;
         const double twopi3 = 2 * M_PI / 3;
-        v[0] += 2.0 / 3 * (sg * cos(twopi3 + theta));
-        v[1] += 2.0 / 3 * (sg * cos(twopi3 - theta));
-        v[2] += 2.0 / 3 * (sg * cos(theta));
+        // deviatoric eigenvalues sk; v = I1/3 + sk
+        const double sk[3] = {2.0 / 3 * (sg * cos(twopi3 + theta)), 2.0 / 3 * (sg * cos(twopi3 - theta)),
+                              2.0 / 3 * (sg * cos(theta))};
+        v[0] += sk[0];
+        v[1] += sk[1];
+        v[2] += sk[2];
         double P2[3][3], P3[3][3], Q1[3][3];
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) {
-            P2[i][j] = M[i][j] - (i == j ? v[1] : 0.0);
-            P3[i][j] = M[i][j] - (i == j ? v[2] : 0.0);
-            Q1[i][j] = M[i][j] - (i == j ? v[0] : 0.0);
+            P2[i][j] = S[i][j] - (i == j ? sk[1] : 0.0);
+            P3[i][j] = S[i][j] - (i == j ? sk[2] : 0.0);
+            Q1[i][j] = S[i][j] - (i == j ? sk[0] : 0.0);
           }
-        const double den1 = (v[0] - v[1]) * (v[0] - v[2]);
-        const double den3 = (v[2] - v[0]) * (v[2] - v[1]);
+        const double den1 = (sk[0] - sk[1]) * (sk[0] - sk[2]);
+        const double den3 = (sk[2] - sk[0]) * (sk[2] - sk[1]);
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) {
             double a = 0, b = 0;

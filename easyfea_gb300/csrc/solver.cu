@@ -37,6 +37,21 @@ struct Scal {
   uint32_t ticket1, ticket2, ticket3, pad;
 };
 
+// Optional CUDA-event timing of the PCG direction/SpMV kernel (the dominant
+// launch of a solve), read back by gfea_profile_read.
+struct KernelProfile {
+  static constexpr int kPairs = 64;
+  bool on = false;
+  bool created = false;
+  cudaEvent_t ev[2 * kPairs];
+  double ms = 0;
+  long long n = 0;
+};
+KernelProfile& prof() {
+  static KernelProfile p;
+  return p;
+}
+
 template <typename T>
 struct SysT {
   int64_t Nn;
@@ -228,16 +243,18 @@ __global__ void bjacobi_kernel(SysT<T> S, T* __restrict__ dinv, int32_t* flag) {
   }
 }
 
-// z = D^-1 r (+ optional x/r update), partial r.z and r.r; last block derives
-// beta and the convergence state.
+// z = D^-1 r, partial r.z and r.r; the last block derives beta and the
+// convergence state.  mode 0: PCG iteration (x += alpha p, r -= alpha Ap
+// first); mode 1: start (beta = 0); mode 2: residual replaced by a reliable
+// update (beta = r.z / previous r.z, the search direction is kept).
 template <int D, typename T>
 __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint8_t* __restrict__ known,
                                                           const T* __restrict__ dinv, T* __restrict__ x,
                                                           T* __restrict__ r, T* __restrict__ z,
                                                           const T* __restrict__ p, const T* __restrict__ Ap,
-                                                          double* partials, Scal* sc, int init) {
-  if (!init && sc->done) return;
-  const double alpha = init ? 0.0 : sc->alpha;
+                                                          double* partials, Scal* sc, int mode) {
+  if (mode == 0 && sc->done) return;
+  const double alpha = mode == 0 ? sc->alpha : 0.0;
   double v[2] = {0, 0};
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
     T rl[D];
@@ -245,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
     for (int i = 0; i < D; ++i) {
       const int64_t dof = a * D + i;
       T ri = r[dof];
-      if (!init) {
+      if (mode == 0) {
         x[dof] += (T)alpha * p[dof];
         ri -= (T)alpha * Ap[dof];
         r[dof] = ri;
@@ -266,10 +283,10 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
   double out[2];
   if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
     const double rz_new = out[0], rr = out[1];
-    sc->beta = init ? 0.0 : rz_new / sc->rz;
+    sc->beta = mode == 1 ? 0.0 : rz_new / sc->rz;
     sc->rz = rz_new;
     sc->rr = rr;
-    if (init) return;  // convergence of the start is judged by init_scal_kernel
+    if (mode != 0) return;  // the host sets the next stopping threshold
     sc->iters += 1;
     if (!isfinite(rr) || !isfinite(rz_new)) {
       sc->status = GFEA_ERR_NAN;
@@ -343,17 +360,19 @@ __global__ void zero_unknown_kernel(double* __restrict__ x, const uint8_t* known
     if (!known[i]) x[i] = 0.0;
 }
 
-// Runs after the start's update (rz, rr known): sets the stopping threshold,
-// relative to bb (rel_to_rr = 0) or to the starting rr (rel_to_rr = 1).
-__global__ void init_scal_kernel(Scal* sc, double tol2_rel, int max_iters, int rel_to_rr) {
-  const double ref = rel_to_rr ? sc->rr : sc->bb;
-  sc->tol2 = tol2_rel * ref;
-  sc->iters = 0;
-  sc->status = GFEA_OK;
+// Sets the threshold at which the device stops iterating (the next reliable
+// update), keeping the iteration count.
+__global__ void set_trigger_kernel(Scal* sc, double tol2, int max_iters) {
+  sc->tol2 = tol2;
   sc->max_iters = max_iters;
-  sc->beta = 0;
-  sc->done = !isfinite(sc->rr) ? 1 : (sc->rr <= sc->tol2 ? 1 : 0);
-  if (!isfinite(sc->rr)) sc->status = GFEA_ERR_NAN;
+  sc->status = GFEA_OK;
+  if (!isfinite(sc->rr) || !isfinite(sc->rz)) {
+    sc->status = GFEA_ERR_NAN;
+    sc->done = 1;
+  } else {
+    sc->done = (sc->rr <= tol2 || sc->iters >= max_iters) ? 1 : 0;
+    if (sc->iters >= max_iters) sc->status = GFEA_ERR_NOT_CONVERGED;
+  }
 }
 
 // reaction / energy
@@ -521,11 +540,11 @@ int launch_bjacobi(const gfea_system* s, PcgWork& w, cudaStream_t st) {
 }
 
 template <typename T>
-int launch_update(const gfea_system* s, PcgWork& w, T* x, T* p, int init, cudaStream_t st) {
+int launch_update(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaStream_t st) {
   const int grid = grid_elems(s->n_nodes);
   GFEA_D_SWITCH(s->dof_n, (update_kernel<DD, T><<<grid, kThreads, 0, st>>>(s->n_nodes, s->known, (const T*)w.dinv, x,
                                                                             (T*)w.r, (T*)w.z, p, (const T*)w.Ap,
-                                                                            w.partials + 2 * kMaxBlocks, w.sc, init)));
+                                                                            w.partials + 2 * kMaxBlocks, w.sc, mode)));
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -540,23 +559,44 @@ int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new
   return GFEA_OK;
 }
 
-// Runs PCG iterations until the device flags done; checks every 'check' iterations.
+// Runs PCG iterations until the device flags done; checks every 'check'
+// iterations.  pa holds the current search direction on entry and exit.
 template <typename T>
-int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* host_sc, cudaStream_t st) {
-  T* pa = (T*)w.pa;
-  T* pb = (T*)w.pb;
-  for (;;) {
-    for (int it = 0; it < check; ++it) {
-      int e = launch_dir<T>(s, G, w, pa, pb, st);
+int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* host_sc, T*& pa, T*& pb,
+             int iters0, cudaStream_t st) {
+  // iteration j reads direction buf[j % 2] and writes buf[(j + 1) % 2]; launches
+  // after the device set 'done' are no-ops, so the current direction follows
+  // from the number of iterations actually performed
+  T* buf[2] = {pa, pb};
+  KernelProfile& P = prof();
+  const bool timed = P.on && check <= KernelProfile::kPairs;
+  int before = iters0;
+  for (int j = 0;;) {
+    for (int it = 0; it < check; ++it, ++j) {
+      if (timed) GFEA_CUDA_TRY(cudaEventRecord(P.ev[2 * it], st));
+      int e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
       if (e) return e;
-      e = launch_update<T>(s, w, x, pb, 0, st);
+      if (timed) GFEA_CUDA_TRY(cudaEventRecord(P.ev[2 * it + 1], st));
+      e = launch_update<T>(s, w, x, buf[(j + 1) & 1], 0, st);
       if (e) return e;
-      T* t = pa; pa = pb; pb = t;
     }
     GFEA_CUDA_TRY(cudaMemcpyAsync(host_sc, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    if (timed) {  // durations of the direction/SpMV launches that did work
+      const int performed = host_sc->iters - before;
+      for (int it = 0; it < performed && it < check; ++it) {
+        float ms = 0;
+        GFEA_CUDA_TRY(cudaEventElapsedTime(&ms, P.ev[2 * it], P.ev[2 * it + 1]));
+        P.ms += ms;
+        P.n += 1;
+      }
+    }
+    before = host_sc->iters;
     if (host_sc->done) break;
   }
+  const int performed = host_sc->iters - iters0;
+  pa = buf[performed & 1];
+  pb = buf[(performed + 1) & 1];
   return GFEA_OK;
 }
 
@@ -566,13 +606,15 @@ int fetch(Scal* h, PcgWork& w, cudaStream_t st) {
   return GFEA_OK;
 }
 
-// Iterative refinement around a T-precision PCG:
-//   r = P(b - A x) in FP64; stop when ||r|| <= max(rtol ||P(b - A x_c)||,
-//   floor), floor = 32 eps64 ||P(|A||x| + |b|)|| (the rounding level of an FP64
-//   residual); else solve A d = r with PCG (T values and vectors, FP64 dots),
-//   x += d, repeat.  FP64 inner solves aim at the target directly and the next
-//   residual corrects the recursive-residual drift; FP32 inner solves reduce the
-//   residual by inner_rtol per step.
+// PCG in T precision with reliable updates (FP64 residual replacement):
+//   the iteration runs on T values and vectors with FP64 dots and scalar
+//   recurrences, accumulating its correction in dx; whenever the iterated
+//   residual has dropped by delta^2 since the last update, dx is added to the
+//   FP64 solution, r = P(b - A x) is recomputed with the FP64 operator and
+//   replaces the iterated residual, and the iteration continues along the same
+//   search direction.  It stops when the FP64 residual satisfies
+//   ||r|| <= max(rtol ||P(b - A x_c)||, floor), floor = 32 eps64 ||P(|A||x| + |b|)||
+//   (the rounding level of an FP64 residual).
 template <typename T>
 int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
                  size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
@@ -583,6 +625,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   const int check = o->check_every > 0 ? o->check_every : 32;
   const bool fp64 = sizeof(T) == 8;
   const double eps64 = 2.220446049250313e-16;
+  const double delta2 = fp64 ? 1e-6 : (o->inner_rtol > 0 ? o->inner_rtol * o->inner_rtol : 1e-2);
   Scal hs;
   GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
   GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
@@ -604,52 +647,64 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
     res->status = GFEA_OK;
     return GFEA_OK;
   }
-  double rr = hs.rr_true, rr_prev = 0;
-  int total = 0, stall = 0;
-  const int max_ref = o->max_refine > 0 ? o->max_refine : 30;
-  const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+  double rr = hs.rr_true, rr_best = rr;
+  double floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;
+  double tol2 = fmax(o->rtol * o->rtol * bb, floor2);
+  res->rel_residual = sqrt(rr / bb);
+  res->floor_rel = sqrt(floor2 / bb);
+  if (rr <= tol2) { res->status = GFEA_OK; return GFEA_OK; }
+  const int max_upd = o->max_refine > 0 ? o->max_refine : 200;
+  T* pa = (T*)w.pa;
+  T* pb = (T*)w.pb;
+  // start: r (T) = r64, dx = 0, p = 0, z = D^-1 r
+  cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.r, N);
+  GFEA_LAUNCH_CHECK();
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
+  GFEA_CUDA_TRY(cudaMemsetAsync(pa, 0, sizeof(T) * N, st));
+  e = launch_update<T>(s, w, (T*)w.dx, pa, 1, st);
+  if (e) return e;
+  set_trigger_kernel<<<1, 1, 0, st>>>(w.sc, fmax(delta2 * rr, 0.25 * tol2), o->max_iters);
+  GFEA_LAUNCH_CHECK();
   res->status = GFEA_ERR_NOT_CONVERGED;
-  for (int k = 0;; ++k) {
-    const double floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;
-    const double tol2 = fmax(o->rtol * o->rtol * bb, floor2);
-    res->rel_residual = sqrt(rr / bb);
-    res->floor_rel = sqrt(floor2 / bb);
-    if (rr <= tol2) { res->status = GFEA_OK; break; }
-    if (k > 0) {
-      stall = rr > 0.25 * rr_prev ? stall + 1 : 0;
-      if (stall >= 3) break;  // refinement no longer reduces the residual
-    }
-    if (k >= max_ref || total >= o->max_iters) break;
-    res->refinements = k + 1;
-    rr_prev = rr;
-    // inner solve A d = r (d = 0 start; known DOFs stay 0)
-    double inner2 = fp64 ? fmax(0.1 * tol2 / rr, 1e-30) : fmax(inner * inner, 0.1 * tol2 / rr);
-    cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.r, N);
-    GFEA_LAUNCH_CHECK();
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pa, 0, sizeof(T) * N, st));
-    GFEA_CUDA_TRY(cudaMemsetAsync(w.pb, 0, sizeof(T) * N, st));
-    e = launch_update<T>(s, w, (T*)w.dx, (T*)w.pa, 1, st);
+  int stall = 0;
+  int iters0 = 0;
+  for (int upd = 0;; ++upd) {
+    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, &hs, pa, pb, iters0, st);
     if (e) return e;
-    init_scal_kernel<<<1, 1, 0, st>>>(w.sc, inner2, o->max_iters - total, 1);
-    GFEA_LAUNCH_CHECK();
-    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, &hs, st);
-    if (e) return e;
-    total += hs.iters;
-    if (hs.status == GFEA_ERR_NAN || hs.status == GFEA_ERR_BREAKDOWN) {
-      // breakdown after some progress: keep the correction of the completed iterations
-      if (hs.status == GFEA_ERR_NAN || hs.iters == 0) { res->status = hs.status; break; }
-    }
+    res->iterations = hs.iters;
+    const int st_inner = hs.status;
+    // reliable update: x += dx (FP64), r = P(b - A x) in FP64
     add_correction_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(x, (const T*)w.dx, s->known, N);
     GFEA_LAUNCH_CHECK();
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
     e = launch_resid(s, G, b, x, w, st);
     if (e) return e;
     e = fetch(&hs, w, st);
     if (e) return e;
     rr = hs.rr_true;
+    iters0 = hs.iters;
+    res->refinements = upd + 1;
+    floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;
+    tol2 = fmax(o->rtol * o->rtol * bb, floor2);
+    res->rel_residual = sqrt(rr / bb);
+    res->floor_rel = sqrt(floor2 / bb);
     if (!isfinite(rr)) { res->status = GFEA_ERR_NAN; break; }
+    if (rr <= tol2) { res->status = GFEA_OK; break; }
+    if (st_inner == GFEA_ERR_NAN || st_inner == GFEA_ERR_BREAKDOWN || st_inner == GFEA_ERR_NOT_CONVERGED) {
+      res->status = st_inner;
+      break;
+    }
+    stall = rr > 0.9 * rr_best ? stall + 1 : 0;
+    if (rr < rr_best) rr_best = rr;
+    if (stall >= 8 || upd + 1 >= max_upd) break;
+    // continue on the replaced residual along the same direction
+    cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.r, N);
+    GFEA_LAUNCH_CHECK();
+    e = launch_update<T>(s, w, (T*)w.dx, pa, 2, st);
+    if (e) return e;
+    set_trigger_kernel<<<1, 1, 0, st>>>(w.sc, fmax(delta2 * rr, 0.25 * tol2), o->max_iters);
+    GFEA_LAUNCH_CHECK();
   }
-  res->iterations = total;
   return res->status;
 }
 
@@ -758,5 +813,27 @@ extern "C" int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void*
   if (n == 0) return GFEA_OK;
   cast_kernel<float><<<grid_elems(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, n);
   GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+extern "C" long long gfea_launch_count(void) { return gfea::launch_counter().load(); }
+
+extern "C" int gfea_profile_enable(int on) {
+  gfea::KernelProfile& P = gfea::prof();
+  if (on && !P.created) {
+    for (int i = 0; i < 2 * gfea::KernelProfile::kPairs; ++i) GFEA_CUDA_TRY(cudaEventCreate(&P.ev[i]));
+    P.created = true;
+  }
+  P.on = on != 0;
+  return GFEA_OK;
+}
+
+extern "C" int gfea_profile_read(double* ms_host, long long* launches_host) {
+  if (!ms_host || !launches_host) return GFEA_ERR_ARG;
+  gfea::KernelProfile& P = gfea::prof();
+  *ms_host = P.ms;
+  *launches_host = P.n;
+  P.ms = 0;
+  P.n = 0;
   return GFEA_OK;
 }

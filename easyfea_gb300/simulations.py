@@ -332,10 +332,14 @@ class Elastic(_Simu):
 
     def Solve(self) -> np.ndarray:
         """Solve K u = b with the Dirichlet conditions; returns u (host copy)."""
+        return self.Solve_device().cpu().numpy()
+
+    def Solve_device(self) -> torch.Tensor:
+        """Same as Solve, leaving u on the device (no host copy)."""
         op = self.K_device
         b = self._neumann_vec(self.problemType)
         self.__u = self._solve_system(op, b, self.problemType)
-        return self.__u.cpu().numpy()
+        return self.__u
 
     @property
     def u_device(self) -> Optional[torch.Tensor]:

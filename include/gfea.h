@@ -235,6 +235,13 @@ int gfea_reaction_energy(const gfea_system* sys_host, const double* x, const int
 int gfea_max_abs_diff(const double* a, const double* b, int64_t n, double* out_host,
                       void* work, void* stream);
 
+/* Instrumentation: kernels launched by the library so far; optional
+ * CUDA-event timing of the PCG direction/SpMV kernel (total ms and launches
+ * since the last read; reading resets). */
+long long gfea_launch_count(void);
+int gfea_profile_enable(int on);
+int gfea_profile_read(double* ms_host, long long* launches_host);
+
 /* FP64 -> FP32 copy of CSR values (mixed-precision operator) */
 int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void* stream);
 

@@ -526,6 +526,8 @@ def eigen_projectors(eps, robust=False):
     reproduces that exactly; ``robust=True`` is the GPU kernels' rule: branches
     chosen with the relative tolerances EIG_TOL_SQ (2D discriminant, 3D g) and
     EIG_TOL_ARG (3D arccos argument to +-1), argument clipped to [-1, 1]."""
+    if robust:
+        return _eigen_projectors_robust(eps)
     M = vec_to_mat(eps)
     dim = M.shape[-1]
     I = np.zeros_like(M)
@@ -618,6 +620,74 @@ def eigen_projectors(eps, robust=False):
     M3 = M3 / np.linalg.norm(M3, axis=(-2, -1))[..., None, None]
     M2 = I - (M1 + M3)
     return vals, [M1, M2, M3]
+
+
+def _eigen_projectors_robust(eps):
+    """The GPU kernels' form of the same decomposition: eigenvalues from the
+    deviator (2D: m -+ sqrt(h^2 + M01^2); 3D: g = 3/2 tr(s^2), arccos argument
+    13.5 det(s) / g^1.5), repeated-eigenvalue branches chosen with the
+    tolerances EIG_TOL_SQ / EIG_TOL_ARG, projectors built from s."""
+    M = vec_to_mat(eps)
+    dim = M.shape[-1]
+    I = np.broadcast_to(np.eye(dim), M.shape)
+    shp = eps.shape[:-1]
+    if dim == 2:
+        tr = M[..., 0, 0] + M[..., 1, 1]
+        h = (M[..., 0, 0] - M[..., 1, 1]) / 2
+        rad2 = h * h + M[..., 0, 1] ** 2
+        F2 = M[..., 0, 0] ** 2 + M[..., 1, 1] ** 2 + 2 * M[..., 0, 1] ** 2
+        rep = rad2 <= 0.25 * EIG_TOL_SQ * F2
+        rad = np.sqrt(np.where(rep, 0.0, rad2))
+        vals = np.stack([tr / 2 - rad, tr / 2 + rad], -1)
+        safe = np.where(rep, 1.0, 2 * rad)
+        M1 = np.zeros_like(M)
+        M1[..., 0, 0] = np.where(rep, 1.0, (rad - h) / safe)
+        M1[..., 1, 1] = np.where(rep, 0.0, (rad + h) / safe)
+        M1[..., 0, 1] = M1[..., 1, 0] = np.where(rep, 0.0, -M[..., 0, 1] / safe)
+        return vals, [M1, I - M1]
+    I1 = M[..., 0, 0] + M[..., 1, 1] + M[..., 2, 2]
+    trMM = np.einsum("...ik,...ki->...", M, M)
+    S = M - (I1 / 3)[..., None, None] * I
+    trSS = np.einsum("...ik,...ki->...", S, S)
+    g = 1.5 * trSS
+    g = np.where(g <= EIG_TOL_SQ * trMM, 0.0, g)
+    sg = np.sqrt(g)
+    gnz = g != 0
+    sgs = np.where(gnz, sg, 1.0)
+    arg = np.where(gnz, 13.5 * det(S) / (np.where(gnz, g, 1.0) * sgs), 0.0)
+    arg = np.clip(arg, -1.0, 1.0)
+    c2 = gnz & (arg <= -1 + EIG_TOL_ARG)
+    c3 = gnz & ~c2 & (arg >= 1 - EIG_TOL_ARG)
+    c1 = gnz & ~c2 & ~c3
+    theta = np.arccos(arg) / 3
+    sk = np.zeros(shp + (3,))
+    sk[..., 0] = np.where(c2, -2 / 3 * sg, np.where(c3, -1 / 3 * sg, 2 / 3 * (sg * np.cos(2 * np.pi / 3 + theta))))
+    sk[..., 1] = np.where(c2, 1 / 3 * sg, np.where(c3, -1 / 3 * sg, 2 / 3 * (sg * np.cos(2 * np.pi / 3 - theta))))
+    sk[..., 2] = np.where(c2, 1 / 3 * sg, np.where(c3, 2 / 3 * sg, 2 / 3 * (sg * np.cos(theta))))
+    sk = np.where(gnz[..., None], sk, 0.0)
+    vals = (I1 / 3)[..., None] + sk
+    M1 = np.zeros_like(M)
+    M1[..., 0, 0] = 1
+    M3 = np.zeros_like(M)
+    M3[..., 2, 2] = 1
+    Sp = S + (sg / 3)[..., None, None] * I
+    gm = (1 / sgs)[..., None, None]
+    m1c2 = -gm * Sp
+    M1 = np.where(c2[..., None, None], m1c2, M1)
+    M3 = np.where(c2[..., None, None], 0.5 * (I - m1c2), M3)
+    m3c3 = gm * Sp
+    M3 = np.where(c3[..., None, None], m3c3, M3)
+    M1 = np.where(c3[..., None, None], 0.5 * (I - m3c3), M1)
+    if c1.any():
+        s0, s1, s2 = sk[..., 0, None, None], sk[..., 1, None, None], sk[..., 2, None, None]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m1 = (S - s1 * I) @ (S - s2 * I) / ((s0 - s1) * (s0 - s2))
+            m3 = (S - s0 * I) @ (S - s1 * I) / ((s2 - s0) * (s2 - s1))
+        M1 = np.where(c1[..., None, None], m1, M1)
+        M3 = np.where(c1[..., None, None], m3, M3)
+    M1 = M1 / np.linalg.norm(M1, axis=(-2, -1))[..., None, None]
+    M3 = M3 / np.linalg.norm(M3, axis=(-2, -1))[..., None, None]
+    return vals, [M1, I - (M1 + M3), M3]
 
 
 def spectral_projectors(eps, robust=False):

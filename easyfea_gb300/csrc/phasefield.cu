@@ -28,6 +28,8 @@ constexpr double kSqrt2 = 1.41421356237309504880;
 // the squared Frobenius norm; 3D arccos argument distance to +-1
 constexpr double kEigTolSq = 1e-14;
 constexpr double kEigTolArg = 1e-12;
+// eigenvalues within kEigTolZero * ||eps|| of zero are zero (Heaviside(0) = 1/2)
+constexpr double kEigTolZero = 1e-12;
 
 struct PF {
   int split, regu, dim;
@@ -79,7 +81,10 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
     const bool repeated = rad2 <= 0.25 * kEigTolSq * (M00 * M00 + M11 * M11 + 2 * M01 * M01);
     if (repeated) rad2 = 0;
     const double rad = sqrt(rad2);
-    const double v1 = trM / 2 - rad, v2 = trM / 2 + rad;
+    const double zero_tol = kEigTolZero * sqrt(M00 * M00 + M11 * M11 + 2 * M01 * M01);
+    double v1 = trM / 2 - rad, v2 = trM / 2 + rad;
+    if (fabs(v1) <= zero_tol) v1 = 0;
+    if (fabs(v2) <= zero_tol) v2 = 0;
     double A00 = 1, A11 = 0, A01 = 0;  // M1 = (M - v2 I) / (v1 - v2)
     if (!repeated) {
       A00 = (rad - h) / (2 * rad);
@@ -173,6 +178,9 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
           }
       }
     }
+    const double zero_tol = kEigTolZero * sqrt(trMM);
+    for (int k = 0; k < 3; ++k)
+      if (fabs(v[k]) <= zero_tol) v[k] = 0;
     double n1 = 0, n3 = 0;
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {

@@ -511,7 +511,8 @@ def mat_to_vec(M):
 
 
 EIG_TOL_SQ = 1e-14
-EIG_TOL_ARG = 4e-15
+EIG_TOL_ARG = 1e-12
+EIG_TOL_ZERO = 1e-12
 
 
 def eigen_projectors(eps, robust=False):
@@ -523,9 +524,8 @@ def eigen_projectors(eps, robust=False):
     The reference chooses its repeated-eigenvalue branches by exact equality
     (v1 == v2, g == 0, theta == 0 or pi/3), and evaluates ``arccos`` of an
     argument that rounding can push just past +-1 (NaN there).  ``robust=False``
-    reproduces that exactly; ``robust=True`` is the GPU kernels' rule: branches
-    chosen with the relative tolerances EIG_TOL_SQ (2D discriminant, 3D g) and
-    EIG_TOL_ARG (3D arccos argument to +-1), argument clipped to [-1, 1]."""
+    reproduces that exactly; ``robust=True`` is the GPU kernels' form
+    (_eigen_projectors_robust)."""
     if robust:
         return _eigen_projectors_robust(eps)
     M = vec_to_mat(eps)
@@ -538,9 +538,6 @@ def eigen_projectors(eps, robust=False):
         D = det(M)
         tr = M[..., 0, 0] + M[..., 1, 1]
         delta = tr**2 - 4 * D
-        if robust:
-            F2 = M[..., 0, 0] ** 2 + M[..., 1, 1] ** 2 + 2 * M[..., 0, 1] ** 2
-            delta = np.where(delta <= EIG_TOL_SQ * F2, 0.0, delta)
         vals = np.zeros(shp + (2,))
         vals[..., 0] = (tr - np.sqrt(delta)) / 2
         vals[..., 1] = (tr + np.sqrt(delta)) / 2
@@ -560,16 +557,10 @@ def eigen_projectors(eps, robust=False):
     I2 = 0.5 * (I1**2 - (MM[..., 0, 0] + MM[..., 1, 1] + MM[..., 2, 2]))
     I3 = det(M)
     g = I1**2 - 3 * I2
-    if robust:
-        trMM = MM[..., 0, 0] + MM[..., 1, 1] + MM[..., 2, 2]
-        g = np.where(g <= EIG_TOL_SQ * trMM, 0.0, g)
     sg = np.sqrt(g)
     gnz = g != 0
     arg = 0.5 * (2 * I1**3 - 9 * I1 * I2 + 27 * I3)
     arg = np.divide(arg, g ** (3 / 2), out=arg, where=gnz)
-    if robust:
-        arg = np.clip(arg, -1.0, 1.0)
-        arg = np.where(arg <= -1 + EIG_TOL_ARG, -1.0, np.where(arg >= 1 - EIG_TOL_ARG, 1.0, arg))
     with np.errstate(invalid="ignore"):
         theta = np.arccos(arg) / 3
     v1 = I1 / 3
@@ -626,7 +617,8 @@ def _eigen_projectors_robust(eps):
     """The GPU kernels' form of the same decomposition: eigenvalues from the
     deviator (2D: m -+ sqrt(h^2 + M01^2); 3D: g = 3/2 tr(s^2), arccos argument
     13.5 det(s) / g^1.5), repeated-eigenvalue branches chosen with the
-    tolerances EIG_TOL_SQ / EIG_TOL_ARG, projectors built from s."""
+    tolerances EIG_TOL_SQ / EIG_TOL_ARG, eigenvalues within EIG_TOL_ZERO of
+    zero set to zero (Heaviside(0) = 1/2), projectors built from s."""
     M = vec_to_mat(eps)
     dim = M.shape[-1]
     I = np.broadcast_to(np.eye(dim), M.shape)
@@ -639,6 +631,7 @@ def _eigen_projectors_robust(eps):
         rep = rad2 <= 0.25 * EIG_TOL_SQ * F2
         rad = np.sqrt(np.where(rep, 0.0, rad2))
         vals = np.stack([tr / 2 - rad, tr / 2 + rad], -1)
+        vals = np.where(np.abs(vals) <= EIG_TOL_ZERO * np.sqrt(F2)[..., None], 0.0, vals)
         safe = np.where(rep, 1.0, 2 * rad)
         M1 = np.zeros_like(M)
         M1[..., 0, 0] = np.where(rep, 1.0, (rad - h) / safe)
@@ -666,6 +659,7 @@ def _eigen_projectors_robust(eps):
     sk[..., 2] = np.where(c2, 1 / 3 * sg, np.where(c3, 2 / 3 * sg, 2 / 3 * (sg * np.cos(theta))))
     sk = np.where(gnz[..., None], sk, 0.0)
     vals = (I1 / 3)[..., None] + sk
+    vals = np.where(np.abs(vals) <= EIG_TOL_ZERO * np.sqrt(trMM)[..., None], 0.0, vals)
     M1 = np.zeros_like(M)
     M1[..., 0, 0] = 1
     M3 = np.zeros_like(M)

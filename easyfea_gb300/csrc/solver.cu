@@ -21,6 +21,8 @@
 // run more iterations than needed at no cost.
 
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "common.cuh"
@@ -686,6 +688,9 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
     e = fetch(&hs, w, st);
     if (e) return e;
     rr = hs.rr_true;
+    if (getenv("GFEA_DEBUG"))
+      fprintf(stderr, "[gfea pcg%d] update %d: iterations %d, inner status %d, rel residual %.3e\n",
+              fp64 ? 64 : 32, upd + 1, hs.iters, st_inner, sqrt(rr / bb));
     iters0 = hs.iters;
     res->refinements = upd + 1;
     floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;

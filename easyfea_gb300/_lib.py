@@ -44,6 +44,8 @@ class System(ctypes.Structure):
         ("vals64", c_void_p),
         ("vals32", c_void_p),
         ("known", c_void_p),
+        ("translation_invariant", c_int32),
+        ("pad", c_int32),
     ]
 
 

@@ -61,6 +61,7 @@ struct SysT {
   const int32_t* nbr;
   const T* vals;
   const uint8_t* known;
+  int diff;  // difference form sum_b K_ab (x_b - x_a) (translation-invariant operators)
 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -119,17 +120,31 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
 
 // acc[i] = sum over row (a,i) of vals * xf(col) (|vals| * xf with ABS);
 // reduced across the G lanes.
-template <int D, int G, typename T, typename A, bool ABS = false, typename XF>
+//
+// With DIFF the product is evaluated as sum_b K_ab (x_b - x_a): identical for an
+// operator whose node block rows sum to zero (rigid translations), but its
+// rounding then scales with the local differences of x rather than with |x|
+// (used by the FP32 products of elastic stiffness matrices).
+template <int D, int G, typename T, typename A, bool ABS = false, bool DIFF = false, typename XF>
 __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S, XF xf, A (&acc)[D]) {
   const int32_t p0 = S.node_ptr[a];
   const int32_t W = D * (S.node_ptr[a + 1] - p0);
   const T* base = S.vals + (int64_t)D * D * p0;
+  A self[D];
 #pragma unroll
-  for (int i = 0; i < D; ++i) acc[i] = 0;
+  for (int i = 0; i < D; ++i) {
+    acc[i] = 0;
+    self[i] = DIFF ? xf(a * D + i) : (A)0;
+  }
   for (int32_t t = lane; t < W; t += G) {
     const int32_t k = t / D, j = t - k * D;
     const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
-    const A xv = xf(col);
+    A xv = xf(col);
+    if (DIFF) {
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj)
+        if (jj == j) xv -= self[jj];
+    }
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       const A v = (A)__ldg(base + (int64_t)i * W + t);
@@ -321,7 +336,11 @@ __global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* 
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
     T acc[D];
-    node_rows<D, G, T, T>(ac, lane, S, [&](int64_t c) { return z[c] + beta * p_old[c]; }, acc);
+    auto dir = [&](int64_t c) { return z[c] + beta * p_old[c]; };
+    if (sizeof(T) == 4 && S.diff)
+      node_rows<D, G, T, T, false, true>(ac, lane, S, dir, acc);
+    else
+      node_rows<D, G, T, T>(ac, lane, S, dir, acc);
     if (a < Nn && lane < D) {
       T av = acc[0];
 #pragma unroll
@@ -494,11 +513,11 @@ template <typename T>
 SysT<T> sys_t(const gfea_system* s);
 template <>
 SysT<double> sys_t<double>(const gfea_system* s) {
-  return SysT<double>{s->n_nodes, s->node_ptr, s->nbr, s->vals64, s->known};
+  return SysT<double>{s->n_nodes, s->node_ptr, s->nbr, s->vals64, s->known, s->translation_invariant};
 }
 template <>
 SysT<float> sys_t<float>(const gfea_system* s) {
-  return SysT<float>{s->n_nodes, s->node_ptr, s->nbr, s->vals32, s->known};
+  return SysT<float>{s->n_nodes, s->node_ptr, s->nbr, s->vals32, s->known, s->translation_invariant};
 }
 
 // Launch helpers dispatching (D, G).

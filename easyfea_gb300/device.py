@@ -91,9 +91,13 @@ class DeviceMesh:
 class CsrOperator:
     """CSR values on the node graph of a DeviceMesh (dof_n components/node)."""
 
-    def __init__(self, dmesh: DeviceMesh, dof_n: int, with_f32: bool = False):
+    def __init__(self, dmesh: DeviceMesh, dof_n: int, with_f32: bool = False,
+                 translation_invariant: bool = False):
+        """``translation_invariant``: node block rows sum to zero (elastic
+        stiffness); lets the FP32 products use the difference form."""
         self.dmesh = dmesh
         self.dof_n = dof_n
+        self.translation_invariant = translation_invariant
         self.N = dmesh.Nn * dof_n
         self.nnz = dmesh.nnz(dof_n)
         self.vals64 = torch.zeros(self.nnz, dtype=torch.float64, device=_dev())
@@ -109,7 +113,8 @@ class CsrOperator:
     def system(self, known: torch.Tensor | None) -> _lib.System:
         d = self.dmesh
         return _lib.System(_lib.ABI_VERSION, self.dof_n, d.Nn, d.n_pairs, _lib.ptr(d.node_ptr), _lib.ptr(d.nbr),
-                           _lib.ptr(self.vals64), _lib.ptr(self.vals32), _lib.ptr(known))
+                           _lib.ptr(self.vals64), _lib.ptr(self.vals32), _lib.ptr(known),
+                           int(self.translation_invariant), 0)
 
     def matvec(self, x: torch.Tensor) -> torch.Tensor:
         y = torch.empty_like(x)

@@ -289,7 +289,7 @@ class Elastic(_Simu):
     def Assembly(self, problemType=None) -> CsrOperator:
         """K = sum_e K_e x thickness on the device (_elastic.py:123-152, _simu.py:1104-1144)."""
         dm = self.dmesh
-        op = self.__K if self.__K is not None else CsrOperator(dm, self.dim)
+        op = self.__K if self.__K is not None else CsrOperator(dm, self.dim, translation_invariant=True)
         C, per_elem = self._C_device()
         g = dm.main
         factor = self.material.thickness if self.dim == 2 else 1.0
@@ -512,7 +512,7 @@ class PhaseField(_Simu):
         u, d = self._state()
         g = dm.main
         if self.__Ku is None:
-            self.__Ku = CsrOperator(dm, self.dim)
+            self.__Ku = CsrOperator(dm, self.dim, translation_invariant=True)
         self.__Ku.vals64.zero_()
         p = self._params()
         _lib.check(_lib.load().gfea_pf_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,

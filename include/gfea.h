@@ -187,6 +187,9 @@ typedef struct gfea_system {
   const double* vals64;     /* CSR values, FP64 (may be NULL for FP32-only use) */
   const float* vals32;      /* CSR values, FP32 (may be NULL for FP64-only use) */
   const uint8_t* known;     /* per-DOF Dirichlet mask (1 = known) */
+  int32_t translation_invariant; /* 1: node block rows sum to zero (elastic stiffness);
+                               the FP32 products then use y_a = sum_b K_ab (x_b - x_a) */
+  int32_t pad;
 } gfea_system;
 
 typedef struct gfea_pcg_opts {

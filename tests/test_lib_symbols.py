@@ -39,7 +39,7 @@ def test_host_only_entry_points():
     ws = ctypes.c_size_t()
     assert lib.gfea_graph_workspace_size(100, 50, 4, ctypes.byref(ws)) == 0 and ws.value > 0
     assert lib.gfea_graph_workspace_size(100, 50, 0, ctypes.byref(ws)) == 1  # invalid nPe
-    sysd = _lib.System(_lib.ABI_VERSION, 2, 10, 30, 0, 0, 0, 0, 0)
+    sysd = _lib.System(_lib.ABI_VERSION, 2, 10, 30, 0, 0, 0, 0, 0, 0, 0)
     opts = _lib.PcgOpts(_lib.ABI_VERSION, _lib.F64, 100, 10, 1e-10, 1e-4, 10, 0)
     assert lib.gfea_pcg_workspace_size(ctypes.byref(sysd), ctypes.byref(opts), ctypes.byref(ws)) == 0
     assert ws.value > 20 * 8

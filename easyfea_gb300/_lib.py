@@ -118,6 +118,8 @@ SIGNATURES = {
     "gfea_pcg_workspace_size": (c_int, [POINTER(System), POINTER(PcgOpts), POINTER(c_size_t)]),
     "gfea_pcg_solve": (c_int, [POINTER(System), c_void_p, c_void_p, POINTER(PcgOpts), c_void_p, c_size_t,
                                POINTER(PcgResult), c_void_p]),
+    "gfea_pcg_solve_noalloc": (c_int, [POINTER(System), c_void_p, c_void_p, POINTER(PcgOpts), POINTER(PcgResult),
+                                       c_void_p]),
     "gfea_reduce_workspace_size": (c_size_t, []),
     "gfea_reaction_energy": (c_int, [POINTER(System), c_void_p, c_void_p, c_int64, c_void_p, POINTER(c_double),
                                      c_void_p, c_void_p]),

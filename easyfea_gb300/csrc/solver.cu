@@ -865,3 +865,69 @@ extern "C" int gfea_profile_read(double* ms_host, long long* launches_host) {
   P.n = 0;
   return GFEA_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free PCG.
+//
+// For callers that cannot allocate device memory themselves: a solver embedded
+// in a host application whose device memory is owned by another allocator or
+// pre-reserved pool, or a latency-critical loop where allocation (and the
+// synchronisation it can imply) is not allowed.  The scratch of the solve
+// lives in the file-scope array below, which every GPU that loads this library
+// holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace gfea {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
+
+// Device address of g_static_scratch on the current device (looked up once per
+// device; the array's name in host code is only a host-side stand-in).
+int static_scratch(void** out) {
+  int dev = 0;
+  GFEA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return GFEA_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    GFEA_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return GFEA_OK;
+}
+
+}  // namespace
+}  // namespace gfea
+
+extern "C" int gfea_pcg_solve_noalloc(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o,
+                                      gfea_pcg_result* res, void* stream) {
+  if (!s || !o || !b || !x || !res) return GFEA_ERR_ARG;
+  if (s->version != GFEA_ABI_VERSION || o->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
+  if (s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3 || !s->node_ptr || !s->nbr || !s->known || !s->vals64)
+    return GFEA_ERR_ARG;
+  if (o->max_iters < 1 || !(o->rtol > 0)) return GFEA_ERR_ARG;
+  if (o->precision != GFEA_F64 && (o->precision != GFEA_F32 || !s->vals32)) return GFEA_ERR_ARG;
+  // reject problems whose scratch exceeds the static array, before any device work
+  const size_t need = o->precision == GFEA_F64 ? pcg_layout<double>(s->n_nodes, s->dof_n, nullptr, nullptr)
+                                               : pcg_layout<float>(s->n_nodes, s->dof_n, nullptr, nullptr);
+  if (need > kStaticScratchBytes) return GFEA_ERR_WORKSPACE;
+  void* scratch = nullptr;
+  const int e = static_scratch(&scratch);
+  if (e) return e;
+  res->status = GFEA_OK;
+  res->iterations = 0;
+  res->refinements = 0;
+  res->rel_residual = 0;
+  res->floor_rel = 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (o->precision == GFEA_F64) return refine_solve<double>(s, b, x, o, scratch, kStaticScratchBytes, res, st);
+  return refine_solve<float>(s, b, x, o, scratch, kStaticScratchBytes, res, st);
+}

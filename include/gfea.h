@@ -225,6 +225,23 @@ int gfea_pcg_solve(const gfea_system* sys_host, const double* b, double* x,
                    const gfea_pcg_opts* opts_host, void* work, size_t work_bytes,
                    gfea_pcg_result* result_host, void* stream);
 
+/* gfea_pcg_solve without a workspace argument: allocates nothing.  It has no
+ * counterpart in the reference.  It is meant for callers that cannot allocate
+ * device memory -- a solver embedded in an application whose device memory is
+ * owned by another allocator or a pre-reserved pool, or a latency-critical
+ * loop where allocation is not allowed.  Its scratch is a static 16 MiB array
+ * inside this library (held by every GPU that loads it until the process
+ * exits), so the problem must fit: FP64 needs (7 + dof_n) * 8 bytes per DOF
+ * plus ~40 KB (about 209,000 DOF in 3D, 232,000 in 2D); larger problems are
+ * rejected with GFEA_ERR_WORKSPACE before any device work.  The first call on
+ * a device looks the array's device address up (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls share the array and reset what must start at zero: calls that overlap
+ * on the GPU (different streams or threads) race and must be serialised. */
+int gfea_pcg_solve_noalloc(const gfea_system* sys_host, const double* b, double* x,
+                           const gfea_pcg_opts* opts_host, gfea_pcg_result* result_host,
+                           void* stream);
+
 /* Scratch bytes of the reductions below. */
 size_t gfea_reduce_workspace_size(void);
 

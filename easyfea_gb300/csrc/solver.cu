@@ -125,10 +125,15 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
 // operator whose node block rows sum to zero (rigid translations), but its
 // rounding then scales with the local differences of x rather than with |x|
 // (used by the FP32 products of elastic stiffness matrices).
+//
+// Lane k of the G-lane group takes neighbour k (k, k+G, ...): one index load and
+// D gathers of x per neighbour, then the D x D block of that neighbour (row i
+// of the block is the D consecutive values at base + i W + D k).
 template <int D, int G, typename T, typename A, bool ABS = false, bool DIFF = false, typename XF>
 __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S, XF xf, A (&acc)[D]) {
   const int32_t p0 = S.node_ptr[a];
-  const int32_t W = D * (S.node_ptr[a + 1] - p0);
+  const int32_t nb = S.node_ptr[a + 1] - p0;
+  const int32_t W = D * nb;
   const T* base = S.vals + (int64_t)D * D * p0;
   A self[D];
 #pragma unroll
@@ -136,19 +141,19 @@ __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S,
     acc[i] = 0;
     self[i] = DIFF ? xf(a * D + i) : (A)0;
   }
-  for (int32_t t = lane; t < W; t += G) {
-    const int32_t k = t / D, j = t - k * D;
-    const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
-    A xv = xf(col);
-    if (DIFF) {
+  for (int32_t k = lane; k < nb; k += G) {
+    const int64_t c = (int64_t)__ldg(S.nbr + p0 + k) * D;
+    A xv[D];
 #pragma unroll
-      for (int jj = 0; jj < D; ++jj)
-        if (jj == j) xv -= self[jj];
-    }
+    for (int j = 0; j < D; ++j) xv[j] = DIFF ? xf(c + j) - self[j] : xf(c + j);
+    const T* blk = base + D * k;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      const A v = (A)__ldg(base + (int64_t)i * W + t);
-      acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv;
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const A v = (A)__ldg(blk + (int64_t)i * W + j);
+        acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv[j];
+      }
     }
   }
 #pragma unroll
@@ -454,10 +459,11 @@ size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int pick_lanes(const gfea_system* s, int requested) {
   if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
-  const double W = s->n_nodes > 0 ? (double)s->dof_n * (double)s->n_pairs / (double)s->n_nodes : 1.0;
-  if (W <= 10) return 4;
-  if (W <= 24) return 8;
-  if (W <= 56) return 16;
+  // lanes take neighbours: cover the average neighbour count in one pass
+  const double nb = s->n_nodes > 0 ? (double)s->n_pairs / (double)s->n_nodes : 1.0;
+  if (nb <= 4.5) return 4;
+  if (nb <= 8.5) return 8;
+  if (nb <= 16.5) return 16;
   return 32;
 }
 
@@ -648,9 +654,11 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   const int check = o->check_every > 0 ? o->check_every : 32;
   const bool fp64 = sizeof(T) == 8;
   const double eps64 = 2.220446049250313e-16;
-  // reliable update after the iterated residual fell by delta: 10x in FP32 (its
-  // recursive residual drifts from the true one by ~eps32 * condition), 1000x in FP64
-  const double delta2 = fp64 ? 1e-6 : 1e-2;
+  // reliable update after the iterated residual fell by delta: inner_rtol
+  // (default 0.1) in FP32, whose recursive residual drifts from the true one
+  // by ~eps32 * condition; 1000x in FP64
+  const double dlt = (o->inner_rtol > 0 && o->inner_rtol < 1) ? o->inner_rtol : 0.1;
+  const double delta2 = fp64 ? 1e-6 : dlt * dlt;
   Scal hs;
   GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
   GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));

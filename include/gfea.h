@@ -199,7 +199,8 @@ typedef struct gfea_pcg_opts {
   int32_t check_every;      /* host convergence check period (iterations) */
   double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)||; the solve
                                stops at max(rtol, rounding floor), see gfea_pcg_result */
-  double inner_rtol;        /* FP32 inner solve reduction per refinement step */
+  double inner_rtol;        /* FP32: reduction of the iterated residual between FP64
+                               residual replacements (reliable updates), default 0.1 */
   int32_t max_refine;       /* refinement steps cap (mixed precision) */
   int32_t lanes;            /* SpMV lanes per node (0 = automatic) */
 } gfea_pcg_opts;

@@ -126,33 +126,31 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
 // rounding then scales with the local differences of x rather than with |x|
 // (used by the FP32 products of elastic stiffness matrices).
 //
-// Lane k of the G-lane group takes neighbour k (k, k+G, ...): one index load and
-// D gathers of x per neighbour, then the D x D block of that neighbour (row i
-// of the block is the D consecutive values at base + i W + D k).
+// Lane l of the G-lane group owns component j = l % D of neighbours
+// k = l / D, l / D + G/D, ... (the first G - G % D lanes are active): its slot
+// t = D k + j advances by G - G % D, so the value loads of a row stay
+// contiguous across lanes, and the component, the own-node value of the
+// difference form and the slot stride are fixed per lane.
 template <int D, int G, typename T, typename A, bool ABS = false, bool DIFF = false, typename XF>
 __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S, XF xf, A (&acc)[D]) {
+  constexpr int LA = G - G % D;  // active lanes
+  constexpr int NPP = LA / D;    // neighbours per pass
   const int32_t p0 = S.node_ptr[a];
   const int32_t nb = S.node_ptr[a + 1] - p0;
   const int32_t W = D * nb;
   const T* base = S.vals + (int64_t)D * D * p0;
-  A self[D];
+  const int j = lane % D;
 #pragma unroll
-  for (int i = 0; i < D; ++i) {
-    acc[i] = 0;
-    self[i] = DIFF ? xf(a * D + i) : (A)0;
-  }
-  for (int32_t k = lane; k < nb; k += G) {
-    const int64_t c = (int64_t)__ldg(S.nbr + p0 + k) * D;
-    A xv[D];
+  for (int i = 0; i < D; ++i) acc[i] = 0;
+  if (lane < LA) {
+    const A self = DIFF ? xf(a * D + j) : (A)0;
+    for (int32_t k = lane / D, t = lane; k < nb; k += NPP, t += LA) {
+      const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
+      const A xv = DIFF ? xf(col) - self : xf(col);
 #pragma unroll
-    for (int j = 0; j < D; ++j) xv[j] = DIFF ? xf(c + j) - self[j] : xf(c + j);
-    const T* blk = base + D * k;
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-#pragma unroll
-      for (int j = 0; j < D; ++j) {
-        const A v = (A)__ldg(blk + (int64_t)i * W + j);
-        acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv[j];
+      for (int i = 0; i < D; ++i) {
+        const A v = (A)__ldg(base + (int64_t)i * W + t);
+        acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv;
       }
     }
   }
@@ -459,11 +457,11 @@ size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int pick_lanes(const gfea_system* s, int requested) {
   if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
-  // lanes take neighbours: cover the average neighbour count in one pass
-  const double nb = s->n_nodes > 0 ? (double)s->n_pairs / (double)s->n_nodes : 1.0;
-  if (nb <= 4.5) return 4;
-  if (nb <= 8.5) return 8;
-  if (nb <= 16.5) return 16;
+  // values per row W = dof_n * neighbours: small groups for short rows
+  const double W = s->n_nodes > 0 ? (double)s->dof_n * (double)s->n_pairs / (double)s->n_nodes : 1.0;
+  if (W <= 10) return 4;
+  if (W <= 24) return 8;
+  if (W <= 56) return 16;
   return 32;
 }
 

@@ -73,6 +73,27 @@ class PcgResult(ctypes.Structure):
     ]
 
 
+class BatchInstance(ctypes.Structure):
+    _fields_ = [
+        ("version", c_int32),
+        ("dof_n", c_int32),
+        ("n_nodes", c_int64),
+        ("n_pairs", c_int64),
+        ("node_ptr", c_void_p),
+        ("nbr", c_void_p),
+        ("vals64", c_void_p),
+        ("vals32", c_void_p),
+        ("known", c_void_p),
+        ("translation_invariant", c_int32),
+        ("max_iters", c_int32),
+        ("rtol", c_double),
+        ("b", c_void_p),
+        ("x", c_void_p),
+        ("work", c_void_p),
+        ("result", c_void_p),
+    ]
+
+
 class PfParams(ctypes.Structure):
     _fields_ = [
         ("version", c_int32),
@@ -120,6 +141,9 @@ SIGNATURES = {
                                POINTER(PcgResult), c_void_p]),
     "gfea_pcg_solve_noalloc": (c_int, [POINTER(System), c_void_p, c_void_p, POINTER(PcgOpts), POINTER(PcgResult),
                                        c_void_p]),
+    "gfea_batch_workspace_size": (c_size_t, [c_int64, c_int, c_int]),
+    "gfea_batch_scratch_size": (c_size_t, [c_int]),
+    "gfea_batch_pcg": (c_int, [POINTER(BatchInstance), c_int, c_void_p, c_size_t, POINTER(PcgOpts), c_void_p]),
     "gfea_reduce_workspace_size": (c_size_t, []),
     "gfea_reaction_energy": (c_int, [POINTER(System), c_void_p, c_void_p, c_int64, c_void_p, POINTER(c_double),
                                      c_void_p, c_void_p]),

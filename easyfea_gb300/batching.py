@@ -1,0 +1,150 @@
+"""Batched solves: many independent systems assembled and solved together.
+
+The reference solves instances one after another (one ``Simulations.*.Solve``
+and one SuperLU factorisation each, EasyFEA/Simulations/Solvers.py:361).
+Here a batch of Dirichlet-reduced systems of any sizes goes to
+``gfea_batch_pcg``: one persistent launch in which each thread-block cluster
+solves one system at a time (largest first), with per-system scalars and
+convergence, so a system's result does not depend on the rest of the batch.
+
+``random_material_cantilevers`` builds the random-material workload: 2D
+plane-stress cantilevers (the L = 120, h = 13 bar) with sizes drawn
+log-uniform in DOF and a per-element Young's modulus
+E_e = 210000 exp(0.3 g(x_e)), g a zero-mean, unit-variance Gaussian field from
+64 random Fourier features (Rahimi & Recht 2007) with correlation length
+0.1 L, evaluated at element centroids.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import CsrOperator, PcgInfo
+
+
+def _dev():
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+@dataclass
+class BatchSystem:
+    """One Dirichlet-reduced system: x holds the known values (and the initial
+    guess) on entry and the solution on exit."""
+
+    op: CsrOperator
+    b: torch.Tensor
+    x: torch.Tensor
+    known: torch.Tensor
+    rtol: float = 1e-10
+    max_iters: int = 200000
+
+
+RESULT_BYTES = ctypes.sizeof(_lib.PcgResult)
+
+
+class BatchSolver:
+    """Reusable buffers for repeated batches (workspace arena, descriptors, results)."""
+
+    def __init__(self):
+        self._arena = None
+        self._scratch = None
+        self._results = None
+
+    def _ensure(self, t: Optional[torch.Tensor], nbytes: int) -> torch.Tensor:
+        if t is None or t.numel() < nbytes:
+            t = torch.empty(max(nbytes, 1 << 16), dtype=torch.uint8, device=_dev())
+        return t
+
+    def launch(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1):
+        """Enqueue the batch on the current stream (asynchronous)."""
+        L = _lib.load()
+        prec = _lib.F64 if precision == "fp64" else _lib.F32
+        n = len(systems)
+        sizes = []
+        for s in systems:
+            if prec == _lib.F32 and s.op.vals32 is None:
+                s.op.ensure_f32()
+            sizes.append(int(L.gfea_batch_workspace_size(s.op.dmesh.Nn, s.op.dof_n, prec)))
+        offs = np.concatenate([[0], np.cumsum([(z + 255) // 256 * 256 for z in sizes])]).astype(np.int64)
+        self._arena = self._ensure(self._arena, int(offs[-1]))
+        self._results = self._ensure(self._results, n * RESULT_BYTES)
+        nscr = int(L.gfea_batch_scratch_size(n))
+        self._scratch = self._ensure(self._scratch, nscr)
+        arr = (_lib.BatchInstance * n)()
+        base = self._arena.data_ptr()
+        rbase = self._results.data_ptr()
+        for i, s in enumerate(systems):
+            d = s.op.dmesh
+            arr[i] = _lib.BatchInstance(
+                _lib.ABI_VERSION, s.op.dof_n, d.Nn, d.n_pairs, _lib.ptr(d.node_ptr), _lib.ptr(d.nbr),
+                _lib.ptr(s.op.vals64), _lib.ptr(s.op.vals32) if prec == _lib.F32 else 0, _lib.ptr(s.known),
+                int(s.op.translation_invariant), int(s.max_iters), float(s.rtol), _lib.ptr(s.b), _lib.ptr(s.x),
+                base + int(offs[i]), rbase + i * RESULT_BYTES)
+        opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 0, 0, 0.0, float(inner_rtol), 0, 0)
+        _lib.check(L.gfea_batch_pcg(arr, n, _lib.ptr(self._scratch), self._scratch.numel(), ctypes.byref(opts),
+                                    _lib.stream()), "batch pcg")
+        self._n = n
+
+    def results(self) -> List[PcgInfo]:
+        """Per-system outcome (synchronises the stream)."""
+        raw = self._results[: self._n * RESULT_BYTES].cpu().numpy().tobytes()
+        out = []
+        for i in range(self._n):
+            r = _lib.PcgResult.from_buffer_copy(raw[i * RESULT_BYTES:(i + 1) * RESULT_BYTES])
+            out.append(PcgInfo(int(r.status), int(r.iterations), int(r.refinements), float(r.rel_residual),
+                               float(r.floor_rel)))
+        return out
+
+    def solve(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
+              raise_on_fail: bool = True) -> List[PcgInfo]:
+        self.launch(systems, precision, inner_rtol)
+        infos = self.results()
+        if raise_on_fail:
+            for i, info in enumerate(infos):
+                _lib.check(info.status, f"batch system {i} (iterations {info.iterations}, "
+                                        f"rel residual {info.rel_residual:.3e})")
+        return infos
+
+
+def solve_batch(systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
+                raise_on_fail: bool = True) -> List[PcgInfo]:
+    return BatchSolver().solve(systems, precision, inner_rtol, raise_on_fail)
+
+
+# ---------------------------------------------------------------------------
+# random-material workload
+# ---------------------------------------------------------------------------
+
+def fourier_field(points: np.ndarray, rng: np.random.Generator, ell: float, modes: int = 64) -> np.ndarray:
+    """Zero-mean, unit-variance Gaussian field with squared-exponential
+    correlation of length ``ell``: sqrt(2/M) sum cos(k_m . x + phi_m),
+    k_m ~ N(0, ell^-2 I), phi_m ~ U(0, 2 pi)."""
+    dim = points.shape[1]
+    k = rng.normal(0.0, 1.0 / ell, size=(modes, dim))
+    phi = rng.uniform(0.0, 2 * np.pi, size=modes)
+    return np.sqrt(2.0 / modes) * np.cos(points @ k.T + phi).sum(axis=1)
+
+
+def random_material_cantilevers(n: int = 256, seed: int = 0, dof_min: float = 2e3, dof_max: float = 2e5,
+                                L: float = 120.0, h: float = 13.0):
+    """[(mesh, E_e)] for ``n`` cantilevers with per-instance seeds ``seed + i``."""
+    from .mesh import Mesh_Quad4_Rect
+
+    out = []
+    for i in range(n):
+        rng = np.random.default_rng(seed + i)
+        N = np.exp(rng.uniform(np.log(dof_min), np.log(dof_max)))
+        ny = max(1, int(round(np.sqrt(N / 2 * h / L))))
+        nx = max(1, int(round(ny * L / h)))
+        m = Mesh_Quad4_Rect(L, h, nx, ny)
+        cent = m.coord[np.asarray(m.connect)].mean(axis=1)[:, :2]
+        g = fourier_field(cent, rng, 0.1 * L)
+        E = 210000.0 * np.exp(0.3 * g)
+        out.append((m, E))
+    return out

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
   __shared__ RefTables<ELEM, false> ref;
   __shared__ R Csh[NS * NS];
   ref.fill();
-  if (CMODE == 0)
+  if (CMODE != 1)  // homogeneous C, or the reference C of mode 2
     for (int i = threadIdx.x; i < NS * NS; i += blockDim.x) Csh[i] = (R)Cglob[i];
   __syncthreads();
 
@@ -151,6 +151,8 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
       const int32_t p0 = node_ptr[a];
       const int32_t nb = node_ptr[a + 1] - p0;
       const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
+      // mode 2: per-element factor of the reference C (e.g. a per-element Young's modulus)
+      const double f = CMODE == 2 ? factor * __ldg(Cglob + NS * NS + ec) : factor;
 #pragma unroll
       for (int i = 0; i < D; ++i) {
         T* row = vals + (int64_t)D * D * p0 + (int64_t)i * D * nb;
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
         for (int q = 0; q < nPe; ++q) {
           const int r = rk[q];
 #pragma unroll
-          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + D * r + j, (T)(factor * (double)acc[q][i][j]));
+          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + D * r + j, (T)(f * (double)acc[q][i][j]));
         }
       }
     }
@@ -267,8 +269,10 @@ int launch_elastic(const double* coord, const int32_t* connect, int64_t Ne, cons
   const int64_t warps = ceil_div(Ne, 32 / G);
   int blocks = grid_for(warps * 32, 128);
   if (blocks > kSMs * 64) blocks = kSMs * 64;
-  if (cpe)
+  if (cpe == 1)
     elastic_kernel<ELEM, T, R, 1><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
+  else if (cpe == 2)
+    elastic_kernel<ELEM, T, R, 2><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
   else
     elastic_kernel<ELEM, T, R, 0><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
   GFEA_LAUNCH_CHECK();

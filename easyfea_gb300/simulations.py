@@ -282,9 +282,17 @@ class Elastic(_Simu):
             self.__M = None
 
     def _C_device(self):
-        C = self.material.C
-        per_elem = C.ndim == 3
-        return torch.as_tensor(np.ascontiguousarray(C, dtype=np.float64), device=_dev()), per_elem
+        """(C tensor, mode) for gfea_assemble_elastic: homogeneous (0), or a
+        reference C for E = 1 followed by the per-element moduli (2)."""
+        mat = self.material
+        if getattr(mat, "isHeterogeneous", False) and isinstance(mat, ElasticModels.Isotropic):
+            E = np.asarray(mat.E, dtype=np.float64).ravel()
+            assert E.size == self.mesh.Ne, "per-element E must have one value per element"
+            ref = ElasticModels.Isotropic(mat.dim, E=1.0, v=mat.v, planeStress=mat.planeStress).C
+            buf = np.concatenate([ref.ravel(), E])
+            return torch.as_tensor(buf, device=_dev()), 2
+        C = mat.C
+        return torch.as_tensor(np.ascontiguousarray(C, dtype=np.float64), device=_dev()), 1 if C.ndim == 3 else 0
 
     def Assembly(self, problemType=None) -> CsrOperator:
         """K = sum_e K_e x thickness on the device (_elastic.py:123-152, _simu.py:1104-1144)."""

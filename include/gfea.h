@@ -100,7 +100,9 @@ int gfea_csr_pattern(const int32_t* node_ptr, const int32_t* nbr, int64_t n_node
  * (EasyFEA/Simulations/_elastic.py:123-152) and _Simu.__Assemble_csr's
  * bincount (EasyFEA/Simulations/_simu.py:989-1060).
  * C: Kelvin-Mandel (3x3 in 2D, 6x6 in 3D), c_per_elem = 0 homogeneous,
- * 1 per element (Ne x n x n, Models/_utils.py:69-108).
+ * 1 per element (Ne x n x n, Models/_utils.py:69-108), 2 a reference n x n
+ * matrix followed by Ne per-element factors (C_e = f_e C_ref, e.g. a
+ * per-element Young's modulus with a constant Poisson ratio).
  * values (value_type GFEA_F64/F32, n_values = dof_n^2 * n_pairs entries) are
  * zeroed first unless accumulate != 0. */
 int gfea_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
@@ -213,6 +215,43 @@ typedef struct gfea_pcg_result {
   double rel_residual;      /* final FP64 ||P(b - A x)|| / ||P(b - A x_c)|| */
   double floor_rel;         /* rounding floor of that residual: 32 eps ||P(|A||x|+|b|)|| / ||P(b - A x_c)|| */
 } gfea_pcg_result;
+
+/* ------------------------------------------------------------------------
+ * Batched solves: many independent Dirichlet-reduced systems (different
+ * sizes, dof_n 1-3) solved in one persistent launch.  Each thread-block
+ * cluster takes one system at a time and runs its whole PCG (FP32 iteration
+ * with FP64 reliable updates, or FP64) with cluster-wide reductions, so a
+ * system's result does not depend on the other systems in the batch.  This
+ * is the batched driver behind the reference's per-instance loop of
+ * Simulations.*.Solve calls (one SuperLU solve each, Solvers.py:361).
+ * ---------------------------------------------------------------------- */
+typedef struct gfea_batch_instance {
+  int32_t version;          /* GFEA_ABI_VERSION */
+  int32_t dof_n;
+  int64_t n_nodes;
+  int64_t n_pairs;
+  const int32_t* node_ptr;
+  const int32_t* nbr;
+  const double* vals64;     /* FP64 CSR values (residuals) */
+  const float* vals32;      /* FP32 copy (FP32 iteration); may be NULL for FP64 batches */
+  const uint8_t* known;
+  int32_t translation_invariant;
+  int32_t max_iters;
+  double rtol;
+  const double* b;          /* right-hand side */
+  double* x;                /* in: known values + initial guess; out: solution */
+  void* work;               /* gfea_batch_workspace_size() bytes, 256-byte aligned */
+  gfea_pcg_result* result;  /* device pointer, written when the system's solve ends */
+} gfea_batch_instance;
+
+size_t gfea_batch_workspace_size(int64_t n_nodes, int dof_n, int precision);
+size_t gfea_batch_scratch_size(int n_instances);
+/* Enqueues the batch on the stream and returns; results are valid once the
+ * stream has completed.  scratch: gfea_batch_scratch_size(n) device bytes
+ * (work counter + descriptors).  opts: precision (GFEA_F32 / GFEA_F64) and
+ * inner_rtol (FP32 reliable-update trigger); rtol and max_iters are per system. */
+int gfea_batch_pcg(const gfea_batch_instance* instances_host, int n, void* scratch, size_t scratch_bytes,
+                   const gfea_pcg_opts* opts_host, void* stream);
 
 /* y = A x (unmasked), value_type selects vals64/x,y double or vals32/x,y float. */
 int gfea_spmv(const gfea_system* sys_host, int value_type, const void* x, void* y, void* stream);

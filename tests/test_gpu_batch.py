@@ -1,0 +1,88 @@
+"""Batched cluster-resident PCG (gfea_batch_pcg) against single solves and the oracle."""
+
+import numpy as np
+import pytest
+
+from easyfea_gb300 import mesh as gmesh
+
+pytestmark = pytest.mark.gpu
+
+
+def elastic_system(m, E, v=0.3, thickness=13.0, load=-800 / 13**2, rtol=1e-10):
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import simulations as Simulations
+    from easyfea_gb300.batching import BatchSystem
+
+    dim = m.dim
+    mat = Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=True, thickness=thickness)
+    simu = Simulations.Elastic(m, mat)
+    L = m.coord[:, 0].max()
+    left = m.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = m.Nodes_Conditions(lambda x, y, z: x == L)
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    simu.add_dirichlet(left, [0.0] * dim, unk)
+    simu.add_surfLoad(right, [load], ["y" if dim == 2 else "z"])
+    op = simu.K_device
+    b = simu._neumann_vec("elastic")
+    known, x = simu._dirichlet_state("elastic", b)
+    return simu, BatchSystem(op, b, x, known, rtol=rtol), (left, right)
+
+
+def mixed_batch():
+    ms = [gmesh.Mesh_Quad4_Rect(120.0, 13.0, 48, 6), gmesh.Mesh_Tri3_Rect(120.0, 13.0, 30, 5),
+          gmesh.Mesh_Quad9_Rect(120.0, 13.0, 12, 3), gmesh.Mesh_Hexa8_Box(60.0, 10.0, 10.0, 12, 2, 2),
+          gmesh.Mesh_Quad4_Rect(120.0, 13.0, 120, 13)]
+    return [elastic_system(m, 210000.0)[1] for m in ms]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_single_solves(precision):
+    from easyfea_gb300.batching import solve_batch
+    from easyfea_gb300.device import pcg
+
+    systems = mixed_batch()
+    x0 = [s.x.clone() for s in systems]
+    infos = solve_batch(systems, precision=precision)
+    for s, x_init, info in zip(systems, x0, infos):
+        assert info.status == 0
+        assert info.rel_residual <= max(1e-10, info.floor_rel)
+        xs = x_init.clone()
+        pcg(s.op, s.b, xs, s.known, rtol=1e-12, precision="fp64")
+        ref = xs.cpu().numpy()
+        err = np.abs(s.x.cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err <= 1e-7, f"relative difference {err:.3e}"
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_result_identical_alone_and_in_the_mix(precision):
+    """A system's solution does not depend on the other systems of the batch."""
+    from easyfea_gb300.batching import solve_batch
+
+    systems = mixed_batch()
+    x0 = [s.x.clone() for s in systems]
+    solve_batch(systems, precision=precision)
+    mixed = [s.x.clone() for s in systems]
+    for k in (0, 3, 4):
+        s = systems[k]
+        s.x.copy_(x0[k])
+        solve_batch([s], precision=precision)
+        assert np.array_equal(s.x.cpu().numpy(), mixed[k].cpu().numpy()), f"system {k} differs alone / in the mix"
+
+
+def test_random_material_batch_matches_oracle():
+    """Per-element E from a random Fourier field (the batched random-material
+    workload), against the oracle's SuperLU solves."""
+    from easyfea_gb300.batching import random_material_cantilevers, solve_batch
+    from oracle.simulate import OracleMesh, elastic_solve
+
+    inst = random_material_cantilevers(n=6, seed=100, dof_min=300, dof_max=3000)
+    sims = [elastic_system(m, E) for m, E in inst]
+    infos = solve_batch([s[1] for s in sims], precision="mixed")
+    for (m, E), (simu, sys_, (left, right)), info in zip(inst, sims, infos):
+        assert info.status == 0
+        u_ref, K_ref, _ = elastic_solve(OracleMesh.from_mesh(m), E, 0.3, True, 13.0,
+                                        [(left, [0.0, 0.0], ["x", "y"])], [(right, [-800 / 13**2], ["y"])])
+        K = simu.Get_K_C_M_F()[0]
+        assert abs(K - K_ref).max() <= 1e-12 * abs(K_ref).max()
+        u = sys_.x.cpu().numpy()
+        assert np.abs(u - u_ref).max() <= 1e-8 * np.abs(u_ref).max()

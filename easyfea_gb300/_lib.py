@@ -46,6 +46,7 @@ class System(ctypes.Structure):
         ("known", c_void_p),
         ("translation_invariant", c_int32),
         ("pad", c_int32),
+        ("coord", c_void_p),
     ]
 
 
@@ -59,6 +60,8 @@ class PcgOpts(ctypes.Structure):
         ("inner_rtol", c_double),
         ("max_refine", c_int32),
         ("lanes", c_int32),
+        ("coarse", c_int32),
+        ("coarse_reuse", c_int32),
     ]
 
 

@@ -260,6 +260,357 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
   }
 }
 
+// ---------------------------------------------------------------------------
+// Two-level preconditioner: M^-1 r = D^-1 r + P A_c^-1 P^T r.  P maps each
+// aggregate (a cell of a regular grid over the bounding box) to the rigid-body
+// modes of its nodes -- translations and rotations about the cell centre
+// (constants for a scalar field) -- with known DOFs masked out; A_c = P^T A P
+// is assembled from the FP64 CSR values and inverted densely (FP64
+// Gauss-Jordan) once per solve.  Per iteration: restriction fused into the
+// residual update, one dense coarse GEMV, prolongation fused into z.
+// ---------------------------------------------------------------------------
+
+constexpr int kCoarseMax = 1536;  // largest coarse dimension nr * n_agg
+
+// Aggregation kept at the start of the coarse workspace, so that a later
+// solve on the same mesh can reuse it.
+struct CoarseHdr {
+  int32_t n_agg, nc, nr, valid;
+  int64_t Nn;
+};
+
+struct CoarseDev {
+  int nr = 0, n_agg = 0, nc = 0;
+  CoarseHdr* hdr = nullptr;
+  int32_t* agg = nullptr;  // node -> aggregate
+  float4* off = nullptr;   // node offset from its cell centre / largest cell size
+  double* Ac = nullptr;    // nc x nc, inverted in place
+  double* rowb = nullptr;  // 2 x nc: pivot-row snapshots (by step parity)
+  double* colb = nullptr;  // 2 x nc: pivot-column snapshots
+  double* rc = nullptr;    // nc: restriction accumulator
+  double* ec = nullptr;    // nc: coarse correction
+};
+
+template <int D>
+struct Modes {
+  static constexpr int nr = D == 1 ? 1 : (D == 2 ? 3 : 6);
+};
+
+// Rigid-body modes at one node (D x nr), rows of known DOFs zeroed.
+template <int D>
+__device__ __forceinline__ void node_modes(float4 o, const uint8_t* kn, double (&R)[D][Modes<D>::nr]) {
+  if constexpr (D == 1) {
+    R[0][0] = kn[0] ? 0.0 : 1.0;
+  } else if constexpr (D == 2) {
+    const double dx = o.x, dy = o.y;
+    const double r0[3] = {1, 0, -dy}, r1[3] = {0, 1, dx};
+    const bool k0 = kn[0], k1 = kn[1];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      R[0][m] = k0 ? 0.0 : r0[m];
+      R[1][m] = k1 ? 0.0 : r1[m];
+    }
+  } else {
+    const double dx = o.x, dy = o.y, dz = o.z;
+    const double r0[6] = {1, 0, 0, 0, dz, -dy}, r1[6] = {0, 1, 0, -dz, 0, dx}, r2[6] = {0, 0, 1, dy, -dx, 0};
+    const bool k0 = kn[0], k1 = kn[1], k2 = kn[2];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      R[0][m] = k0 ? 0.0 : r0[m];
+      R[1][m] = k1 ? 0.0 : r1[m];
+      R[2][m] = k2 ? 0.0 : r2[m];
+    }
+  }
+}
+
+__global__ void bbox_kernel(const double* __restrict__ coord, int64_t Nn, double* partials) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fmin(lo[k], coord[a * 3 + k]);
+      hi[k] = fmax(hi[k], coord[a * 3 + k]);
+    }
+  __shared__ double s[6][kThreads];
+  for (int k = 0; k < 3; ++k) {
+    s[k][threadIdx.x] = lo[k];
+    s[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 3; ++k) {
+        s[k][threadIdx.x] = fmin(s[k][threadIdx.x], s[k][threadIdx.x + o]);
+        s[3 + k][threadIdx.x] = fmax(s[3 + k][threadIdx.x], s[3 + k][threadIdx.x + o]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) partials[blockIdx.x * 6 + k] = s[k][0];
+}
+
+// Cell of each node (the longest extent varies slowest, which keeps the
+// coarse matrix banded) and its offset from the cell centre, scaled by hinv.
+__global__ void aggregate_kernel(const double* __restrict__ coord, int64_t Nn, double3 lo, double3 h, int3 cells,
+                                 int3 order, double hinv, int32_t* agg, float4* off) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    const double x = coord[a * 3], y = coord[a * 3 + 1], z = coord[a * 3 + 2];
+    int ix = (int)floor((x - lo.x) / h.x), iy = (int)floor((y - lo.y) / h.y), iz = (int)floor((z - lo.z) / h.z);
+    ix = ix < 0 ? 0 : (ix >= cells.x ? cells.x - 1 : ix);
+    iy = iy < 0 ? 0 : (iy >= cells.y ? cells.y - 1 : iy);
+    iz = iz < 0 ? 0 : (iz >= cells.z ? cells.z - 1 : iz);
+    const int idx[3] = {ix, iy, iz}, n[3] = {cells.x, cells.y, cells.z};
+    // order.x varies fastest, order.z slowest
+    agg[a] = idx[order.x] + n[order.x] * (idx[order.y] + n[order.y] * idx[order.z]);
+    off[a] = make_float4((float)((x - (lo.x + (ix + 0.5) * h.x)) * hinv),
+                         (float)((y - (lo.y + (iy + 0.5) * h.y)) * hinv),
+                         (float)((z - (lo.z + (iz + 0.5) * h.z)) * hinv), 0.f);
+  }
+}
+
+// A_c += R_a^T K_ab R_b, summed per node over neighbours sharing an aggregate.
+template <int D>
+__global__ void coarse_assemble_kernel(SysT<double> S, CoarseDev C) {
+  constexpr int nr = Modes<D>::nr;
+  constexpr int kSlots = 8;
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < S.Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    const int ga = C.agg[a];
+    double Ra[D][nr];
+    node_modes<D>(C.off[a], S.known + a * D, Ra);
+    int sid[kSlots];
+    double acc[kSlots][nr][nr];
+    int ns = 0;
+    const int32_t p0 = S.node_ptr[a], nb = S.node_ptr[a + 1] - p0;
+    const int32_t W = D * nb;
+    for (int k = 0; k < nb; ++k) {
+      const int32_t b = S.nbr[p0 + k];
+      const int gb = C.agg[b];
+      double Rb[D][nr];
+      node_modes<D>(C.off[b], S.known + (int64_t)b * D, Rb);
+      // K_ab R_b (D x nr)
+      double KR[D][nr];
+      for (int i = 0; i < D; ++i)
+        for (int m = 0; m < nr; ++m) {
+          double v = 0;
+          for (int j = 0; j < D; ++j) v += S.vals[(int64_t)D * D * p0 + (int64_t)i * W + D * k + j] * Rb[j][m];
+          KR[i][m] = v;
+        }
+      int slot = -1;
+      for (int q = 0; q < ns; ++q)
+        if (sid[q] == gb) slot = q;
+      if (slot < 0) {
+        if (ns == kSlots) {  // flush (rare: more distinct neighbour aggregates than slots)
+          for (int q = 0; q < ns; ++q)
+            for (int m = 0; m < nr; ++m)
+              for (int l = 0; l < nr; ++l)
+                atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], acc[q][m][l]);
+          ns = 0;
+        }
+        slot = ns++;
+        sid[slot] = gb;
+        for (int m = 0; m < nr; ++m)
+          for (int l = 0; l < nr; ++l) acc[slot][m][l] = 0;
+      }
+      for (int m = 0; m < nr; ++m)
+        for (int l = 0; l < nr; ++l) {
+          double v = 0;
+          for (int i = 0; i < D; ++i) v += Ra[i][m] * KR[i][l];
+          acc[slot][m][l] += v;
+        }
+    }
+    for (int q = 0; q < ns; ++q)
+      for (int m = 0; m < nr; ++m)
+        for (int l = 0; l < nr; ++l)
+          atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], acc[q][m][l]);
+  }
+}
+
+// Unit diagonal for empty or fully constrained coarse DOFs, a 1e-10 relative
+// shift elsewhere (rotation modes of degenerate aggregates), identity in inv.
+__global__ void coarse_regularize_kernel(CoarseDev C) {
+  __shared__ double smax[256];
+  double m = 0;
+  for (int i = threadIdx.x; i < C.nc; i += blockDim.x) m = fmax(m, fabs(C.Ac[(int64_t)i * C.nc + i]));
+  smax[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const double dmax = smax[0] > 0 ? smax[0] : 1.0;
+  for (int i = threadIdx.x; i < C.nc; i += blockDim.x) {
+    double& d = C.Ac[(int64_t)i * C.nc + i];
+    d = d > 1e-14 * dmax ? d + 1e-10 * dmax : dmax;
+  }
+}
+
+// In-place Gauss-Jordan inversion of the SPD coarse matrix (no pivoting:
+// every pivot of an SPD matrix is positive), one launch per pivot k.  Each
+// element is read and written by one thread; the pivot row and column of step
+// k come from snapshots written by step k - 1 (gj_init for k = 0).
+__global__ void gj_init_kernel(CoarseDev C) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) {
+    C.rowb[i] = C.Ac[i];
+    C.colb[i] = C.Ac[(int64_t)i * C.nc];
+  }
+}
+
+// Pivot step k: block (bx, by) owns column j = bx * blockDim + tid and rows
+// by, by + gridDim.y, ...; coalesced along rows, one FMA per element.
+__global__ void gj_step_kernel(CoarseDev C, int k) {
+  const int n = C.nc;
+  const double* row = C.rowb + (k & 1) * n;
+  const double* col = C.colb + (k & 1) * n;
+  double* nrow = C.rowb + ((k + 1) & 1) * n;
+  double* ncol = C.colb + ((k + 1) & 1) * n;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double ip = 1.0 / row[k];
+  const double rj = row[j] * ip;
+  for (int i = blockIdx.y; i < n; i += gridDim.y) {
+    double* p = C.Ac + (int64_t)i * n + j;
+    double v;
+    if (i == k)
+      v = j == k ? ip : rj;
+    else
+      v = j == k ? -col[i] * ip : *p - col[i] * rj;
+    *p = v;
+    if (i == k + 1) nrow[j] = v;
+    if (j == k + 1) ncol[i] = v;
+  }
+}
+
+// Sum of nr per-lane values into rc[g * nr + m] (g < 0: lane without a node):
+// a segmented warp scan over runs of equal g, one atomic per run and mode.
+template <int nr>
+__device__ __forceinline__ void restrict_add(double* rc, int g, double (&v)[nr]) {
+  const int lane = threadIdx.x & 31;
+  const int gp = __shfl_up_sync(0xffffffffu, g, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || g != gp);
+  const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // first lane of this lane's run
+  const int gn = __shfl_down_sync(0xffffffffu, g, 1);
+  const bool tail = lane == 31 || gn != g;
+#pragma unroll
+  for (int m = 0; m < nr; ++m) {
+    double s = v[m];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane - d >= start) s += t;
+    }
+    if (tail && g >= 0 && s != 0) atomicAdd(&rc[g * nr + m], s);
+  }
+}
+
+// x, r update (mode 0) and restriction rc += R_a^T r_a.  The node loop runs
+// whole warps (stride a multiple of 32) for the warp-level pre-reduction.
+template <int D, typename T>
+__global__ void __launch_bounds__(kThreads) update_r_kernel(int64_t Nn, const uint8_t* __restrict__ known,
+                                                            T* __restrict__ x,
+                                                            T* __restrict__ r, const T* __restrict__ p,
+                                                            const T* __restrict__ Ap, Scal* sc, CoarseDev C,
+                                                            int mode) {
+  if (mode == 0 && sc->done) return;
+  constexpr int nr = Modes<D>::nr;
+  const double alpha = mode == 0 ? sc->alpha : 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a - (threadIdx.x & 31) < Nn; a += stride) {
+    double v[nr];
+#pragma unroll
+    for (int m = 0; m < nr; ++m) v[m] = 0;
+    int g = -1;
+    if (a < Nn) {
+      double rl[D];
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        const int64_t dof = a * D + i;
+        T ri = r[dof];
+        if (mode == 0) {
+          x[dof] += (T)alpha * p[dof];
+          ri -= (T)alpha * Ap[dof];
+          r[dof] = ri;
+        }
+        rl[i] = (double)ri;
+      }
+      g = C.agg[a];
+      double R[D][nr];
+      node_modes<D>(C.off[a], known + a * D, R);
+#pragma unroll
+      for (int m = 0; m < nr; ++m)
+#pragma unroll
+        for (int i = 0; i < D; ++i) v[m] += R[i][m] * rl[i];
+    }
+    restrict_add<nr>(C.rc, g, v);
+  }
+}
+
+// ec = A_c^-1 rc (one warp per coarse row)
+__global__ void coarse_gemv_kernel(CoarseDev C, const Scal* sc, int mode) {
+  if (mode == 0 && sc->done) return;
+  const int lane = threadIdx.x & 31;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < C.nc; i += (gridDim.x * blockDim.x) >> 5) {
+    double v = 0;
+    for (int j = lane; j < C.nc; j += 32) v += C.Ac[(int64_t)i * C.nc + j] * C.rc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) C.ec[i] = v;
+  }
+}
+
+// z = D^-1 r + R_a ec (masked), partial r.z and r.r, rc reset; the last block
+// derives beta and the convergence state exactly as update_kernel does.
+template <int D, typename T>
+__global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const uint8_t* __restrict__ known,
+                                                            const T* __restrict__ dinv, const T* __restrict__ r,
+                                                            T* __restrict__ z, double* partials, Scal* sc,
+                                                            CoarseDev C, int mode) {
+  if (mode == 0 && sc->done) return;
+  constexpr int nr = Modes<D>::nr;
+  double v[2] = {0, 0};
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    T rl[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) rl[i] = r[a * D + i];
+    const int g = C.agg[a];
+    double R[D][nr];
+    node_modes<D>(C.off[a], known + a * D, R);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      T zi = 0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) zi += dinv[a * D * D + i * D + j] * rl[j];
+      double zc = 0;
+#pragma unroll
+      for (int m = 0; m < nr; ++m) zc += R[i][m] * C.ec[g * nr + m];
+      zi += (T)zc;
+      if (known[a * D + i]) zi = 0;
+      z[a * D + i] = zi;
+      v[0] += (double)rl[i] * (double)zi;
+      v[1] += (double)rl[i] * (double)rl[i];
+    }
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) C.rc[i] = 0;
+  double out[2];
+  if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
+    const double rz_new = out[0], rr = out[1];
+    sc->beta = mode == 1 ? 0.0 : rz_new / sc->rz;
+    if (mode == 2 && !(sc->beta <= 1.0)) sc->beta = 0.0;
+    sc->rz = rz_new;
+    sc->rr = rr;
+    if (mode != 0) return;
+    sc->iters += 1;
+    if (!isfinite(rr) || !isfinite(rz_new)) {
+      sc->status = GFEA_ERR_NAN;
+      sc->done = 1;
+    } else if (rr <= sc->tol2) {
+      sc->status = GFEA_OK;
+      sc->done = 1;
+    } else if (sc->iters >= sc->max_iters) {
+      sc->status = GFEA_ERR_NOT_CONVERGED;
+      sc->done = 1;
+    }
+  }
+}
+
 // p' = z + beta p (own rows), Ap' = masked A p'; partial p'.Ap'; last block sets alpha.
 template <int D, int G, typename T>
 __global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* __restrict__ z,
@@ -423,10 +774,28 @@ struct PcgWork {
   double* partials;
   Scal* sc;
   int32_t* flag;
+  bool coarse = false;
+  CoarseDev C;
 };
 
+int coarse_nr(int D) { return D == 1 ? 1 : (D == 2 ? 3 : 6); }
+
+// Number of aggregates of the coarse level (0: block-Jacobi only).
+// Automatic: k Nn^0.43 (k = 0.6 for 3D elasticity, 1.5 otherwise), which
+// balances the coarse inverse (~ nc^3) against the iterations it saves
+// (~ (H/h) ~ (Nn / n_agg)^(1/dim)) per node-row product (~ Nn).
+int coarse_target(const gfea_system* s, const gfea_pcg_opts* o) {
+  if (!o || o->coarse == 0 || !s->coord) return 0;
+  const int64_t cap = kCoarseMax / coarse_nr(s->dof_n);
+  int64_t t = o->coarse > 0 ? o->coarse
+                            : (int64_t)((s->dof_n == 3 ? 0.6 : 1.5) * pow((double)s->n_nodes, 0.43));
+  if (t > cap) t = cap;
+  if (t < 1) t = 1;
+  return (int)t;
+}
+
 template <typename T>
-size_t pcg_layout(int64_t Nn, int D, PcgWork* w, char* base) {
+size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
   size_t off = 0;
   const int64_t N = Nn * D;
   auto take = [&](size_t bytes) {
@@ -447,6 +816,18 @@ size_t pcg_layout(int64_t Nn, int D, PcgWork* w, char* base) {
   w->partials = reinterpret_cast<double*>(take(sizeof(double) * 4 * kMaxBlocks));
   w->sc = reinterpret_cast<Scal*>(take(sizeof(Scal)));
   w->flag = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * 4));
+  w->coarse = n_agg_max > 0;
+  if (w->coarse) {
+    const int64_t nc = (int64_t)n_agg_max * coarse_nr(D);
+    w->C.hdr = reinterpret_cast<CoarseHdr*>(take(sizeof(CoarseHdr)));
+    w->C.agg = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * Nn));
+    w->C.off = reinterpret_cast<float4*>(take(sizeof(float4) * Nn));
+    w->C.Ac = reinterpret_cast<double*>(take(sizeof(double) * nc * nc));
+    w->C.rowb = reinterpret_cast<double*>(take(sizeof(double) * 2 * nc));
+    w->C.colb = reinterpret_cast<double*>(take(sizeof(double) * 2 * nc));
+    w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
+    w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
+  }
   return off;
 }
 
@@ -523,6 +904,150 @@ int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new
   return GFEA_OK;
 }
 
+// z = M^-1 r (with the x, r update in mode 0): update_kernel alone, or the
+// restriction / coarse solve / prolongation sequence of the two-level
+// preconditioner.
+template <typename T>
+int launch_precond(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaStream_t st) {
+  if (!w.coarse) return launch_update<T>(s, w, x, p, mode, st);
+  const int grid = grid_elems(s->n_nodes);
+  GFEA_D_SWITCH(s->dof_n, (update_r_kernel<DD, T><<<grid, kThreads, 0, st>>>(s->n_nodes, s->known, x,
+                                                                              (T*)w.r, p, (const T*)w.Ap, w.sc, w.C,
+                                                                              mode)));
+  GFEA_LAUNCH_CHECK();
+  coarse_gemv_kernel<<<(int)ceil_div((int64_t)w.C.nc * 32, kThreads), kThreads, 0, st>>>(w.C, w.sc, mode);
+  GFEA_LAUNCH_CHECK();
+  GFEA_D_SWITCH(s->dof_n, (finish_z_kernel<DD, T><<<grid, kThreads, 0, st>>>(s->n_nodes, s->known,
+                                                                              (const T*)w.dinv, (const T*)w.r,
+                                                                              (T*)w.z, w.partials + 2 * kMaxBlocks,
+                                                                              w.sc, w.C, mode)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+// Coarse level of the two-level preconditioner: aggregates = cells of a grid
+// of about 'target' cells over the bounding box of the nodes (degenerate
+// extents get one cell), A_c = R^T A R from the FP64 values, inverted in place.
+constexpr int32_t kHdrValid = 0x5eed;
+
+int coarse_aggregate(const gfea_system* s, int target, PcgWork& w, cudaStream_t st) {
+  CoarseDev& C = w.C;
+  const int64_t Nn = s->n_nodes;
+  const int D = s->dof_n;
+  bbox_kernel<<<kSMs, kThreads, 0, st>>>(s->coord, Nn, w.partials);
+  GFEA_LAUNCH_CHECK();
+  double hb[6 * kSMs];
+  GFEA_CUDA_TRY(cudaMemcpyAsync(hb, w.partials, sizeof(hb), cudaMemcpyDeviceToHost, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  double lo[3], ext[3], emax = 0;
+  for (int k = 0; k < 3; ++k) {
+    double l = INFINITY, h = -INFINITY;
+    for (int b = 0; b < kSMs; ++b) {
+      l = fmin(l, hb[b * 6 + k]);
+      h = fmax(h, hb[b * 6 + 3 + k]);
+    }
+    if (!isfinite(l) || !isfinite(h)) return GFEA_ERR_NAN;
+    lo[k] = l;
+    ext[k] = h - l;
+    emax = fmax(emax, ext[k]);
+  }
+  bool act[3];
+  int n_act = 0;
+  double vol = 1;
+  for (int k = 0; k < 3; ++k) {
+    act[k] = ext[k] > 1e-9 * emax;
+    if (act[k]) { ++n_act; vol *= ext[k]; }
+  }
+  int cells[3] = {1, 1, 1};
+  if (n_act > 0) {
+    const double h = pow(vol / target, 1.0 / n_act);
+    for (int k = 0; k < 3; ++k)
+      if (act[k]) cells[k] = (int)fmax(1.0, floor(ext[k] / h));
+    auto prod = [&]() { return (int64_t)cells[0] * cells[1] * cells[2]; };
+    while (prod() > target) {  // too many: coarsen the finest direction
+      int kb = 0;
+      for (int k = 1; k < 3; ++k) if (cells[k] > cells[kb]) kb = k;
+      cells[kb] -= 1;
+    }
+    for (;;) {  // room left: refine the direction with the longest cells that still fits
+      int kb = -1;
+      for (int k = 0; k < 3; ++k)
+        if (act[k] && prod() / cells[k] * (cells[k] + 1) <= target &&
+            (kb < 0 || ext[k] / cells[k] > ext[kb] / cells[kb]))
+          kb = k;
+      if (kb < 0) break;
+      cells[kb] += 1;
+    }
+  }
+  double hk[3], hmax = 0;
+  for (int k = 0; k < 3; ++k) {
+    hk[k] = act[k] ? ext[k] / cells[k] : 1.0;
+    if (act[k]) hmax = fmax(hmax, hk[k]);
+  }
+  int order[3] = {0, 1, 2};  // by number of cells, ascending (stable)
+  for (int i = 1; i < 3; ++i)
+    for (int j = i; j > 0 && cells[order[j]] < cells[order[j - 1]]; --j) {
+      const int t = order[j]; order[j] = order[j - 1]; order[j - 1] = t;
+    }
+  C.nr = coarse_nr(D);
+  C.n_agg = cells[0] * cells[1] * cells[2];
+  C.nc = C.nr * C.n_agg;
+  aggregate_kernel<<<grid_elems(Nn), kThreads, 0, st>>>(
+      s->coord, Nn, make_double3(lo[0], lo[1], lo[2]), make_double3(hk[0], hk[1], hk[2]),
+      make_int3(cells[0], cells[1], cells[2]), make_int3(order[0], order[1], order[2]),
+      hmax > 0 ? 1.0 / hmax : 1.0, C.agg, C.off);
+  GFEA_LAUNCH_CHECK();
+  CoarseHdr h{C.n_agg, C.nc, C.nr, kHdrValid, Nn};
+  GFEA_CUDA_TRY(cudaMemcpyAsync(C.hdr, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));  // h leaves scope
+  return GFEA_OK;
+}
+
+// Coarse level of the two-level preconditioner: aggregates = cells of a grid
+// of about 'target' cells over the bounding box of the nodes (degenerate
+// extents get one cell), A_c = R^T A R from the FP64 values, inverted in place.
+// With 'reuse', an aggregation left in the workspace by an earlier call on the
+// same node count and target is kept.
+int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaStream_t st, cudaEvent_t mark) {
+  CoarseDev& C = w.C;
+  const int64_t Nn = s->n_nodes;
+  const int D = s->dof_n;
+  bool have = false;
+  if (reuse) {
+    CoarseHdr h;
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&h, C.hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    have = h.valid == kHdrValid && h.Nn == Nn && h.nr == coarse_nr(D) && h.n_agg >= 1 && h.n_agg <= target &&
+           h.nc == h.nr * h.n_agg;
+    if (have) {
+      C.nr = h.nr;
+      C.n_agg = h.n_agg;
+      C.nc = h.nc;
+    }
+  }
+  if (!have) {
+    const int e = coarse_aggregate(s, target, w, st);
+    if (e) return e;
+  }
+  GFEA_CUDA_TRY(cudaMemsetAsync(C.Ac, 0, sizeof(double) * C.nc * C.nc, st));
+  const SysT<double> S = sys_t<double>(s);
+  GFEA_D_SWITCH(D, (coarse_assemble_kernel<DD><<<grid_elems(Nn), kThreads, 0, st>>>(S, C)));
+  GFEA_LAUNCH_CHECK();
+  coarse_regularize_kernel<<<1, 256, 0, st>>>(C);
+  GFEA_LAUNCH_CHECK();
+  if (mark) GFEA_CUDA_TRY(cudaEventRecord(mark, st));
+  gj_init_kernel<<<grid_elems(C.nc), kThreads, 0, st>>>(C);
+  GFEA_LAUNCH_CHECK();
+  const int gx = (int)ceil_div(C.nc, 128);
+  const int gy = (int)std::min<int64_t>(C.nc, ceil_div(kMaxBlocks, gx));
+  for (int k = 0; k < C.nc; ++k) {
+    gj_step_kernel<<<dim3(gx, gy), 128, 0, st>>>(C, k);
+    GFEA_LAUNCH_CHECK();
+  }
+  GFEA_CUDA_TRY(cudaMemsetAsync(C.rc, 0, sizeof(double) * C.nc, st));
+  return GFEA_OK;
+}
+
 // Runs PCG iterations until the device flags done; checks every 'check'
 // iterations.  pa holds the current search direction on entry and exit.
 template <typename T>
@@ -541,7 +1066,7 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* hos
       int e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
       if (e) return e;
       if (timed) GFEA_CUDA_TRY(cudaEventRecord(P.ev[2 * it + 1], st));
-      e = launch_update<T>(s, w, x, buf[(j + 1) & 1], 0, st);
+      e = launch_precond<T>(s, w, x, buf[(j + 1) & 1], 0, st);
       if (e) return e;
     }
     GFEA_CUDA_TRY(cudaMemcpyAsync(host_sc, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
@@ -583,7 +1108,9 @@ template <typename T>
 int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
                  size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
   PcgWork w;
-  if (pcg_layout<T>(s->n_nodes, s->dof_n, &w, static_cast<char*>(work)) > work_bytes) return GFEA_ERR_WORKSPACE;
+  const int target = coarse_target(s, o);
+  if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work)) > work_bytes)
+    return GFEA_ERR_WORKSPACE;
   const int G = pick_lanes(s, o->lanes);
   const int64_t N = s->n_nodes * s->dof_n;
   const int check = o->check_every > 0 ? o->check_every : 32;
@@ -599,6 +1126,26 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
   int e = launch_bjacobi<T>(s, w, st);
   if (e) return e;
+  if (w.coarse) {
+    const bool dbg = getenv("GFEA_DEBUG") != nullptr;
+    cudaEvent_t ev[3];
+    if (dbg) {
+      for (int i = 0; i < 3; ++i) GFEA_CUDA_TRY(cudaEventCreate(&ev[i]));
+      GFEA_CUDA_TRY(cudaEventRecord(ev[0], st));
+    }
+    e = coarse_setup(s, target, o->coarse_reuse != 0, w, st, dbg ? ev[1] : nullptr);
+    if (e) return e;
+    if (dbg) {
+      GFEA_CUDA_TRY(cudaEventRecord(ev[2], st));
+      GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+      float t1 = 0, t2 = 0;
+      GFEA_CUDA_TRY(cudaEventElapsedTime(&t1, ev[0], ev[1]));
+      GFEA_CUDA_TRY(cudaEventElapsedTime(&t2, ev[1], ev[2]));
+      fprintf(stderr, "[gfea pcg] coarse level: %d aggregates, dimension %d; setup %.3f ms + inverse %.3f ms\n",
+              w.C.n_agg, w.C.nc, t1, t2);
+      for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
+    }
+  }
   e = launch_resid(s, G, b, x, w, st);
   if (e) return e;
   int32_t flag = 0;
@@ -629,7 +1176,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   GFEA_LAUNCH_CHECK();
   GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
   GFEA_CUDA_TRY(cudaMemsetAsync(pa, 0, sizeof(T) * N, st));
-  e = launch_update<T>(s, w, (T*)w.dx, pa, 1, st);
+  e = launch_precond<T>(s, w, (T*)w.dx, pa, 1, st);
   if (e) return e;
   set_trigger_kernel<<<1, 1, 0, st>>>(w.sc, fmax(delta2 * rr, 0.25 * tol2), o->max_iters);
   GFEA_LAUNCH_CHECK();
@@ -671,7 +1218,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
     // continue on the replaced residual along the same direction
     cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.r, N);
     GFEA_LAUNCH_CHECK();
-    e = launch_update<T>(s, w, (T*)w.dx, pa, 2, st);
+    e = launch_precond<T>(s, w, (T*)w.dx, pa, 2, st);
     if (e) return e;
     set_trigger_kernel<<<1, 1, 0, st>>>(w.sc, fmax(delta2 * rr, 0.25 * tol2), o->max_iters);
     GFEA_LAUNCH_CHECK();
@@ -706,10 +1253,11 @@ extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, vo
 
 extern "C" int gfea_pcg_workspace_size(const gfea_system* s, const gfea_pcg_opts* o, size_t* bytes) {
   if (!s || !o || !bytes || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3) return GFEA_ERR_ARG;
+  const int target = coarse_target(s, o);
   if (o->precision == GFEA_F64)
-    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, nullptr, nullptr);
+    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, target, nullptr, nullptr);
   else
-    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, nullptr, nullptr);
+    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, target, nullptr, nullptr);
   return GFEA_OK;
 }
 
@@ -859,8 +1407,10 @@ extern "C" int gfea_pcg_solve_noalloc(const gfea_system* s, const double* b, dou
   if (o->max_iters < 1 || !(o->rtol > 0)) return GFEA_ERR_ARG;
   if (o->precision != GFEA_F64 && (o->precision != GFEA_F32 || !s->vals32)) return GFEA_ERR_ARG;
   // reject problems whose scratch exceeds the static array, before any device work
-  const size_t need = o->precision == GFEA_F64 ? pcg_layout<double>(s->n_nodes, s->dof_n, nullptr, nullptr)
-                                               : pcg_layout<float>(s->n_nodes, s->dof_n, nullptr, nullptr);
+  const int target = coarse_target(s, o);
+  const size_t need = o->precision == GFEA_F64
+                          ? pcg_layout<double>(s->n_nodes, s->dof_n, target, nullptr, nullptr)
+                          : pcg_layout<float>(s->n_nodes, s->dof_n, target, nullptr, nullptr);
   if (need > kStaticScratchBytes) return GFEA_ERR_WORKSPACE;
   void* scratch = nullptr;
   const int e = static_scratch(&scratch);

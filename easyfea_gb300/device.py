@@ -114,7 +114,7 @@ class CsrOperator:
         d = self.dmesh
         return _lib.System(_lib.ABI_VERSION, self.dof_n, d.Nn, d.n_pairs, _lib.ptr(d.node_ptr), _lib.ptr(d.nbr),
                            _lib.ptr(self.vals64), _lib.ptr(self.vals32), _lib.ptr(known),
-                           int(self.translation_invariant), 0)
+                           int(self.translation_invariant), 0, _lib.ptr(d.coord))
 
     def matvec(self, x: torch.Tensor) -> torch.Tensor:
         y = torch.empty_like(x)
@@ -148,27 +148,60 @@ class PcgInfo:
 
 def pcg(op: CsrOperator, b: torch.Tensor, x: torch.Tensor, known: torch.Tensor, rtol: float = 1e-12,
         precision: str = "fp64", max_iters: int = 200000, check_every: int = 64, inner_rtol: float = 0.1,
-        lanes: int = 0, raise_on_fail: bool = True) -> PcgInfo:
+        lanes: int = 0, raise_on_fail: bool = True, coarse: int = 0, workspace: "Workspace | None" = None
+        ) -> PcgInfo:
     """Solve the Dirichlet-reduced system in place: x holds the known values on
-    known DOFs and the initial guess elsewhere; on return, the solution."""
+    known DOFs and the initial guess elsewhere; on return, the solution.
+
+    ``coarse``: aggregates of the two-level preconditioner's coarse level
+    (0: block-Jacobi only, -1: chosen from the mesh size).  ``workspace``: a
+    ``Workspace`` owned by the caller for solves on one mesh, which keeps the
+    coarse aggregation between solves (otherwise a shared scratch buffer)."""
     L = _lib.load()
     prec = _lib.F64 if precision == "fp64" else _lib.F32
     if prec == _lib.F32:
         op.ensure_f32()
     sys = op.system(known)
+    key = (id(op.dmesh), op.dmesh.Nn, op.dof_n, prec, int(coarse))
+    reuse = int(workspace is not None and coarse != 0 and workspace.key == key)
     opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, int(max_iters), int(check_every), float(rtol), float(inner_rtol),
-                        30, int(lanes))
+                        30, int(lanes), int(coarse), reuse)
     ws = ctypes.c_size_t()
     _lib.check(L.gfea_pcg_workspace_size(ctypes.byref(sys), ctypes.byref(opts), ctypes.byref(ws)), "pcg workspace")
-    work = _workspace(int(ws.value))
+    if workspace is None:
+        work = _workspace(int(ws.value))
+    else:
+        work = workspace.buffer(int(ws.value))
+        if work is not workspace.last:
+            opts.coarse_reuse = 0
+        workspace.key = None
     res = _lib.PcgResult()
     st = L.gfea_pcg_solve(ctypes.byref(sys), _lib.ptr(b), _lib.ptr(x), ctypes.byref(opts), _lib.ptr(work),
                           work.numel(), ctypes.byref(res), _lib.stream())
     info = PcgInfo(int(res.status), int(res.iterations), int(res.refinements), float(res.rel_residual),
                    float(res.floor_rel))
+    if workspace is not None and st in (_lib.OK, _lib.ERR_NOT_CONVERGED):
+        workspace.key = key
+        workspace.last = work
     if raise_on_fail:
         _lib.check(st, f"pcg (iterations {info.iterations}, rel residual {info.rel_residual:.3e})")
     return info
+
+
+class Workspace:
+    """Device scratch of the solves on one mesh; it keeps the coarse
+    aggregation of the two-level preconditioner from one solve to the next."""
+
+    def __init__(self):
+        self.t = None
+        self.key = None
+        self.last = None
+
+    def buffer(self, nbytes: int) -> torch.Tensor:
+        if self.t is None or self.t.numel() < nbytes:
+            self.t = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8, device=_dev())
+            self.key = None
+        return self.t
 
 
 _WS = {}

@@ -7,9 +7,10 @@ the solve running on the GPU (libgb300fea.so).  Boundary-condition bookkeeping
 is host code, as in the reference (EasyFEA/Simulations/_simu.py:2400-3050).
 
 Differences from the reference that a user sees:
-  * the linear solve is block-Jacobi PCG (FP64, or FP32 with FP64 refinement
-    when ``precision = "mixed"``) to relative residual ``rtol`` instead of
-    SuperLU; ``last_solve`` reports iterations and the final residual;
+  * the linear solve is PCG preconditioned by nodal block-Jacobi plus a
+    rigid-body-mode coarse level (FP64, or FP32 with FP64 refinement when
+    ``precision = "mixed"``) to relative residual ``rtol`` instead of SuperLU;
+    ``last_solve`` reports iterations and the final residual;
   * state stays on the device between calls; ``Solve`` returns host copies.
 """
 
@@ -21,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import CsrOperator, DeviceMesh, max_abs_diff, pcg, reaction_energy
+from .device import CsrOperator, DeviceMesh, Workspace, max_abs_diff, pcg, reaction_energy
 from .mesh import Mesh
 from .models import Elastic as ElasticModels
 from .models import PhaseField as PhaseFieldModel
@@ -54,6 +55,12 @@ class _Simu:
         self.precision = "fp64"
         self.rtol = 1e-12
         self.max_iters = 200000
+        # aggregates of the two-level preconditioner's coarse level for
+        # vector (displacement) and scalar (damage) systems: -1 automatic,
+        # 0 block-Jacobi only
+        self.coarse = -1
+        self.coarse_scalar = 0
+        self._workspaces: dict = {}
         self.last_solve = None
         self._dmesh: Optional[DeviceMesh] = None
         self._results: list = []
@@ -229,8 +236,10 @@ class _Simu:
         known, x = self._dirichlet_state(problemType, b)
         if x0 is not None:
             x = torch.where(known.bool(), x, x0)
+        coarse = self.coarse if op.dof_n > 1 else self.coarse_scalar
+        ws = self._workspaces.setdefault(str(problemType), Workspace())
         info = pcg(op, b, x, known, rtol=self.rtol, precision="fp64" if self.precision == "fp64" else "mixed",
-                   max_iters=self.max_iters)
+                   max_iters=self.max_iters, coarse=coarse, workspace=ws)
         self.last_solve = info
         return x
 

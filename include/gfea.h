@@ -192,6 +192,7 @@ typedef struct gfea_system {
   int32_t translation_invariant; /* 1: node block rows sum to zero (elastic stiffness);
                                the FP32 products then use y_a = sum_b K_ab (x_b - x_a) */
   int32_t pad;
+  const double* coord;      /* node coordinates (Nn x 3) for the coarse level; may be NULL */
 } gfea_system;
 
 typedef struct gfea_pcg_opts {
@@ -205,6 +206,11 @@ typedef struct gfea_pcg_opts {
                                residual replacements (reliable updates), default 0.1 */
   int32_t max_refine;       /* refinement steps cap (mixed precision) */
   int32_t lanes;            /* SpMV lanes per node (0 = automatic) */
+  int32_t coarse;           /* two-level preconditioner: target number of aggregates
+                               (0 = block-Jacobi only, -1 = automatic); needs sys.coord */
+  int32_t coarse_reuse;     /* 1: the workspace holds the aggregation of an earlier call
+                               on the same mesh (same coordinates, node count and
+                               'coarse'); it is kept and only the coarse matrix is rebuilt */
 } gfea_pcg_opts;
 
 typedef struct gfea_pcg_result {

@@ -11,9 +11,12 @@
 // operator P A P + (I - P) (P = diag(unknown)); search directions vanish on
 // known DOFs, so the product is a plain SpMV with known rows zeroed.
 //
-// One PCG iteration is two kernels:
-//   dir_spmv : p' = z + beta p  (own rows), Ap' (gathered z + beta p), p'.Ap'
-//   update   : x += alpha p', r -= alpha Ap', z = D^-1 r, r.z, r.r
+// One PCG iteration is three kernels (block-Jacobi) or five (two-level):
+//   dir      : p' = z + beta p
+//   apply    : Ap' (masked SpMV), p'.Ap', alpha
+//   update   : x += alpha p', r -= alpha Ap', z = D^-1 r, r.z, r.r, beta
+// with the coarse level, update is split into update_r (x, r, restriction),
+// coarse_gemv and finish_z (z = D^-1 r + prolonged correction, dots, beta).
 // Reductions are per-block partials summed in a fixed order by the last block
 // to finish (atomic ticket, no spinning), which also derives the scalar
 // recurrences (alpha, beta, convergence) on the device.  Kernels return early
@@ -24,6 +27,10 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <atomic>
+#include <chrono>
+#include <mutex>
 
 #include "common.cuh"
 #include "rowops.cuh"
@@ -40,19 +47,47 @@ struct Scal {
   uint32_t ticket1, ticket2, ticket3, pad;
 };
 
-// Optional CUDA-event timing of the PCG direction/SpMV kernel (the dominant
-// launch of a solve), read back by gfea_profile_read.
+// Optional CUDA-event timing of the launches of the PCG iterations, per
+// kernel kind; gfea_profile_read returns the SpMV kernel's (the dominant
+// launch of a solve).  Events are recorded after each launch of a chunk of
+// iterations and attributed once the chunk's performed iterations are known.
+enum ProfTag { kTagDir, kTagApply, kTagUpdate, kTagRestrict, kTagGemv, kTagFinish, kNumTags };
+const char* const kTagNames[kNumTags] = {"direction", "spmv", "update", "update+restrict", "coarse gemv",
+                                         "finish z"};
+
+// Solves may run concurrently from several host threads (one stream each):
+// the events of a chunk are per thread, the totals are shared under a mutex.
 struct KernelProfile {
-  static constexpr int kPairs = 64;
-  bool on = false;
-  bool created = false;
-  cudaEvent_t ev[2 * kPairs];
-  double ms = 0;
-  long long n = 0;
+  std::atomic<bool> on{false};
+  std::mutex mu;
+  double ms[kNumTags] = {};
+  long long n[kNumTags] = {};
 };
 KernelProfile& prof() {
   static KernelProfile p;
   return p;
+}
+
+struct ChunkEvents {
+  static constexpr int kEvents = 512;
+  bool created = false;
+  bool active = false;  // inside a timed chunk
+  cudaEvent_t ev[kEvents];
+  int tag[kEvents];
+  int cur = 0;
+};
+ChunkEvents& chunk_events() {
+  thread_local ChunkEvents c;
+  return c;
+}
+
+// Event after a launch of kind 'tag' (tag < 0: iteration start).
+int prof_mark(cudaStream_t st, int tag) {
+  ChunkEvents& E = chunk_events();
+  if (!E.active || E.cur >= ChunkEvents::kEvents) return GFEA_OK;
+  GFEA_CUDA_TRY(cudaEventRecord(E.ev[E.cur], st));
+  E.tag[E.cur++] = tag;
+  return GFEA_OK;
 }
 
 
@@ -119,22 +154,50 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SysT<T> S, const T* __re
 // FP64 residual of the reduced system: r = P (b - A x); partials r.r,
 // ||P (b - A x_c)||^2 (x_c: x on known columns only, the reference norm) and
 // ||P |A| |x|||^2 (scale of the rounding floor of r).
-template <int D, int G, typename T>
+// The three products share one pass over the values; KN = false skips the
+// known-column product (b - A x_c does not change between reliable updates).
+template <int D, int G, typename T, bool KN>
 __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double* __restrict__ b,
                                                          const double* __restrict__ x, double* __restrict__ r,
                                                          double* partials, Scal* sc) {
+  constexpr int LA = G - G % D;
+  constexpr int NPP = LA / D;
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
   const int64_t Nn = S.Nn;
+  const int j = lane % D;
   double v[3] = {0, 0, 0};
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
     double all[D], kn[D], ab[D];
-    node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return x[c]; }, all);
-    node_rows<D, G, T, double>(ac, lane, S, [&](int64_t c) { return S.known[c] ? x[c] : 0.0; }, kn);
-    node_rows<D, G, T, double, true>(ac, lane, S, [&](int64_t c) { return fabs(x[c]); }, ab);
+#pragma unroll
+    for (int i = 0; i < D; ++i) all[i] = kn[i] = ab[i] = 0;
+    if (lane < LA) {
+      const int32_t p0 = S.node_ptr[ac], nb = S.node_ptr[ac + 1] - p0;
+      const int32_t W = D * nb;
+      const T* base = S.vals + (int64_t)D * D * p0;
+      for (int32_t k = lane / D, t = lane; k < nb; k += NPP, t += LA) {
+        const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
+        const double xv = x[col];
+        const double xk = (KN && S.known[col]) ? xv : 0.0;
+        const double xa = fabs(xv);
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          const double w = (double)__ldg(base + (int64_t)i * W + t);
+          all[i] += w * xv;
+          if (KN) kn[i] += w * xk;
+          ab[i] += fabs(w) * xa;
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      all[i] = group_sum<G, double>(all[i]);
+      if (KN) kn[i] = group_sum<G, double>(kn[i]);
+      ab[i] = group_sum<G, double>(ab[i]);
+    }
     if (a < Nn && lane == 0) {
 #pragma unroll
       for (int i = 0; i < D; ++i) {
@@ -153,7 +216,7 @@ __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double
   double out[3];
   if (reduce_last<3>(v, partials, &sc->ticket3, out) && threadIdx.x == 0) {
     sc->rr_true = out[0];
-    sc->bb = out[1];
+    if (KN) sc->bb = out[1];
     sc->absAx = out[2];
   }
 }
@@ -285,8 +348,9 @@ struct CoarseDev {
   int32_t* agg = nullptr;  // node -> aggregate
   float4* off = nullptr;   // node offset from its cell centre / largest cell size
   double* Ac = nullptr;    // nc x nc, inverted in place
-  double* rowb = nullptr;  // 2 x nc: pivot-row snapshots (by step parity)
-  double* colb = nullptr;  // 2 x nc: pivot-column snapshots
+  double* rowp = nullptr;  // kGJB x nc: row panel of the pivot block
+  double* colp = nullptr;  // nc x kGJB: column panel of the pivot block
+  double* pinv = nullptr;  // kGJB x kGJB: inverse of the pivot block
   double* rc = nullptr;    // nc: restriction accumulator
   double* ec = nullptr;    // nc: coarse correction
 };
@@ -297,28 +361,30 @@ struct Modes {
 };
 
 // Rigid-body modes at one node (D x nr), rows of known DOFs zeroed.
-template <int D>
-__device__ __forceinline__ void node_modes(float4 o, const uint8_t* kn, double (&R)[D][Modes<D>::nr]) {
+// R holds exactly representable products of the float offsets, so the FP32
+// and FP64 iterations apply the same modes.
+template <int D, typename T = double>
+__device__ __forceinline__ void node_modes(float4 o, const uint8_t* kn, T (&R)[D][Modes<D>::nr]) {
   if constexpr (D == 1) {
-    R[0][0] = kn[0] ? 0.0 : 1.0;
+    R[0][0] = kn[0] ? T(0) : T(1);
   } else if constexpr (D == 2) {
-    const double dx = o.x, dy = o.y;
-    const double r0[3] = {1, 0, -dy}, r1[3] = {0, 1, dx};
+    const T dx = o.x, dy = o.y;
+    const T r0[3] = {1, 0, -dy}, r1[3] = {0, 1, dx};
     const bool k0 = kn[0], k1 = kn[1];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      R[0][m] = k0 ? 0.0 : r0[m];
-      R[1][m] = k1 ? 0.0 : r1[m];
+      R[0][m] = k0 ? T(0) : r0[m];
+      R[1][m] = k1 ? T(0) : r1[m];
     }
   } else {
-    const double dx = o.x, dy = o.y, dz = o.z;
-    const double r0[6] = {1, 0, 0, 0, dz, -dy}, r1[6] = {0, 1, 0, -dz, 0, dx}, r2[6] = {0, 0, 1, dy, -dx, 0};
+    const T dx = o.x, dy = o.y, dz = o.z;
+    const T r0[6] = {1, 0, 0, 0, dz, -dy}, r1[6] = {0, 1, 0, -dz, 0, dx}, r2[6] = {0, 0, 1, dy, -dx, 0};
     const bool k0 = kn[0], k1 = kn[1], k2 = kn[2];
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
-      R[0][m] = k0 ? 0.0 : r0[m];
-      R[1][m] = k1 ? 0.0 : r1[m];
-      R[2][m] = k2 ? 0.0 : r2[m];
+      R[0][m] = k0 ? T(0) : r0[m];
+      R[1][m] = k1 ? T(0) : r1[m];
+      R[2][m] = k2 ? T(0) : r2[m];
     }
   }
 }
@@ -443,46 +509,78 @@ __global__ void coarse_regularize_kernel(CoarseDev C) {
   }
 }
 
-// In-place Gauss-Jordan inversion of the SPD coarse matrix (no pivoting:
-// every pivot of an SPD matrix is positive), one launch per pivot k.  Each
-// element is read and written by one thread; the pivot row and column of step
-// k come from snapshots written by step k - 1 (gj_init for k = 0).
-__global__ void gj_init_kernel(CoarseDev C) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) {
-    C.rowb[i] = C.Ac[i];
-    C.colb[i] = C.Ac[(int64_t)i * C.nc];
-  }
-}
+// In-place blocked Gauss-Jordan inversion of the SPD coarse matrix (no
+// pivoting: every pivot block of an SPD matrix is SPD).  For the pivot block
+// K = [k0, k0 + b) of A = [[A11, A12], [A21, A22]]:
+//   A11 <- A11^-1,  A12 <- A11^-1 A12,  A21 <- -A21 A11^-1,
+//   A22 <- A22 - A21 A11^-1 A12,
+// two launches per block: gj_panel saves the row panel A11^-1 A1* (rowp),
+// the old column panel A*1 (colp) and A11^-1 (pinv); gj_update applies the
+// rank-b update to every element (each read and written by one thread).
+constexpr int kGJB = 16;
 
-// Pivot step k: block (bx, by) owns column j = bx * blockDim + tid and rows
-// by, by + gridDim.y, ...; coalesced along rows, one FMA per element.
-__global__ void gj_step_kernel(CoarseDev C, int k) {
+__global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int b) {
   const int n = C.nc;
-  const double* row = C.rowb + (k & 1) * n;
-  const double* col = C.colb + (k & 1) * n;
-  double* nrow = C.rowb + ((k + 1) & 1) * n;
-  double* ncol = C.colb + ((k + 1) & 1) * n;
+  __shared__ double M[kGJB][kGJB + 1], M2[kGJB][kGJB + 1];
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) M[t / b][t % b] = C.Ac[(int64_t)(k0 + t / b) * n + k0 + t % b];
+  __syncthreads();
+  for (int p = 0; p < b; ++p) {  // Gauss-Jordan of the pivot block in shared memory
+    const double ip = 1.0 / M[p][p];
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
+      const int i = t / b, j = t % b;
+      M2[i][j] = i == p ? (j == p ? ip : M[p][j] * ip) : (j == p ? -M[i][p] * ip : M[i][j] - M[i][p] * (M[p][j] * ip));
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) M[t / b][t % b] = M2[t / b][t % b];
+    __syncthreads();
+  }
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) C.pinv[t] = M[t / b][t % b];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const double ip = 1.0 / row[k];
-  const double rj = row[j] * ip;
+  double a[kGJB];
+#pragma unroll
+  for (int m = 0; m < kGJB; ++m) a[m] = m < b ? C.Ac[(int64_t)(k0 + m) * n + j] : 0.0;
+  for (int l = 0; l < b; ++l) {
+    double s = 0;
+#pragma unroll
+    for (int m = 0; m < kGJB; ++m) s += (m < b ? M[l][m] : 0.0) * a[m];
+    C.rowp[(int64_t)l * n + j] = s;
+  }
+#pragma unroll
+  for (int l = 0; l < kGJB; ++l) C.colp[(int64_t)j * kGJB + l] = l < b ? C.Ac[(int64_t)j * n + k0 + l] : 0.0;
+}
+
+// Block (bx, by) owns column j = bx * blockDim + tid and rows by, by + gridDim.y, ...
+__global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int b) {
+  const int n = C.nc;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const bool jk = j >= k0 && j < k0 + b;
+  double r[kGJB];
+#pragma unroll
+  for (int l = 0; l < kGJB; ++l)
+    r[l] = l < b ? (jk ? C.pinv[l * b + (j - k0)] : C.rowp[(int64_t)l * n + j]) : 0.0;
   for (int i = blockIdx.y; i < n; i += gridDim.y) {
     double* p = C.Ac + (int64_t)i * n + j;
     double v;
-    if (i == k)
-      v = j == k ? ip : rj;
-    else
-      v = j == k ? -col[i] * ip : *p - col[i] * rj;
+    if (i >= k0 && i < k0 + b) {
+      v = jk ? C.pinv[(i - k0) * b + (j - k0)] : C.rowp[(int64_t)(i - k0) * n + j];
+    } else {
+      const double* c = C.colp + (int64_t)i * kGJB;
+      double s = 0;
+#pragma unroll
+      for (int l = 0; l < kGJB; ++l) s += __ldg(c + l) * r[l];
+      v = jk ? -s : *p - s;
+    }
     *p = v;
-    if (i == k + 1) nrow[j] = v;
-    if (j == k + 1) ncol[i] = v;
   }
 }
 
 // Sum of nr per-lane values into rc[g * nr + m] (g < 0: lane without a node):
 // a segmented warp scan over runs of equal g, one atomic per run and mode.
-template <int nr>
-__device__ __forceinline__ void restrict_add(double* rc, int g, double (&v)[nr]) {
+template <int nr, typename T>
+__device__ __forceinline__ void restrict_add(double* rc, int g, T (&v)[nr]) {
   const int lane = threadIdx.x & 31;
   const int gp = __shfl_up_sync(0xffffffffu, g, 1);
   const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || g != gp);
@@ -491,13 +589,13 @@ __device__ __forceinline__ void restrict_add(double* rc, int g, double (&v)[nr])
   const bool tail = lane == 31 || gn != g;
 #pragma unroll
   for (int m = 0; m < nr; ++m) {
-    double s = v[m];
+    T s = v[m];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, s, d);
+      const T t = __shfl_up_sync(0xffffffffu, s, d);
       if (lane - d >= start) s += t;
     }
-    if (tail && g >= 0 && s != 0) atomicAdd(&rc[g * nr + m], s);
+    if (tail && g >= 0 && s != 0) atomicAdd(&rc[g * nr + m], (double)s);
   }
 }
 
@@ -514,12 +612,12 @@ __global__ void __launch_bounds__(kThreads) update_r_kernel(int64_t Nn, const ui
   const double alpha = mode == 0 ? sc->alpha : 0.0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a - (threadIdx.x & 31) < Nn; a += stride) {
-    double v[nr];
+    T v[nr];
 #pragma unroll
     for (int m = 0; m < nr; ++m) v[m] = 0;
     int g = -1;
     if (a < Nn) {
-      double rl[D];
+      T rl[D];
 #pragma unroll
       for (int i = 0; i < D; ++i) {
         const int64_t dof = a * D + i;
@@ -529,30 +627,42 @@ __global__ void __launch_bounds__(kThreads) update_r_kernel(int64_t Nn, const ui
           ri -= (T)alpha * Ap[dof];
           r[dof] = ri;
         }
-        rl[i] = (double)ri;
+        rl[i] = ri;
       }
       g = C.agg[a];
-      double R[D][nr];
-      node_modes<D>(C.off[a], known + a * D, R);
+      T R[D][nr];
+      node_modes<D, T>(C.off[a], known + a * D, R);
 #pragma unroll
       for (int m = 0; m < nr; ++m)
 #pragma unroll
         for (int i = 0; i < D; ++i) v[m] += R[i][m] * rl[i];
     }
-    restrict_add<nr>(C.rc, g, v);
+    restrict_add<nr, T>(C.rc, g, v);
   }
 }
 
-// ec = A_c^-1 rc (one warp per coarse row)
-__global__ void coarse_gemv_kernel(CoarseDev C, const Scal* sc, int mode) {
+// ec = A_c^-1 rc: one block of kGemvThreads per coarse row (enough warps in
+// flight to stream the L2-resident inverse), fixed-order block reduction.
+constexpr int kGemvThreads = 128;
+
+__global__ void __launch_bounds__(kGemvThreads) coarse_gemv_kernel(CoarseDev C, const Scal* sc, int mode) {
   if (mode == 0 && sc->done) return;
-  const int lane = threadIdx.x & 31;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < C.nc; i += (gridDim.x * blockDim.x) >> 5) {
+  __shared__ double sh[kGemvThreads / 32];
+  for (int i = blockIdx.x; i < C.nc; i += gridDim.x) {
+    const double* row = C.Ac + (int64_t)i * C.nc;
     double v = 0;
-    for (int j = lane; j < C.nc; j += 32) v += C.Ac[(int64_t)i * C.nc + j] * C.rc[j];
+    for (int j = threadIdx.x; j < C.nc; j += kGemvThreads) v += row[j] * C.rc[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) C.ec[i] = v;
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+#pragma unroll
+      for (int w = 0; w < kGemvThreads / 32; ++w) t += sh[w];
+      C.ec[i] = t;
+    }
+    __syncthreads();
   }
 }
 
@@ -571,17 +681,18 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
 #pragma unroll
     for (int i = 0; i < D; ++i) rl[i] = r[a * D + i];
     const int g = C.agg[a];
-    double R[D][nr];
-    node_modes<D>(C.off[a], known + a * D, R);
+    T R[D][nr];
+    node_modes<D, T>(C.off[a], known + a * D, R);
+    T e[nr];
+#pragma unroll
+    for (int m = 0; m < nr; ++m) e[m] = (T)C.ec[g * nr + m];
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       T zi = 0;
 #pragma unroll
       for (int j = 0; j < D; ++j) zi += dinv[a * D * D + i * D + j] * rl[j];
-      double zc = 0;
 #pragma unroll
-      for (int m = 0; m < nr; ++m) zc += R[i][m] * C.ec[g * nr + m];
-      zi += (T)zc;
+      for (int m = 0; m < nr; ++m) zi += R[i][m] * e[m];
       if (known[a * D + i]) zi = 0;
       z[a * D + i] = zi;
       v[0] += (double)rl[i] * (double)zi;
@@ -611,13 +722,22 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
   }
 }
 
-// p' = z + beta p (own rows), Ap' = masked A p'; partial p'.Ap'; last block sets alpha.
-template <int D, int G, typename T>
-__global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* __restrict__ z,
-                                                            const T* __restrict__ p_old, T* __restrict__ p_new,
-                                                            T* __restrict__ Ap, double* partials, Scal* sc) {
+// p' = z + beta p (streaming; p' vanishes on known DOFs with z and p).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) dir_kernel(int64_t n, const T* __restrict__ z,
+                                                       const T* __restrict__ p_old, T* __restrict__ p_new,
+                                                       const Scal* sc) {
   if (sc->done) return;
   const T beta = (T)sc->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p_new[i] = z[i] + beta * p_old[i];
+}
+
+// Ap = masked A p; partial p.Ap; the last block sets alpha.
+template <int D, int G, typename T>
+__global__ void __launch_bounds__(kThreads) apply_kernel(SysT<T> S, const T* __restrict__ p, T* __restrict__ Ap,
+                                                         double* partials, Scal* sc) {
+  if (sc->done) return;
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
@@ -627,19 +747,18 @@ __global__ void __launch_bounds__(kThreads) dir_spmv_kernel(SysT<T> S, const T* 
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
     T acc[D];
-    auto dir = [&](int64_t c) { return z[c] + beta * p_old[c]; };
+    auto xf = [&](int64_t c) { return p[c]; };
     if (sizeof(T) == 4 && S.diff)
-      node_rows<D, G, T, T, false, true>(ac, lane, S, dir, acc);
+      node_rows<D, G, T, T, false, true>(ac, lane, S, xf, acc);
     else
-      node_rows<D, G, T, T>(ac, lane, S, dir, acc);
+      node_rows<D, G, T, T>(ac, lane, S, xf, acc);
     if (a < Nn && lane < D) {
       T av = acc[0];
 #pragma unroll
       for (int i = 1; i < D; ++i) if (lane == i) av = acc[i];
       const int64_t dof = a * D + lane;
-      const T pn = z[dof] + beta * p_old[dof];
+      const T pn = p[dof];
       if (S.known[dof]) av = 0;
-      p_new[dof] = pn;
       Ap[dof] = av;
       v[0] += (double)pn * (double)av;
     }
@@ -823,8 +942,9 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
     w->C.agg = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * Nn));
     w->C.off = reinterpret_cast<float4*>(take(sizeof(float4) * Nn));
     w->C.Ac = reinterpret_cast<double*>(take(sizeof(double) * nc * nc));
-    w->C.rowb = reinterpret_cast<double*>(take(sizeof(double) * 2 * nc));
-    w->C.colb = reinterpret_cast<double*>(take(sizeof(double) * 2 * nc));
+    w->C.rowp = reinterpret_cast<double*>(take(sizeof(double) * kGJB * nc));
+    w->C.colp = reinterpret_cast<double*>(take(sizeof(double) * kGJB * nc));
+    w->C.pinv = reinterpret_cast<double*>(take(sizeof(double) * kGJB * kGJB));
     w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
   }
@@ -868,10 +988,15 @@ SysT<float> sys_t<float>(const gfea_system* s) {
     default: return GFEA_ERR_ARG;                      \
   }
 
-int launch_resid(const gfea_system* s, int G, const double* b, const double* x, PcgWork& w, cudaStream_t st) {
+int launch_resid(const gfea_system* s, int G, const double* b, const double* x, PcgWork& w, bool kn,
+                 cudaStream_t st) {
   const SysT<double> S = sys_t<double>(s);
   const int grid = grid_nodes(s->n_nodes, G);
-  GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
+  if (kn) {
+    GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double, true><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
+  } else {
+    GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double, false><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
+  }
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -891,17 +1016,22 @@ int launch_update(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaSt
                                                                             (T*)w.r, (T*)w.z, p, (const T*)w.Ap,
                                                                             w.partials + 2 * kMaxBlocks, w.sc, mode)));
   GFEA_LAUNCH_CHECK();
-  return GFEA_OK;
+  return prof_mark(st, kTagUpdate);
 }
 
 template <typename T>
 int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new, cudaStream_t st) {
   const SysT<T> S = sys_t<T>(s);
-  const int grid = grid_nodes(s->n_nodes, G);
-  GFEA_DG_SWITCH(s->dof_n, G, (dir_spmv_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, (const T*)w.z, p_old, p_new, (T*)w.Ap,
-                                                                                      w.partials, w.sc)));
+  const int64_t N = s->n_nodes * s->dof_n;
+  dir_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(N, (const T*)w.z, p_old, p_new, w.sc);
   GFEA_LAUNCH_CHECK();
-  return GFEA_OK;
+  int e = prof_mark(st, kTagDir);
+  if (e) return e;
+  const int grid = grid_nodes(s->n_nodes, G);
+  GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap, w.partials,
+                                                                                   w.sc)));
+  GFEA_LAUNCH_CHECK();
+  return prof_mark(st, kTagApply);
 }
 
 // z = M^-1 r (with the x, r update in mode 0): update_kernel alone, or the
@@ -915,14 +1045,18 @@ int launch_precond(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaS
                                                                               (T*)w.r, p, (const T*)w.Ap, w.sc, w.C,
                                                                               mode)));
   GFEA_LAUNCH_CHECK();
-  coarse_gemv_kernel<<<(int)ceil_div((int64_t)w.C.nc * 32, kThreads), kThreads, 0, st>>>(w.C, w.sc, mode);
+  int e = prof_mark(st, kTagRestrict);
+  if (e) return e;
+  coarse_gemv_kernel<<<std::min(w.C.nc, 8 * kSMs), kGemvThreads, 0, st>>>(w.C, w.sc, mode);
   GFEA_LAUNCH_CHECK();
+  e = prof_mark(st, kTagGemv);
+  if (e) return e;
   GFEA_D_SWITCH(s->dof_n, (finish_z_kernel<DD, T><<<grid, kThreads, 0, st>>>(s->n_nodes, s->known,
                                                                               (const T*)w.dinv, (const T*)w.r,
                                                                               (T*)w.z, w.partials + 2 * kMaxBlocks,
                                                                               w.sc, w.C, mode)));
   GFEA_LAUNCH_CHECK();
-  return GFEA_OK;
+  return prof_mark(st, kTagFinish);
 }
 
 // Coarse level of the two-level preconditioner: aggregates = cells of a grid
@@ -1036,12 +1170,13 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
   coarse_regularize_kernel<<<1, 256, 0, st>>>(C);
   GFEA_LAUNCH_CHECK();
   if (mark) GFEA_CUDA_TRY(cudaEventRecord(mark, st));
-  gj_init_kernel<<<grid_elems(C.nc), kThreads, 0, st>>>(C);
-  GFEA_LAUNCH_CHECK();
   const int gx = (int)ceil_div(C.nc, 128);
-  const int gy = (int)std::min<int64_t>(C.nc, ceil_div(kMaxBlocks, gx));
-  for (int k = 0; k < C.nc; ++k) {
-    gj_step_kernel<<<dim3(gx, gy), 128, 0, st>>>(C, k);
+  const int gy = (int)std::min<int64_t>(C.nc, ceil_div(2 * kMaxBlocks, gx));
+  for (int k0 = 0; k0 < C.nc; k0 += kGJB) {
+    const int b = std::min(kGJB, C.nc - k0);
+    gj_panel_kernel<<<gx, 128, 0, st>>>(C, k0, b);
+    GFEA_LAUNCH_CHECK();
+    gj_update_kernel<<<dim3(gx, gy), 128, 0, st>>>(C, k0, b);
     GFEA_LAUNCH_CHECK();
   }
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rc, 0, sizeof(double) * C.nc, st));
@@ -1058,26 +1193,46 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* hos
   // from the number of iterations actually performed
   T* buf[2] = {pa, pb};
   KernelProfile& P = prof();
-  const bool timed = P.on && check <= KernelProfile::kPairs;
+  ChunkEvents& E = chunk_events();
+  const bool timed = P.on.load() && check <= 64;
+  if (timed && !E.created) {
+    for (int i = 0; i < ChunkEvents::kEvents; ++i) GFEA_CUDA_TRY(cudaEventCreate(&E.ev[i]));
+    E.created = true;
+  }
   int before = iters0;
   for (int j = 0;;) {
+    E.active = timed;
+    E.cur = 0;
     for (int it = 0; it < check; ++it, ++j) {
-      if (timed) GFEA_CUDA_TRY(cudaEventRecord(P.ev[2 * it], st));
-      int e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
+      int e = prof_mark(st, -1);
       if (e) return e;
-      if (timed) GFEA_CUDA_TRY(cudaEventRecord(P.ev[2 * it + 1], st));
+      e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
+      if (e) return e;
       e = launch_precond<T>(s, w, x, buf[(j + 1) & 1], 0, st);
       if (e) return e;
     }
+    E.active = false;
     GFEA_CUDA_TRY(cudaMemcpyAsync(host_sc, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    if (timed) {  // durations of the direction/SpMV launches that did work
+    if (timed) {  // attribute the launches of the iterations that did work
       const int performed = host_sc->iters - before;
-      for (int it = 0; it < performed && it < check; ++it) {
+      double ms_t[kNumTags] = {};
+      long long n_t[kNumTags] = {};
+      int itn = -1;
+      for (int k = 0; k < E.cur; ++k) {
+        if (E.tag[k] < 0) {
+          if (++itn >= performed) break;
+          continue;
+        }
         float ms = 0;
-        GFEA_CUDA_TRY(cudaEventElapsedTime(&ms, P.ev[2 * it], P.ev[2 * it + 1]));
-        P.ms += ms;
-        P.n += 1;
+        GFEA_CUDA_TRY(cudaEventElapsedTime(&ms, E.ev[k - 1], E.ev[k]));
+        ms_t[E.tag[k]] += ms;
+        n_t[E.tag[k]] += 1;
+      }
+      std::lock_guard<std::mutex> lock(P.mu);
+      for (int t = 0; t < kNumTags; ++t) {
+        P.ms[t] += ms_t[t];
+        P.n[t] += n_t[t];
       }
     }
     before = host_sc->iters;
@@ -1107,6 +1262,7 @@ int fetch(Scal* h, PcgWork& w, cudaStream_t st) {
 template <typename T>
 int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
                  size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
+  const auto t_start = std::chrono::steady_clock::now();
   PcgWork w;
   const int target = coarse_target(s, o);
   if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work)) > work_bytes)
@@ -1119,7 +1275,9 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   // reliable update after the iterated residual fell by delta: inner_rtol
   // (default 0.1) in FP32, whose recursive residual drifts from the true one
   // by ~eps32 * condition; 1000x in FP64
-  const double dlt = (o->inner_rtol > 0 && o->inner_rtol < 1) ? o->inner_rtol : 0.1;
+  // default: 0.1 with block-Jacobi alone, 0.01 with the coarse level (its
+  // better conditioned FP32 iteration drifts less between updates)
+  const double dlt = (o->inner_rtol > 0 && o->inner_rtol < 1) ? o->inner_rtol : (w.coarse ? 0.01 : 0.1);
   const double delta2 = fp64 ? 1e-6 : dlt * dlt;
   Scal hs;
   GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
@@ -1146,7 +1304,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
       for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
     }
   }
-  e = launch_resid(s, G, b, x, w, st);
+  e = launch_resid(s, G, b, x, w, true, st);
   if (e) return e;
   int32_t flag = 0;
   GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -1192,14 +1350,15 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
     add_correction_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(x, (const T*)w.dx, s->known, N);
     GFEA_LAUNCH_CHECK();
     GFEA_CUDA_TRY(cudaMemsetAsync(w.dx, 0, sizeof(T) * N, st));
-    e = launch_resid(s, G, b, x, w, st);
+    e = launch_resid(s, G, b, x, w, false, st);
     if (e) return e;
     e = fetch(&hs, w, st);
     if (e) return e;
     rr = hs.rr_true;
     if (getenv("GFEA_DEBUG"))
-      fprintf(stderr, "[gfea pcg%d] update %d: iterations %d, inner status %d, rel residual %.3e\n",
-              fp64 ? 64 : 32, upd + 1, hs.iters, st_inner, sqrt(rr / bb));
+      fprintf(stderr, "[gfea pcg%d] update %d: iterations %d, inner status %d, rel residual %.3e, %.2f ms\n",
+              fp64 ? 64 : 32, upd + 1, hs.iters, st_inner, sqrt(rr / bb),
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
     iters0 = hs.iters;
     res->refinements = upd + 1;
     floor2 = (32 * eps64) * (32 * eps64) * hs.absAx;
@@ -1338,22 +1497,25 @@ extern "C" int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void*
 extern "C" long long gfea_launch_count(void) { return gfea::launch_counter().load(); }
 
 extern "C" int gfea_profile_enable(int on) {
-  gfea::KernelProfile& P = gfea::prof();
-  if (on && !P.created) {
-    for (int i = 0; i < 2 * gfea::KernelProfile::kPairs; ++i) GFEA_CUDA_TRY(cudaEventCreate(&P.ev[i]));
-    P.created = true;
-  }
-  P.on = on != 0;
+  gfea::prof().on = on != 0;
   return GFEA_OK;
 }
 
 extern "C" int gfea_profile_read(double* ms_host, long long* launches_host) {
   if (!ms_host || !launches_host) return GFEA_ERR_ARG;
   gfea::KernelProfile& P = gfea::prof();
-  *ms_host = P.ms;
-  *launches_host = P.n;
-  P.ms = 0;
-  P.n = 0;
+  std::lock_guard<std::mutex> lock(P.mu);
+  *ms_host = P.ms[gfea::kTagApply];
+  *launches_host = P.n[gfea::kTagApply];
+  if (getenv("GFEA_DEBUG"))
+    for (int t = 0; t < gfea::kNumTags; ++t)
+      if (P.n[t] > 0)
+        fprintf(stderr, "[gfea profile] %-16s %7lld launches, %.4f ms per launch\n", gfea::kTagNames[t], P.n[t],
+                P.ms[t] / P.n[t]);
+  for (int t = 0; t < gfea::kNumTags; ++t) {
+    P.ms[t] = 0;
+    P.n[t] = 0;
+  }
   return GFEA_OK;
 }
 
@@ -1367,7 +1529,6 @@ extern "C" int gfea_profile_read(double* ms_host, long long* launches_host) {
 // lives in the file-scope array below, which every GPU that loads this library
 // holds until the process exits.
 // ---------------------------------------------------------------------------
-#include <mutex>
 
 namespace gfea {
 namespace {

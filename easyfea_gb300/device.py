@@ -15,6 +15,7 @@ stream; every computation is a call into the C ABI.
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -147,7 +148,7 @@ class PcgInfo:
 
 
 def pcg(op: CsrOperator, b: torch.Tensor, x: torch.Tensor, known: torch.Tensor, rtol: float = 1e-12,
-        precision: str = "fp64", max_iters: int = 200000, check_every: int = 64, inner_rtol: float = 0.1,
+        precision: str = "fp64", max_iters: int = 200000, check_every: int = 64, inner_rtol: float = 0.0,
         lanes: int = 0, raise_on_fail: bool = True, coarse: int = 0, workspace: "Workspace | None" = None
         ) -> PcgInfo:
     """Solve the Dirichlet-reduced system in place: x holds the known values on
@@ -204,16 +205,27 @@ class Workspace:
         return self.t
 
 
-_WS = {}
+# shared scratch, one per device and host thread (solves on several threads,
+# each with its own stream, run concurrently)
+_TLS = threading.local()
+
+
+def _per_thread(name: str) -> dict:
+    d = getattr(_TLS, name, None)
+    if d is None:
+        d = {}
+        setattr(_TLS, name, d)
+    return d
 
 
 def _workspace(nbytes: int) -> torch.Tensor:
-    """Reusable scratch buffer (grown on demand, one per device)."""
+    """Reusable scratch buffer (grown on demand)."""
+    ws = _per_thread("ws")
     dev = torch.cuda.current_device()
-    w = _WS.get(dev)
+    w = ws.get(dev)
     if w is None or w.numel() < nbytes:
         w = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8, device=_dev())
-        _WS[dev] = w
+        ws[dev] = w
     return w
 
 
@@ -230,15 +242,13 @@ def reaction_energy(op: CsrOperator, x: torch.Tensor, dofs: torch.Tensor | None)
     return out[0], out[1], Ax
 
 
-_RED = {}
-
-
 def _scratch_reduce() -> torch.Tensor:
+    red = _per_thread("red")
     dev = torch.cuda.current_device()
-    if dev not in _RED:
+    if dev not in red:
         n = int(_lib.load().gfea_reduce_workspace_size())
-        _RED[dev] = torch.empty(n, dtype=torch.uint8, device=_dev())
-    return _RED[dev]
+        red[dev] = torch.empty(n, dtype=torch.uint8, device=_dev())
+    return red[dev]
 
 
 def max_abs_diff(a: torch.Tensor, b: torch.Tensor) -> float:

@@ -203,7 +203,8 @@ typedef struct gfea_pcg_opts {
   double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)||; the solve
                                stops at max(rtol, rounding floor), see gfea_pcg_result */
   double inner_rtol;        /* FP32: reduction of the iterated residual between FP64
-                               residual replacements (reliable updates), default 0.1 */
+                               residual replacements (reliable updates); outside (0, 1):
+                               0.1 with block-Jacobi alone, 0.01 with the coarse level */
   int32_t max_refine;       /* refinement steps cap (mixed precision) */
   int32_t lanes;            /* SpMV lanes per node (0 = automatic) */
   int32_t coarse;           /* two-level preconditioner: target number of aggregates

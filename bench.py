@@ -1,24 +1,36 @@
 """Benchmark of the GB300 finite-element path.
 
-Workload (one "step" = one full linear-elastic solve):
-  3D box 1000 x 100 x 100 mm, organised HEXA8 400 x 40 x 40 (640,000 elements,
-  674,081 nodes, 2,022,243 DOF, 158,254,569 CSR entries), E = 210000 MPa,
-  nu = 0.3, clamped at x = 0, traction -1 MPa in z on the x = 1000 face.
-  Step = FP64 element assembly into the CSR values + FP32 copy + Neumann load
-  + Dirichlet state + mixed-precision PCG (FP32 SpMV / block-Jacobi / vectors,
-  FP64 dots and reliable-update residuals) to relative residual 1e-10.
+Headline workload -- the serving stream: seeded Poisson arrivals (rate 400
+req/s, 60 requests per step) mixing 2D QUAD4 / QUAD9 cantilever elastic
+solves (1k-500k DOF), 3D HEXA8 box elastic solves (10k-2M DOF) and single
+phase-field staggered load steps on notched TRI3 plates of 20k-320k elements
+(AT2, Miehe split); sizes log-uniform over 6 classes per kind.  One step = one
+replay of the stream through ``serving.Server`` (8 workers, one CUDA stream
+each, HBM-footprint admission), mixed precision (FP64 assembly, FP32 SpMV /
+preconditioner / vectors, FP64 dots and reliable-update residuals) to relative
+residual 1e-10.  Meshes and phase-field states stay resident on the device
+across steps; every elastic request assembles its stiffness and solves.
 
-Prints one JSON line.  ``value`` (solves/s) is measured with inputs resident
-in HBM; ``e2e`` goes through the public ``Simulations.Elastic`` API with the
-per-step boundary conditions uploaded from pinned host memory and the
-displacement read back.  ``--impl reference`` times the CPU oracle (a numpy /
-scipy restatement of the reference's path) on a bounded sample of the same
-workload.
+Reported beside it, on the same requests:
+  * ``plain_gpu``: one request at a time through the drop-in API, FP64 (same
+    two-level preconditioner); ``plain_gpu_block_jacobi``: the same with
+    block-Jacobi PCG alone;
+  * ``single_solve``: the 3D HEXA8 400 x 40 x 40 box (2,022,243 DOF) solved
+    alone -- the source of the SpMV roofline;
+  * ``batch``: 256 random-material plane-stress cantilevers (2k-200k DOF,
+    per-element E) served largest first.
+
+``value`` is the served solves/s with solutions left on the device; ``e2e``
+replays the stream reading every solution back to pinned host memory.
+``--impl reference`` times the CPU oracle (a numpy/scipy restatement of the
+reference's path) on small samples of each request kind and extrapolates to
+the stream by DOF.
 """
 
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -30,13 +42,13 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "solves/s (HEXA8 2.02M-DOF elastic solve, mixed precision, rel residual 1e-10)"
+METRIC = "solves/s + p50/p99 latency: served mixed-precision vs plain GPU, rel err ≤1e-8"
 UNIT = "solves/s"
-NX, NY, NZ = 400, 40, 40
-L, H, W = 1000.0, 100.0, 100.0
+RATE = 400.0
+NREQ = 60
+SEED = 11
 RTOL = 1e-10
-# CPU sample: same box aspect, material and boundary conditions
-SAMPLE = (80, 8, 8)
+C1 = (400, 40, 40)
 
 
 def parse():
@@ -45,32 +57,89 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--size", type=int, nargs=3, default=None, help="override nx ny nz (testing)")
+    p.add_argument("--requests", type=int, default=NREQ)
+    p.add_argument("--rate", type=float, default=RATE)
+    p.add_argument("--workers", type=int, default=8)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the single-solve and batch measurements")
+    p.add_argument("--workload", default="stream", choices=["stream", "single", "batch"],
+                   help="stream: the full benchmark; single / batch: only that measurement, printed as "
+                        "its own JSON object (for profiling)")
     return p.parse_args()
 
 
 # --------------------------------------------------------------------------
-# CPU oracle sample (reference arm and cpu_baseline)
+# CPU oracle samples (reference arm and cpu_baseline)
 # --------------------------------------------------------------------------
 
-def cpu_sample(nx, ny, nz):
-    """Oracle assembly + SuperLU solve of a small box with the same aspect; returns (seconds, dof)."""
+def _oracle_elastic(spec):
     import numpy as np
 
-    from easyfea_gb300 import mesh as gmesh
     from oracle.simulate import OracleMesh, elastic_solve
 
-    m = gmesh.Mesh_Hexa8_Box(L, H, W, nx, ny, nz)
+    m = spec.build()
     om = OracleMesh.from_mesh(m)
-    left = m.Nodes_Conditions(lambda x, y, z: x == 0)
-    right = m.Nodes_Conditions(lambda x, y, z: x == L)
+    x = m.coord
+    left = np.where(x[:, 0] == 0)[0]
+    right = np.where(x[:, 0] == x[:, 0].max())[0]
     t0 = time.perf_counter()
-    u, K, b = elastic_solve(om, 210000.0, 0.3, False, 1.0, [(left, [0.0, 0.0, 0.0], ["x", "y", "z"])],
-                            [(right, [-1.0], ["z"])])
+    if spec.dim == 2:
+        u, _, _ = elastic_solve(om, 210000.0, 0.3, True, 13.0, [(left, [0.0, 0.0], ["x", "y"])],
+                                [(right, [-800 / 13**2], ["y"])])
+    else:
+        u, _, _ = elastic_solve(om, 210000.0, 0.3, False, 1.0, [(left, [0.0, 0.0, 0.0], ["x", "y", "z"])],
+                                [(right, [-1.0], ["z"])])
     dt = time.perf_counter() - t0
     assert np.isfinite(u).all()
-    return dt, u.size
+    return dt
+
+
+def _oracle_pf_step(spec, step=1, dU=1e-5):
+    import numpy as np
+
+    from oracle.simulate import OracleMesh, PhaseFieldOracle
+
+    m = spec.build()
+    om = OracleMesh.from_mesh(m)
+    x = m.coord
+    pf = PhaseFieldOracle(om, 210e3, 0.3, False, 1.0, "Miehe", "AT2", 2.7, 0.01)
+    notch = np.where((np.abs(x[:, 1] - 0.5) < 1e-12) & (x[:, 0] <= 0.5))[0]
+    pf.dir_d = [(notch, [1.0], ["d"])]
+    pf.dir_u = [(np.where(x[:, 1] == 0)[0], [0.0, 0.0], ["x", "y"]),
+                (np.where(x[:, 1] == 1.0)[0], [0.0, step * dU], ["x", "y"])]
+    t0 = time.perf_counter()
+    pf.solve(1e-3, 500, 0)
+    pf.save_iter()
+    return time.perf_counter() - t0
+
+
+def oracle_rates(budget_s=12.0):
+    """Seconds per DOF of the oracle for each request kind, from small
+    samples (about budget_s of CPU work in total)."""
+    from easyfea_gb300 import serving
+
+    samples = {"quad4": serving.cantilever_spec("quad4", 8e3), "quad9": serving.cantilever_spec("quad9", 8e3),
+               "hexa8": serving.box_spec(2e4), "phasefield": serving.MeshSpec("tri3_sen", 40, 40)}
+    rates, desc = {}, []
+    t_end = time.perf_counter() + budget_s
+    for kind, spec in samples.items():
+        times = []
+        while not times or (time.perf_counter() < t_end - budget_s * 0.6 and len(times) < 3):
+            times.append(_oracle_pf_step(spec) if kind == "phasefield" else _oracle_elastic(spec))
+        t = statistics.median(times)
+        rates[kind] = t / spec.dof
+        desc.append(f"{kind} {spec.dof} DOF {t:.2f} s")
+    return rates, "; ".join(desc)
+
+
+def oracle_stream_value(reqs, rates):
+    """Stream solves/s of the oracle, extrapolated linearly in DOF from the
+    samples (favours the CPU: a direct solve grows faster than linearly)."""
+    total = 0.0
+    for r in reqs:
+        kind = "phasefield" if r.kind == "phasefield" else r.spec.kind
+        total += rates[kind] * r.spec.dof
+    return len(reqs) / total
 
 
 def cpu_threads():
@@ -82,53 +151,29 @@ def cpu_threads():
         return 1
 
 
-def dof_of(nx, ny, nz):
-    return 3 * (nx + 1) * (ny + 1) * (nz + 1)
-
-
-def cpu_baseline_value(steps=1):
-    times = []
-    for _ in range(steps):
-        dt, dof = cpu_sample(*SAMPLE)
-        times.append(dt)
-    t = statistics.median(times)
-    # linear extrapolation of DOF/s to the full workload (favours the CPU:
-    # a direct solve's cost grows faster than linearly with the DOF count)
-    value = (dof / t) / dof_of(NX, NY, NZ)
-    return value, t, dof
-
-
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from easyfea_gb300 import serving
+
+    _, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
     for _ in range(args.warmup):
-        cpu_sample(*SAMPLE)
-    times = []
+        oracle_rates(budget_s=2.0)
+    values, descs = [], []
     for _ in range(args.steps):
-        dt, dof = cpu_sample(*SAMPLE)
-        times.append(dt)
-    total = sum(times)
-    value = (dof * args.steps / total) / dof_of(NX, NY, NZ)
-    sample = (f"oracle (numpy/scipy restatement of EasyFEA's path: einsum element matrices, bincount "
-              f"assembly, SuperLU spsolve) on HEXA8 {SAMPLE[0]}x{SAMPLE[1]}x{SAMPLE[2]} box ({dof} DOF, same "
-              f"aspect/material/BCs), {total / args.steps:.2f} s per solve; value = DOF/s / 2,022,243 DOF "
-              f"(linear extrapolation, favours the CPU)")
+        rates, desc = oracle_rates(budget_s=6.0)
+        values.append(oracle_stream_value(reqs, rates))
+        descs.append(desc)
+    value = statistics.median(values)
+    sample = (f"oracle (numpy/scipy restatement of EasyFEA's path: einsum element matrices, bincount assembly, "
+              f"SuperLU spsolve, staggered phase field) on one small request per kind ({descs[-1]}); "
+              f"stream time = sum over the {args.requests} requests of DOF x seconds-per-DOF of their kind")
     line = {
-        "impl": "reference",
-        "metric": METRIC,
-        "value": value,
-        "unit": UNIT,
-        "n_gpus": args.gpus,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": 1000.0 / value,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"hexa8_box_{NX}x{NY}x{NZ}_elastic_solve", "dof": dof_of(NX, NY, NZ)},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.requests / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"serving_stream_poisson_{args.rate:g}rps_{args.requests}req_seed{SEED}"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -189,6 +234,92 @@ class Clocks:
 # GPU arm
 # --------------------------------------------------------------------------
 
+def flush_l2(buf):
+    buf.add_(1)  # 256 MB written: larger than the 129 MB L2
+
+
+def single_solve(lib, peak):
+    """The HEXA8 400x40x40 box alone (assembly + mixed solve), with the SpMV
+    kernel timed by CUDA events on its stream."""
+    import torch
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    m = gmesh.Mesh_Hexa8_Box(1000.0, 100.0, 100.0, *C1)
+    simu = Simulations.Elastic(m, Models.Elastic.Isotropic(3, E=210000.0, v=0.3, planeStress=False))
+    simu.precision = "mixed"
+    simu.rtol = RTOL
+    simu.add_dirichlet(m.Nodes_Conditions(lambda x, y, z: x == 0), [0.0, 0.0, 0.0], ["x", "y", "z"])
+    simu.add_surfLoad(m.Nodes_Conditions(lambda x, y, z: x == 1000.0), [-1.0], ["z"])
+    for _ in range(2):
+        simu.Need_Update()
+        simu.Solve_device()
+    torch.cuda.synchronize()
+    ms, n = ctypes.c_double(), ctypes.c_longlong()
+    lib.gfea_profile_read(ctypes.byref(ms), ctypes.byref(n))
+    lib.gfea_profile_enable(1)
+    t = []
+    iters = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        simu.Need_Update()
+        simu.Solve_device()
+        torch.cuda.synchronize()
+        t.append(time.perf_counter() - t0)
+        iters.append(simu.last_solve.iterations)
+    lib.gfea_profile_enable(0)
+    lib.gfea_profile_read(ctypes.byref(ms), ctypes.byref(n))
+    dm = simu.dmesh
+    N = 3 * m.Nn
+    nnz = dm.nnz(3)
+    # algorithmic bytes of one SpMV launch: FP32 values, neighbour indices and
+    # row pointers once, p gathered once, known mask, Ap written
+    spmv_bytes = nnz * 4 + dm.n_pairs * 4 + (m.Nn + 1) * 4 + N * 4 + N + N * 4
+    avg_ms = ms.value / max(n.value, 1)
+    achieved = spmv_bytes / (avg_ms * 1e-3) / 1e9 if n.value else None
+    return {
+        "workload": "hexa8_box_400x40x40_elastic_solve", "dof": N, "csr_nnz": nnz,
+        "solves_per_s": 1.0 / statistics.median(t), "ms": 1e3 * statistics.median(t), "pcg_iterations": iters,
+        "final_rel_residual": simu.last_solve.rel_residual, "reliable_updates": simu.last_solve.refinements,
+    }, {"spmv_bytes": spmv_bytes, "avg_ms": avg_ms, "launches": int(n.value), "achieved": achieved}
+
+
+def batch_measure(workers):
+    import numpy as np
+    import torch
+
+    from easyfea_gb300 import serving
+    from easyfea_gb300.batching import random_material_cantilevers
+
+    inst = random_material_cantilevers(n=256, seed=0)
+    cache = serving.MeshCache()
+    reqs = []
+    for i, (m, E) in enumerate(inst):
+        x = m.coord
+        spec = serving.MeshSpec("quad4", len(np.unique(x[:, 0])) - 1, len(np.unique(x[:, 1])) - 1)
+        reqs.append(serving.ElasticRequest(spec, E=E, rid=i, keep_solution=False))
+    cache.prebuild({r.spec for r in reqs})
+    serving.run_plain(reqs[:8], cache, precision="mixed")
+    order = sorted(reqs, key=lambda r: -r.spec.dof)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with serving.Server(workers=workers, precision="mixed", cache=cache, tune=False) as srv:
+        for r in order:
+            srv.submit(r)
+        srv.drain()
+    dt = time.perf_counter() - t0
+    bad = sum(1 for r in srv.results.values() if r.status != 0)
+    t0 = time.perf_counter()
+    serving.run_plain(reqs, cache, precision="fp64")
+    dt_plain = time.perf_counter() - t0
+    return {"workload": "256 random-material QUAD4 cantilevers, 2k-200k DOF, per-element E",
+            "dof_total": int(sum(r.spec.dof for r in reqs)), "served_solves_per_s": len(reqs) / dt,
+            "plain_fp64_solves_per_s": len(reqs) / dt_plain, "failed": bad}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -212,100 +343,127 @@ def main():
 
             dist.barrier()
 
-    from easyfea_gb300 import Models, _lib
-    from easyfea_gb300 import mesh as gmesh
-    from easyfea_gb300 import simulations as Simulations
+    from easyfea_gb300 import _lib, serving
 
-    nx, ny, nz = args.size or (NX, NY, NZ)
-    m = gmesh.Mesh_Hexa8_Box(L, H, W, nx, ny, nz)
-    mat = Models.Elastic.Isotropic(3, E=210000.0, v=0.3, planeStress=False)
-    simu = Simulations.Elastic(m, mat)
-    simu.precision = "mixed"
-    simu.rtol = RTOL
-    left = m.Nodes_Conditions(lambda x, y, z: x == 0)
-    right = m.Nodes_Conditions(lambda x, y, z: x == L)
-    t0 = time.perf_counter()
-    dm = simu.dmesh  # node graph + slot ranks: once per mesh
-    torch.cuda.synchronize()
-    t_graph = time.perf_counter() - t0
-    simu.add_dirichlet(left, [0.0, 0.0, 0.0], ["x", "y", "z"])
-    simu.add_surfLoad(right, [-1.0], ["z"])
     lib = _lib.load()
-    N = 3 * m.Nn
+    if args.workload == "single":
+        for _ in range(max(args.steps, 1)):
+            out, roof = single_solve(lib, 0.0)
+        out["spmv"] = roof
+        print(json.dumps(out), flush=True)
+        return
+    if args.workload == "batch":
+        print(json.dumps(batch_measure(args.workers)), flush=True)
+        return
+    cache = serving.MeshCache()
+    offsets, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    cache.prebuild({r.spec for r in reqs})
+    working_set = sum(s.footprint("mixed") for s in {r.spec for r in reqs})
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def step():
-        simu.Need_Update()  # re-assemble every step
-        return simu.Solve_device()
+    def replay(server, keep):
+        _, rq, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED, sessions=sessions)
+        for r in rq:
+            r.keep_solution = keep
+        return serving.run_stream(server, offsets, rq)
 
+    # autotuner: one request per mesh class, one at a time on the quiet GPU,
+    # records the SpMV and element schedules the served stream then uses
+    from easyfea_gb300 import autotune
+
+    autotune.set_mode(autotune.TUNE)
+    _, tune_reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    seen, first = set(), []
+    for r in tune_reqs:
+        if r.spec not in seen:
+            seen.add(r.spec)
+            first.append(r)
+    serving.run_plain(first, cache, precision="mixed")
+    autotune.set_mode(autotune.USE)
+    _, _, sessions = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    server = serving.Server(workers=args.workers, precision="mixed", cache=cache, tune=False)
     for _ in range(max(args.warmup, 0)):
-        step()
+        replay(server, False)
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    st = torch.cuda.current_stream()
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    lib.gfea_profile_enable(1)
-    import ctypes
-
-    _ms, _n = ctypes.c_double(), ctypes.c_longlong()
-    lib.gfea_profile_read(ctypes.byref(_ms), ctypes.byref(_n))  # reset
     launches0 = lib.gfea_launch_count()
-    iters = []
+    results = []
+    step_s = []
     with Clocks(local) as clk:
-        evs[0].record(st)
-        for k in range(args.steps):
-            step()
-            iters.append(simu.last_solve.iterations)
-            evs[k + 1].record(st)
-        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = replay(server, False)
+            torch.cuda.synchronize()
+            step_s.append(time.perf_counter() - t0)
+            results += res
     launches = lib.gfea_launch_count() - launches0
-    lib.gfea_profile_read(ctypes.byref(_ms), ctypes.byref(_n))
-    lib.gfea_profile_enable(0)
-    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    total_ms = evs[0].elapsed_time(evs[-1])
+    total_s = sum(step_s)
     if world > 1:
         import torch.distributed as dist
 
-        t = torch.tensor([total_ms], device="cuda")
+        t = torch.tensor([total_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    info = simu.last_solve
-    u = simu.u_device
+        total_s = float(t.item())
+    value = world * args.steps * args.requests / total_s
+    lat = np.array([r.latency for r in results]) * 1e3
 
-    # dominant kernel: PCG direction + SpMV (FP32 values, node-block CSR)
-    nnz = dm.nnz(3)
-    spmv_bytes = nnz * 4 + dm.n_pairs * 4 + (m.Nn + 1) * 4 + N * 4 * 4 + N
-    avg_ms = _ms.value / max(_n.value, 1)
+    # e2e: solutions read back to the host
+    e2e_s = []
+    e2e_res = []
+    for _ in range(max(1, min(args.steps, 2))):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_res = replay(server, True)
+        e2e_s.append(time.perf_counter() - t0)
+    server.close()
+    d2h = sum(r.u.nbytes + (r.d.nbytes if r.d is not None else 0) for r in e2e_res)
+    # per request: Dirichlet mask (1 B/DOF) and values (8 B/DOF) uploaded
+    h2d = sum(9 * r.dof for r in e2e_res)
+
+    # plain GPU paths on the same requests, one at a time, FP64: (1) the
+    # two-level preconditioner, with phase-field sessions advanced as the
+    # served ones were (so that every result is compared at the same state);
+    # (2) block-Jacobi PCG alone (the drop-in path's preconditioner before the
+    # coarse level), fresh sessions
+    _, plain_reqs, plain_sessions = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    for _ in range(args.warmup + args.steps + len(e2e_s) - 1):
+        serving.run_plain([r for r in plain_reqs if r.kind == "phasefield"], cache, precision="fp64")
+    torch.cuda.synchronize()
+    flush_l2(flush)
+    plain = serving.run_plain(plain_reqs, cache, offsets=offsets, precision="fp64")
+    plain_sum = serving.latency_summary(plain)
+    errs = [float(np.abs(a.u - b.u).max() / np.abs(b.u).max()) for a, b in zip(e2e_res, plain)
+            if a.kind == "elastic"]
+    derr = [float(np.abs(a.d - b.d).max()) for a, b in zip(e2e_res, plain) if a.kind == "phasefield"]
+    _, bj_reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    flush_l2(flush)
+    torch.cuda.synchronize()
+    bj = serving.run_plain(bj_reqs, cache, offsets=offsets, precision="fp64", coarse=0)
+    bj_sum = serving.latency_summary(bj)
+    bj_err = [float(np.abs(a.u - b.u).max() / np.abs(b.u).max()) for a, b in zip(plain, bj) if a.kind == "elastic"]
+
+    extras = {}
+    roof = None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
-    achieved = spmv_bytes / (avg_ms * 1e-3) / 1e9 if _n.value else None
+    if not args.no_extras:
+        extras["single_solve"], roof = single_solve(lib, peak)
+        extras["batch"] = batch_measure(args.workers)
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        tr = json.load(open(tpath)).get("dir_spmv_f32_hexa8_400x40x40")
-        traffic = tr if tr else None
+        traffic = json.load(open(tpath)).get("apply_f32_hexa8_400x40x40")
 
-    # e2e through the public API: boundary conditions up, displacement down
-    pinned_known = torch.zeros(N, dtype=torch.uint8).pin_memory()
-    e2e_ms = []
-    h2d = d2h = 0
-    for k in range(max(1, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        simu.Bc_Init()
-        simu.add_dirichlet(left, [0.0, 0.0, 0.0], ["x", "y", "z"])
-        simu.add_surfLoad(right, [-1.0], ["z"])
-        simu.Need_Update()
-        u_host = simu.Solve()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        h2d = N * 1 + N * 8 + m.Nn * 1 + right.size * 8 + left.size * 0
-        d2h = N * 8
-    del pinned_known
-
-    value = world * args.steps / (total_ms / 1e3)
+    kinds = {}
+    for r in results:
+        kinds[r.kind] = kinds.get(r.kind, 0) + 1
     line = {
         "metric": METRIC,
         "value": value,
@@ -313,48 +471,53 @@ def main():
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps,
-        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "ms_per_step": 1e3 * total_s / args.steps,
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "plain_gpu": {"solves_per_s": plain_sum["solves_per_s"], "p50_ms": plain_sum["p50_ms"],
+                      "p99_ms": plain_sum["p99_ms"],
+                      "path": "drop-in API, FP64, two-level preconditioner, one request at a time"},
+        "plain_gpu_block_jacobi": {"solves_per_s": bj_sum["solves_per_s"], "p50_ms": bj_sum["p50_ms"],
+                                   "p99_ms": bj_sum["p99_ms"],
+                                   "path": "drop-in API, FP64, block-Jacobi PCG, one request at a time",
+                                   "elastic_u_rel_diff_vs_two_level_max": max(bj_err) if bj_err else None},
+        "rel_err_vs_plain_fp64": {"elastic_u_max": max(errs) if errs else None,
+                                  "phasefield_d_max_abs": max(derr) if derr else None},
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic",
         "config": {
-            "workload": f"hexa8_box_{nx}x{ny}x{nz}_elastic_solve",
-            "dof": N, "elements": m.Ne, "csr_nnz": nnz, "rtol": RTOL,
-            "precision": "FP64 assembly; FP32 SpMV/block-Jacobi/vectors; FP64 dots, scalars, reliable-update residuals",
-            "pcg_iterations": iters, "final_rel_residual": info.rel_residual,
-            "reliable_updates": info.refinements,
-            "graph_setup_s": t_graph,
-            "l2": "inputs larger than L2 (FP32 CSR values 0.63 GB, FP64 1.27 GB per step)",
+            "workload": f"serving_stream_poisson_{args.rate:g}rps_{args.requests}req_seed{SEED}",
+            "requests_per_step": args.requests, "mix": kinds, "workers": args.workers,
+            "precision": "FP64 assembly; FP32 SpMV/preconditioner/vectors; FP64 dots, scalars, coarse solve, "
+                         "reliable-update residuals",
+            "rtol": RTOL,
+            "l2": f"256 MB buffer written between steps; per-step working set {working_set / 1e9:.1f} GB",
             "parallelism": "replicas" if world > 1 else "single GPU",
+            "autotuner": f"{len(autotune.decisions())} schedule decisions, tuned one request per mesh class "
+                         f"on the idle GPU before the timed region",
         },
-        "dof_per_s": value * N,
         "gpu_launches": int(launches),
-        "roofline": {
-            "kernel": "dir_spmv_kernel<3,32,float> (PCG direction update + masked SpMV)",
-            "bound": "hbm",
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None,
-            "traffic": traffic,
-            "bytes_per_launch": spmv_bytes,
-            "avg_launch_ms": avg_ms,
-            "launches": int(_n.value),
-            "peak_source": peak_src,
-        },
-        "e2e": {"value": 1000.0 / statistics.median(e2e_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": {"value": args.requests / statistics.median(e2e_s), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
         "clocks": clk.summary(),
     }
+    if roof is not None:
+        line["roofline"] = {
+            "kernel": "apply_kernel<3,32,float> (masked FP32 node-block SpMV, HEXA8 2.02M DOF)",
+            "bound": "hbm", "achieved": roof["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": (roof["achieved"] / peak) if roof["achieved"] else None, "traffic": traffic,
+            "bytes_per_launch": roof["spmv_bytes"], "avg_launch_ms": roof["avg_ms"],
+            "launches": roof["launches"], "peak_source": peak_src,
+        }
+    line.update(extras)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, t, dof = cpu_baseline_value(2)
+        rates, desc = oracle_rates(budget_s=12.0)
         line["cpu_baseline"] = {
-            "value": v, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-            "sample": f"oracle on HEXA8 {SAMPLE[0]}x{SAMPLE[1]}x{SAMPLE[2]} box ({dof} DOF), {t:.2f} s per solve, "
-                      f"DOF/s linearly extrapolated to 2,022,243 DOF",
+            "value": oracle_stream_value(reqs, rates), "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+            "sample": f"oracle on one small request per kind ({desc}); stream time = sum of DOF x "
+                      f"seconds-per-DOF of each request's kind (linear in DOF, favours the CPU)",
         }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -362,7 +525,6 @@ def main():
         import torch.distributed as dist
 
         dist.destroy_process_group()
-    assert u is not None and np.isfinite(u_host).all()
 
 
 if __name__ == "__main__":

@@ -147,6 +147,8 @@ SIGNATURES = {
     "gfea_batch_workspace_size": (c_size_t, [c_int64, c_int, c_int]),
     "gfea_batch_scratch_size": (c_size_t, [c_int]),
     "gfea_batch_pcg": (c_int, [POINTER(BatchInstance), c_int, c_void_p, c_size_t, POINTER(PcgOpts), c_void_p]),
+    "gfea_batch_prepare": (c_int, [POINTER(BatchInstance), c_int, c_void_p, c_size_t, POINTER(PcgOpts), c_void_p]),
+    "gfea_batch_launch": (c_int, [c_void_p, c_int, POINTER(PcgOpts), c_void_p]),
     "gfea_reduce_workspace_size": (c_size_t, []),
     "gfea_reaction_energy": (c_int, [POINTER(System), c_void_p, c_void_p, c_int64, c_void_p, POINTER(c_double),
                                      c_void_p, c_void_p]),
@@ -155,6 +157,15 @@ SIGNATURES = {
     "gfea_launch_count": (ctypes.c_longlong, []),
     "gfea_profile_enable": (c_int, [c_int]),
     "gfea_profile_read": (c_int, [POINTER(c_double), POINTER(ctypes.c_longlong)]),
+    "gfea_tune_mode": (c_int, [c_int]),
+    "gfea_tune_clear": (c_int, []),
+    "gfea_tune_spmv": (c_int, [POINTER(System), c_int, c_void_p, c_void_p, POINTER(c_int32), POINTER(c_float),
+                               c_void_p]),
+    "gfea_tune_assemble_elastic": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                                           c_double, c_int, c_void_p, c_int64, POINTER(c_int32), POINTER(c_float),
+                                           c_void_p]),
+    "gfea_tune_export": (c_int, [POINTER(c_int64), POINTER(c_int32), c_int, POINTER(c_int)]),
+    "gfea_tune_import": (c_int, [POINTER(c_int64), POINTER(c_int32), c_int]),
 }
 
 

@@ -63,6 +63,16 @@ class BatchSolver:
 
     def launch(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1):
         """Enqueue the batch on the current stream (asynchronous)."""
+        self.prepare(systems, precision, inner_rtol)
+        self.launch_prepared()
+
+    def launch_prepared(self):
+        """Enqueue the prepared batch's device work only (capturable)."""
+        _lib.check(_lib.load().gfea_batch_launch(_lib.ptr(self._scratch), self._n, ctypes.byref(self._opts),
+                                                 _lib.stream()), "batch launch")
+
+    def prepare(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1):
+        """Validate the systems and upload their descriptors (largest first)."""
         L = _lib.load()
         prec = _lib.F64 if precision == "fp64" else _lib.F32
         n = len(systems)
@@ -86,9 +96,9 @@ class BatchSolver:
                 _lib.ptr(s.op.vals64), _lib.ptr(s.op.vals32) if prec == _lib.F32 else 0, _lib.ptr(s.known),
                 int(s.op.translation_invariant), int(s.max_iters), float(s.rtol), _lib.ptr(s.b), _lib.ptr(s.x),
                 base + int(offs[i]), rbase + i * RESULT_BYTES)
-        opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 0, 0, 0.0, float(inner_rtol), 0, 0)
-        _lib.check(L.gfea_batch_pcg(arr, n, _lib.ptr(self._scratch), self._scratch.numel(), ctypes.byref(opts),
-                                    _lib.stream()), "batch pcg")
+        self._opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 0, 0, 0.0, float(inner_rtol), 0, 0)
+        _lib.check(L.gfea_batch_prepare(arr, n, _lib.ptr(self._scratch), self._scratch.numel(),
+                                        ctypes.byref(self._opts), _lib.stream()), "batch prepare")
         self._n = n
 
     def results(self) -> List[PcgInfo]:
@@ -110,6 +120,45 @@ class BatchSolver:
                 _lib.check(info.status, f"batch system {i} (iterations {info.iterations}, "
                                         f"rel residual {info.rel_residual:.3e})")
         return infos
+
+
+class GraphBatch:
+    """A batch captured as one CUDA graph: optional device work ``pre`` (e.g.
+    re-assembling every instance's operator), the reset of each x to its
+    initial state and the persistent batched solve.  ``replay`` re-runs all of
+    it with one graph launch; buffers (values, b, x) are read in place, so new
+    values written into them between replays are picked up."""
+
+    def __init__(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
+                 pre=None):
+        from . import autotune
+
+        self.systems = systems
+        self.x0 = [s.x.clone() for s in systems]
+        self.solver = BatchSolver()
+        self.solver.prepare(systems, precision, inner_rtol)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        prev = autotune.get_mode()
+        autotune.set_mode(autotune.USE)  # no timing runs inside the capture
+        try:
+            with torch.cuda.graph(self.graph, stream=stream):
+                if pre is not None:
+                    pre()
+                for s, x0 in zip(systems, self.x0):
+                    s.x.copy_(x0)
+                self.solver.launch_prepared()
+        finally:
+            autotune.set_mode(prev)
+        torch.cuda.synchronize()
+
+    def replay(self):
+        self.graph.replay()
+
+    def results(self) -> List[PcgInfo]:
+        return self.solver.results()
 
 
 def solve_batch(systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,

@@ -10,6 +10,7 @@
 // Element matrices never touch global memory.
 
 #include "common.cuh"
+#include "tune.cuh"
 
 namespace gfea {
 namespace {
@@ -262,13 +263,25 @@ __global__ void surface_load_kernel(const double* __restrict__ coord, const int3
   }
 }
 
+int64_t assemble_key(int elem, int value_type, int cpe, int64_t Ne) {
+  return tune_key(kTuneAssemble, elem, value_type, cpe, tune_log2((double)Ne));
+}
+
+// Element tile schedule: the grid is capped at per_sm blocks of 128 threads
+// per SM (each block then strides over its elements); per_sm = 0 takes the
+// autotuner's decision for this class, else 64.
 template <int ELEM, typename T, typename R>
 int launch_elastic(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
-                   const uint8_t* rank, const double* C, int cpe, double factor, T* vals, cudaStream_t s) {
+                   const uint8_t* rank, const double* C, int cpe, double factor, T* vals, cudaStream_t s,
+                   int per_sm = 0) {
   constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
+  if (per_sm <= 0) {
+    int32_t tuned = 0;
+    per_sm = tune_get(assemble_key(ELEM, sizeof(T) == 4 ? GFEA_F32 : GFEA_F64, cpe, Ne), &tuned) ? tuned : 64;
+  }
   const int64_t warps = ceil_div(Ne, 32 / G);
   int blocks = grid_for(warps * 32, 128);
-  if (blocks > kSMs * 64) blocks = kSMs * 64;
+  if (blocks > kSMs * per_sm) blocks = kSMs * per_sm;
   if (cpe == 1)
     elastic_kernel<ELEM, T, R, 1><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
   else if (cpe == 2)
@@ -302,6 +315,58 @@ int elem_nPe(int elem) {
   }
 }
 
+// Times the element kernel with 4 .. 64 blocks per SM (values zeroed before
+// each candidate), records the fastest and leaves the values assembled by it.
+template <int ELEM, typename T, typename R>
+int tune_elastic(const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                 const uint8_t* rank, const double* C, int cpe, double factor, T* vals, int64_t n_values,
+                 cudaStream_t s, int32_t* best, float* best_ms) {
+  const int cand[5] = {4, 8, 16, 32, 64};
+  float bm = INFINITY, t_def = INFINITY;
+  int bc = 64;
+  for (int c = 0; c < 5; ++c) {
+    GFEA_CUDA_TRY(cudaMemsetAsync(vals, 0, sizeof(T) * (size_t)n_values, s));
+    float ms = 0;
+    const int e = time_launches(
+        [&]() { return launch_elastic<ELEM, T, R>(coord, connect, Ne, node_ptr, rank, C, cpe, factor, vals, s, cand[c]); },
+        2, s, &ms);
+    if (e) return e;
+    if (cand[c] == 64) t_def = ms;
+    if (ms < bm) {
+      bm = ms;
+      bc = cand[c];
+    }
+  }
+  if (!(bm < 0.95f * t_def)) {  // keep the default unless clearly beaten
+    bc = 64;
+    bm = t_def;
+  }
+  tune_put(assemble_key(ELEM, sizeof(T) == 4 ? GFEA_F32 : GFEA_F64, cpe, Ne), bc);
+  GFEA_CUDA_TRY(cudaMemsetAsync(vals, 0, sizeof(T) * (size_t)n_values, s));
+  *best = bc;
+  *best_ms = bm;
+  return launch_elastic<ELEM, T, R>(coord, connect, Ne, node_ptr, rank, C, cpe, factor, vals, s, bc);
+}
+
+template <typename T>
+int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* connect, int64_t Ne,
+                     const int32_t* node_ptr, const uint8_t* rank, const double* C, int cpe, double factor, T* v,
+                     int64_t n_values, cudaStream_t s, int32_t* best, float* ms) {
+#define GFEA_ELASTIC_CASE(EL)                                                                                   \
+  case EL:                                                                                                      \
+    return tune ? tune_elastic<EL, T, T>(coord, connect, Ne, node_ptr, rank, C, cpe, factor, v, n_values, s, best, \
+                                         ms)                                                                    \
+                : launch_elastic<EL, T, T>(coord, connect, Ne, node_ptr, rank, C, cpe, factor, v, s);
+  switch (elem) {
+    GFEA_ELASTIC_CASE(GFEA_TRI3)
+    GFEA_ELASTIC_CASE(GFEA_QUAD4)
+    GFEA_ELASTIC_CASE(GFEA_QUAD9)
+    GFEA_ELASTIC_CASE(GFEA_HEXA8)
+    default: return GFEA_ERR_ARG;
+  }
+#undef GFEA_ELASTIC_CASE
+}
+
 int elem_dim(int elem) {
   switch (elem) {
     case GFEA_SEG2: return 1;
@@ -323,30 +388,38 @@ extern "C" int gfea_assemble_elastic(int elem, const double* coord, const int32_
   if (!coord || !connect || !node_ptr || !rank || !C || !values || n_elems < 0) return GFEA_ERR_ARG;
   const int d = elem_dim(elem);
   if (d < 2) return GFEA_ERR_ARG;
+  if (value_type != GFEA_F64 && value_type != GFEA_F32) return GFEA_ERR_ARG;
   if (n_elems == 0) return GFEA_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (!accumulate && n_values > 0)
+  // first assembly of this class in tuning mode: choose the tile schedule
+  int32_t tuned = 0;
+  float ms = 0;
+  const bool tune = !accumulate && n_values > 0 && tune_cache().mode.load() == 2 &&
+                    !tune_get(assemble_key(elem, value_type, c_per_elem, n_elems), &tuned);
+  if (!accumulate && n_values > 0 && !tune)
     GFEA_CUDA_TRY(cudaMemsetAsync(values, 0, (value_type == GFEA_F64 ? 8 : 4) * (size_t)n_values, s));
-  if (value_type == GFEA_F64) {
-    auto* v = static_cast<double*>(values);
-    switch (elem) {
-      case GFEA_TRI3: return launch_elastic<GFEA_TRI3, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_QUAD4: return launch_elastic<GFEA_QUAD4, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_QUAD9: return launch_elastic<GFEA_QUAD9, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_HEXA8: return launch_elastic<GFEA_HEXA8, double, double>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      default: return GFEA_ERR_ARG;
-    }
-  } else if (value_type == GFEA_F32) {
-    auto* v = static_cast<float*>(values);
-    switch (elem) {
-      case GFEA_TRI3: return launch_elastic<GFEA_TRI3, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_QUAD4: return launch_elastic<GFEA_QUAD4, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_QUAD9: return launch_elastic<GFEA_QUAD9, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      case GFEA_HEXA8: return launch_elastic<GFEA_HEXA8, float, float>(coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor, v, s);
-      default: return GFEA_ERR_ARG;
-    }
-  }
-  return GFEA_ERR_ARG;
+  if (value_type == GFEA_F64)
+    return dispatch_elastic<double>(elem, tune, coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor,
+                                    static_cast<double*>(values), n_values, s, &tuned, &ms);
+  return dispatch_elastic<float>(elem, tune, coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor,
+                                 static_cast<float*>(values), n_values, s, &tuned, &ms);
+}
+
+extern "C" int gfea_tune_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                                          const int32_t* node_ptr, const uint8_t* rank, const double* C,
+                                          int c_per_elem, double factor, int value_type, void* values,
+                                          int64_t n_values, int32_t* blocks_per_sm_host, float* ms_host,
+                                          void* stream) {
+  if (!coord || !connect || !node_ptr || !rank || !C || !values || n_elems <= 0 || n_values <= 0 ||
+      !blocks_per_sm_host || !ms_host)
+    return GFEA_ERR_ARG;
+  if (elem_dim(elem) < 2 || (value_type != GFEA_F64 && value_type != GFEA_F32)) return GFEA_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (value_type == GFEA_F64)
+    return dispatch_elastic<double>(elem, true, coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor,
+                                    static_cast<double*>(values), n_values, s, blocks_per_sm_host, ms_host);
+  return dispatch_elastic<float>(elem, true, coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor,
+                                 static_cast<float*>(values), n_values, s, blocks_per_sm_host, ms_host);
 }
 
 extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* connect, int64_t n_elems,

@@ -252,6 +252,7 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
     for (;;) {
       // direction p' = z + beta p and Ap' (masked SpMV); partial p'.Ap'
       double va[1] = {0}, oa[1];
+      DotAcc<T> pap_acc;
       const T bt = (T)beta;
       for (int64_t a0 = grp - sub; a0 < Nn; a0 += ngrp) {
         const int64_t a = a0 + sub;
@@ -272,9 +273,10 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
           if (S.known[dof]) av = 0;
           pb[dof] = pn;
           w.Ap[dof] = av;
-          va[0] += (double)pn * (double)av;
+          pap_acc.add_prod(pn, av);
         }
       }
+      va[0] = pap_acc.value();
       csum<1>(c, va, oa);
       const double pap = oa[0];
       if (!(pap > 0) || !isfinite(pap)) {
@@ -284,6 +286,7 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
       const double alpha = rz / pap;
       // x, r, z update; partials r.z, r.r
       double vb[2] = {0, 0}, ob[2];
+      DotAcc<T> rz_acc, rr_acc;
       const T al = (T)alpha;
       for (int64_t a = gtid; a < Nn; a += nthr) {
         T rl[D];
@@ -301,10 +304,12 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
           for (int j = 0; j < D; ++j) zi += w.dinv[a * D * D + i * D + j] * rl[j];
           if (I.known[a * D + i]) zi = 0;
           w.z[a * D + i] = zi;
-          vb[0] += (double)rl[i] * (double)zi;
-          vb[1] += (double)rl[i] * (double)rl[i];
+          rz_acc.add_prod(rl[i], zi);
+          rr_acc.add_prod(rl[i], rl[i]);
         }
       }
+      vb[0] = rz_acc.value();
+      vb[1] = rr_acc.value();
       csum<2>(c, vb, ob);
       beta = ob[0] / rz;
       rz = ob[0];
@@ -412,10 +417,9 @@ extern "C" size_t gfea_batch_scratch_size(int n_instances) {
   return a256(sizeof(int)) + a256(sizeof(gfea_batch_instance) * (size_t)n_instances);
 }
 
-extern "C" int gfea_batch_pcg(const gfea_batch_instance* inst_host, int n, void* scratch, size_t scratch_bytes,
-                              const gfea_pcg_opts* opts_host, void* stream) {
+extern "C" int gfea_batch_prepare(const gfea_batch_instance* inst_host, int n, void* scratch, size_t scratch_bytes,
+                                  const gfea_pcg_opts* opts_host, void* stream) {
   if (!inst_host || n < 0 || !scratch || !opts_host || opts_host->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
-  if (n == 0) return GFEA_OK;
   if (scratch_bytes < gfea_batch_scratch_size(n)) return GFEA_ERR_WORKSPACE;
   const int prec = opts_host->precision;
   if (prec != GFEA_F64 && prec != GFEA_F32) return GFEA_ERR_ARG;
@@ -427,24 +431,41 @@ extern "C" int gfea_batch_pcg(const gfea_batch_instance* inst_host, int n, void*
     if (prec == GFEA_F32 && !I.vals32) return GFEA_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(I.work) & 255) != 0) return GFEA_ERR_ARG;
   }
+  if (n == 0) return GFEA_OK;
   // largest systems first (longest-processing-time order over the clusters)
   std::vector<gfea_batch_instance> order(inst_host, inst_host + n);
   std::stable_sort(order.begin(), order.end(), [](const gfea_batch_instance& a, const gfea_batch_instance& b) {
     return a.n_pairs * a.dof_n * a.dof_n > b.n_pairs * b.dof_n * b.dof_n;
   });
+  auto* desc = reinterpret_cast<gfea_batch_instance*>(static_cast<char*>(scratch) + a256(sizeof(int)));
+  GFEA_CUDA_TRY(cudaMemcpyAsync(desc, order.data(), sizeof(gfea_batch_instance) * (size_t)n, cudaMemcpyHostToDevice,
+                                static_cast<cudaStream_t>(stream)));
+  // (a copy from pageable host memory has been staged when cudaMemcpyAsync
+  // returns, so the local descriptor array may go out of scope)
+  return GFEA_OK;
+}
+
+extern "C" int gfea_batch_launch(void* scratch, int n, const gfea_pcg_opts* opts_host, void* stream) {
+  if (!scratch || n < 0 || !opts_host || opts_host->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
+  const int prec = opts_host->precision;
+  if (prec != GFEA_F64 && prec != GFEA_F32) return GFEA_ERR_ARG;
+  if (n == 0) return GFEA_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int* next = static_cast<int*>(scratch);
   auto* desc = reinterpret_cast<gfea_batch_instance*>(static_cast<char*>(scratch) + a256(sizeof(int)));
   GFEA_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), s));
-  GFEA_CUDA_TRY(cudaMemcpyAsync(desc, order.data(), sizeof(gfea_batch_instance) * (size_t)n,
-                                cudaMemcpyHostToDevice, s));
   // persistent clusters: enough to fill the GPU, never more than the systems
   int clusters = std::min(n, 2 * kSMs / kCL);
   if (clusters < 1) clusters = 1;
   const double d = (opts_host->inner_rtol > 0 && opts_host->inner_rtol < 1) ? opts_host->inner_rtol : 0.1;
   batch_pcg_kernel<<<clusters * kCL, kBT, 0, s>>>(desc, n, next, prec == GFEA_F64 ? 1 : 0, d * d);
   GFEA_LAUNCH_CHECK();
-  // (a copy from pageable host memory has been staged when cudaMemcpyAsync
-  // returns, so the local descriptor array may go out of scope)
   return GFEA_OK;
+}
+
+extern "C" int gfea_batch_pcg(const gfea_batch_instance* inst_host, int n, void* scratch, size_t scratch_bytes,
+                              const gfea_pcg_opts* opts_host, void* stream) {
+  int e = gfea_batch_prepare(inst_host, n, scratch, scratch_bytes, opts_host, stream);
+  if (e) return e;
+  return gfea_batch_launch(scratch, n, opts_host, stream);
 }

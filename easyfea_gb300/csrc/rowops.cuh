@@ -16,6 +16,35 @@ struct SysT {
   int diff;  // difference form sum_b K_ab (x_b - x_a) (translation-invariant operators)
 };
 
+// Per-thread accumulator of dot-product terms.  For FP32 operands the sum is
+// kept as an unevaluated pair s + c of floats: each product is split exactly
+// (p = a b, e = fma(a, b, -p)) and added with TwoSum (Knuth), so the pair
+// carries the sum of the exact products to ~2^-48 relative -- FP64-class
+// accuracy without FP64 instructions, which on GB300 run at 1/64 of the FP32
+// rate and were the bound of the FP32 PCG kernels.  value() returns the
+// double to reduce across threads in FP64.
+template <typename T>
+struct DotAcc {
+  double v = 0;
+  __device__ __forceinline__ void add_prod(T a, T b) { v += (double)a * (double)b; }
+  __device__ __forceinline__ double value() const { return v; }
+};
+
+template <>
+struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float t = s + p;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (p - bp);
+    s = t;
+    c += err + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // warp then block reduction with a fixed tree (deterministic); result valid in thread 0
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   // warp then block reduction with a fixed tree (deterministic)
@@ -72,6 +101,77 @@ __device__ __forceinline__ void node_rows(int64_t a, int lane, const SysT<T>& S,
   }
 #pragma unroll
   for (int i = 0; i < D; ++i) acc[i] = group_sum<G, A>(acc[i]);
+}
+
+// Sum of D per-lane values over a G-lane group with a transposing butterfly:
+// the first log2(V) exchange steps (V = D rounded up to a power of two) swap
+// half of the remaining values with the partner lane instead of adding all of
+// them, so D sums cost log2(G) + V - 2 shuffles instead of D log2(G).
+// Returns row r's sum in lanes r * (G / V) .. (the other lanes hold the
+// other rows' sums or padding); row_lane<D, G>(r) gives the lane.
+template <int D, int G>
+__host__ __device__ constexpr int row_lane(int r) {
+  return r * (G / (D == 1 ? 1 : (D == 2 ? 2 : 4)));
+}
+
+template <int D, int G, typename A>
+__device__ __forceinline__ A group_sum_rows(const A (&v)[D], int lane) {
+  if constexpr (D == 1) {
+    return group_sum<G, A>(v[0]);
+  } else if constexpr (D == 2) {
+    const bool hi = lane & (G / 2);
+    const A send = hi ? v[0] : v[1];
+    A keep = hi ? v[1] : v[0];
+    keep += __shfl_xor_sync(0xffffffffu, send, G / 2, G);
+#pragma unroll
+    for (int o = G / 4; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o, G);
+    return keep;
+  } else {
+    static_assert(D == 3 && G >= 4, "three rows need at least four lanes");
+    const A w3 = 0;
+    const bool b1 = lane & (G / 2);
+    // step 1: keep {0, 1} (low half) or {2, 3} (high half), send the other pair
+    A k0 = b1 ? v[2] : v[0], k1 = b1 ? w3 : v[1];
+    const A s0 = b1 ? v[0] : v[2], s1 = b1 ? v[1] : w3;
+    k0 += __shfl_xor_sync(0xffffffffu, s0, G / 2, G);
+    k1 += __shfl_xor_sync(0xffffffffu, s1, G / 2, G);
+    // step 2: keep one of the pair
+    const bool b2 = lane & (G / 4);
+    A keep = b2 ? k1 : k0;
+    keep += __shfl_xor_sync(0xffffffffu, b2 ? k0 : k1, G / 4, G);
+#pragma unroll
+    for (int o = G / 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o, G);
+    return keep;
+  }
+}
+
+// node_rows with the transposing reduction: the returned value is row r's
+// sum in lane row_lane<D, G>(r) (r < D) of the group.
+template <int D, int G, typename T, typename A, bool ABS = false, bool DIFF = false, typename XF>
+__device__ __forceinline__ A node_rows_t(int64_t a, int lane, const SysT<T>& S, XF xf) {
+  constexpr int LA = G - G % D;
+  constexpr int NPP = LA / D;
+  const int32_t p0 = S.node_ptr[a];
+  const int32_t nb = S.node_ptr[a + 1] - p0;
+  const int32_t W = D * nb;
+  const T* base = S.vals + (int64_t)D * D * p0;
+  const int j = lane % D;
+  A acc[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) acc[i] = 0;
+  if (lane < LA) {
+    const A self = DIFF ? xf(a * D + j) : (A)0;
+    for (int32_t k = lane / D, t = lane; k < nb; k += NPP, t += LA) {
+      const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
+      const A xv = DIFF ? xf(col) - self : xf(col);
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        const A v = (A)__ldg(base + (int64_t)i * W + t);
+        acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv;
+      }
+    }
+  }
+  return group_sum_rows<D, G, A>(acc, lane);
 }
 
 }  // namespace gfea

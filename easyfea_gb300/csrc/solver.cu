@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "rowops.cuh"
+#include "tune.cuh"
 
 namespace gfea {
 namespace {
@@ -130,9 +131,11 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
 // ---------------------------------------------------------------------------
 
 
-// y = A x (unmasked)
-template <int D, int G, typename T>
-__global__ void __launch_bounds__(kThreads) spmv_kernel(SysT<T> S, const T* __restrict__ x, T* __restrict__ y) {
+// y = A x (unmasked); DIFF: the difference form of the PCG's FP32 products
+// (used to time the same loads and arithmetic when tuning)
+template <int D, int G, typename T, bool DIFF = false>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 8 : 6) spmv_kernel(SysT<T> S, const T* __restrict__ x,
+                                                                             T* __restrict__ y) {
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
@@ -140,14 +143,11 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SysT<T> S, const T* __re
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    T acc[D];
-    node_rows<D, G, T, T>(ac, lane, S, [&](int64_t c) { return x[c]; }, acc);
-    if (a < Nn && lane < D) {
-      T v = acc[0];
+    const T v = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [&](int64_t c) { return x[c]; });
+    int r = -1;
 #pragma unroll
-      for (int i = 1; i < D; ++i) if (lane == i) v = acc[i];
-      y[a * D + lane] = v;
-    }
+    for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) r = i;
+    if (a < Nn && r >= 0) y[a * D + r] = v;
   }
 }
 
@@ -192,25 +192,23 @@ __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double
         }
       }
     }
+    // row i's three sums land in lane row_lane(i)
+    const double s_all = group_sum_rows<D, G, double>(all, lane);
+    const double s_kn = KN ? group_sum_rows<D, G, double>(kn, lane) : 0.0;
+    const double s_ab = group_sum_rows<D, G, double>(ab, lane);
+    int ri_row = -1;
 #pragma unroll
-    for (int i = 0; i < D; ++i) {
-      all[i] = group_sum<G, double>(all[i]);
-      if (KN) kn[i] = group_sum<G, double>(kn[i]);
-      ab[i] = group_sum<G, double>(ab[i]);
-    }
-    if (a < Nn && lane == 0) {
-#pragma unroll
-      for (int i = 0; i < D; ++i) {
-        const int64_t dof = a * D + i;
-        const bool unk = !S.known[dof];
-        const double ri = unk ? b[dof] - all[i] : 0.0;
-        const double rci = unk ? b[dof] - kn[i] : 0.0;
-        const double ai = unk ? ab[i] + fabs(b[dof]) : 0.0;
-        r[dof] = ri;
-        v[0] += ri * ri;
-        v[1] += rci * rci;
-        v[2] += ai * ai;
-      }
+    for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) ri_row = i;
+    if (a < Nn && ri_row >= 0) {
+      const int64_t dof = a * D + ri_row;
+      const bool unk = !S.known[dof];
+      const double ri = unk ? b[dof] - s_all : 0.0;
+      const double rci = unk ? b[dof] - s_kn : 0.0;
+      const double ai = unk ? s_ab + fabs(b[dof]) : 0.0;
+      r[dof] = ri;
+      v[0] += ri * ri;
+      v[1] += rci * rci;
+      v[2] += ai * ai;
     }
   }
   double out[3];
@@ -275,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
                                                           double* partials, Scal* sc, int mode) {
   if (mode == 0 && sc->done) return;
   const double alpha = mode == 0 ? sc->alpha : 0.0;
-  double v[2] = {0, 0};
+  DotAcc<T> rz, rr;
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
     T rl[D];
 #pragma unroll
@@ -296,10 +294,11 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
       for (int j = 0; j < D; ++j) zi += dinv[a * D * D + i * D + j] * rl[j];
       if (known[a * D + i]) zi = 0;
       z[a * D + i] = zi;
-      v[0] += (double)rl[i] * (double)zi;
-      v[1] += (double)rl[i] * (double)rl[i];
+      rz.add_prod(rl[i], zi);
+      rr.add_prod(rl[i], rl[i]);
     }
   }
+  const double v[2] = {rz.value(), rr.value()};
   double out[2];
   if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
     const double rz_new = out[0], rr = out[1];
@@ -353,6 +352,7 @@ struct CoarseDev {
   double* pinv = nullptr;  // kGJB x kGJB: inverse of the pivot block
   double* rc = nullptr;    // nc: restriction accumulator
   double* ec = nullptr;    // nc: coarse correction
+  float* ecf = nullptr;    // nc: its FP32 copy (read by the FP32 prolongation)
 };
 
 template <int D>
@@ -661,6 +661,7 @@ __global__ void __launch_bounds__(kGemvThreads) coarse_gemv_kernel(CoarseDev C, 
 #pragma unroll
       for (int w = 0; w < kGemvThreads / 32; ++w) t += sh[w];
       C.ec[i] = t;
+      C.ecf[i] = (float)t;
     }
     __syncthreads();
   }
@@ -675,7 +676,8 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
                                                             CoarseDev C, int mode) {
   if (mode == 0 && sc->done) return;
   constexpr int nr = Modes<D>::nr;
-  double v[2] = {0, 0};
+  DotAcc<T> rz, rr;
+  const T* ec = sizeof(T) == 4 ? (const T*)C.ecf : (const T*)C.ec;
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
     T rl[D];
 #pragma unroll
@@ -685,7 +687,7 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
     node_modes<D, T>(C.off[a], known + a * D, R);
     T e[nr];
 #pragma unroll
-    for (int m = 0; m < nr; ++m) e[m] = (T)C.ec[g * nr + m];
+    for (int m = 0; m < nr; ++m) e[m] = ec[g * nr + m];
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       T zi = 0;
@@ -695,11 +697,12 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
       for (int m = 0; m < nr; ++m) zi += R[i][m] * e[m];
       if (known[a * D + i]) zi = 0;
       z[a * D + i] = zi;
-      v[0] += (double)rl[i] * (double)zi;
-      v[1] += (double)rl[i] * (double)rl[i];
+      rz.add_prod(rl[i], zi);
+      rr.add_prod(rl[i], rl[i]);
     }
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) C.rc[i] = 0;
+  const double v[2] = {rz.value(), rr.value()};
   double out[2];
   if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
     const double rz_new = out[0], rr = out[1];
@@ -734,35 +737,32 @@ __global__ void __launch_bounds__(kThreads) dir_kernel(int64_t n, const T* __res
 }
 
 // Ap = masked A p; partial p.Ap; the last block sets alpha.
-template <int D, int G, typename T>
-__global__ void __launch_bounds__(kThreads) apply_kernel(SysT<T> S, const T* __restrict__ p, T* __restrict__ Ap,
+template <int D, int G, typename T, bool DIFF>
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) apply_kernel(SysT<T> S, const T* __restrict__ p,
+                                                                              T* __restrict__ Ap,
                                                          double* partials, Scal* sc) {
   if (sc->done) return;
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
   const int64_t Nn = S.Nn;
-  double v[1] = {0};
+  DotAcc<T> pap;
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    T acc[D];
-    auto xf = [&](int64_t c) { return p[c]; };
-    if (sizeof(T) == 4 && S.diff)
-      node_rows<D, G, T, T, false, true>(ac, lane, S, xf, acc);
-    else
-      node_rows<D, G, T, T>(ac, lane, S, xf, acc);
-    if (a < Nn && lane < D) {
-      T av = acc[0];
+    T av = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [&](int64_t c) { return p[c]; });
+    int r = -1;
 #pragma unroll
-      for (int i = 1; i < D; ++i) if (lane == i) av = acc[i];
-      const int64_t dof = a * D + lane;
+    for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) r = i;
+    if (a < Nn && r >= 0) {
+      const int64_t dof = a * D + r;
       const T pn = p[dof];
       if (S.known[dof]) av = 0;
       Ap[dof] = av;
-      v[0] += (double)pn * (double)av;
+      pap.add_prod(pn, av);
     }
   }
+  const double v[1] = {pap.value()};
   double out[1];
   if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
     sc->pap = out[0];
@@ -862,14 +862,27 @@ __global__ void max_abs_diff_kernel(const double* __restrict__ a, const double* 
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-int pick_lanes(const gfea_system* s, int requested) {
-  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
-  // values per row W = dof_n * neighbours: small groups for short rows
+int64_t spmv_key(const gfea_system* s, int value_type) {
+  const double W = s->n_nodes > 0 ? (double)s->dof_n * (double)s->n_pairs / (double)s->n_nodes : 1.0;
+  return tune_key(kTuneSpmv, s->dof_n, value_type, tune_log2(4 * W), tune_log2((double)s->n_nodes));
+}
+
+// values per row W = dof_n * neighbours: small groups for short rows
+int lanes_rule(const gfea_system* s) {
   const double W = s->n_nodes > 0 ? (double)s->dof_n * (double)s->n_pairs / (double)s->n_nodes : 1.0;
   if (W <= 10) return 4;
   if (W <= 24) return 8;
   if (W <= 56) return 16;
   return 32;
+}
+
+// Lanes per node of the node-row products: the request, else the autotuner's
+// decision for this problem class, else a rule on the row length.
+int pick_lanes(const gfea_system* s, int requested, int value_type) {
+  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
+  int32_t tuned = 0;
+  if (tune_get(spmv_key(s, value_type), &tuned)) return tuned;
+  return lanes_rule(s);
 }
 
 int grid_nodes(int64_t Nn, int G) {
@@ -947,6 +960,7 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
     w->C.pinv = reinterpret_cast<double*>(take(sizeof(double) * kGJB * kGJB));
     w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
+    w->C.ecf = reinterpret_cast<float*>(take(sizeof(float) * nc));
   }
   return off;
 }
@@ -1028,8 +1042,13 @@ int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new
   int e = prof_mark(st, kTagDir);
   if (e) return e;
   const int grid = grid_nodes(s->n_nodes, G);
-  GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap, w.partials,
-                                                                                   w.sc)));
+  if (sizeof(T) == 4 && s->translation_invariant) {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap,
+                                                                                         w.partials, w.sc)));
+  } else {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap,
+                                                                                          w.partials, w.sc)));
+  }
   GFEA_LAUNCH_CHECK();
   return prof_mark(st, kTagApply);
 }
@@ -1183,17 +1202,116 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
   return GFEA_OK;
 }
 
-// Runs PCG iterations until the device flags done; checks every 'check'
-// iterations.  pa holds the current search direction on entry and exit.
+// SpMV row-block schedule: times the node-row product with 4, 8, 16 and 32
+// lanes per node (CUDA events, 5 launches each after a warm-up) and records
+// the fastest for this problem class.
 template <typename T>
-int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* host_sc, T*& pa, T*& pb,
-             int iters0, cudaStream_t st) {
+int tune_spmv_impl(const gfea_system* s, const T* x, T* y, cudaStream_t st, int32_t* best, float* best_ms) {
+  const SysT<T> S = sys_t<T>(s);
+  const bool diff = sizeof(T) == 4 && s->translation_invariant;
+  const int vt = sizeof(T) == 4 ? GFEA_F32 : GFEA_F64;
+  const int cand[4] = {4, 8, 16, 32};
+  const int rule = lanes_rule(s);
+  float bm = INFINITY, t_rule = INFINITY;
+  int bg = 0;
+  for (int c = 0; c < 4; ++c) {
+    const int G = cand[c];
+    if (G < s->dof_n) continue;
+    const int grid = grid_nodes(s->n_nodes, G);
+    float ms = 0;
+    const int e = time_launches(
+        [&]() -> int {
+          if (diff) {
+            GFEA_DG_SWITCH(s->dof_n, G, (spmv_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(S, x, y)));
+          } else {
+            GFEA_DG_SWITCH(s->dof_n, G, (spmv_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(S, x, y)));
+          }
+          GFEA_LAUNCH_CHECK();
+          return GFEA_OK;
+        },
+        5, st, &ms);
+    if (e) return e;
+    if (G == rule) t_rule = ms;
+    if (ms < bm) {
+      bm = ms;
+      bg = G;
+    }
+  }
+  if (bg == 0) return GFEA_ERR_ARG;
+  if (!(bm < 0.95f * t_rule)) {  // keep the rule unless clearly beaten
+    bg = rule;
+    bm = t_rule;
+  }
+  tune_put(spmv_key(s, vt), bg);
+  *best = bg;
+  *best_ms = bm;
+  return GFEA_OK;
+}
+
+// Row-block schedule chosen on the PCG's own masked SpMV (apply_kernel, with
+// the p.Ap reduction): each candidate is timed twice (5 launches after a
+// warm-up) and the faster round counts; the rule's choice is kept unless a
+// candidate beats it by more than 5 %.  p = w.pa must hold a direction with
+// p.Ap > 0 on the unknowns.
+template <typename T>
+int tune_apply_impl(const gfea_system* s, PcgWork& w, cudaStream_t st, int* G_out) {
+  const SysT<T> S = sys_t<T>(s);
+  const int vt = sizeof(T) == 4 ? GFEA_F32 : GFEA_F64;
+  const int rule = lanes_rule(s);
+  const int cand[4] = {4, 8, 16, 32};
+  float t_rule = INFINITY, bm = INFINITY;
+  int bg = rule;
+  for (int c = 0; c < 4; ++c) {
+    const int G = cand[c];
+    if (G < s->dof_n) continue;
+    const int grid = grid_nodes(s->n_nodes, G);
+    float best = INFINITY;
+    for (int round = 0; round < 2; ++round) {
+      GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
+      float ms = 0;
+      const int e = time_launches(
+          [&]() -> int {
+            if (sizeof(T) == 4 && s->translation_invariant) {
+              GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(
+                                               S, (const T*)w.pa, (T*)w.Ap, w.partials, w.sc)));
+            } else {
+              GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(
+                                               S, (const T*)w.pa, (T*)w.Ap, w.partials, w.sc)));
+            }
+            GFEA_LAUNCH_CHECK();
+            return GFEA_OK;
+          },
+          5, st, &ms);
+      if (e) return e;
+      best = fminf(best, ms);
+    }
+    if (G == rule) t_rule = best;
+    if (best < bm) {
+      bm = best;
+      bg = G;
+    }
+  }
+  const int choice = (bm < 0.95f * t_rule) ? bg : rule;
+  tune_put(spmv_key(s, vt), choice);
+  *G_out = choice;
+  return GFEA_OK;
+}
+
+// Runs PCG iterations until the device flags done, checking after chunks of
+// 'check' iterations (doubled after each chunk that did not finish when
+// 'grow' is set, so that few launches after convergence are wasted).  pa
+// holds the current search direction on entry and exit.
+template <typename T>
+int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow, Scal* host_sc, T*& pa,
+             T*& pb, int iters0, cudaStream_t st) {
   // iteration j reads direction buf[j % 2] and writes buf[(j + 1) % 2]; launches
   // after the device set 'done' are no-ops, so the current direction follows
   // from the number of iterations actually performed
   T* buf[2] = {pa, pb};
   KernelProfile& P = prof();
   ChunkEvents& E = chunk_events();
+  const int cap = P.on.load() ? 64 : 256;  // events of a timed chunk: 64 iterations at most
+  if (grow && check > cap) check = cap;
   const bool timed = P.on.load() && check <= 64;
   if (timed && !E.created) {
     for (int i = 0; i < ChunkEvents::kEvents; ++i) GFEA_CUDA_TRY(cudaEventCreate(&E.ev[i]));
@@ -1237,6 +1355,7 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, Scal* hos
     }
     before = host_sc->iters;
     if (host_sc->done) break;
+    if (grow) check = check * 2 > cap ? cap : check * 2;
   }
   const int performed = host_sc->iters - iters0;
   pa = buf[performed & 1];
@@ -1267,9 +1386,12 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   const int target = coarse_target(s, o);
   if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work)) > work_bytes)
     return GFEA_ERR_WORKSPACE;
-  const int G = pick_lanes(s, o->lanes);
+  const int vt = sizeof(T) == 4 ? GFEA_F32 : GFEA_F64;
   const int64_t N = s->n_nodes * s->dof_n;
-  const int check = o->check_every > 0 ? o->check_every : 32;
+  // host checks: every check_every iterations, or (check_every <= 0) after a
+  // first chunk sized from the previous reliable-update cycle, then doubling
+  const bool adaptive = o->check_every <= 0;
+  int check = adaptive ? 16 : o->check_every;
   const bool fp64 = sizeof(T) == 8;
   const double eps64 = 2.220446049250313e-16;
   // reliable update after the iterated residual fell by delta: inner_rtol
@@ -1284,6 +1406,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t) * 4, st));
   int e = launch_bjacobi<T>(s, w, st);
   if (e) return e;
+  int G = pick_lanes(s, o->lanes, vt);
   if (w.coarse) {
     const bool dbg = getenv("GFEA_DEBUG") != nullptr;
     cudaEvent_t ev[3];
@@ -1311,6 +1434,16 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   e = fetch(&hs, w, st);
   if (e) return e;
   if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
+  int32_t tuned = 0;
+  if (o->lanes == 0 && tune_cache().mode.load() == 2 && !tune_get(spmv_key(s, vt), &tuned) && hs.rr_true > 0) {
+    // first solve of this problem class: time the PCG's own SpMV kernel on the
+    // initial residual, then reset the scalar record it wrote
+    cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.pa, N);
+    GFEA_LAUNCH_CHECK();
+    e = tune_apply_impl<T>(s, w, st, &G);
+    if (e) return e;
+    GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
+  }
   const double bb = hs.bb;
   if (!(bb == bb) || !isfinite(hs.rr_true)) { res->status = GFEA_ERR_NAN; return GFEA_ERR_NAN; }
   if (bb == 0) {  // b_i - A_ic x_c = 0: the unknowns are zero
@@ -1342,7 +1475,11 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   int stall = 0;
   int iters0 = 0;
   for (int upd = 0;; ++upd) {
-    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, &hs, pa, pb, iters0, st);
+    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, adaptive, &hs, pa, pb, iters0, st);
+    if (adaptive) {
+      const int cycle = hs.iters - iters0;
+      check = cycle + 2 < 4 ? 4 : (cycle + 2 > 64 ? 64 : cycle + 2);
+    }
     if (e) return e;
     res->iterations = hs.iters;
     const int st_inner = hs.status;
@@ -1393,7 +1530,7 @@ using namespace gfea;
 extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, void* y, void* stream) {
   if (!s || s->version != GFEA_ABI_VERSION || !x || !y || s->n_nodes <= 0) return GFEA_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int G = pick_lanes(s, 0);
+  const int G = pick_lanes(s, 0, value_type);
   const int grid = grid_nodes(s->n_nodes, G);
   if (value_type == GFEA_F64) {
     if (!s->vals64) return GFEA_ERR_ARG;
@@ -1408,6 +1545,23 @@ extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, vo
   }
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
+}
+
+extern "C" int gfea_tune_spmv(const gfea_system* s, int value_type, const void* x, void* y, int32_t* lanes_host,
+                              float* ms_host, void* stream) {
+  if (!s || s->version != GFEA_ABI_VERSION || !x || !y || !lanes_host || !ms_host || s->n_nodes <= 0 ||
+      s->dof_n < 1 || s->dof_n > 3)
+    return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (value_type == GFEA_F64) {
+    if (!s->vals64) return GFEA_ERR_ARG;
+    return tune_spmv_impl<double>(s, (const double*)x, (double*)y, st, lanes_host, ms_host);
+  }
+  if (value_type == GFEA_F32) {
+    if (!s->vals32) return GFEA_ERR_ARG;
+    return tune_spmv_impl<float>(s, (const float*)x, (float*)y, st, lanes_host, ms_host);
+  }
+  return GFEA_ERR_ARG;
 }
 
 extern "C" int gfea_pcg_workspace_size(const gfea_system* s, const gfea_pcg_opts* o, size_t* bytes) {
@@ -1450,7 +1604,7 @@ extern "C" int gfea_reaction_energy(const gfea_system* s, const double* x, const
   double* partials = static_cast<double*>(work);
   Scal* sc = reinterpret_cast<Scal*>(partials + 4 * kMaxBlocks);
   GFEA_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(Scal), st));
-  const int G = pick_lanes(s, 0);
+  const int G = pick_lanes(s, 0, GFEA_F64);
   const SysT<double> S = sys_t<double>(s);
   const int grid = grid_nodes(s->n_nodes, G);
   GFEA_DG_SWITCH(s->dof_n, G, (reaction_kernel<DD, GG><<<grid, kThreads, 0, st>>>(S, x, Ax, partials, sc)));

@@ -148,7 +148,7 @@ class PcgInfo:
 
 
 def pcg(op: CsrOperator, b: torch.Tensor, x: torch.Tensor, known: torch.Tensor, rtol: float = 1e-12,
-        precision: str = "fp64", max_iters: int = 200000, check_every: int = 64, inner_rtol: float = 0.0,
+        precision: str = "fp64", max_iters: int = 200000, check_every: int = 0, inner_rtol: float = 0.0,
         lanes: int = 0, raise_on_fail: bool = True, coarse: int = 0, workspace: "Workspace | None" = None
         ) -> PcgInfo:
     """Solve the Dirichlet-reduced system in place: x holds the known values on

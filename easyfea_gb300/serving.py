@@ -244,7 +244,7 @@ class PhaseFieldSession:
         self.simu = None
         self.lock = threading.Lock()
 
-    def _ensure(self, cache: MeshCache, precision: str):
+    def _ensure(self, cache: MeshCache, precision: str, coarse: int = -1):
         if self.simu is None:
             from .simulations import PhaseField
 
@@ -255,12 +255,13 @@ class PhaseFieldSession:
             simu._dmesh = dm
             simu.precision = precision
             simu.rtol = 1e-10
+            simu.coarse = coarse
             self.simu = simu
             self.nodes = nodes
         return self.simu
 
-    def run_step(self, cache: MeshCache, precision: str):
-        simu = self._ensure(cache, precision)
+    def run_step(self, cache: MeshCache, precision: str, coarse: int = -1):
+        simu = self._ensure(cache, precision, coarse)
         self.step += 1
         k = self.step
         n = self.nodes
@@ -273,8 +274,9 @@ class PhaseFieldSession:
         return u, d, simu.Niter
 
 
-def run_elastic(req: ElasticRequest, cache: MeshCache, precision: str, rtol: float = 1e-10):
-    """Assemble and solve one elastic request on the current stream."""
+def run_elastic(req: ElasticRequest, cache: MeshCache, precision: str, rtol: float = 1e-10, coarse: int = -1):
+    """Assemble and solve one elastic request on the current stream
+    (``coarse``: aggregates of the two-level preconditioner, 0 = block-Jacobi)."""
     from .simulations import Elastic
 
     m, dm, nodes = cache.get(req.spec)
@@ -288,6 +290,7 @@ def run_elastic(req: ElasticRequest, cache: MeshCache, precision: str, rtol: flo
     simu._dmesh = dm
     simu.precision = precision
     simu.rtol = rtol
+    simu.coarse = coarse
     simu.add_dirichlet(nodes["left"], [0.0] * dim, ["x", "y"] if dim == 2 else ["x", "y", "z"])
     if dim == 2:
         simu.add_surfLoad(nodes["right"], [-800 / 13**2], ["y"])
@@ -306,9 +309,15 @@ class Server:
 
     def __init__(self, workers: int = 8, hbm_budget: Optional[int] = None, precision: str = "mixed",
                  rtol: float = 1e-10, max_bypass: int = 8, cache: Optional[MeshCache] = None,
-                 executor=None):
+                 executor=None, tune: bool = True):
         """``executor(request, result)``: runs one request (default: the GPU
-        path on the worker's stream); replaceable to test the scheduling."""
+        path on the worker's stream); replaceable to test the scheduling.
+        ``tune``: the first request of each problem class tunes the SpMV and
+        element-kernel schedules (process-wide autotuner mode 2)."""
+        if executor is None and tune:
+            from . import autotune
+
+            autotune.set_mode(autotune.TUNE)
         self.precision = precision
         self.rtol = rtol
         self.cache = cache or MeshCache()
@@ -521,9 +530,10 @@ def run_stream(server: Server, offsets, reqs, time_scale: float = 1.0) -> List[R
 
 
 def run_plain(reqs, cache: MeshCache, offsets=None, precision: str = "fp64", rtol: float = 1e-10,
-              time_scale: float = 1.0) -> List[Result]:
+              time_scale: float = 1.0, coarse: int = -1) -> List[Result]:
     """One request at a time on the default stream (the plain GPU path); with
-    ``offsets`` a request starts no earlier than its arrival."""
+    ``offsets`` a request starts no earlier than its arrival; ``coarse = 0``
+    solves with block-Jacobi PCG alone."""
     out = []
     t0 = time.perf_counter()
     for i, r in enumerate(reqs):
@@ -533,13 +543,13 @@ def run_plain(reqs, cache: MeshCache, offsets=None, precision: str = "fp64", rto
             time.sleep(arrival - now)
         res = Result(r.rid, r.kind, r.spec.dof, arrival=arrival, start=time.perf_counter())
         if r.kind == "elastic":
-            simu, u = run_elastic(r, cache, precision, rtol)
+            simu, u = run_elastic(r, cache, precision, rtol, coarse)
             info = simu.last_solve
             res.iterations, res.rel_residual, res.status = info.iterations, info.rel_residual, info.status
             res.u = u.cpu().numpy() if r.keep_solution else None
             torch.cuda.synchronize()
         else:
-            u, d, niter = r.session.run_step(cache, precision)
+            u, d, niter = r.session.run_step(cache, precision, coarse)
             res.iterations = niter
             res.u, res.d = (u, d) if r.keep_solution else (None, None)
         res.end = time.perf_counter()

@@ -199,7 +199,9 @@ typedef struct gfea_pcg_opts {
   int32_t version;          /* GFEA_ABI_VERSION */
   int32_t precision;        /* GFEA_F64: FP64 PCG; GFEA_F32: FP32 inner PCG + FP64 refinement */
   int32_t max_iters;        /* total PCG iteration cap */
-  int32_t check_every;      /* host convergence check period (iterations) */
+  int32_t check_every;      /* host convergence check period (iterations); <= 0: adaptive
+                               (first check after about as many iterations as the
+                               previous reliable-update cycle took, then doubling) */
   double rtol;              /* target ||P(b - A x)|| / ||P(b - A x_c)||; the solve
                                stops at max(rtol, rounding floor), see gfea_pcg_result */
   double inner_rtol;        /* FP32: reduction of the iterated residual between FP64
@@ -259,6 +261,15 @@ size_t gfea_batch_scratch_size(int n_instances);
  * inner_rtol (FP32 reliable-update trigger); rtol and max_iters are per system. */
 int gfea_batch_pcg(const gfea_batch_instance* instances_host, int n, void* scratch, size_t scratch_bytes,
                    const gfea_pcg_opts* opts_host, void* stream);
+/* gfea_batch_pcg in two parts, for CUDA-graph capture of the solve:
+ * gfea_batch_prepare validates the instances and uploads their descriptors
+ * (largest first) into scratch; gfea_batch_launch enqueues only device work
+ * (a counter reset and the persistent kernel), so it can be captured and
+ * replayed while the descriptors' buffers stay valid.  n and opts must be the
+ * ones given to the prepare call. */
+int gfea_batch_prepare(const gfea_batch_instance* instances_host, int n, void* scratch, size_t scratch_bytes,
+                       const gfea_pcg_opts* opts_host, void* stream);
+int gfea_batch_launch(void* scratch, int n, const gfea_pcg_opts* opts_host, void* stream);
 
 /* y = A x (unmasked), value_type selects vals64/x,y double or vals32/x,y float. */
 int gfea_spmv(const gfea_system* sys_host, int value_type, const void* x, void* y, void* stream);
@@ -303,14 +314,44 @@ int gfea_max_abs_diff(const double* a, const double* b, int64_t n, double* out_h
                       void* work, void* stream);
 
 /* Instrumentation: kernels launched by the library so far; optional
- * CUDA-event timing of the PCG direction/SpMV kernel (total ms and launches
- * since the last read; reading resets). */
+ * CUDA-event timing of the launches of PCG iterations (per kernel kind, from
+ * every host thread); gfea_profile_read returns the SpMV kernel's total ms and
+ * launches since the last read (reading resets; with GFEA_DEBUG set in the
+ * environment the per-kind table is printed to stderr). */
 long long gfea_launch_count(void);
 int gfea_profile_enable(int on);
 int gfea_profile_read(double* ms_host, long long* launches_host);
 
 /* FP64 -> FP32 copy of CSR values (mixed-precision operator) */
 int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Autotuner (no counterpart in the reference).  Two schedules are chosen by
+ * measurement and kept per problem class: the SpMV row-block schedule (lanes
+ * per node of the node-row products, keyed by dof_n, value type and the log2
+ * buckets of the row length and node count) and the element-kernel tile
+ * schedule (blocks of 128 threads per SM, keyed by element, value type,
+ * C mode and the log2 bucket of the element count).
+ * mode 0: fixed rules; 1 (default): use recorded decisions; 2: also tune a
+ * class on its first gfea_pcg_solve / gfea_assemble_elastic (not accumulating).
+ * ---------------------------------------------------------------------- */
+int gfea_tune_mode(int mode);
+int gfea_tune_clear(void);
+/* Times y = A x with 4, 8, 16, 32 lanes per node; records and returns the
+ * fastest (lanes_host) and its time (ms_host). */
+int gfea_tune_spmv(const gfea_system* sys_host, int value_type, const void* x, void* y,
+                   int32_t* lanes_host, float* ms_host, void* stream);
+/* gfea_assemble_elastic (accumulate = 0) timed with 4..64 blocks per SM;
+ * records the fastest and leaves the values assembled. */
+int gfea_tune_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                               const int32_t* node_ptr, const uint8_t* rank, const double* C,
+                               int c_per_elem, double factor, int value_type, void* values,
+                               int64_t n_values, int32_t* blocks_per_sm_host, float* ms_host,
+                               void* stream);
+/* Recorded decisions as (key, value) pairs: export writes up to max_entries
+ * and sets *n_host to the total; import adds or replaces entries. */
+int gfea_tune_export(int64_t* keys_host, int32_t* values_host, int max_entries, int* n_host);
+int gfea_tune_import(const int64_t* keys_host, const int32_t* values_host, int n);
 
 #ifdef __cplusplus
 }

@@ -86,3 +86,36 @@ def test_random_material_batch_matches_oracle():
         assert abs(K - K_ref).max() <= 1e-12 * abs(K_ref).max()
         u = sys_.x.cpu().numpy()
         assert np.abs(u - u_ref).max() <= 1e-8 * np.abs(u_ref).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_captured_batch_replays(precision):
+    """Re-assembly of every operator, reset of x and the persistent solve
+    captured as one CUDA graph: each replay gives the direct batch's result."""
+    import torch
+
+    from easyfea_gb300.batching import GraphBatch, solve_batch
+
+    systems = mixed_batch()
+    x0 = [s.x.clone() for s in systems]
+    solve_batch(systems, precision=precision)
+    direct = [s.x.clone() for s in systems]
+    for s, x in zip(systems, x0):
+        s.x.copy_(x)
+    vals = [s.op.vals64.clone() for s in systems]
+
+    def pre():  # stand-in for re-assembly: rewrite the values in place
+        for s, v in zip(systems, vals):
+            s.op.vals64.copy_(v)
+            if s.op.vals32 is not None:
+                s.op.vals32.copy_(v)
+
+    gb = GraphBatch(systems, precision=precision, pre=pre)
+    for _ in range(2):
+        for s in systems:
+            s.x.zero_()
+        gb.replay()
+        infos = gb.results()
+        assert all(i.status == 0 for i in infos)
+        for s, d in zip(systems, direct):
+            assert torch.equal(s.x, d)

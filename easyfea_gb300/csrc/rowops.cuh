@@ -161,13 +161,28 @@ __device__ __forceinline__ A node_rows_t(int64_t a, int lane, const SysT<T>& S, 
   for (int i = 0; i < D; ++i) acc[i] = 0;
   if (lane < LA) {
     const A self = DIFF ? xf(a * D + j) : (A)0;
-    for (int32_t k = lane / D, t = lane; k < nb; k += NPP, t += LA) {
-      const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
-      const A xv = DIFF ? xf(col) - self : xf(col);
+    // PF passes at a time with every load issued before the arithmetic: the
+    // index -> gather chains of the passes overlap (the product is bound by
+    // memory latency, not bandwidth, at one pass at a time)
+    constexpr int PF = 3;
+    for (int32_t k0 = lane / D, t0 = lane; k0 < nb; k0 += PF * NPP, t0 += PF * LA) {
+      int32_t c[PF];
+      T v[PF][D];
 #pragma unroll
-      for (int i = 0; i < D; ++i) {
-        const A v = (A)__ldg(base + (int64_t)i * W + t);
-        acc[i] += (ABS ? (v < 0 ? -v : v) : v) * xv;
+      for (int m = 0; m < PF; ++m) {
+        const bool in = k0 + m * NPP < nb;
+        c[m] = in ? __ldg(S.nbr + p0 + k0 + m * NPP) : -1;
+#pragma unroll
+        for (int i = 0; i < D; ++i) v[m][i] = in ? __ldcs(base + (int64_t)i * W + t0 + m * LA) : (T)0;
+      }
+#pragma unroll
+      for (int m = 0; m < PF; ++m) {
+        const A xv = c[m] < 0 ? (A)0 : (DIFF ? xf((int64_t)c[m] * D + j) - self : xf((int64_t)c[m] * D + j));
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          const A w = (A)v[m][i];
+          acc[i] += (ABS ? (w < 0 ? -w : w) : w) * xv;
+        }
       }
     }
   }

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 8 : 6) spmv_kernel(
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    const T v = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [&](int64_t c) { return x[c]; });
+    const T v = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [x](int64_t c) { return __ldg(x + c); });
     int r = -1;
 #pragma unroll
     for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) r = i;
@@ -327,8 +327,8 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
 // aggregate (a cell of a regular grid over the bounding box) to the rigid-body
 // modes of its nodes -- translations and rotations about the cell centre
 // (constants for a scalar field) -- with known DOFs masked out; A_c = P^T A P
-// is assembled from the FP64 CSR values and inverted densely (FP64
-// Gauss-Jordan) once per solve.  Per iteration: restriction fused into the
+// is assembled from the CSR values of the iteration's precision (sums in
+// FP64) and inverted densely (FP64 Gauss-Jordan) once per solve.  Per iteration: restriction fused into the
 // residual update, one dense coarse GEMV, prolongation fused into z.
 // ---------------------------------------------------------------------------
 
@@ -433,30 +433,33 @@ __global__ void aggregate_kernel(const double* __restrict__ coord, int64_t Nn, d
   }
 }
 
-// A_c += R_a^T K_ab R_b, summed per node over neighbours sharing an aggregate.
-template <int D>
-__global__ void coarse_assemble_kernel(SysT<double> S, CoarseDev C) {
+// A_c += R_a^T K_ab R_b, summed per node over neighbours sharing an aggregate
+// (T: the iteration's value type -- the FP32 operator of the mixed path gives
+// a coarse matrix accurate to ~1e-6, plenty for a preconditioner, on the FP32
+// pipe; sums go to A_c in FP64).
+template <int D, typename T>
+__global__ void coarse_assemble_kernel(SysT<T> S, CoarseDev C) {
   constexpr int nr = Modes<D>::nr;
   constexpr int kSlots = 8;
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < S.Nn; a += (int64_t)gridDim.x * blockDim.x) {
     const int ga = C.agg[a];
-    double Ra[D][nr];
-    node_modes<D>(C.off[a], S.known + a * D, Ra);
+    T Ra[D][nr];
+    node_modes<D, T>(C.off[a], S.known + a * D, Ra);
     int sid[kSlots];
-    double acc[kSlots][nr][nr];
+    T acc[kSlots][nr][nr];
     int ns = 0;
     const int32_t p0 = S.node_ptr[a], nb = S.node_ptr[a + 1] - p0;
     const int32_t W = D * nb;
     for (int k = 0; k < nb; ++k) {
       const int32_t b = S.nbr[p0 + k];
       const int gb = C.agg[b];
-      double Rb[D][nr];
-      node_modes<D>(C.off[b], S.known + (int64_t)b * D, Rb);
+      T Rb[D][nr];
+      node_modes<D, T>(C.off[b], S.known + (int64_t)b * D, Rb);
       // K_ab R_b (D x nr)
-      double KR[D][nr];
+      T KR[D][nr];
       for (int i = 0; i < D; ++i)
         for (int m = 0; m < nr; ++m) {
-          double v = 0;
+          T v = 0;
           for (int j = 0; j < D; ++j) v += S.vals[(int64_t)D * D * p0 + (int64_t)i * W + D * k + j] * Rb[j][m];
           KR[i][m] = v;
         }
@@ -468,7 +471,7 @@ __global__ void coarse_assemble_kernel(SysT<double> S, CoarseDev C) {
           for (int q = 0; q < ns; ++q)
             for (int m = 0; m < nr; ++m)
               for (int l = 0; l < nr; ++l)
-                atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], acc[q][m][l]);
+                atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], (double)acc[q][m][l]);
           ns = 0;
         }
         slot = ns++;
@@ -478,7 +481,7 @@ __global__ void coarse_assemble_kernel(SysT<double> S, CoarseDev C) {
       }
       for (int m = 0; m < nr; ++m)
         for (int l = 0; l < nr; ++l) {
-          double v = 0;
+          T v = 0;
           for (int i = 0; i < D; ++i) v += Ra[i][m] * KR[i][l];
           acc[slot][m][l] += v;
         }
@@ -486,13 +489,16 @@ __global__ void coarse_assemble_kernel(SysT<double> S, CoarseDev C) {
     for (int q = 0; q < ns; ++q)
       for (int m = 0; m < nr; ++m)
         for (int l = 0; l < nr; ++l)
-          atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], acc[q][m][l]);
+          atomicAdd(&C.Ac[(int64_t)(ga * nr + m) * C.nc + sid[q] * nr + l], (double)acc[q][m][l]);
   }
 }
 
 // Unit diagonal for empty or fully constrained coarse DOFs, a 1e-10 relative
 // shift elsewhere (rotation modes of degenerate aggregates), identity in inv.
-__global__ void coarse_regularize_kernel(CoarseDev C) {
+// (zero_tol, shift): (1e-14, 1e-10) for a coarse matrix built in FP64,
+// (1e-6, 1e-6) for one built from FP32 values, whose rounding can reach the
+// 1e-6 level in nearly degenerate modes.
+__global__ void coarse_regularize_kernel(CoarseDev C, double zero_tol, double shift) {
   __shared__ double smax[256];
   double m = 0;
   for (int i = threadIdx.x; i < C.nc; i += blockDim.x) m = fmax(m, fabs(C.Ac[(int64_t)i * C.nc + i]));
@@ -505,7 +511,7 @@ __global__ void coarse_regularize_kernel(CoarseDev C) {
   const double dmax = smax[0] > 0 ? smax[0] : 1.0;
   for (int i = threadIdx.x; i < C.nc; i += blockDim.x) {
     double& d = C.Ac[(int64_t)i * C.nc + i];
-    d = d > 1e-14 * dmax ? d + 1e-10 * dmax : dmax;
+    d = d > zero_tol * dmax ? d + shift * dmax : dmax;
   }
 }
 
@@ -750,7 +756,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) a
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    T av = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [&](int64_t c) { return p[c]; });
+    T av = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [p](int64_t c) { return __ldg(p + c); });
     int r = -1;
 #pragma unroll
     for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) r = i;
@@ -1161,6 +1167,7 @@ int coarse_aggregate(const gfea_system* s, int target, PcgWork& w, cudaStream_t 
 // extents get one cell), A_c = R^T A R from the FP64 values, inverted in place.
 // With 'reuse', an aggregation left in the workspace by an earlier call on the
 // same node count and target is kept.
+template <typename T>
 int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaStream_t st, cudaEvent_t mark) {
   CoarseDev& C = w.C;
   const int64_t Nn = s->n_nodes;
@@ -1183,10 +1190,13 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
     if (e) return e;
   }
   GFEA_CUDA_TRY(cudaMemsetAsync(C.Ac, 0, sizeof(double) * C.nc * C.nc, st));
-  const SysT<double> S = sys_t<double>(s);
-  GFEA_D_SWITCH(D, (coarse_assemble_kernel<DD><<<grid_elems(Nn), kThreads, 0, st>>>(S, C)));
+  const SysT<T> S = sys_t<T>(s);
+  GFEA_D_SWITCH(D, (coarse_assemble_kernel<DD, T><<<grid_elems(Nn), kThreads, 0, st>>>(S, C)));
   GFEA_LAUNCH_CHECK();
-  coarse_regularize_kernel<<<1, 256, 0, st>>>(C);
+  if (sizeof(T) == 4)
+    coarse_regularize_kernel<<<1, 256, 0, st>>>(C, 1e-6, 1e-6);
+  else
+    coarse_regularize_kernel<<<1, 256, 0, st>>>(C, 1e-14, 1e-10);
   GFEA_LAUNCH_CHECK();
   if (mark) GFEA_CUDA_TRY(cudaEventRecord(mark, st));
   const int gx = (int)ceil_div(C.nc, 128);
@@ -1414,7 +1424,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
       for (int i = 0; i < 3; ++i) GFEA_CUDA_TRY(cudaEventCreate(&ev[i]));
       GFEA_CUDA_TRY(cudaEventRecord(ev[0], st));
     }
-    e = coarse_setup(s, target, o->coarse_reuse != 0, w, st, dbg ? ev[1] : nullptr);
+    e = coarse_setup<T>(s, target, o->coarse_reuse != 0, w, st, dbg ? ev[1] : nullptr);
     if (e) return e;
     if (dbg) {
       GFEA_CUDA_TRY(cudaEventRecord(ev[2], st));

@@ -3,9 +3,10 @@
 // One group of G = next_pow2(nPe) lanes per element; lane p owns local node p:
 // it loads that node's coordinates, contributes dN_p (x) X_p to the Jacobian
 // (reduced across the group with shuffles), computes its physical gradient
-// invF.dN_p, and accumulates the block row K_pq (q = 0..nPe-1, gradients of
-// the other nodes arrive by shuffle).  The block row is scattered into the
-// CSR values with one atomic add per entry at slot
+// invF.dN_p, and accumulates the blocks K_pq of half of the element matrix
+// (q = p .. p + nPe/2 mod nPe; gradients of the other nodes arrive by
+// shuffle).  Each block is scattered into row p and, transposed, into row q,
+// with one atomic add per entry at slot
 //   dof_n^2 node_ptr[a] + i dof_n nnb(a) + dof_n rank[e,p,q] + j.
 // Element matrices never touch global memory.
 
@@ -127,13 +128,19 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
       for (int i = 0; i < NS * NS; ++i) Cl[i] = (R)__ldg(Cglob + ec * NS * NS + i);
       C = Cl;
     }
-    R acc[nPe][D][D];
+    // K_e is symmetric: lane p computes the blocks K_pq for q = p + d (mod nPe),
+    // d = 0 .. nPe/2 (the opposite pair of an even nPe only on lanes p < nPe/2),
+    // which covers every unordered pair once; each block is scattered into
+    // row p and, transposed, into row q
+    constexpr int NB = nPe / 2 + 1;
+    const bool extra = (nPe % 2 == 1) || lane < nPe / 2;  // lane owns d = nPe/2 (odd nPe: always)
+    R acc[NB][D][D];
 #pragma unroll
-    for (int q = 0; q < nPe; ++q)
+    for (int d = 0; d < NB; ++d)
 #pragma unroll
       for (int i = 0; i < D; ++i)
 #pragma unroll
-        for (int j = 0; j < D; ++j) acc[q][i][j] = 0;
+        for (int j = 0; j < D; ++j) acc[d][i][j] = 0;
 
     for (int g = 0; g < RefTables<ELEM, false>::nPg; ++g) {
       R grad[D];
@@ -141,27 +148,44 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
       R BtC[D][NS];
       btc<D, R>(grad, C, wJ, BtC);
 #pragma unroll
-      for (int q = 0; q < nPe; ++q) {
+      for (int d = 0; d < NB; ++d) {
+        const int q = node_lane ? (lane + d) % nPe : 0;
         R h[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) h[k] = group_bcast<G, R>(grad[k], q);
-        btcb<D, R>(BtC, h, acc[q]);
+        if (d < NB - 1 || extra) btcb<D, R>(BtC, h, acc[d]);
       }
     }
     if (act) {
-      const int32_t p0 = node_ptr[a];
-      const int32_t nb = node_ptr[a + 1] - p0;
-      const uint8_t* rk = rank + (ec * nPe + lane) * nPe;
       // mode 2: per-element factor of the reference C (e.g. a per-element Young's modulus)
       const double f = CMODE == 2 ? factor * __ldg(Cglob + NS * NS + ec) : factor;
+      const int32_t* ce = connect + ec * nPe;
+      const uint8_t* rke = rank + ec * nPe * nPe;
+      const int32_t pa0 = node_ptr[a];
+      const int32_t nba = node_ptr[a + 1] - pa0;
 #pragma unroll
-      for (int i = 0; i < D; ++i) {
-        T* row = vals + (int64_t)D * D * p0 + (int64_t)i * D * nb;
+      for (int d = 0; d < NB; ++d) {
+        if (d == NB - 1 && !extra) continue;
+        const int q = (lane + d) % nPe;
+        // row p (node a), block q
+        const int r_pq = rke[lane * nPe + q];
 #pragma unroll
-        for (int q = 0; q < nPe; ++q) {
-          const int r = rk[q];
+        for (int i = 0; i < D; ++i) {
+          T* row = vals + (int64_t)D * D * pa0 + (int64_t)i * D * nba + D * r_pq;
 #pragma unroll
-          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + D * r + j, (T)(f * (double)acc[q][i][j]));
+          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + j, (T)(f * (double)acc[d][i][j]));
+        }
+        if (d == 0) continue;
+        // row q (node b), block p: the transpose
+        const int32_t b = ce[q];
+        const int32_t pb0 = node_ptr[b];
+        const int32_t nbb = node_ptr[b + 1] - pb0;
+        const int r_qp = rke[q * nPe + lane];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T* row = vals + (int64_t)D * D * pb0 + (int64_t)i * D * nbb + D * r_qp;
+#pragma unroll
+          for (int j = 0; j < D; ++j) atomic_add_t<T>(row + j, (T)(f * (double)acc[d][j][i]));
         }
       }
     }

@@ -103,8 +103,10 @@ int gfea_csr_pattern(const int32_t* node_ptr, const int32_t* nbr, int64_t n_node
  * 1 per element (Ne x n x n, Models/_utils.py:69-108), 2 a reference n x n
  * matrix followed by Ne per-element factors (C_e = f_e C_ref, e.g. a
  * per-element Young's modulus with a constant Poisson ratio).
- * values (value_type GFEA_F64/F32, n_values = dof_n^2 * n_pairs entries) are
- * zeroed first unless accumulate != 0. */
+ * C must be symmetric (as every elastic law's Kelvin-Mandel matrix is): each
+ * element computes K_pq for one of each pair of nodes and scatters K_qp =
+ * K_pq^T.  values (value_type GFEA_F64/F32, n_values = dof_n^2 * n_pairs
+ * entries) are zeroed first unless accumulate != 0. */
 int gfea_assemble_elastic(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
                           const int32_t* node_ptr, const uint8_t* rank, const double* C,
                           int c_per_elem, double factor, int value_type, void* values,

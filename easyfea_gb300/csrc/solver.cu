@@ -156,8 +156,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 8 : 6) spmv_kernel(
 // ||P |A| |x|||^2 (scale of the rounding floor of r).
 // The three products share one pass over the values; KN = false skips the
 // known-column product (b - A x_c does not change between reliable updates).
-template <int D, int G, typename T, bool KN>
-__global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double* __restrict__ b,
+// AB32: the |A||x| product (only a floor estimate, 1e-6 accuracy is plenty)
+// from the FP32 values and an FP32 copy of x, on the FP32 pipe; the residual
+// itself stays FP64.
+template <int D, int G, typename T, bool KN, bool AB32>
+__global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const float* __restrict__ v32,
+                                                         const float* __restrict__ x32,
+                                                         const double* __restrict__ b,
                                                          const double* __restrict__ x, double* __restrict__ r,
                                                          double* partials, Scal* sc) {
   constexpr int LA = G - G % D;
@@ -172,30 +177,38 @@ __global__ void __launch_bounds__(kThreads) resid_kernel(SysT<T> S, const double
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
     double all[D], kn[D], ab[D];
+    float ab32[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i) all[i] = kn[i] = ab[i] = 0;
+    for (int i = 0; i < D; ++i) {
+      all[i] = kn[i] = ab[i] = 0;
+      ab32[i] = 0.f;
+    }
     if (lane < LA) {
       const int32_t p0 = S.node_ptr[ac], nb = S.node_ptr[ac + 1] - p0;
       const int32_t W = D * nb;
       const T* base = S.vals + (int64_t)D * D * p0;
+      const float* base32 = AB32 ? v32 + (int64_t)D * D * p0 : nullptr;
       for (int32_t k = lane / D, t = lane; k < nb; k += NPP, t += LA) {
         const int64_t col = (int64_t)__ldg(S.nbr + p0 + k) * D + j;
-        const double xv = x[col];
+        const double xv = __ldg(x + col);
         const double xk = (KN && S.known[col]) ? xv : 0.0;
-        const double xa = fabs(xv);
+        const float xa32 = AB32 ? fabsf(__ldg(x32 + col)) : 0.f;
 #pragma unroll
         for (int i = 0; i < D; ++i) {
           const double w = (double)__ldg(base + (int64_t)i * W + t);
           all[i] += w * xv;
           if (KN) kn[i] += w * xk;
-          ab[i] += fabs(w) * xa;
+          if (AB32)
+            ab32[i] += fabsf(__ldg(base32 + (int64_t)i * W + t)) * xa32;
+          else
+            ab[i] += fabs(w) * fabs(xv);
         }
       }
     }
     // row i's three sums land in lane row_lane(i)
     const double s_all = group_sum_rows<D, G, double>(all, lane);
     const double s_kn = KN ? group_sum_rows<D, G, double>(kn, lane) : 0.0;
-    const double s_ab = group_sum_rows<D, G, double>(ab, lane);
+    const double s_ab = AB32 ? (double)group_sum_rows<D, G, float>(ab32, lane) : group_sum_rows<D, G, double>(ab, lane);
     int ri_row = -1;
 #pragma unroll
     for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) ri_row = i;
@@ -913,6 +926,7 @@ struct PcgWork {
   Scal* sc;
   int32_t* flag;
   bool coarse = false;
+  bool is_f32 = false;  // T-typed buffers hold floats
   CoarseDev C;
 };
 
@@ -943,6 +957,7 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
   };
   PcgWork t;
   if (!w) w = &t;
+  w->is_f32 = sizeof(T) == 4;
   w->r = take(sizeof(T) * N);
   w->z = take(sizeof(T) * N);
   w->pa = take(sizeof(T) * N);
@@ -1012,11 +1027,23 @@ int launch_resid(const gfea_system* s, int G, const double* b, const double* x, 
                  cudaStream_t st) {
   const SysT<double> S = sys_t<double>(s);
   const int grid = grid_nodes(s->n_nodes, G);
-  if (kn) {
-    GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double, true><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
-  } else {
-    GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double, false><<<grid, kThreads, 0, st>>>(S, b, x, w.r64, w.partials, w.sc)));
+  const int64_t N = s->n_nodes * s->dof_n;
+  const float* v32 = s->vals32;
+  float* x32 = nullptr;
+  if (v32 && w.is_f32) {  // FP32 copy of x for the floor product (the A.p buffer is free here)
+    x32 = static_cast<float*>(w.Ap);
+    cast_kernel<float><<<grid_elems(N), kThreads, 0, st>>>(x, x32, N);
+    GFEA_LAUNCH_CHECK();
   }
+#define GFEA_RESID(KN_, AB_)                                                                                   \
+  GFEA_DG_SWITCH(s->dof_n, G, (resid_kernel<DD, GG, double, KN_, AB_><<<grid, kThreads, 0, st>>>(               \
+                                  S, v32, x32, b, x, w.r64, w.partials, w.sc)))
+  if (kn) {
+    if (x32) { GFEA_RESID(true, true); } else { GFEA_RESID(true, false); }
+  } else {
+    if (x32) { GFEA_RESID(false, true); } else { GFEA_RESID(false, false); }
+  }
+#undef GFEA_RESID
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }

@@ -928,6 +928,17 @@ struct PcgWork {
   bool coarse = false;
   bool is_f32 = false;  // T-typed buffers hold floats
   CoarseDev C;
+  // CUDA graphs of kGraphIters PCG iterations, one per direction-buffer order
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  long long gkernels = 0;
+  bool graphs_ok = true;
+  PcgWork() = default;
+  PcgWork(const PcgWork&) = delete;
+  PcgWork& operator=(const PcgWork&) = delete;
+  ~PcgWork() {
+    for (int i = 0; i < 2; ++i)
+      if (gexec[i]) cudaGraphExecDestroy(gexec[i]);
+  }
 };
 
 int coarse_nr(int D) { return D == 1 ? 1 : (D == 2 ? 3 : 6); }
@@ -1334,6 +1345,50 @@ int tune_apply_impl(const gfea_system* s, PcgWork& w, cudaStream_t st, int* G_ou
   return GFEA_OK;
 }
 
+// A chunk of PCG iterations is launched as CUDA graphs of kGraphIters
+// iterations (captured once per solve on a private stream of the calling
+// thread, so that the caller's stream may be the legacy default stream):
+// one graph launch replaces 4 x (3 or 5) kernel launches, which dominate the
+// iteration time of small systems.
+constexpr int kGraphIters = 4;
+
+cudaStream_t capture_stream() {
+  thread_local cudaStream_t cs = nullptr;
+  if (!cs && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) cs = nullptr;
+  return cs;
+}
+
+template <typename T>
+int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* p1, cudaGraphExec_t* out) {
+  cudaStream_t cs = capture_stream();
+  if (!cs) return GFEA_ERR_CUDA;
+  const long long k0 = launch_counter().load();
+  GFEA_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  T* buf[2] = {p0, p1};
+  int e = GFEA_OK;
+  for (int j = 0; j < kGraphIters && !e; ++j) {
+    e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], cs);
+    if (!e) e = launch_precond<T>(s, w, x, buf[(j + 1) & 1], 0, cs);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(cs, &g);
+  w.gkernels = launch_counter().load() - k0;
+  launch_counter().fetch_sub(w.gkernels);  // counted when the graph runs
+  if (e || ce != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return e ? e : GFEA_ERR_CUDA;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    *out = nullptr;
+    cudaGetLastError();
+    return GFEA_ERR_CUDA;
+  }
+  return GFEA_OK;
+}
+
 // Runs PCG iterations until the device flags done, checking after chunks of
 // 'check' iterations (doubled after each chunk that did not finish when
 // 'grow' is set, so that few launches after convergence are wasted).  pa
@@ -1355,16 +1410,29 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow
     E.created = true;
   }
   int before = iters0;
+  // graphs are used outside timed chunks (their events need direct launches)
+  const int order = pa == (T*)w.pa ? 0 : 1;
+  if (!timed && w.graphs_ok && !w.gexec[order] &&
+      capture_iterations<T>(s, G, w, x, buf[0], buf[1], &w.gexec[order]) != GFEA_OK)
+    w.graphs_ok = false;  // direct launches from here on
+  const bool graphs = !timed && w.graphs_ok && w.gexec[order];
   for (int j = 0;;) {
     E.active = timed;
     E.cur = 0;
-    for (int it = 0; it < check; ++it, ++j) {
-      int e = prof_mark(st, -1);
-      if (e) return e;
-      e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
-      if (e) return e;
-      e = launch_precond<T>(s, w, x, buf[(j + 1) & 1], 0, st);
-      if (e) return e;
+    if (graphs) {  // an even number of iterations per graph keeps the buffer order
+      for (int it = 0; it < check; it += kGraphIters, j += kGraphIters) {
+        GFEA_CUDA_TRY(cudaGraphLaunch(w.gexec[order], st));
+        launch_counter().fetch_add(w.gkernels);
+      }
+    } else {
+      for (int it = 0; it < check; ++it, ++j) {
+        int e = prof_mark(st, -1);
+        if (e) return e;
+        e = launch_dir<T>(s, G, w, buf[j & 1], buf[(j + 1) & 1], st);
+        if (e) return e;
+        e = launch_precond<T>(s, w, x, buf[(j + 1) & 1], 0, st);
+        if (e) return e;
+      }
     }
     E.active = false;
     GFEA_CUDA_TRY(cudaMemcpyAsync(host_sc, w.sc, sizeof(Scal), cudaMemcpyDeviceToHost, st));

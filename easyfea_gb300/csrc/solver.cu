@@ -1352,6 +1352,20 @@ int tune_apply_impl(const gfea_system* s, PcgWork& w, cudaStream_t st, int* G_ou
 // iteration time of small systems.
 constexpr int kGraphIters = 4;
 
+// Solves in flight in this process (several host threads may solve at once).
+// Concurrent solves hide each other's launch latency, while graph
+// instantiation serialises them, so a solve that starts its iterations while
+// others run launches its kernels directly.
+std::atomic<int>& active_solves() {
+  static std::atomic<int> n{0};
+  return n;
+}
+
+struct ActiveSolve {
+  ActiveSolve() { active_solves().fetch_add(1); }
+  ~ActiveSolve() { active_solves().fetch_sub(1); }
+};
+
 cudaStream_t capture_stream() {
   thread_local cudaStream_t cs = nullptr;
   if (!cs && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) cs = nullptr;
@@ -1362,7 +1376,6 @@ template <typename T>
 int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* p1, cudaGraphExec_t* out) {
   cudaStream_t cs = capture_stream();
   if (!cs) return GFEA_ERR_CUDA;
-  const long long k0 = launch_counter().load();
   GFEA_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   T* buf[2] = {p0, p1};
   int e = GFEA_OK;
@@ -1372,8 +1385,11 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
   }
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(cs, &g);
-  w.gkernels = launch_counter().load() - k0;
-  launch_counter().fetch_sub(w.gkernels);  // counted when the graph runs
+  // kernels per iteration: direction + SpMV, then update (block-Jacobi) or
+  // update/restrict + coarse GEMV + finish (two-level); counted when the
+  // graph runs, not when it is captured
+  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? 3 : 1));
+  launch_counter().fetch_sub(w.gkernels);
   if (e || ce != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
@@ -1412,6 +1428,11 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow
   int before = iters0;
   // graphs are used outside timed chunks (their events need direct launches)
   const int order = pa == (T*)w.pa ? 0 : 1;
+  static const bool graphs_env = [] {
+    const char* v = getenv("GFEA_PCG_GRAPHS");  // "0": direct launches only
+    return !(v && v[0] == '0');
+  }();
+  if (!graphs_env || (!w.gexec[0] && !w.gexec[1] && active_solves().load() > 1)) w.graphs_ok = false;
   if (!timed && w.graphs_ok && !w.gexec[order] &&
       capture_iterations<T>(s, G, w, x, buf[0], buf[1], &w.gexec[order]) != GFEA_OK)
     w.graphs_ok = false;  // direct launches from here on
@@ -1487,6 +1508,7 @@ template <typename T>
 int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
                  size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
   const auto t_start = std::chrono::steady_clock::now();
+  const ActiveSolve active;
   PcgWork w;
   const int target = coarse_target(s, o);
   if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work)) > work_bytes)

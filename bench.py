@@ -389,18 +389,12 @@ def main():
     import numpy as np
     import torch
 
+    from easyfea_gb300 import replicas
+
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+    replicas.init("nccl")
+    barrier = replicas.barrier
 
     from easyfea_gb300 import _lib, serving
 
@@ -458,15 +452,11 @@ def main():
             torch.cuda.synchronize()
             step_s.append(time.perf_counter() - t0)
             results += res
+    torch.cuda.synchronize()
+    barrier()
     launches = lib.gfea_launch_count() - launches0
-    total_s = sum(step_s)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * args.steps * args.requests / total_s
+    # whole job: every rank served the stream args.steps times; the slowest rank's time
+    value, total_s = replicas.job_throughput(args.steps * args.requests, sum(step_s))
     lat = np.array([r.latency for r in results]) * 1e3
 
     # e2e: solutions read back to the host
@@ -582,10 +572,7 @@ def main():
         }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    replicas.finish()
 
 
 if __name__ == "__main__":

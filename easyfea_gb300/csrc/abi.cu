@@ -14,6 +14,7 @@ extern "C" const char* gfea_status_string(int status) {
     case GFEA_ERR_BREAKDOWN: return "PCG breakdown (p.Ap <= 0: operator not SPD on the unknowns)";
     case GFEA_ERR_NAN: return "non-finite value";
     case GFEA_ERR_WORKSPACE: return "workspace too small";
+    case GFEA_ERR_TIMEOUT: return "bounded device wait timed out (or a staged tile out of order)";
     default: return "unknown status";
   }
 }

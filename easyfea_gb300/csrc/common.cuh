@@ -4,15 +4,23 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 
 #include <atomic>
 
 #include "../../include/gfea.h"
 
-#define GFEA_CUDA_TRY(expr)                        \
-  do {                                             \
-    cudaError_t _e = (expr);                       \
-    if (_e != cudaSuccess) return GFEA_ERR_CUDA;   \
+// A failed CUDA runtime call returns GFEA_ERR_CUDA; with GFEA_DEBUG set the
+// call and the runtime's error string go to stderr.
+#define GFEA_CUDA_TRY(expr)                                                                      \
+  do {                                                                                           \
+    cudaError_t _e = (expr);                                                                     \
+    if (_e != cudaSuccess) {                                                                     \
+      if (getenv("GFEA_DEBUG"))                                                                  \
+        fprintf(stderr, "gfea: %s:%d %s: %s\n", __FILE__, __LINE__, #expr, cudaGetErrorString(_e)); \
+      return GFEA_ERR_CUDA;                                                                      \
+    }                                                                                            \
   } while (0)
 
 namespace gfea {

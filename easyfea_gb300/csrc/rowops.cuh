@@ -189,4 +189,38 @@ __device__ __forceinline__ A node_rows_t(int64_t a, int lane, const SysT<T>& S, 
   return group_sum_rows<D, G, A>(acc, lane);
 }
 
+// node_rows_t over a node whose rows were staged in shared memory: 'vrow'
+// holds its D rows of W = D nb values, 'nrow' its nb neighbour indices.  The
+// gathers of x for PF passes are issued before their products.
+template <int D, int G, typename T, typename A, bool DIFF, typename XF>
+__device__ __forceinline__ A node_rows_s(const T* vrow, const int32_t* nrow, int nb, int64_t a, int lane, XF xf) {
+  constexpr int LA = G - G % D;
+  constexpr int NPP = LA / D;
+  constexpr int PF = 3;
+  const int W = D * nb;
+  const int j = lane % D;
+  A acc[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) acc[i] = 0;
+  if (lane < LA) {
+    const A self = DIFF ? xf(a * D + j) : (A)0;
+    for (int k0 = lane / D, t0 = lane; k0 < nb; k0 += PF * NPP, t0 += PF * LA) {
+      A xv[PF];
+#pragma unroll
+      for (int m = 0; m < PF; ++m) {
+        const int k = k0 + m * NPP;
+        xv[m] = k < nb ? (DIFF ? xf((int64_t)nrow[k] * D + j) - self : xf((int64_t)nrow[k] * D + j)) : (A)0;
+      }
+#pragma unroll
+      for (int m = 0; m < PF; ++m) {
+        if (k0 + m * NPP < nb) {
+#pragma unroll
+          for (int i = 0; i < D; ++i) acc[i] += (A)vrow[i * W + t0 + m * LA] * xv[m];
+        }
+      }
+    }
+  }
+  return group_sum_rows<D, G, A>(acc, lane);
+}
+
 }  // namespace gfea

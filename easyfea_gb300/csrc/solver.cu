@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "rowops.cuh"
+#include "stage.cuh"
 #include "tune.cuh"
 
 namespace gfea {
@@ -794,6 +795,278 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) a
   }
 }
 
+// apply_kernel with the operator streamed through shared memory.  Nodes are
+// cut into tiles of nt = 32 / D consecutive nodes (one node component per
+// lane of a warp).  Once per solve, pack_tiles_kernel lays each tile out as
+// one contiguous block of the workspace,
+//   [node offsets (nt + 1, relative) | neighbour indices | CSR values],
+// so that a producer warp moves a whole tile by ONE bulk asynchronous copy
+// (cp.async.bulk, completing on the stage's 'full' mbarrier) into a ring of
+// shared-memory stages: the copy engine has a fixed cost per copy that made
+// separate copies of the three short ranges the bound.  Each block takes a
+// contiguous range of tiles (consecutive tiles share neighbourhoods, so their
+// gathers of p hit the SM's L1); tile i of a block goes to consumer warp
+// i % 8, which owns stage i % stages alone (stages is a multiple of 8).  A
+// lane owns one component j of one node: it gathers p at component j of each
+// neighbour once and accumulates its share of all D rows; the D lanes of the
+// node then exchange partial rows (D - 1 shuffles).  A tile with more
+// neighbour slots than a stage holds is not packed and is read from global
+// memory by the same lanes.  Every wait is bounded (2 s): on expiry the
+// kernel sets GFEA_ERR_TIMEOUT, waits (bounded) for its copies in flight and
+// returns.
+struct StageGeom {
+  int64_t ntiles;
+  int32_t nt;          // nodes per tile
+  int32_t cap_slots;   // neighbour slots a packed tile holds
+  int32_t stages;      // ring depth (a multiple of the consumer warps, <= kMaxStages)
+  uint32_t hdr_bytes;  // node offsets region
+  uint32_t tile_bytes; // packed tile stride = shared-memory stage size
+};
+
+constexpr int kMaxStages = 32;
+constexpr int kStagedThreads = kThreads + 32;  // consumer warps + the producer warp
+constexpr int kConsumerWarps = kThreads / 32;
+
+__host__ __device__ inline uint32_t align16u(uint64_t b) { return (uint32_t)((b + 15) & ~uint64_t(15)); }
+
+// Bytes of packed tile k's used part (node offsets, indices, values).
+template <int D, typename T>
+__device__ __forceinline__ uint32_t packed_used(const StageGeom& g, int64_t slots) {
+  return g.hdr_bytes + align16u(4 * slots) + align16u((uint64_t)slots * D * D * sizeof(T));
+}
+
+// Packs tile k (one warp per tile): node offsets relative to the tile's
+// first slot, its neighbour indices and its CSR values (row (a, i) of the
+// tile's node a keeps the CSR order: D^2 q0 + i D nb + D k + j from the tile
+// start, q0 = a's relative offset).  Tiles over capacity are skipped.
+template <int D, typename T>
+__global__ void __launch_bounds__(kThreads) pack_tiles_kernel(SysT<T> S, StageGeom g, unsigned char* __restrict__ packed) {
+  const int wl = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = w0; k < g.ntiles; k += nw) {
+    const int64_t a0 = k * g.nt, a1 = min(a0 + g.nt, S.Nn);
+    const int64_t s0 = S.node_ptr[a0], slots = S.node_ptr[a1] - s0;
+    if (slots > g.cap_slots) continue;
+    unsigned char* base = packed + k * (int64_t)g.tile_bytes;
+    int32_t* __restrict__ P = reinterpret_cast<int32_t*>(base);
+    int32_t* __restrict__ Nb = reinterpret_cast<int32_t*>(base + g.hdr_bytes);
+    T* __restrict__ V = reinterpret_cast<T*>(base + g.hdr_bytes + align16u(4 * slots));
+    for (int t = wl; t <= (int)(a1 - a0); t += 32) P[t] = (int32_t)(__ldg(S.node_ptr + a0 + t) - s0);
+    const int32_t* __restrict__ nsrc = S.nbr + s0;
+    for (int q = wl; q < (int)slots; q += 32) Nb[q] = __ldg(nsrc + q);
+    // four loads in flight per lane
+    const T* __restrict__ src = S.vals + (int64_t)D * D * s0;
+    const int n = (int)slots * D * D;
+    for (int e = wl; e < n; e += 128) {
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = e + 32 * u < n ? __ldcs(src + e + 32 * u) : (T)0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (e + 32 * u < n) V[e + 32 * u] = v[u];
+    }
+  }
+}
+
+// Row j of the node from the partial rows of its D component lanes: in step
+// s the lane of component j' offers its partial of row (j' - s) mod D, and
+// the lane of component j takes the offer of lane j + s (mod D).
+template <int D, typename T>
+__device__ __forceinline__ T node_rows_exchange(const T (&acc)[D], int j, int lane) {
+  T row = acc[0];
+#pragma unroll
+  for (int i = 1; i < D; ++i) row = (j == i) ? acc[i] : row;
+#pragma unroll
+  for (int st = 1; st < D; ++st) {
+    const int oi = j >= st ? j - st : j - st + D;  // (j - st) mod D
+    const int sj = j + st < D ? j + st : j + st - D;  // (j + st) mod D
+    T offer = acc[0];
+#pragma unroll
+    for (int i = 1; i < D; ++i) offer = (oi == i) ? acc[i] : offer;
+    row += __shfl_sync(0xffffffffu, offer, lane - j + sj);
+  }
+  return row;
+}
+
+// Partial rows (all D rows, component j) of node a over its nb neighbours:
+// the lane gathers p at component j of every neighbour once and accumulates
+// vrow(i W + D k + j) x (W = D nb) into row i; nrow(k) are the neighbour
+// indices.
+// The gathers of a chunk of kGatherChunk neighbours are all issued before
+// their products, so that a chunk costs one trip to L2 for the gathers that
+// miss L1 (neighbours in other planes of the mesh live on other SMs).
+constexpr int kGatherChunk = 27;
+
+template <int D, typename T, bool DIFF, typename VR, typename NR>
+__device__ __forceinline__ void node_component_partials(VR vrow, NR nrow, int nb, int64_t a, int j,
+                                                        const T* __restrict__ p, T (&acc)[D]) {
+  const int W = D * nb;
+  const T self = DIFF ? __ldg(p + a * D + j) : (T)0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) acc[i] = 0;
+  for (int k0 = 0; k0 < nb; k0 += kGatherChunk) {
+    T x[kGatherChunk];
+#pragma unroll
+    for (int m = 0; m < kGatherChunk; ++m) {
+      const int k = k0 + m;
+      x[m] = k < nb ? __ldg(p + ((uint32_t)nrow(k) * D + j)) : (T)0;
+    }
+#pragma unroll
+    for (int m = 0; m < kGatherChunk; ++m) {
+      const int k = k0 + m;
+      if (k < nb) {
+        const T xv = DIFF ? x[m] - self : x[m];
+#pragma unroll
+        for (int i = 0; i < D; ++i) acc[i] += vrow(i * W + D * k + j) * xv;
+      }
+    }
+  }
+}
+
+template <int D, typename T, bool DIFF>
+__global__ void __launch_bounds__(kStagedThreads, 2) apply_staged_kernel(SysT<T> S, StageGeom g,
+                                                                         const unsigned char* __restrict__ packed,
+                                                                         const T* __restrict__ p, T* __restrict__ Ap,
+                                                                         double* partials, Scal* sc) {
+  if (sc->done) return;
+  extern __shared__ __align__(128) unsigned char stage_mem[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages];
+  __shared__ int64_t tile_of[kMaxStages];  // tile held by each stage (-1 - k: read directly)
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, wl = threadIdx.x & 31;
+  if (g.stages % kConsumerWarps || g.stages > kMaxStages) {  // the stage -> warp ownership needs this
+    if (threadIdx.x == 0) {
+      sc->status = GFEA_ERR_ARG;
+      sc->done = 1;
+    }
+    return;
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < g.stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+      tile_of[s] = INT64_MIN;
+    }
+    abort_flag = 0;
+  }
+  __syncthreads();
+  const int64_t Nn = S.Nn;
+  // each block takes a contiguous range of tiles, so that the gathers of p
+  // by consecutive tiles (overlapping neighbourhoods) hit the SM's L1
+  const int64_t per_block = ceil_div(g.ntiles, gridDim.x);
+  const int64_t t_begin = blockIdx.x * per_block;
+  const int64_t t_end = min(t_begin + per_block, g.ntiles);
+  DotAcc<T> pap;
+  if (warp == kConsumerWarps) {
+    // producer (lane 0); the tiles' slot counts come from node_ptr at the
+    // tile boundaries, loaded 32 tiles at a time, one tile per lane
+    const uint64_t pol = l2_evict_first();
+    int i = 0;
+    int64_t sl = 0;
+    for (int64_t k = t_begin; k < t_end; ++k, ++i) {
+      const int m = i & 31;
+      if (m == 0) {
+        const int64_t kl = k + wl;
+        if (kl < t_end) sl = __ldg(S.node_ptr + min((kl + 1) * g.nt, Nn)) - __ldg(S.node_ptr + kl * g.nt);
+      }
+      const int64_t slots = __shfl_sync(0xffffffffu, sl, m);
+      const int s = i % g.stages;
+      // warp-uniform outcome of the bounded wait (the lanes leave together)
+      if (i >= g.stages &&
+          !__all_sync(0xffffffffu, mbar_wait(&empty[s], ((i / g.stages) - 1) & 1, &abort_flag))) {
+        sc->status = GFEA_ERR_TIMEOUT;  // the last block ends the solve
+        *(volatile int*)&abort_flag = 1;
+        break;
+      }
+      if (wl == 0) {
+        const bool dir = slots > g.cap_slots;
+        tile_of[s] = dir ? -1 - k : k;
+        if (dir) {
+          mbar_arrive(&full[s]);
+        } else {
+          const uint32_t bytes = packed_used<D, T>(g, slots);
+          mbar_expect_tx(&full[s], bytes);
+          bulk_g2s(stage_mem + (size_t)s * g.tile_bytes, packed + k * (int64_t)g.tile_bytes, bytes, &full[s], pol);
+          mbar_arrive(&full[s]);
+        }
+      }
+      __syncwarp();
+    }
+    // the copies of the last tiles issued land before the block may exit
+    if (wl == 0)
+      for (int j = i > g.stages ? i - g.stages : 0; j < i; ++j) mbar_wait(&full[j % g.stages], (j / g.stages) & 1);
+    __syncwarp();
+  } else {
+    // consumer warp 'warp' takes tiles warp, warp + 8, ... of the block
+    int i = warp;
+    for (int64_t k = t_begin + warp; k < t_end; k += kConsumerWarps, i += kConsumerWarps) {
+      const int s = i % g.stages;
+      if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (i / g.stages) & 1, &abort_flag))) {
+        sc->status = GFEA_ERR_TIMEOUT;
+        *(volatile int*)&abort_flag = 1;
+        break;
+      }
+      const int64_t held = tile_of[s];
+      if (held != k && held != -1 - k) {  // a stage filled for another tile: never read it
+        sc->status = GFEA_ERR_TIMEOUT;
+        *(volatile int*)&abort_flag = 1;
+        break;
+      }
+      const int64_t a0 = k * g.nt, a1 = min(a0 + g.nt, Nn);
+      // lane D n + j: node a0 + n, component j; lanes past the tile only
+      // take part in the exchange
+      const bool live = wl < D * g.nt && a0 + wl / D < a1;
+      const int64_t a = live ? a0 + wl / D : a1 - 1;
+      const int j = live ? wl % D : 0;
+      T acc[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) acc[q] = 0;
+      if (!live) {
+      } else if (held < 0) {
+        const int32_t q0 = __ldg(S.node_ptr + a), q1 = __ldg(S.node_ptr + a + 1);
+        const T* vr = S.vals + (int64_t)D * D * q0;
+        const int32_t* nr = S.nbr + q0;
+        node_component_partials<D, T, DIFF>([vr](int t) { return __ldg(vr + t); },
+                                            [nr](int t) { return __ldg(nr + t); }, q1 - q0, a, j, p, acc);
+      } else {
+        const unsigned char* base = stage_mem + (size_t)s * g.tile_bytes;
+        const int32_t* P = reinterpret_cast<const int32_t*>(base);
+        const int32_t* Nb = reinterpret_cast<const int32_t*>(base + g.hdr_bytes);
+        const T* V = reinterpret_cast<const T*>(base + g.hdr_bytes + align16u(4 * (int64_t)P[a1 - a0]));
+        const int32_t q0 = P[a - a0], q1 = P[a + 1 - a0];
+        const T* vr = V + D * D * q0;
+        const int32_t* nr = Nb + q0;
+        node_component_partials<D, T, DIFF>([vr](int t) { return vr[t]; }, [nr](int t) { return nr[t]; }, q1 - q0,
+                                            a, j, p, acc);
+      }
+      // lanes of a node are consecutive: the exchange's sources stay inside it
+      T av = node_rows_exchange<D, T>(acc, j, live ? wl : wl - wl % D);
+      if (live) {
+        const int64_t dof = a * D + j;
+        if (S.known[dof]) av = 0;
+        Ap[dof] = av;
+        pap.add_prod(__ldg(p + dof), av);
+      }
+      __syncwarp();
+      if (wl == 0) mbar_arrive(&empty[s]);
+    }
+  }
+  const double v[1] = {pap.value()};
+  double out[1];
+  if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
+    sc->pap = out[0];
+    if (sc->status == GFEA_ERR_TIMEOUT) {
+      sc->done = 1;
+    } else if (!(out[0] > 0) || !isfinite(out[0])) {
+      sc->status = isfinite(out[0]) ? GFEA_ERR_BREAKDOWN : GFEA_ERR_NAN;
+      sc->done = 1;
+    } else {
+      sc->alpha = sc->rz / out[0];
+    }
+  }
+}
+
 template <typename T>
 __global__ void cast_kernel(const double* __restrict__ s, T* __restrict__ d, int64_t n) {
   // FP64 -> T copy
@@ -928,6 +1201,8 @@ struct PcgWork {
   bool coarse = false;
   bool is_f32 = false;  // T-typed buffers hold floats
   CoarseDev C;
+  unsigned char* packed = nullptr;  // tiles of the staged SpMV (nullptr: apply_kernel)
+  StageGeom geom{};
   // CUDA graphs of kGraphIters PCG iterations, one per direction-buffer order
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   long long gkernels = 0;
@@ -958,7 +1233,7 @@ int coarse_target(const gfea_system* s, const gfea_pcg_opts* o) {
 }
 
 template <typename T>
-size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
+size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base, size_t packed = 0) {
   size_t off = 0;
   const int64_t N = Nn * D;
   auto take = [&](size_t bytes) {
@@ -994,6 +1269,7 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base) {
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.ecf = reinterpret_cast<float*>(take(sizeof(float) * nc));
   }
+  w->packed = packed ? reinterpret_cast<unsigned char*>(take(packed)) : nullptr;
   return off;
 }
 
@@ -1077,23 +1353,120 @@ int launch_update(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaSt
   return prof_mark(st, kTagUpdate);
 }
 
+// Shared memory of the staged apply: one packed tile per stage, one stage
+// per consumer warp (a deeper ring at one block per SM measured slower than
+// this at two blocks per SM: twice the warps gathering p).
+constexpr size_t kSmemMax = 220 * 1024;  // dynamic part (the opt-in limit is 227 KB with the static part)
+
+// Tiles of apply_staged_kernel for this operator; false when it cannot be
+// staged (no nodes or values, arrays not 4-byte aligned, tiles too large).
+// A packed tile holds 15 % more neighbour slots than an average tile; larger
+// tiles are read directly by the kernel.
+template <typename T>
+bool stage_geom(const gfea_system* s, const T* vals, StageGeom* g) {
+  if (s->n_nodes <= 0 || !vals || s->n_pairs <= 0) return false;
+  if (((uintptr_t)vals % sizeof(T)) | ((uintptr_t)s->nbr & 3) | ((uintptr_t)s->node_ptr & 3)) return false;
+  const int D = s->dof_n;
+  const double avg = (double)s->n_pairs / (double)s->n_nodes;
+  const int nt = 32 / D;
+  g->nt = nt;
+  g->cap_slots = (int32_t)ceil(1.15 * avg * nt) + 8;
+  g->hdr_bytes = align16u(4 * (uint64_t)(nt + 1));
+  g->tile_bytes = g->hdr_bytes + align16u(4 * (uint64_t)g->cap_slots) +
+                  align16u((uint64_t)g->cap_slots * D * D * sizeof(T));
+  g->ntiles = ceil_div(s->n_nodes, nt);
+  g->stages = kConsumerWarps;
+  return (size_t)g->stages * g->tile_bytes <= kSmemMax;
+}
+
+// Workspace bytes of the packed tiles (0: not staged).  'query': sizes only
+// (the arrays may not exist yet; a solve checks them again).
+template <typename T>
+size_t packed_bytes(const gfea_system* s, bool query = false) {
+  StageGeom g;
+  const T* vals = sizeof(T) == 4 ? (const T*)s->vals32 : (const T*)s->vals64;
+  gfea_system q = *s;
+  if (query) {  // stand-in aligned addresses for the checks on pointers
+    vals = reinterpret_cast<const T*>(alignof(double));
+    q.nbr = q.node_ptr = reinterpret_cast<const int32_t*>(alignof(double));
+  }
+  if (!stage_geom<T>(&q, vals, &g)) return 0;
+  return (size_t)g.ntiles * g.tile_bytes;
+}
+
+template <typename T>
+int launch_pack(const gfea_system* s, PcgWork& w, cudaStream_t st) {
+  const SysT<T> S = sys_t<T>(s);
+  GFEA_D_SWITCH(s->dof_n, (pack_tiles_kernel<DD, T><<<kSMs * 8, kThreads, 0, st>>>(S, w.geom, w.packed)));
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+// Persistent grid of the staged apply: as many blocks as fit on the SMs.
+template <int D, typename T, bool DIFF>
+int launch_apply_staged(const SysT<T>& S, const StageGeom& g, const unsigned char* packed, const T* p, T* Ap,
+                        double* partials, Scal* sc, cudaStream_t st) {
+  auto kern = apply_staged_kernel<D, T, DIFF>;
+  const size_t smem = (size_t)g.stages * g.tile_bytes;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [&] { attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax); });
+  GFEA_CUDA_TRY(attr);
+  static std::atomic<int64_t> occ{0};  // (smem << 8) | blocks per SM of the last query
+  int64_t o = occ.load(std::memory_order_relaxed);
+  int per_sm = (int)(o & 255);
+  if ((o >> 8) != (int64_t)smem || per_sm == 0) {
+    GFEA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStagedThreads, smem));
+    if (per_sm < 1) return GFEA_ERR_ARG;
+    occ.store(((int64_t)smem << 8) | per_sm, std::memory_order_relaxed);
+  }
+  int64_t grid = (int64_t)kSMs * per_sm;
+  if (grid > g.ntiles) grid = g.ntiles;
+  if (grid > kMaxBlocks) grid = kMaxBlocks;
+  if (grid < 1) grid = 1;
+  kern<<<(int)grid, kStagedThreads, smem, st>>>(S, g, packed, p, Ap, partials, sc);
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+// Masked SpMV with p.Ap and alpha: the staged kernel over the packed tiles
+// when the workspace holds them, else apply_kernel.
+template <typename T>
+int launch_apply(const gfea_system* s, int G, PcgWork& w, const T* p, cudaStream_t st) {
+  const SysT<T> S = sys_t<T>(s);
+  const bool diff = sizeof(T) == 4 && s->translation_invariant;
+  if (w.packed) {
+    int e = GFEA_OK;
+    if (diff) {
+      GFEA_D_SWITCH(s->dof_n, (e = launch_apply_staged<DD, T, true>(S, w.geom, w.packed, p, (T*)w.Ap, w.partials,
+                                                                    w.sc, st)));
+    } else {
+      GFEA_D_SWITCH(s->dof_n, (e = launch_apply_staged<DD, T, false>(S, w.geom, w.packed, p, (T*)w.Ap,
+                                                                     w.partials, w.sc, st)));
+    }
+    return e;
+  }
+  const int grid = grid_nodes(s->n_nodes, G);
+  if (diff) {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(S, p, (T*)w.Ap,
+                                                                                         w.partials, w.sc)));
+  } else {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(S, p, (T*)w.Ap,
+                                                                                          w.partials, w.sc)));
+  }
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
 template <typename T>
 int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new, cudaStream_t st) {
-  const SysT<T> S = sys_t<T>(s);
   const int64_t N = s->n_nodes * s->dof_n;
   dir_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(N, (const T*)w.z, p_old, p_new, w.sc);
   GFEA_LAUNCH_CHECK();
   int e = prof_mark(st, kTagDir);
   if (e) return e;
-  const int grid = grid_nodes(s->n_nodes, G);
-  if (sizeof(T) == 4 && s->translation_invariant) {
-    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap,
-                                                                                         w.partials, w.sc)));
-  } else {
-    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(S, p_new, (T*)w.Ap,
-                                                                                          w.partials, w.sc)));
-  }
-  GFEA_LAUNCH_CHECK();
+  e = launch_apply<T>(s, G, w, p_new, st);
+  if (e) return e;
   return prof_mark(st, kTagApply);
 }
 
@@ -1303,7 +1676,6 @@ int tune_spmv_impl(const gfea_system* s, const T* x, T* y, cudaStream_t st, int3
 // p.Ap > 0 on the unknowns.
 template <typename T>
 int tune_apply_impl(const gfea_system* s, PcgWork& w, cudaStream_t st, int* G_out) {
-  const SysT<T> S = sys_t<T>(s);
   const int vt = sizeof(T) == 4 ? GFEA_F32 : GFEA_F64;
   const int rule = lanes_rule(s);
   const int cand[4] = {4, 8, 16, 32};
@@ -1312,24 +1684,11 @@ int tune_apply_impl(const gfea_system* s, PcgWork& w, cudaStream_t st, int* G_ou
   for (int c = 0; c < 4; ++c) {
     const int G = cand[c];
     if (G < s->dof_n) continue;
-    const int grid = grid_nodes(s->n_nodes, G);
     float best = INFINITY;
     for (int round = 0; round < 2; ++round) {
       GFEA_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(Scal), st));
       float ms = 0;
-      const int e = time_launches(
-          [&]() -> int {
-            if (sizeof(T) == 4 && s->translation_invariant) {
-              GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(
-                                               S, (const T*)w.pa, (T*)w.Ap, w.partials, w.sc)));
-            } else {
-              GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false><<<grid, kThreads, 0, st>>>(
-                                               S, (const T*)w.pa, (T*)w.Ap, w.partials, w.sc)));
-            }
-            GFEA_LAUNCH_CHECK();
-            return GFEA_OK;
-          },
-          5, st, &ms);
+      const int e = time_launches([&]() -> int { return launch_apply<T>(s, G, w, (const T*)w.pa, st); }, 5, st, &ms);
       if (e) return e;
       best = fminf(best, ms);
     }
@@ -1511,8 +1870,17 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   const ActiveSolve active;
   PcgWork w;
   const int target = coarse_target(s, o);
-  if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work)) > work_bytes)
+  // the packed tiles of the staged SpMV when the workspace has room for them
+  size_t pk = packed_bytes<T>(s);
+  if (const char* e = getenv("GFEA_APPLY_STAGED")) if (e[0] == '0') pk = 0;  // the unstaged kernel (A/B runs)
+  if (pk && pcg_layout<T>(s->n_nodes, s->dof_n, target, nullptr, nullptr, pk) > work_bytes) pk = 0;
+  if (pcg_layout<T>(s->n_nodes, s->dof_n, target, &w, static_cast<char*>(work), pk) > work_bytes)
     return GFEA_ERR_WORKSPACE;
+  if (pk) {
+    stage_geom<T>(s, sys_t<T>(s).vals, &w.geom);
+    const int ep = launch_pack<T>(s, w, st);
+    if (ep) return ep;
+  }
   const int vt = sizeof(T) == 4 ? GFEA_F32 : GFEA_F64;
   const int64_t N = s->n_nodes * s->dof_n;
   // host checks: every check_every iterations, or (check_every <= 0) after a
@@ -1695,9 +2063,9 @@ extern "C" int gfea_pcg_workspace_size(const gfea_system* s, const gfea_pcg_opts
   if (!s || !o || !bytes || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3) return GFEA_ERR_ARG;
   const int target = coarse_target(s, o);
   if (o->precision == GFEA_F64)
-    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, target, nullptr, nullptr);
+    *bytes = pcg_layout<double>(s->n_nodes, s->dof_n, target, nullptr, nullptr, packed_bytes<double>(s, true));
   else
-    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, target, nullptr, nullptr);
+    *bytes = pcg_layout<float>(s->n_nodes, s->dof_n, target, nullptr, nullptr, packed_bytes<float>(s, true));
   return GFEA_OK;
 }
 

@@ -87,7 +87,8 @@ class MeshSpec:
 
     def footprint(self, precision: str) -> int:
         """Device bytes of a solve on this mesh (graph, values, vectors, PCG
-        workspace), an upper estimate used for admission."""
+        workspace with the packed tiles of the staged SpMV), an upper estimate
+        used for admission."""
         D = self.dim
         nbr = {"quad4": 9, "quad9": 25, "hexa8": 27, "tri3_sen": 7}[self.kind]
         Nn = self.n_nodes
@@ -95,10 +96,12 @@ class MeshSpec:
         nnz = D * D * pairs
         npe = {"quad4": 4, "quad9": 9, "hexa8": 8, "tri3_sen": 3}[self.kind]
         graph = 4 * (Nn + 1) + 4 * pairs + self.n_elems * npe * (npe + 4) + 24 * Nn
+        iterated = 4 if precision == "mixed" else 8
         values = nnz * (12 if precision == "mixed" else 8)
-        vectors = D * Nn * 8 * 6 + D * Nn * (4 if precision == "mixed" else 8) * (8 + D)
+        vectors = D * Nn * 8 * 6 + D * Nn * iterated * (8 + D)
         coarse = 1536 * 1536 * 8 + 20 * Nn
-        return graph + values + vectors + coarse + (1 << 20)
+        packed = int(1.2 * (nnz * iterated + 4 * pairs)) + 64 * Nn
+        return graph + values + vectors + coarse + packed + (1 << 20)
 
 
 def cantilever_spec(kind: str, dof: float) -> MeshSpec:

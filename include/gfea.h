@@ -46,6 +46,7 @@ extern "C" {
 #define GFEA_ERR_BREAKDOWN 6    /* PCG p.Ap <= 0 (matrix not SPD on unknowns)    */
 #define GFEA_ERR_NAN 7          /* non-finite value met                          */
 #define GFEA_ERR_WORKSPACE 8    /* workspace too small                           */
+#define GFEA_ERR_TIMEOUT 9      /* a bounded device wait gave up (staged copies)  */
 
 /* element codes */
 #define GFEA_SEG2 0

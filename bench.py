@@ -510,7 +510,7 @@ def main():
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("apply_f32_hexa8_400x40x40")
+        traffic = json.load(open(tpath)).get("apply_staged_f32_hexa8_400x40x40")
 
     kinds = {}
     for r in results:
@@ -556,7 +556,8 @@ def main():
     }
     if roof is not None:
         line["roofline"] = {
-            "kernel": "apply_kernel<3,32,float> (masked FP32 node-block SpMV, HEXA8 2.02M DOF)",
+            "kernel": "apply_staged_kernel<3,float> (masked FP32 node-block SpMV over packed tiles streamed "
+                      "by bulk async copies, HEXA8 2.02M DOF)",
             "bound": "hbm", "achieved": roof["achieved"], "peak": peak, "unit": "GB/s",
             "frac": (roof["achieved"] / peak) if roof["achieved"] else None, "traffic": traffic,
             "bytes_per_launch": roof["spmv_bytes"], "avg_launch_ms": roof["avg_ms"],

@@ -45,6 +45,31 @@ struct DotAcc<float> {
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
+// Warp sum of dot accumulators (every lane receives it).  FP32 pairs are
+// combined with TwoSum at each butterfly step, so the sum keeps the pairs'
+// accuracy with one FP64 conversion per lane instead of FP64 shuffles and
+// adds (GB300's FP64 pipe made those a visible share of short kernels).
+__device__ __forceinline__ double warp_sum_acc(const DotAcc<double>& a) {
+  double v = a.v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_acc(const DotAcc<float>& a) {
+  float s = a.s, c = a.c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    const float t = s + s2;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (s2 - bp);
+    s = t;
+    c = (c + c2) + err;
+  }
+  return (double)s + (double)c;
+}
+
 // warp then block reduction with a fixed tree (deterministic); result valid in thread 0
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   // warp then block reduction with a fixed tree (deterministic)

@@ -94,6 +94,27 @@ int prof_mark(cudaStream_t st, int tag) {
 
 
 
+// The last block to finish (atomic ticket, no waiting) sums the NV block
+// partials in a fixed order; out[] holds the totals in every thread of it.
+template <int NV>
+__device__ bool reduce_last_tail(double* partials, uint32_t* ticket, double (&out)[NV], double* sh, bool& last) {
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double a = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) a += ((volatile double*)partials)[k * gridDim.x + i];
+    out[k] = block_sum(a, sh);
+    if (threadIdx.x == 0) sh[31] = out[k];
+    __syncthreads();
+    out[k] = sh[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+  return true;
+}
+
 // Publish NV block partials; returns true in the last block, where out[] holds
 // the fixed-order totals (valid in every thread of that block).
 template <int NV>
@@ -110,21 +131,35 @@ __device__ bool reduce_last(const double (&v)[NV], double* partials, uint32_t* t
     const uint32_t t = atomicAdd(ticket, 1u);
     last = (t == gridDim.x - 1);
   }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
+  return reduce_last_tail<NV>(partials, ticket, out, sh, last);
+}
+
+// reduce_last for dot accumulators: warp sums by warp_sum_acc (FP32 pairs
+// stay in FP32), then the warps' doubles in a fixed order.
+template <int NV, typename T>
+__device__ bool reduce_last_acc(const DotAcc<T> (&acc)[NV], double* partials, uint32_t* ticket, double (&out)[NV]) {
+  __shared__ double sh[32];
+  __shared__ double shw[NV][32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double a = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) a += ((volatile double*)partials)[k * gridDim.x + i];
-    out[k] = block_sum(a, sh);
-    if (threadIdx.x == 0) sh[31] = out[k];
-    __syncthreads();
-    out[k] = sh[31];
-    __syncthreads();
+    const double v = warp_sum_acc(acc[k]);
+    if (lane == 0) shw[k][w] = v;
   }
-  if (threadIdx.x == 0) *ticket = 0;
-  return true;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += shw[k][i];
+      partials[k * gridDim.x + blockIdx.x] = t;
+    }
+    __threadfence();
+    const uint32_t t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  return reduce_last_tail<NV>(partials, ticket, out, sh, last);
 }
 
 // ---------------------------------------------------------------------------
@@ -312,9 +347,9 @@ __global__ void __launch_bounds__(kThreads) update_kernel(int64_t Nn, const uint
       rr.add_prod(rl[i], rl[i]);
     }
   }
-  const double v[2] = {rz.value(), rr.value()};
+  const DotAcc<T> v[2] = {rz, rr};
   double out[2];
-  if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
+  if (reduce_last_acc<2, T>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
     const double rz_new = out[0], rr = out[1];
     sc->beta = mode == 1 ? 0.0 : rz_new / sc->rz;
     // a replaced residual larger than the iterated one (drift) restarts the direction
@@ -355,6 +390,11 @@ struct CoarseHdr {
   int64_t Nn;
 };
 
+// The restriction's FP64 atomics go to kRcCopies copies of the coarse vector
+// (block b adds into copy b % kRcCopies): one copy held them all on a few L2
+// slices, where they serialised.
+constexpr int kRcCopies = 16;
+
 struct CoarseDev {
   int nr = 0, n_agg = 0, nc = 0;
   CoarseHdr* hdr = nullptr;
@@ -364,7 +404,8 @@ struct CoarseDev {
   double* rowp = nullptr;  // kGJB x nc: row panel of the pivot block
   double* colp = nullptr;  // nc x kGJB: column panel of the pivot block
   double* pinv = nullptr;  // kGJB x kGJB: inverse of the pivot block
-  double* rc = nullptr;    // nc: restriction accumulator
+  double* rc = nullptr;    // nc: restriction R^T r (summed from the copies)
+  double* rcp = nullptr;   // kRcCopies x nc: restriction accumulators, one per group of blocks
   double* ec = nullptr;    // nc: coarse correction
   float* ecf = nullptr;    // nc: its FP32 copy (read by the FP32 prolongation)
 };
@@ -657,7 +698,23 @@ __global__ void __launch_bounds__(kThreads) update_r_kernel(int64_t Nn, const ui
 #pragma unroll
         for (int i = 0; i < D; ++i) v[m] += R[i][m] * rl[i];
     }
-    restrict_add<nr, T>(C.rc, g, v);
+    restrict_add<nr, T>(C.rcp + (int64_t)(blockIdx.x % kRcCopies) * C.nc, g, v);
+  }
+}
+
+// rc = sum of the restriction copies, which are cleared for the next
+// iteration (fixed summation order).
+__global__ void __launch_bounds__(kThreads) rc_sum_kernel(CoarseDev C, const Scal* sc, int mode) {
+  if (mode == 0 && sc->done) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < C.nc; j += gridDim.x * blockDim.x) {
+    double t = 0;
+#pragma unroll
+    for (int k = 0; k < kRcCopies; ++k) {
+      double* q = C.rcp + (int64_t)k * C.nc + j;
+      t += *q;
+      *q = 0;
+    }
+    C.rc[j] = t;
   }
 }
 
@@ -721,10 +778,9 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
       rr.add_prod(rl[i], rl[i]);
     }
   }
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) C.rc[i] = 0;
-  const double v[2] = {rz.value(), rr.value()};
+  const DotAcc<T> v[2] = {rz, rr};
   double out[2];
-  if (reduce_last<2>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
+  if (reduce_last_acc<2, T>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
     const double rz_new = out[0], rr = out[1];
     sc->beta = mode == 1 ? 0.0 : rz_new / sc->rz;
     if (mode == 2 && !(sc->beta <= 1.0)) sc->beta = 0.0;
@@ -782,9 +838,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) a
       pap.add_prod(pn, av);
     }
   }
-  const double v[1] = {pap.value()};
+  const DotAcc<T> v[1] = {pap};
   double out[1];
-  if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
+  if (reduce_last_acc<1, T>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
     sc->pap = out[0];
     if (!(out[0] > 0) || !isfinite(out[0])) {
       sc->status = isfinite(out[0]) ? GFEA_ERR_BREAKDOWN : GFEA_ERR_NAN;
@@ -1052,9 +1108,9 @@ __global__ void __launch_bounds__(kStagedThreads, 2) apply_staged_kernel(SysT<T>
       if (wl == 0) mbar_arrive(&empty[s]);
     }
   }
-  const double v[1] = {pap.value()};
+  const DotAcc<T> v[1] = {pap};
   double out[1];
-  if (reduce_last<1>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
+  if (reduce_last_acc<1, T>(v, partials, &sc->ticket1, out) && threadIdx.x == 0) {
     sc->pap = out[0];
     if (sc->status == GFEA_ERR_TIMEOUT) {
       sc->done = 1;
@@ -1266,6 +1322,7 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base, size
     w->C.colp = reinterpret_cast<double*>(take(sizeof(double) * kGJB * nc));
     w->C.pinv = reinterpret_cast<double*>(take(sizeof(double) * kGJB * kGJB));
     w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
+    w->C.rcp = reinterpret_cast<double*>(take(sizeof(double) * nc * kRcCopies));
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.ecf = reinterpret_cast<float*>(take(sizeof(float) * nc));
   }
@@ -1483,6 +1540,8 @@ int launch_precond(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaS
   GFEA_LAUNCH_CHECK();
   int e = prof_mark(st, kTagRestrict);
   if (e) return e;
+  rc_sum_kernel<<<(int)ceil_div(w.C.nc, kThreads), kThreads, 0, st>>>(w.C, w.sc, mode);
+  GFEA_LAUNCH_CHECK();
   coarse_gemv_kernel<<<std::min(w.C.nc, 8 * kSMs), kGemvThreads, 0, st>>>(w.C, w.sc, mode);
   GFEA_LAUNCH_CHECK();
   e = prof_mark(st, kTagGemv);
@@ -1620,6 +1679,7 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
     GFEA_LAUNCH_CHECK();
   }
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rc, 0, sizeof(double) * C.nc, st));
+  GFEA_CUDA_TRY(cudaMemsetAsync(C.rcp, 0, sizeof(double) * C.nc * kRcCopies, st));
   return GFEA_OK;
 }
 
@@ -1745,9 +1805,9 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(cs, &g);
   // kernels per iteration: direction + SpMV, then update (block-Jacobi) or
-  // update/restrict + coarse GEMV + finish (two-level); counted when the
-  // graph runs, not when it is captured
-  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? 3 : 1));
+  // update/restrict + restriction sum + coarse GEMV + finish (two-level);
+  // counted when the graph runs, not when it is captured
+  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? 4 : 1));
   launch_counter().fetch_sub(w.gkernels);
   if (e || ce != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);

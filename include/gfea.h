@@ -277,6 +277,11 @@ int gfea_batch_launch(void* scratch, int n, const gfea_pcg_opts* opts_host, void
 /* y = A x (unmasked), value_type selects vals64/x,y double or vals32/x,y float. */
 int gfea_spmv(const gfea_system* sys_host, int value_type, const void* x, void* y, void* stream);
 
+/* The workspace holds the PCG vectors, the coarse level and, when the
+ * operator can be staged, a packed copy of it in node tiles (about 1.15x the
+ * iterated values plus the neighbour indices) that the staged SpMV streams
+ * with one bulk copy per tile.  A smaller workspace that still holds the rest
+ * is accepted: the solve then runs the unstaged SpMV. */
 int gfea_pcg_workspace_size(const gfea_system* sys_host, const gfea_pcg_opts* opts_host,
                             size_t* bytes_host);
 

@@ -47,3 +47,30 @@ def test_host_only_entry_points():
     res = _lib.PcgResult()
     assert lib.gfea_pcg_solve(ctypes.byref(sysd), 0, 0, ctypes.byref(opts), 0, 0, ctypes.byref(res), 0) == 1
     assert lib.gfea_reduce_workspace_size() > 0
+
+
+def test_pcg_workspace_holds_packed_tiles():
+    """The PCG workspace query includes the packed node tiles of the staged
+    SpMV (each tile: node offsets, neighbour indices and CSR values, 15 %
+    headroom) when a ring of eight tiles fits in shared memory, and leaves
+    them out otherwise (the unstaged kernel then runs)."""
+    import ctypes
+
+    lib = _lib.load()
+    ws = ctypes.c_size_t()
+
+    def size(D, Nn, deg, prec):
+        sysd = _lib.System(_lib.ABI_VERSION, D, Nn, Nn * deg, 0, 0, 0, 0, 0, 0, 0)
+        opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 100, 0, 1e-10, 0.0, 10, 0, 0, 0)
+        assert lib.gfea_pcg_workspace_size(ctypes.byref(sysd), ctypes.byref(opts), ctypes.byref(ws)) == 0
+        return ws.value
+
+    Nn = 10_000
+    for D, deg in ((3, 27), (2, 9), (1, 7)):
+        for prec, s in ((_lib.F32, 4), (_lib.F64, 8)):
+            operator = D * D * Nn * deg * s + 4 * Nn * deg
+            assert size(D, Nn, deg, prec) >= 1.15 * operator
+    # HEXA8-sized rows of 40 neighbours in FP64: eight tiles exceed shared
+    # memory, no tiles are reserved (the workspace stays below the operator)
+    assert size(3, Nn, 40, _lib.F64) < 9 * Nn * 40 * 8
+    assert size(3, Nn, 40, _lib.F32) >= 1.15 * (9 * Nn * 40 * 4 + 4 * Nn * 40)

@@ -99,12 +99,18 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
   using E = Elem<ELEM>;
   constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value, NS = D == 2 ? 3 : 6;
   constexpr int EPW = 32 / G;  // elements per warp
+  // modes 3, 4: isotropic law given by (lambda, mu): K_pq = lambda M + mu M^T
+  // + mu tr(M) I with M = sum_g wJ grad N_p (x) grad N_q -- the same matrix as
+  // B^T C B for C = lambda 1 (x) 1 + 2 mu I (Kelvin-Mandel), with D^2 FMAs per
+  // block and Gauss point instead of B^T C (D x NS x 3) plus B^T C B
+  constexpr bool ISO = CMODE == 3 || CMODE == 4;
   __shared__ RefTables<ELEM, false> ref;
   __shared__ R Csh[NS * NS];
   ref.fill();
-  if (CMODE != 1)  // homogeneous C, or the reference C of mode 2
+  if (CMODE == 0 || CMODE == 2)  // homogeneous C, or the reference C of mode 2
     for (int i = threadIdx.x; i < NS * NS; i += blockDim.x) Csh[i] = (R)Cglob[i];
   __syncthreads();
+  const R lam = ISO ? (R)Cglob[0] : (R)0, mu = ISO ? (R)Cglob[1] : (R)0;
 
   const int lane = threadIdx.x % G;
   const int sub = (threadIdx.x & 31) / G;
@@ -145,20 +151,58 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
     for (int g = 0; g < RefTables<ELEM, false>::nPg; ++g) {
       R grad[D];
       const R wJ = lane_geometry<ELEM, false, G, R>(ref, g, lane, node_lane, X, grad);
-      R BtC[D][NS];
-      btc<D, R>(grad, C, wJ, BtC);
+      if constexpr (ISO) {
+        R wa[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) wa[k] = wJ * grad[k];
+#pragma unroll
+        for (int d = 0; d < NB; ++d) {
+          const int q = node_lane ? (lane + d) % nPe : 0;
+          R h[D];
+#pragma unroll
+          for (int k = 0; k < D; ++k) h[k] = group_bcast<G, R>(grad[k], q);
+          if (d < NB - 1 || extra) {
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+#pragma unroll
+              for (int j = 0; j < D; ++j) acc[d][i][j] += wa[i] * h[j];
+          }
+        }
+      } else {
+        R BtC[D][NS];
+        btc<D, R>(grad, C, wJ, BtC);
+#pragma unroll
+        for (int d = 0; d < NB; ++d) {
+          const int q = node_lane ? (lane + d) % nPe : 0;
+          R h[D];
+#pragma unroll
+          for (int k = 0; k < D; ++k) h[k] = group_bcast<G, R>(grad[k], q);
+          if (d < NB - 1 || extra) btcb<D, R>(BtC, h, acc[d]);
+        }
+      }
+    }
+    if constexpr (ISO) {
 #pragma unroll
       for (int d = 0; d < NB; ++d) {
-        const int q = node_lane ? (lane + d) % nPe : 0;
-        R h[D];
+        R tr = 0;
 #pragma unroll
-        for (int k = 0; k < D; ++k) h[k] = group_bcast<G, R>(grad[k], q);
-        if (d < NB - 1 || extra) btcb<D, R>(BtC, h, acc[d]);
+        for (int i = 0; i < D; ++i) tr += acc[d][i][i];
+        R K[D][D];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) K[i][j] = lam * acc[d][i][j] + mu * acc[d][j][i] + (i == j ? mu * tr : (R)0);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) acc[d][i][j] = K[i][j];
       }
     }
     if (act) {
-      // mode 2: per-element factor of the reference C (e.g. a per-element Young's modulus)
-      const double f = CMODE == 2 ? factor * __ldg(Cglob + NS * NS + ec) : factor;
+      // modes 2, 4: per-element factor of the reference law (e.g. a per-element Young's modulus)
+      const double f = CMODE == 2   ? factor * __ldg(Cglob + NS * NS + ec)
+                       : CMODE == 4 ? factor * __ldg(Cglob + 2 + ec)
+                                    : factor;
       const int32_t* ce = connect + ec * nPe;
       const uint8_t* rke = rank + ec * nPe * nPe;
       const int32_t pa0 = node_ptr[a];
@@ -306,12 +350,13 @@ int launch_elastic(const double* coord, const int32_t* connect, int64_t Ne, cons
   const int64_t warps = ceil_div(Ne, 32 / G);
   int blocks = grid_for(warps * 32, 128);
   if (blocks > kSMs * per_sm) blocks = kSMs * per_sm;
-  if (cpe == 1)
-    elastic_kernel<ELEM, T, R, 1><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
-  else if (cpe == 2)
-    elastic_kernel<ELEM, T, R, 2><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
-  else
-    elastic_kernel<ELEM, T, R, 0><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals);
+  switch (cpe) {
+    case 1: elastic_kernel<ELEM, T, R, 1><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals); break;
+    case 2: elastic_kernel<ELEM, T, R, 2><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals); break;
+    case 3: elastic_kernel<ELEM, T, R, 3><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals); break;
+    case 4: elastic_kernel<ELEM, T, R, 4><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals); break;
+    default: elastic_kernel<ELEM, T, R, 0><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, C, factor, vals); break;
+  }
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -410,6 +455,7 @@ extern "C" int gfea_assemble_elastic(int elem, const double* coord, const int32_
                                      int c_per_elem, double factor, int value_type, void* values,
                                      int64_t n_values, int accumulate, void* stream) {
   if (!coord || !connect || !node_ptr || !rank || !C || !values || n_elems < 0) return GFEA_ERR_ARG;
+  if (c_per_elem < 0 || c_per_elem > 4) return GFEA_ERR_ARG;
   const int d = elem_dim(elem);
   if (d < 2) return GFEA_ERR_ARG;
   if (value_type != GFEA_F64 && value_type != GFEA_F32) return GFEA_ERR_ARG;
@@ -438,6 +484,7 @@ extern "C" int gfea_tune_assemble_elastic(int elem, const double* coord, const i
       !blocks_per_sm_host || !ms_host)
     return GFEA_ERR_ARG;
   if (elem_dim(elem) < 2 || (value_type != GFEA_F64 && value_type != GFEA_F32)) return GFEA_ERR_ARG;
+  if (c_per_elem < 0 || c_per_elem > 4) return GFEA_ERR_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (value_type == GFEA_F64)
     return dispatch_elastic<double>(elem, true, coord, connect, n_elems, node_ptr, rank, C, c_per_elem, factor,

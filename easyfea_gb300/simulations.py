@@ -33,6 +33,26 @@ def _dev():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+
+def isotropic_lame(C: np.ndarray):
+    """(lambda, mu) when the Kelvin-Mandel matrix C (3x3 in 2D, 6x6 in 3D) is
+    isotropic, C = lambda 1 (x) 1 + 2 mu I on the normal / shear blocks
+    (plane stress included, with its reduced lambda); else None."""
+    C = np.asarray(C, dtype=np.float64)
+    n = C.shape[0]
+    if C.shape != (n, n) or n not in (3, 6):
+        return None
+    nn = 2 if n == 3 else 3
+    lam = C[0, 1]
+    mu = 0.5 * C[n - 1, n - 1]
+    iso = np.zeros_like(C)
+    iso[:nn, :nn] = lam
+    iso += 2.0 * mu * np.eye(n)
+    scale = np.abs(C).max()
+    if not scale > 0 or np.abs(C - iso).max() > 1e-13 * scale:
+        return None
+    return np.array([lam, mu], dtype=np.float64)
+
 class _BC:
     def __init__(self, problemType, nodes, dofs, values, unknowns, description):
         self.problemType = problemType
@@ -291,17 +311,25 @@ class Elastic(_Simu):
             self.__M = None
 
     def _C_device(self):
-        """(C tensor, mode) for gfea_assemble_elastic: homogeneous (0), or a
-        reference C for E = 1 followed by the per-element moduli (2)."""
+        """(C tensor, mode) for gfea_assemble_elastic: an isotropic law as
+        (lambda, mu) (3), or (lambda, mu) for E = 1 followed by the per-element
+        moduli (4); other laws as the Kelvin-Mandel C, homogeneous (0) or per
+        element (1)."""
         mat = self.material
         if getattr(mat, "isHeterogeneous", False) and isinstance(mat, ElasticModels.Isotropic):
             E = np.asarray(mat.E, dtype=np.float64).ravel()
             assert E.size == self.mesh.Ne, "per-element E must have one value per element"
             ref = ElasticModels.Isotropic(mat.dim, E=1.0, v=mat.v, planeStress=mat.planeStress).C
-            buf = np.concatenate([ref.ravel(), E])
-            return torch.as_tensor(buf, device=_dev()), 2
-        C = mat.C
-        return torch.as_tensor(np.ascontiguousarray(C, dtype=np.float64), device=_dev()), 1 if C.ndim == 3 else 0
+            lame = isotropic_lame(ref)
+            if lame is not None:
+                return torch.as_tensor(np.concatenate([lame, E]), device=_dev()), 4
+            return torch.as_tensor(np.concatenate([ref.ravel(), E]), device=_dev()), 2
+        C = np.ascontiguousarray(mat.C, dtype=np.float64)
+        if C.ndim == 2:
+            lame = isotropic_lame(C)
+            if lame is not None:
+                return torch.as_tensor(lame, device=_dev()), 3
+        return torch.as_tensor(C, device=_dev()), 1 if C.ndim == 3 else 0
 
     def Assembly(self, problemType=None) -> CsrOperator:
         """K = sum_e K_e x thickness on the device (_elastic.py:123-152, _simu.py:1104-1144)."""

@@ -103,7 +103,12 @@ int gfea_csr_pattern(const int32_t* node_ptr, const int32_t* nbr, int64_t n_node
  * C: Kelvin-Mandel (3x3 in 2D, 6x6 in 3D), c_per_elem = 0 homogeneous,
  * 1 per element (Ne x n x n, Models/_utils.py:69-108), 2 a reference n x n
  * matrix followed by Ne per-element factors (C_e = f_e C_ref, e.g. a
- * per-element Young's modulus with a constant Poisson ratio).
+ * per-element Young's modulus with a constant Poisson ratio); for an
+ * isotropic law C = lambda 1 (x) 1 + 2 mu I (Kelvin-Mandel; plane stress with
+ * its reduced lambda), c_per_elem = 3 passes C = {lambda, mu} and 4 passes
+ * {lambda, mu} followed by Ne per-element factors: the same matrix from
+ * K_pq = sum wJ (lambda a b^T + mu b a^T + mu (a.b) I), a = grad N_p,
+ * b = grad N_q, with about a third of the floating-point work.
  * C must be symmetric (as every elastic law's Kelvin-Mandel matrix is): each
  * element computes K_pq for one of each pair of nodes and scatters K_qp =
  * K_pq^T.  values (value_type GFEA_F64/F32, n_values = dof_n^2 * n_pairs

@@ -96,3 +96,23 @@ def test_model_observers_trigger_update():
     pfm.Gc = 1.0
     assert o2.n == 2
     np.testing.assert_allclose(mat.C, fem.isotropic_C(1.0, 0.25, 2, True))
+
+
+def test_isotropic_lame_detection():
+    """Kelvin-Mandel matrices of isotropic laws are recognised (3D, plane
+    strain, plane stress with its reduced lambda); anisotropic ones are not."""
+    import numpy as np
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300.simulations import isotropic_lame
+
+    E, v = 210000.0, 0.3
+    lam, mu = E * v / ((1 + v) * (1 - 2 * v)), E / (2 * (1 + v))
+    for dim, ps, l_exp in ((3, False, lam), (2, False, lam), (2, True, 2 * lam * mu / (lam + 2 * mu))):
+        got = isotropic_lame(Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=ps).C)
+        assert got is not None
+        np.testing.assert_allclose(got, [l_exp, mu], rtol=1e-14)
+    C = Models.Elastic.Isotropic(3, E=1.0, v=0.3).C.copy()
+    C[0, 3] = C[3, 0] = 0.01
+    assert isotropic_lame(C) is None
+    assert isotropic_lame(np.zeros((6, 6))) is None

@@ -401,9 +401,15 @@ struct CoarseDev {
   int32_t* agg = nullptr;  // node -> aggregate
   float4* off = nullptr;   // node offset from its cell centre / largest cell size
   double* Ac = nullptr;    // nc x nc, inverted in place
-  double* rowp = nullptr;  // kGJB x nc: row panel of the pivot block
-  double* colp = nullptr;  // nc x kGJB: column panel of the pivot block
-  double* pinv = nullptr;  // kGJB x kGJB: inverse of the pivot block
+  // working storage of the inversion: float-float pairs (hi, lo)
+  float* Ahi = nullptr;    // nc x nc
+  float* Alo = nullptr;
+  float* rowph = nullptr;  // kGJB x nc: row panel of the pivot block
+  float* rowpl = nullptr;
+  float* colph = nullptr;  // nc x kGJB: column panel of the pivot block
+  float* colpl = nullptr;
+  float* pinvh = nullptr;  // kGJB x kGJB: inverse of the pivot block
+  float* pinvl = nullptr;
   double* rc = nullptr;    // nc: restriction R^T r (summed from the copies)
   double* rcp = nullptr;   // kRcCopies x nc: restriction accumulators, one per group of blocks
   double* ec = nullptr;    // nc: coarse correction
@@ -580,10 +586,57 @@ __global__ void coarse_regularize_kernel(CoarseDev C, double zero_tol, double sh
 // rank-b update to every element (each read and written by one thread).
 constexpr int kGJB = 16;
 
+// Float-float arithmetic of the inversion's trailing updates: a value is an
+// unevaluated pair hi + lo of floats (~2^-44 relative), products by the exact
+// FMA split, sums by TwoSum (Knuth); GB300 runs FP32 at 64x its FP64 rate, so
+// the n^3 update FMAs cost less than in FP64 even at ~12 FP32 operations each.
+__device__ __forceinline__ void ff_split(double d, float& hi, float& lo) {
+  hi = (float)d;
+  lo = (float)(d - (double)hi);
+}
+
+// (sh, sl) += (ah, al) (bh, bl); the al bl term is below the pair's precision
+__device__ __forceinline__ void ff_fma_acc(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  const float e = fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
+  const float t = sh + p;
+  const float bp = t - sh;
+  sl += ((sh - (t - bp)) + (p - bp)) + e;
+  sh = t;
+}
+
+// (ah, al) - (sh, sl), normalised
+__device__ __forceinline__ void ff_sub(float ah, float al, float sh, float sl, float& hi, float& lo) {
+  const float t = ah - sh;
+  const float bp = t - ah;
+  const float err = (ah - (t - bp)) + (-sh - bp);
+  const float l = err + (al - sl);
+  hi = t + l;
+  lo = l - (hi - t);
+}
+
+__global__ void ff_split_kernel(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    ff_split(a[i], hi[i], lo[i]);
+}
+
+__global__ void ff_merge_kernel(double* __restrict__ a, const float* __restrict__ hi, const float* __restrict__ lo,
+                                int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = (double)hi[i] + (double)lo[i];
+}
+
 __global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int b) {
+  // block (bx, l): row l of the transformed row panel for columns bx * 128 ..;
+  // every block inverts the b x b pivot block itself (b steps in shared
+  // memory, FP64), so the panel's work spreads over n / 128 x b blocks
   const int n = C.nc;
+  const int l = blockIdx.y;
   __shared__ double M[kGJB][kGJB + 1], M2[kGJB][kGJB + 1];
-  for (int t = threadIdx.x; t < b * b; t += blockDim.x) M[t / b][t % b] = C.Ac[(int64_t)(k0 + t / b) * n + k0 + t % b];
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
+    const int64_t q = (int64_t)(k0 + t / b) * n + k0 + t % b;
+    M[t / b][t % b] = (double)C.Ahi[q] + (double)C.Alo[q];
+  }
   __syncthreads();
   for (int p = 0; p < b; ++p) {  // Gauss-Jordan of the pivot block in shared memory
     const double ip = 1.0 / M[p][p];
@@ -595,21 +648,26 @@ __global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int 
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) M[t / b][t % b] = M2[t / b][t % b];
     __syncthreads();
   }
-  if (blockIdx.x == 0)
-    for (int t = threadIdx.x; t < b * b; t += blockDim.x) C.pinv[t] = M[t / b][t % b];
+  if (blockIdx.x == 0 && l == 0)
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) ff_split(M[t / b][t % b], C.pinvh[t], C.pinvl[t]);
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  double a[kGJB];
+  double s = 0;
 #pragma unroll
-  for (int m = 0; m < kGJB; ++m) a[m] = m < b ? C.Ac[(int64_t)(k0 + m) * n + j] : 0.0;
-  for (int l = 0; l < b; ++l) {
-    double s = 0;
+  for (int m = 0; m < kGJB; ++m)
+    if (m < b) {
+      const int64_t q = (int64_t)(k0 + m) * n + j;
+      s += M[l][m] * ((double)C.Ahi[q] + (double)C.Alo[q]);
+    }
+  ff_split(s, C.rowph[(int64_t)l * n + j], C.rowpl[(int64_t)l * n + j]);
+  if (l == 0) {
 #pragma unroll
-    for (int m = 0; m < kGJB; ++m) s += (m < b ? M[l][m] : 0.0) * a[m];
-    C.rowp[(int64_t)l * n + j] = s;
+    for (int q = 0; q < kGJB; ++q) {
+      const int64_t src = (int64_t)j * n + k0 + q;
+      C.colph[(int64_t)j * kGJB + q] = q < b ? C.Ahi[src] : 0.f;
+      C.colpl[(int64_t)j * kGJB + q] = q < b ? C.Alo[src] : 0.f;
+    }
   }
-#pragma unroll
-  for (int l = 0; l < kGJB; ++l) C.colp[(int64_t)j * kGJB + l] = l < b ? C.Ac[(int64_t)j * n + k0 + l] : 0.0;
 }
 
 // Block (bx, by) owns column j = bx * blockDim + tid and rows by, by + gridDim.y, ...
@@ -618,28 +676,33 @@ __global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const bool jk = j >= k0 && j < k0 + b;
-  double r[kGJB];
+  float rh[kGJB], rl[kGJB];
 #pragma unroll
-  for (int l = 0; l < kGJB; ++l)
-    r[l] = l < b ? (jk ? C.pinv[l * b + (j - k0)] : C.rowp[(int64_t)l * n + j]) : 0.0;
+  for (int l = 0; l < kGJB; ++l) {
+    const int64_t q = jk ? (int64_t)l * b + (j - k0) : (int64_t)l * n + j;
+    rh[l] = l < b ? (jk ? C.pinvh[q] : C.rowph[q]) : 0.f;
+    rl[l] = l < b ? (jk ? C.pinvl[q] : C.rowpl[q]) : 0.f;
+  }
   for (int i = blockIdx.y; i < n; i += gridDim.y) {
-    double* p = C.Ac + (int64_t)i * n + j;
-    double v;
+    const int64_t q = (int64_t)i * n + j;
+    float vh, vl;
     if (i >= k0 && i < k0 + b) {
-      v = jk ? C.pinv[(i - k0) * b + (j - k0)] : C.rowp[(int64_t)(i - k0) * n + j];
+      const int64_t r = jk ? (int64_t)(i - k0) * b + (j - k0) : (int64_t)(i - k0) * n + j;
+      vh = jk ? C.pinvh[r] : C.rowph[r];
+      vl = jk ? C.pinvl[r] : C.rowpl[r];
     } else {
-      const double* c = C.colp + (int64_t)i * kGJB;
-      double s = 0;
+      const float* ch = C.colph + (int64_t)i * kGJB;
+      const float* cl = C.colpl + (int64_t)i * kGJB;
+      float sh = 0.f, sl = 0.f;
 #pragma unroll
-      for (int l = 0; l < kGJB; ++l) s += __ldg(c + l) * r[l];
-      v = jk ? -s : *p - s;
+      for (int l = 0; l < kGJB; ++l) ff_fma_acc(sh, sl, __ldg(ch + l), __ldg(cl + l), rh[l], rl[l]);
+      ff_sub(jk ? 0.f : C.Ahi[q], jk ? 0.f : C.Alo[q], sh, sl, vh, vl);
     }
-    *p = v;
+    C.Ahi[q] = vh;
+    C.Alo[q] = vl;
   }
 }
 
-// Sum of nr per-lane values into rc[g * nr + m] (g < 0: lane without a node):
-// a segmented warp scan over runs of equal g, one atomic per run and mode.
 template <int nr, typename T>
 __device__ __forceinline__ void restrict_add(double* rc, int g, T (&v)[nr]) {
   const int lane = threadIdx.x & 31;
@@ -1318,9 +1381,14 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base, size
     w->C.agg = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * Nn));
     w->C.off = reinterpret_cast<float4*>(take(sizeof(float4) * Nn));
     w->C.Ac = reinterpret_cast<double*>(take(sizeof(double) * nc * nc));
-    w->C.rowp = reinterpret_cast<double*>(take(sizeof(double) * kGJB * nc));
-    w->C.colp = reinterpret_cast<double*>(take(sizeof(double) * kGJB * nc));
-    w->C.pinv = reinterpret_cast<double*>(take(sizeof(double) * kGJB * kGJB));
+    w->C.Ahi = reinterpret_cast<float*>(take(sizeof(float) * nc * nc));
+    w->C.Alo = reinterpret_cast<float*>(take(sizeof(float) * nc * nc));
+    w->C.rowph = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+    w->C.rowpl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+    w->C.colph = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+    w->C.colpl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+    w->C.pinvh = reinterpret_cast<float*>(take(sizeof(float) * kGJB * kGJB));
+    w->C.pinvl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * kGJB));
     w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.rcp = reinterpret_cast<double*>(take(sizeof(double) * nc * kRcCopies));
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
@@ -1669,15 +1737,20 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
     coarse_regularize_kernel<<<1, 256, 0, st>>>(C, 1e-14, 1e-10);
   GFEA_LAUNCH_CHECK();
   if (mark) GFEA_CUDA_TRY(cudaEventRecord(mark, st));
+  const int64_t n2 = (int64_t)C.nc * C.nc;
+  ff_split_kernel<<<grid_elems(n2), kThreads, 0, st>>>(C.Ac, C.Ahi, C.Alo, n2);
+  GFEA_LAUNCH_CHECK();
   const int gx = (int)ceil_div(C.nc, 128);
   const int gy = (int)std::min<int64_t>(C.nc, ceil_div(2 * kMaxBlocks, gx));
   for (int k0 = 0; k0 < C.nc; k0 += kGJB) {
     const int b = std::min(kGJB, C.nc - k0);
-    gj_panel_kernel<<<gx, 128, 0, st>>>(C, k0, b);
+    gj_panel_kernel<<<dim3(gx, b), 128, 0, st>>>(C, k0, b);
     GFEA_LAUNCH_CHECK();
     gj_update_kernel<<<dim3(gx, gy), 128, 0, st>>>(C, k0, b);
     GFEA_LAUNCH_CHECK();
   }
+  ff_merge_kernel<<<grid_elems(n2), kThreads, 0, st>>>(C.Ac, C.Ahi, C.Alo, n2);
+  GFEA_LAUNCH_CHECK();
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rc, 0, sizeof(double) * C.nc, st));
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rcp, 0, sizeof(double) * C.nc * kRcCopies, st));
   return GFEA_OK;

@@ -66,27 +66,90 @@ __device__ __forceinline__ void btcb(const R (&BtC)[D][D == 2 ? 3 : 6], const R 
 
 // Per-lane geometry at one Gauss point: Jacobian reduced across the group,
 // wJ and the physical gradient of this lane's shape function.
+// Reciprocal by Newton-Raphson iteration on f(r) = 1/r - x (r <- r + r (1 - x r))
+// from an FP32 seed (relative error ~2^-23): two steps reach double precision
+// with four FP64 FMAs; the full division where the seed is out of FP32 range.
+__device__ __forceinline__ double recip_newton(double x) {
+  const float s = 1.0f / (float)x;
+  if (!(fabsf(s) > 0.f) || isinf(s)) return 1.0 / x;
+  double r = (double)s;
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
+}
+
+// Sum of nine per-lane values over a group of 8 lanes (the 3x3 Jacobian of a
+// HEXA8): a reduce-scatter in three exchange steps -- each lane keeps the
+// values owned by its half (value v owned by lane v, value 8 by lane 0) and
+// adds the partner's copies -- then broadcasts from the owners: 10 FP64 adds
+// instead of the butterfly's 27 (FP64 adds, not lanes, cost time on GB300).
+__device__ __forceinline__ void group8_sum9(const double (&v)[9], double (&F)[9], int lane) {
+  const bool b = lane & 4, c = lane & 2, e = lane & 1;
+  double k1[5], k2[3], k3[2];
+  {
+    const double L[5] = {v[0], v[1], v[2], v[3], v[8]}, U[5] = {v[4], v[5], v[6], v[7], 0.0};
+#pragma unroll
+    for (int m = 0; m < 5; ++m) k1[m] = (b ? U[m] : L[m]) + __shfl_xor_sync(0xffffffffu, b ? L[m] : U[m], 4, 8);
+  }
+  {
+    const double L[3] = {k1[0], k1[1], k1[4]}, U[3] = {k1[2], k1[3], 0.0};
+#pragma unroll
+    for (int m = 0; m < 3; ++m) k2[m] = (c ? U[m] : L[m]) + __shfl_xor_sync(0xffffffffu, c ? L[m] : U[m], 2, 8);
+  }
+  {
+    const double L[2] = {k2[0], k2[2]}, U[2] = {k2[1], 0.0};
+#pragma unroll
+    for (int m = 0; m < 2; ++m) k3[m] = (e ? U[m] : L[m]) + __shfl_xor_sync(0xffffffffu, e ? L[m] : U[m], 1, 8);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) F[i] = __shfl_sync(0xffffffffu, k3[0], i, 8);
+  F[8] = __shfl_sync(0xffffffffu, k3[1], 0, 8);
+}
+
 template <int ELEM, bool MASS, int G, typename R>
 __device__ __forceinline__ R lane_geometry(const RefTables<ELEM, MASS>& ref, int g, int lane, bool node_lane,
                                            const R (&X)[Elem<ELEM>::dim], R (&grad)[Elem<ELEM>::dim]) {
   constexpr int D = Elem<ELEM>::dim;
-  double F[D][D];
+  if constexpr (D == 3 && G == 8) {
+    // F[d][k] = sum_p dN_d(p) X_p[k]; grad = F^-1 dN = adj(F) dN / det(F)
+    double dn[3], v[9], F[9];
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const R dn = node_lane ? (R)ref.dN[g][d][lane] : (R)0;
+    for (int d = 0; d < 3; ++d) dn[d] = node_lane ? (double)ref.dN[g][d][lane] : 0.0;
 #pragma unroll
-    for (int k = 0; k < D; ++k) F[d][k] = (double)group_sum<G, R>(dn * X[k]);
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v[d * 3 + k] = dn[d] * (double)X[k];
+    group8_sum9(v, F, lane);
+    const double a11 = F[0], a12 = F[1], a13 = F[2], a21 = F[3], a22 = F[4], a23 = F[5], a31 = F[6], a32 = F[7],
+                 a33 = F[8];
+    const double c11 = a22 * a33 - a32 * a23, c21 = -(a21 * a33 - a31 * a23), c31 = a21 * a32 - a31 * a22;
+    const double det = a11 * c11 + a12 * c21 + a13 * c31;
+    const double id = recip_newton(det);
+    const double adj[3][3] = {{c11, -(a12 * a33 - a32 * a13), a12 * a23 - a22 * a13},
+                              {c21, a11 * a33 - a31 * a13, -(a11 * a23 - a21 * a13)},
+                              {c31, -(a11 * a32 - a31 * a12), a11 * a22 - a21 * a12}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) grad[i] = (R)(id * (adj[i][0] * dn[0] + adj[i][1] * dn[1] + adj[i][2] * dn[2]));
+    return (R)(fabs(det) * ref.w[g]);
+  } else {
+    double F[D][D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const R dn = node_lane ? (R)ref.dN[g][d][lane] : (R)0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) F[d][k] = (double)group_sum<G, R>(dn * X[k]);
+    }
+    double iF[D][D];
+    const double det = det_inv<D>(F, iF);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      double v = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) v += iF[i][d] * (node_lane ? ref.dN[g][d][lane] : 0.0);
+      grad[i] = (R)v;
+    }
+    return (R)(fabs(det) * ref.w[g]);
   }
-  double iF[D][D];
-  const double det = det_inv<D>(F, iF);
-#pragma unroll
-  for (int i = 0; i < D; ++i) {
-    double v = 0;
-#pragma unroll
-    for (int d = 0; d < D; ++d) v += iF[i][d] * (node_lane ? ref.dN[g][d][lane] : 0.0);
-    grad[i] = (R)v;
-  }
-  return (R)(fabs(det) * ref.w[g]);
 }
 
 template <int ELEM, typename T, typename R, int CMODE>

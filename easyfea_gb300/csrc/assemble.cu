@@ -347,11 +347,16 @@ __global__ void __launch_bounds__(128) mass_kernel(const double* __restrict__ co
   }
 }
 
+// Up to four traction components, passed by value to the surface kernel.
+struct Traction4 {
+  double x, y, z, w;
+};
+
 // Boundary (line / face) integration of constant tractions.
 template <int BELEM>
 __global__ void surface_load_kernel(const double* __restrict__ coord, const int32_t* __restrict__ bconnect,
                                     int64_t Nbe, const uint8_t* __restrict__ mask, int dof_n, int nu,
-                                    int4 uidx, double4 uval, double factor, double* __restrict__ b) {
+                                    int4 uidx, Traction4 uval, double factor, double* __restrict__ b) {
   using E = Elem<BELEM>;
   constexpr int nPe = E::nPe, BD = E::dim;
   __shared__ RefTables<BELEM, true> ref;
@@ -434,17 +439,6 @@ int launch_mass(const double* coord, const int32_t* connect, int64_t Ne, const i
   mass_kernel<ELEM, T, R><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, dof_n, rho, factor, vals);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
-}
-
-int elem_nPe(int elem) {
-  switch (elem) {
-    case GFEA_SEG2: return 2;
-    case GFEA_TRI3: return 3;
-    case GFEA_QUAD4: return 4;
-    case GFEA_QUAD9: return 9;
-    case GFEA_HEXA8: return 8;
-    default: return -1;
-  }
 }
 
 // Times the element kernel with 4 .. 64 blocks per SM (values zeroed before
@@ -603,7 +597,7 @@ extern "C" int gfea_surface_load(int belem, const double* coord, const int32_t* 
     uv[u] = values_host[u];
   }
   const int4 uidx = make_int4(ui[0], ui[1], ui[2], ui[3]);
-  const double4 uval = make_double4(uv[0], uv[1], uv[2], uv[3]);
+  const Traction4 uval{uv[0], uv[1], uv[2], uv[3]};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int blocks = grid_for(n_belems, 128);
   switch (belem) {

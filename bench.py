@@ -158,14 +158,11 @@ def _reference_worker(budget_s):
     return oracle_rates(budget_s=budget_s)
 
 
-def reference_rates_all_cores(workers, budget_s):
+def reference_rates_all_cores(pool, workers, budget_s):
     """Per-kind seconds per DOF of the oracle with one worker process per
     host core, all timing their samples at once (so the rates include the
     contention of a fully loaded host); the median over workers."""
-    import multiprocessing as mp
-
-    with mp.get_context("spawn").Pool(workers) as pool:
-        results = pool.map(_reference_worker, [budget_s] * workers)
+    results = pool.map(_reference_worker, [budget_s] * workers)
     rates = {k: statistics.median(r[0][k] for r in results) for k in results[0][0]}
     return rates, results[0][1]
 
@@ -180,15 +177,18 @@ def run_reference(args):
     # oracle single-threaded (its BLAS included)
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[var] = "1"
+    import multiprocessing as mp
+
     workers = max(1, os.cpu_count() or 1)
     _, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
-    for _ in range(args.warmup):
-        reference_rates_all_cores(workers, 1.0)
     values, descs = [], []
-    for _ in range(args.steps):
-        rates, desc = reference_rates_all_cores(workers, 4.0)
-        values.append(workers * oracle_stream_value(reqs, rates))
-        descs.append(desc)
+    with mp.get_context("spawn").Pool(workers) as pool:
+        for _ in range(args.warmup):
+            reference_rates_all_cores(pool, workers, 1.0)
+        for _ in range(args.steps):
+            rates, desc = reference_rates_all_cores(pool, workers, 4.0)
+            values.append(workers * oracle_stream_value(reqs, rates))
+            descs.append(desc)
     value = statistics.median(values)
     sample = (f"oracle (numpy/scipy restatement of EasyFEA's path: einsum element matrices, bincount assembly, "
               f"SuperLU spsolve, staggered phase field) on one small request per kind ({descs[-1]}), "

@@ -2,7 +2,7 @@
 
 Run in a container where matnoel/EasyFEA's sources are importable::
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [/root/reference] [--only=name,...]
 
 gmsh (imported unconditionally by EasyFEA/FEM/_mesher.py:13) is replaced by an
 empty stub module; meshes come from ``easyfea_gb300.mesh``'s organised
@@ -196,8 +196,16 @@ def pf_state_case(R, name, m, split, regu, out, seed=7):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
+    only = set(only[0]) if only else None
+    ref = args[0] if args else "/root/reference"
     R = load_reference(ref)
+    if only is not None:  # regenerate the named fixtures only
+        for name, fn in CASES.items():
+            if name in only:
+                fn(R, HERE)
+        return
     out = HERE
     import scipy
     np.savez(os.path.join(out, "versions.npz"), numpy=np.__version__, scipy=scipy.__version__)
@@ -214,6 +222,7 @@ def main():
     mq = gmesh.Mesh_Quad4_Rect(120.0, 13.0, 12, 3)
     Eh = 210000.0 * np.exp(0.3 * rng.standard_normal(mq.Ne))
     elastic_case(R, "el_quad4_hetero", mq, Eh, 0.3, True, 13.0, -800 / 13**2, "y", out)
+    _el_hexa8_hetero(R, out)
     # full-size 2D cantilever: QUAD4 240x26, L=120, h=13, t=13
     elastic_case(R, "el_cantilever_240x26", gmesh.Mesh_Quad4_Rect(120.0, 13.0, 240, 26), 210000.0, 0.3,
                  True, 13.0, -800 / 13**2, "y", out)
@@ -230,6 +239,17 @@ def main():
         pf_state_case(R, f"pfsys_{m.elemType.value.lower()}_{split.lower()}_{regu.lower()}", m, split, regu, out)
     pf_case(R, "pf_hexa8_miehe_at2", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.25, 6, 6, 1), "Miehe", "AT2", False,
             210000.0, 0.3, 2.7, 0.2, 2, 4e-3, out)
+
+
+def _el_hexa8_hetero(R, out):
+    rng = np.random.default_rng(5)
+    mh = gmesh.Mesh_Hexa8_Box(60.0, 10.0, 10.0, 6, 2, 2)
+    Eh = 210000.0 * np.exp(0.3 * rng.standard_normal(mh.Ne))
+    elastic_case(R, "el_hexa8_hetero", mh, Eh, 0.3, False, 1.0, -1.0, "z", out)
+
+
+# fixtures that can be regenerated alone (--only=name,...)
+CASES = {"el_hexa8_hetero": _el_hexa8_hetero}
 
 
 if __name__ == "__main__":

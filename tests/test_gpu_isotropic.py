@@ -29,7 +29,7 @@ def assemble(simu, C, mode):
     return vals.cpu().numpy()
 
 
-@pytest.mark.parametrize("case", ["el_quad4", "el_quad9", "el_hexa8", "el_tri3", "el_quad4_hetero"])
+@pytest.mark.parametrize("case", ["el_quad4", "el_quad9", "el_hexa8", "el_tri3", "el_quad4_hetero", "el_hexa8_hetero"])
 def test_lame_form_equals_kelvin_mandel(golden, case):
     import scipy.sparse as sp
 

@@ -7,7 +7,7 @@ import scipy.sparse as sp
 from oracle import fem
 from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve
 
-ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_cantilever_240x26"]
+ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26"]
 
 
 def row_scaled_err(A, B):

@@ -17,6 +17,7 @@ ABI_VERSION = 1
 
 OK = 0
 ERR_NOT_CONVERGED = 5
+ERR_TIMEOUT = 9
 
 F64 = 0
 F32 = 1
@@ -157,6 +158,7 @@ SIGNATURES = {
     "gfea_launch_count": (ctypes.c_longlong, []),
     "gfea_profile_enable": (c_int, [c_int]),
     "gfea_profile_read": (c_int, [POINTER(c_double), POINTER(ctypes.c_longlong)]),
+    "gfea_selftest_wait": (c_int, [c_int32, c_int32, POINTER(c_int32), c_void_p]),
     "gfea_tune_mode": (c_int, [c_int]),
     "gfea_tune_clear": (c_int, []),
     "gfea_tune_spmv": (c_int, [POINTER(System), c_int, c_void_p, c_void_p, POINTER(c_int32), POINTER(c_float),

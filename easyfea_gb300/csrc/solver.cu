@@ -2150,10 +2150,42 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   return res->status;
 }
 
+// Self-test of the bounded mbarrier wait the staged SpMV relies on: thread 0
+// initialises a barrier of one arrival, arrives or not, and waits on its
+// first phase with the given limit; the outcome goes to selftest_status.
+__device__ int32_t selftest_status;
+
+__global__ void wait_selftest_kernel(uint64_t limit_ns, int arrive) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (arrive) mbar_arrive(&bar);
+    selftest_status = mbar_wait(&bar, 0, &abort_flag, limit_ns) ? GFEA_OK : GFEA_ERR_TIMEOUT;
+  }
+}
+
 }  // namespace
 }  // namespace gfea
 
 using namespace gfea;
+
+extern "C" int gfea_selftest_wait(int32_t limit_us, int32_t arrive, int32_t* status_host, void* stream) {
+  if (!status_host || limit_us < 1 || limit_us > 1000000) return GFEA_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int32_t unset = -1;
+  GFEA_CUDA_TRY(cudaMemcpyToSymbolAsync(selftest_status, &unset, sizeof(int32_t), 0, cudaMemcpyHostToDevice, st));
+  wait_selftest_kernel<<<1, 32, 0, st>>>((uint64_t)limit_us * 1000ull, arrive != 0);
+  GFEA_LAUNCH_CHECK();
+  GFEA_CUDA_TRY(cudaMemcpyFromSymbolAsync(status_host, selftest_status, sizeof(int32_t), 0, cudaMemcpyDeviceToHost,
+                                          st));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+  return GFEA_OK;
+}
 
 extern "C" int gfea_spmv(const gfea_system* s, int value_type, const void* x, void* y, void* stream) {
   if (!s || s->version != GFEA_ABI_VERSION || !x || !y || s->n_nodes <= 0) return GFEA_ERR_ARG;

@@ -56,15 +56,16 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
 }
 
 // Wait for the completion of the barrier phase of the given parity; false
-// after kWaitLimitNs or once *abort is non-zero.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort = nullptr) {
+// after limit_ns (default kWaitLimitNs) or once *abort is non-zero.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort = nullptr,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_test(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (uint32_t i = 1;; ++i) {
     if (mbar_test(bar, parity)) return true;
     if ((i & 63u) == 0) {
       if (abort && *abort) return false;
-      if (global_ns() - t0 > kWaitLimitNs) return false;
+      if (global_ns() - t0 > limit_ns) return false;
     }
   }
 }

@@ -335,6 +335,13 @@ long long gfea_launch_count(void);
 int gfea_profile_enable(int on);
 int gfea_profile_read(double* ms_host, long long* launches_host);
 
+/* Self-test of the bounded device waits (no reference counterpart): one
+ * thread waits on an mbarrier phase with a limit of limit_us microseconds
+ * (1 .. 1e6), after one arrival (arrive != 0: *status_host = GFEA_OK) or none
+ * (*status_host = GFEA_ERR_TIMEOUT, the status a staged SpMV reports when a
+ * wait runs out); the context stays usable. */
+int gfea_selftest_wait(int32_t limit_us, int32_t arrive, int32_t* status_host, void* stream);
+
 /* FP64 -> FP32 copy of CSR values (mixed-precision operator) */
 int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void* stream);
 

@@ -1504,6 +1504,13 @@ bool stage_geom(const gfea_system* s, const T* vals, StageGeom* g) {
   return (size_t)g->stages * g->tile_bytes <= kSmemMax;
 }
 
+// Operators whose packed tiles fit in half of the 129 MB L2 stay unstaged:
+// the lane-group kernel then reads values that stay L2-resident across
+// iterations, whereas the staged path adds a packing pass per solve and
+// streams its tiles with an evict-first policy (small served solves and the
+// phase-field plate ran ~10 % faster unstaged).
+constexpr size_t kStageMinBytes = size_t(64) << 20;
+
 // Workspace bytes of the packed tiles (0: not staged).  'query': sizes only
 // (the arrays may not exist yet; a solve checks them again).
 template <typename T>
@@ -1516,7 +1523,10 @@ size_t packed_bytes(const gfea_system* s, bool query = false) {
     q.nbr = q.node_ptr = reinterpret_cast<const int32_t*>(alignof(double));
   }
   if (!stage_geom<T>(&q, vals, &g)) return 0;
-  return (size_t)g.ntiles * g.tile_bytes;
+  const size_t bytes = (size_t)g.ntiles * g.tile_bytes;
+  size_t min_bytes = kStageMinBytes;  // GFEA_STAGE_MIN_BYTES overrides (0: stage every operator)
+  if (const char* e = getenv("GFEA_STAGE_MIN_BYTES")) min_bytes = strtoull(e, nullptr, 10);
+  return bytes < min_bytes ? 0 : bytes;
 }
 
 template <typename T>

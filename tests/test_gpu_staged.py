@@ -13,6 +13,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def stage_every_operator(monkeypatch):
+    """These systems are L2-sized; stage them anyway (the library otherwise
+    keeps operators below half of the L2 on the unstaged kernel)."""
+    monkeypatch.setenv("GFEA_STAGE_MIN_BYTES", "0")
+
+
 def hub_graph(Nn, hubs, hub_deg, seed):
     """Sorted neighbour lists (self included): a ring with +-2 neighbours and
     'hubs' consecutive nodes each joined to hub_deg random others."""

@@ -49,11 +49,12 @@ def test_host_only_entry_points():
     assert lib.gfea_reduce_workspace_size() > 0
 
 
-def test_pcg_workspace_holds_packed_tiles():
+def test_pcg_workspace_holds_packed_tiles(monkeypatch):
     """The PCG workspace query includes the packed node tiles of the staged
     SpMV (each tile: node offsets, neighbour indices and CSR values, 15 %
-    headroom) when a ring of eight tiles fits in shared memory, and leaves
-    them out otherwise (the unstaged kernel then runs)."""
+    headroom) when the operator exceeds half of the L2 and a ring of eight
+    tiles fits in shared memory, and leaves them out otherwise (the unstaged
+    kernel then runs)."""
     import ctypes
 
     lib = _lib.load()
@@ -65,12 +66,17 @@ def test_pcg_workspace_holds_packed_tiles():
         assert lib.gfea_pcg_workspace_size(ctypes.byref(sysd), ctypes.byref(opts), ctypes.byref(ws)) == 0
         return ws.value
 
-    Nn = 10_000
+    monkeypatch.delenv("GFEA_STAGE_MIN_BYTES", raising=False)
+    Nn = 4_000_000
     for D, deg in ((3, 27), (2, 9), (1, 7)):
         for prec, s in ((_lib.F32, 4), (_lib.F64, 8)):
             operator = D * D * Nn * deg * s + 4 * Nn * deg
             assert size(D, Nn, deg, prec) >= 1.15 * operator
-    # HEXA8-sized rows of 40 neighbours in FP64: eight tiles exceed shared
-    # memory, no tiles are reserved (the workspace stays below the operator)
-    assert size(3, Nn, 40, _lib.F64) < 9 * Nn * 40 * 8
-    assert size(3, Nn, 40, _lib.F32) >= 1.15 * (9 * Nn * 40 * 4 + 4 * Nn * 40)
+    # an L2-sized operator stays unstaged (no tiles reserved) ...
+    small = 9 * 10_000 * 27 * 4
+    assert size(3, 10_000, 27, _lib.F32) < small
+    # ... unless the threshold is lowered
+    monkeypatch.setenv("GFEA_STAGE_MIN_BYTES", "0")
+    assert size(3, 10_000, 27, _lib.F32) >= 1.15 * (small + 4 * 10_000 * 27)
+    # rows of 40 neighbours in FP64: eight 10-node tiles exceed shared memory
+    assert size(3, 10_000, 40, _lib.F64) < 9 * 10_000 * 40 * 8

@@ -392,11 +392,15 @@ struct CoarseHdr {
 
 // The restriction's FP64 atomics go to kRcCopies copies of the coarse vector
 // (block b adds into copy b % kRcCopies): one copy held them all on a few L2
-// slices, where they serialised.
+// slices, where they serialised.  Below kRcCopyMinNodes nodes the atomics
+// are few and an iteration is launch-latency bound: one copy (rc itself,
+// cleared by finish_z) and no summing launch.
 constexpr int kRcCopies = 16;
+constexpr int64_t kRcCopyMinNodes = 100000;
 
 struct CoarseDev {
   int nr = 0, n_agg = 0, nc = 0;
+  int ncopies = 1;         // 1: restriction into rc; kRcCopies: into rcp, summed by rc_sum_kernel
   CoarseHdr* hdr = nullptr;
   int32_t* agg = nullptr;  // node -> aggregate
   float4* off = nullptr;   // node offset from its cell centre / largest cell size
@@ -761,7 +765,7 @@ __global__ void __launch_bounds__(kThreads) update_r_kernel(int64_t Nn, const ui
 #pragma unroll
         for (int i = 0; i < D; ++i) v[m] += R[i][m] * rl[i];
     }
-    restrict_add<nr, T>(C.rcp + (int64_t)(blockIdx.x % kRcCopies) * C.nc, g, v);
+    restrict_add<nr, T>(C.ncopies > 1 ? C.rcp + (int64_t)(blockIdx.x % kRcCopies) * C.nc : C.rc, g, v);
   }
 }
 
@@ -841,6 +845,8 @@ __global__ void __launch_bounds__(kThreads) finish_z_kernel(int64_t Nn, const ui
       rr.add_prod(rl[i], rl[i]);
     }
   }
+  if (C.ncopies == 1)  // single copy: clear rc (read by this iteration's GEMV) for the next restriction
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.nc; i += gridDim.x * blockDim.x) C.rc[i] = 0;
   const DotAcc<T> v[2] = {rz, rr};
   double out[2];
   if (reduce_last_acc<2, T>(v, partials, &sc->ticket2, out) && threadIdx.x == 0) {
@@ -1391,6 +1397,7 @@ size_t pcg_layout(int64_t Nn, int D, int n_agg_max, PcgWork* w, char* base, size
     w->C.pinvl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * kGJB));
     w->C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.rcp = reinterpret_cast<double*>(take(sizeof(double) * nc * kRcCopies));
+    w->C.ncopies = Nn >= kRcCopyMinNodes ? kRcCopies : 1;
     w->C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
     w->C.ecf = reinterpret_cast<float*>(take(sizeof(float) * nc));
   }
@@ -1619,8 +1626,10 @@ int launch_precond(const gfea_system* s, PcgWork& w, T* x, T* p, int mode, cudaS
   GFEA_LAUNCH_CHECK();
   int e = prof_mark(st, kTagRestrict);
   if (e) return e;
-  rc_sum_kernel<<<(int)ceil_div(w.C.nc, kThreads), kThreads, 0, st>>>(w.C, w.sc, mode);
-  GFEA_LAUNCH_CHECK();
+  if (w.C.ncopies > 1) {
+    rc_sum_kernel<<<(int)ceil_div(w.C.nc, kThreads), kThreads, 0, st>>>(w.C, w.sc, mode);
+    GFEA_LAUNCH_CHECK();
+  }
   coarse_gemv_kernel<<<std::min(w.C.nc, 8 * kSMs), kGemvThreads, 0, st>>>(w.C, w.sc, mode);
   GFEA_LAUNCH_CHECK();
   e = prof_mark(st, kTagGemv);
@@ -1889,9 +1898,10 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(cs, &g);
   // kernels per iteration: direction + SpMV, then update (block-Jacobi) or
-  // update/restrict + restriction sum + coarse GEMV + finish (two-level);
-  // counted when the graph runs, not when it is captured
-  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? 4 : 1));
+  // update/restrict + restriction sum (with restriction copies) + coarse
+  // GEMV + finish (two-level); counted when the graph runs, not when it is
+  // captured
+  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? (w.C.ncopies > 1 ? 4 : 3) : 1));
   launch_counter().fetch_sub(w.gkernels);
   if (e || ce != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);

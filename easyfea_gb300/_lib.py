@@ -156,6 +156,7 @@ SIGNATURES = {
     "gfea_max_abs_diff": (c_int, [c_void_p, c_void_p, c_int64, POINTER(c_double), c_void_p, c_void_p]),
     "gfea_cast_f64_f32": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
     "gfea_launch_count": (ctypes.c_longlong, []),
+    "gfea_cuda_graph_count": (ctypes.c_longlong, []),
     "gfea_profile_enable": (c_int, [c_int]),
     "gfea_profile_read": (c_int, [POINTER(c_double), POINTER(ctypes.c_longlong)]),
     "gfea_selftest_wait": (c_int, [c_int32, c_int32, POINTER(c_int32), c_void_p]),

@@ -1332,6 +1332,9 @@ struct PcgWork {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   long long gkernels = 0;
   bool graphs_ok = true;
+  // direct kernel launches only: no graph capture, no events, no tuning (the
+  // allocation-free entry point, which must create no driver resources)
+  bool direct_only = false;
   PcgWork() = default;
   PcgWork(const PcgWork&) = delete;
   PcgWork& operator=(const PcgWork&) = delete;
@@ -1878,6 +1881,12 @@ struct ActiveSolve {
   ~ActiveSolve() { active_solves().fetch_sub(1); }
 };
 
+// CUDA graphs instantiated by the library in this process (instrumentation).
+std::atomic<long long>& graph_counter() {
+  static std::atomic<long long> n{0};
+  return n;
+}
+
 cudaStream_t capture_stream() {
   thread_local cudaStream_t cs = nullptr;
   if (!cs && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) cs = nullptr;
@@ -1915,6 +1924,7 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
     cudaGetLastError();
     return GFEA_ERR_CUDA;
   }
+  graph_counter().fetch_add(1);
   return GFEA_OK;
 }
 
@@ -1933,7 +1943,7 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow
   ChunkEvents& E = chunk_events();
   const int cap = P.on.load() ? 64 : 256;  // events of a timed chunk: 64 iterations at most
   if (grow && check > cap) check = cap;
-  const bool timed = P.on.load() && check <= 64;
+  const bool timed = !w.direct_only && P.on.load() && check <= 64;
   if (timed && !E.created) {
     for (int i = 0; i < ChunkEvents::kEvents; ++i) GFEA_CUDA_TRY(cudaEventCreate(&E.ev[i]));
     E.created = true;
@@ -1945,7 +1955,8 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow
     const char* v = getenv("GFEA_PCG_GRAPHS");  // "0": direct launches only
     return !(v && v[0] == '0');
   }();
-  if (!graphs_env || (!w.gexec[0] && !w.gexec[1] && active_solves().load() > 1)) w.graphs_ok = false;
+  if (!graphs_env || w.direct_only || (!w.gexec[0] && !w.gexec[1] && active_solves().load() > 1))
+    w.graphs_ok = false;
   if (!timed && w.graphs_ok && !w.gexec[order] &&
       capture_iterations<T>(s, G, w, x, buf[0], buf[1], &w.gexec[order]) != GFEA_OK)
     w.graphs_ok = false;  // direct launches from here on
@@ -2019,10 +2030,11 @@ int fetch(Scal* h, PcgWork& w, cudaStream_t st) {
 //   (the rounding level of an FP64 residual).
 template <typename T>
 int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pcg_opts* o, void* work,
-                 size_t work_bytes, gfea_pcg_result* res, cudaStream_t st) {
+                 size_t work_bytes, gfea_pcg_result* res, cudaStream_t st, bool direct_only = false) {
   const auto t_start = std::chrono::steady_clock::now();
   const ActiveSolve active;
   PcgWork w;
+  w.direct_only = direct_only;
   const int target = coarse_target(s, o);
   // the packed tiles of the staged SpMV when the workspace has room for them
   size_t pk = packed_bytes<T>(s);
@@ -2057,7 +2069,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   if (e) return e;
   int G = pick_lanes(s, o->lanes, vt);
   if (w.coarse) {
-    const bool dbg = getenv("GFEA_DEBUG") != nullptr;
+    const bool dbg = !direct_only && getenv("GFEA_DEBUG") != nullptr;
     cudaEvent_t ev[3];
     if (dbg) {
       for (int i = 0; i < 3; ++i) GFEA_CUDA_TRY(cudaEventCreate(&ev[i]));
@@ -2084,7 +2096,8 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   if (e) return e;
   if (flag) { res->status = GFEA_ERR_SINGULAR; return GFEA_ERR_SINGULAR; }
   int32_t tuned = 0;
-  if (o->lanes == 0 && tune_cache().mode.load() == 2 && !tune_get(spmv_key(s, vt), &tuned) && hs.rr_true > 0) {
+  if (!direct_only && o->lanes == 0 && tune_cache().mode.load() == 2 && !tune_get(spmv_key(s, vt), &tuned) &&
+      hs.rr_true > 0) {
     // first solve of this problem class: time the PCG's own SpMV kernel on the
     // initial residual, then reset the scalar record it wrote
     cast_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(w.r64, (T*)w.pa, N);
@@ -2331,6 +2344,8 @@ extern "C" int gfea_cast_f64_f32(const double* src, float* dst, int64_t n, void*
 
 extern "C" long long gfea_launch_count(void) { return gfea::launch_counter().load(); }
 
+extern "C" long long gfea_cuda_graph_count(void) { return gfea::graph_counter().load(); }
+
 extern "C" int gfea_profile_enable(int on) {
   gfea::prof().on = on != 0;
   return GFEA_OK;
@@ -2371,23 +2386,14 @@ namespace {
 constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
-
-// Device address of g_static_scratch on the current device (looked up once per
-// device; the array's name in host code is only a host-side stand-in).
+// Device address of g_static_scratch in the current device's context.  The
+// array's name in host code is only a host-side stand-in; the lookup is cheap
+// and is repeated on every call, so the address stays valid across device
+// switches and context re-creation (cudaDeviceReset).
 int static_scratch(void** out) {
-  int dev = 0;
-  GFEA_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return GFEA_ERR_ARG;
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    GFEA_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  GFEA_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+  *out = p;
   return GFEA_OK;
 }
 
@@ -2417,6 +2423,11 @@ extern "C" int gfea_pcg_solve_noalloc(const gfea_system* s, const double* b, dou
   res->rel_residual = 0;
   res->floor_rel = 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (o->precision == GFEA_F64) return refine_solve<double>(s, b, x, o, scratch, kStaticScratchBytes, res, st);
-  return refine_solve<float>(s, b, x, o, scratch, kStaticScratchBytes, res, st);
+  // the array keeps whatever the last call (on any mesh) left in it, so a
+  // coarse aggregation is never reused from it
+  gfea_pcg_opts oo = *o;
+  oo.coarse_reuse = 0;
+  // direct launches only: no graph, stream or event is created
+  if (o->precision == GFEA_F64) return refine_solve<double>(s, b, x, &oo, scratch, kStaticScratchBytes, res, st, true);
+  return refine_solve<float>(s, b, x, &oo, scratch, kStaticScratchBytes, res, st, true);
 }

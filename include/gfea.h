@@ -304,9 +304,14 @@ int gfea_pcg_solve(const gfea_system* sys_host, const double* b, double* x,
  * inside this library (held by every GPU that loads it until the process
  * exits), so the problem must fit: FP64 needs (7 + dof_n) * 8 bytes per DOF
  * plus ~40 KB (about 209,000 DOF in 3D, 232,000 in 2D); larger problems are
- * rejected with GFEA_ERR_WORKSPACE before any device work.  The first call on
- * a device looks the array's device address up (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.  All
+ * rejected with GFEA_ERR_WORKSPACE before any device work.  It launches its
+ * kernels directly: it instantiates no CUDA graph and creates no stream or
+ * event, and it skips the schedule tuner and the kernel timing.  Every call
+ * looks the array's device address up (cudaGetSymbolAddress) in the current
+ * device's context; the first call on a device may also load the library's
+ * module there, so make that first call before any stream capture.
+ * opts.coarse_reuse is ignored: the array keeps what the last call (on any
+ * mesh) left in it, so the coarse aggregation is rebuilt every call.  All
  * calls share the array and reset what must start at zero: calls that overlap
  * on the GPU (different streams or threads) race and must be serialised. */
 int gfea_pcg_solve_noalloc(const gfea_system* sys_host, const double* b, double* x,
@@ -332,6 +337,10 @@ int gfea_max_abs_diff(const double* a, const double* b, int64_t n, double* out_h
  * launches since the last read (reading resets; with GFEA_DEBUG set in the
  * environment the per-kind table is printed to stderr). */
 long long gfea_launch_count(void);
+/* CUDA graphs the library has instantiated in this process (the PCG captures
+ * four iterations per graph for a solve running alone; the allocation-free
+ * solve never does). */
+long long gfea_cuda_graph_count(void);
 int gfea_profile_enable(int on);
 int gfea_profile_read(double* ms_host, long long* launches_host);
 

@@ -172,35 +172,88 @@ class PhaseFieldOracle:
         self.Ku = fem.assemble_csr(K_e, inv, ind, ptr, nnz, self.mesh.Nn * self.dim)
         return self.Ku
 
+    # The reference assembles lazily: Get_K_C_M_F re-assembles a system only
+    # when its flag says the other field changed (_phasefield.py:248-269); the
+    # damage solve clears the displacement flag and the elastic solve the
+    # damage flag (:366-374).  The energy criteria (convOption 1, 2) read the
+    # systems through the same flags, which decides which displacement the
+    # History field is computed from when Save_Iter commits it.
+    def _kd(self):
+        if not getattr(self, "_upd_d", False) or self.Kd is None:
+            self.damage_system()
+            self._upd_d = True
+        return self.Kd
+
+    def _ku(self):
+        if not getattr(self, "_upd_u", False) or self.Ku is None:
+            self.elastic_system()
+            self._upd_u = True
+        return self.Ku
+
     def solve_damage(self):
-        Kd, Fd = self.damage_system()
+        Kd, Fd = self._kd(), self.Fd
         dk, dv = dirichlet(self.mesh, self.dir_d, 1)
         self.d = fem.solve_r1(Kd, Fd, dk, dv)
         return self.d
 
     def solve_elastic(self):
-        Ku = self.elastic_system()
+        Ku = self._ku()
         b = np.zeros(self.mesh.Nn * self.dim)
         dk, dv = dirichlet(self.mesh, self.dir_u, self.dim)
         self.u = fem.solve_r1(Ku, b, dk, dv)
         return self.u
 
+    def psi_crack(self):
+        """_Calc_Psi_Crack, _phasefield.py:799-817: 1/2 d.Kd d."""
+        Kd = self._kd()
+        return 0.0 if np.linalg.norm(self.d) == 0 else 0.5 * self.d @ (Kd @ self.d)
+
+    def psi_elas(self):
+        """_Calc_Psi_Elas, _phasefield.py:775-797: 1/2 u.Ku u."""
+        Ku = self._ku()
+        return 0.0 if np.linalg.norm(self.u) == 0 else 0.5 * self.u @ (Ku @ self.u)
+
     def solve(self, tolConv=1.0, maxIter=500, convOption=0):
-        """Staggered loop, _phasefield.py:303-432 (convOption 0 only)."""
-        assert convOption == 0
+        """Staggered loop, _phasefield.py:303-432 (no external forces: the work
+        of f_u in convOption 2 is zero)."""
+        assert convOption in (0, 1, 2, 3)
         Niter = 0
         converged = False
+        convIter = 0.0
         while not converged and Niter < maxIter:
             Niter += 1
             d_n = self.d.copy()
+            u_n = self.u.copy()
+            if convOption == 1:
+                E_n = self.psi_crack()
+            elif convOption == 2:
+                E_n = self.psi_crack() + self.psi_elas()
             d_np1 = self.solve_damage()
-            self.solve_elastic()
-            convIter = np.max(np.abs(d_np1 - d_n))
+            self._upd_u = False
+            u_np1 = self.solve_elastic()
+            self._upd_d = False
+            if convOption == 0:
+                convIter = np.max(np.abs(d_np1 - d_n))
+            elif convOption in (1, 2):
+                E_np1 = self.psi_crack()
+                if convOption == 2:
+                    E_np1 += self.psi_elas()
+                convIter = abs(E_n - E_np1) if E_np1 == 0 else abs((E_n - E_np1) / E_np1)
+            else:
+                diffU = np.abs(u_np1 - u_n)
+                diffU[u_np1 != 0] *= 1 / np.abs(u_np1[u_np1 != 0])
+                diffD = np.abs(d_np1 - d_n)
+                diffD[d_np1 != 0] *= 1 / np.abs(d_np1[d_np1 != 0])
+                convU, convD = np.sum(diffU), np.sum(diffD)
+                convIter = max(convD, convU)
             if tolConv == 1 or d_np1.max() == 0:
                 converged = True
+            elif convOption == 3:
+                converged = (convD <= tolConv) and (convU <= tolConv * 0.999)
             else:
                 converged = convIter <= tolConv
         self.Niter = Niter
+        self.convIter = convIter
         return self.u, self.d, converged
 
     def save_iter(self):
@@ -208,4 +261,4 @@ class PhaseFieldOracle:
 
     def reaction(self, dofs):
         """Calc_Reaction, _simu.py:212-260: Ku[dofs] @ u."""
-        return self.Ku[dofs] @ self.u
+        return self._ku()[dofs] @ self.u

@@ -2,7 +2,9 @@
 
 Run in a container where matnoel/EasyFEA's sources are importable::
 
-    python tests/golden/make_golden.py [/root/reference] [--only=name,...]
+    python tests/golden/make_golden.py <path to EasyFEA sources> [--only=name,...]
+
+The path may instead come from the ``EASYFEA_REFERENCE`` environment variable.
 
 gmsh (imported unconditionally by EasyFEA/FEM/_mesher.py:13) is replaced by an
 empty stub module; meshes come from ``easyfea_gb300.mesh``'s organised
@@ -162,6 +164,105 @@ def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, 
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
 
 
+def pf_conv_case(R, name, m, convOption, steps, dU, out, tol=1e-3, maxIter=100):
+    """Staggered loop of the reference with convergence criterion ``convOption``
+    (1: crack energy, 2: total energy, 3: summed relative increments;
+    Simulations/_phasefield.py:347-405) on a small notched TRI3 plate, through
+    fracture: force, iterations, convergence measure, u and d per step."""
+    dim = m.dim
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=210000.0, v=0.3, planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.1)
+    simu = R.Simulations.PhaseField(rm, pfm)
+    simu.solver = R.SolverType.scipy
+    H = m.coord[:, 1].max()
+    bottom = rm.Nodes_Conditions(lambda x, y, z: y == 0)
+    top = rm.Nodes_Conditions(lambda x, y, z: y == H)
+    notch = rm.Nodes_Conditions(lambda x, y, z: (np.abs(y - H / 2) < 1e-12) & (x <= 0.5 * m.coord[:, 0].max()))
+    top_dofs = simu.Bc_dofs_nodes(top, ["y"])
+    us, ds, Fs, its, convs = [], [], [], [], []
+    for k in range(1, steps + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(notch, [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(bottom, [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(top, [0.0, k * dU], ["x", "y"])
+        u, d, conv = simu.Solve(tol, maxIter, convOption=convOption)
+        simu.Save_Iter()
+        f = np.sum(simu.Calc_Reaction(top_dofs, simu.ProblemTypes.elastic))
+        us.append(u.copy()); ds.append(d.copy()); Fs.append(f)
+        its.append(simu._PhaseField__Niter)
+        convs.append(float(simu._PhaseField__convIter))
+        print(name, "step", k, "F", f, "dmax", d.max(), "Niter", its[-1], "conv", convs[-1])
+    res = dict(mesh_arrays(m), split="Miehe", regu="AT2", planeStress=False, E=210000.0, v=0.3,
+               Gc=2.7, l0=0.1, dU=dU, tol=tol, maxIter=maxIter, convOption=convOption,
+               u=np.array(us), d=np.array(ds), F=np.array(Fs), Niter=np.array(its),
+               convIter=np.array(convs), bottom=bottom, top=top, notch=notch, top_dofs=top_dofs)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+
+
+def _pf_conv_cases(R, out):
+    m = gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16)
+    for opt in (1, 2, 3):
+        pf_conv_case(R, f"pf_tri3_conv{opt}", m, opt, 4, 4e-3, out)
+
+
+def pf_curve_case(R, out, steps=600, dU=1e-5, tol=1e-3, maxIter=500, keep_every=50):
+    """The notched-plate benchmark through its whole load history: 200x200 squares
+    of the unit plate split into 80,000 TRI3, AT2, Miehe split, E = 210000,
+    nu = 0.3, Gc = 2.7, l0 = 0.01, plane strain, d = 1 imposed on the notch
+    (y = 0.5, x <= 0.5), bottom clamped, top uy = k dU for k = 1..steps,
+    ``Solve(tol, maxIter, convOption=0)`` and ``Save_Iter`` per step (the load
+    loop of examples/PhaseField/Shear.py:182-220 with this plate's conditions).
+    Stores per step the top reaction F, staggered iterations, convergence flag
+    and max d, plus the damage field every ``keep_every`` steps, at the force
+    peak and at the last step.  A partial file is rewritten every 10 steps."""
+    name = "pf_curve_tri3_200x200"
+    m = gmesh.Mesh_Tri3_Rect(1.0, 1.0, 200, 200)
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.01)
+    simu = R.Simulations.PhaseField(rm, pfm)
+    simu.solver = R.SolverType.scipy
+    bottom = rm.Nodes_Conditions(lambda x, y, z: y == 0)
+    top = rm.Nodes_Conditions(lambda x, y, z: y == 1.0)
+    notch = rm.Nodes_Conditions(lambda x, y, z: (np.abs(y - 0.5) < 1e-12) & (x <= 0.5))
+    top_dofs = simu.Bc_dofs_nodes(top, ["y"])
+    Fs, its, convd, dmax, secs = [], [], [], [], []
+    kept = {}      # step -> damage field
+    peak = None    # (step, damage) at the running force maximum
+    import time
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        ts = time.perf_counter()
+        simu.Bc_Init()
+        simu.add_dirichlet(notch, [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(bottom, [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(top, [0.0, k * dU], ["x", "y"])
+        u, d, conv = simu.Solve(tol, maxIter, convOption=0)
+        simu.Save_Iter()
+        f = float(np.sum(simu.Calc_Reaction(top_dofs, simu.ProblemTypes.elastic)))
+        if not Fs or f >= max(Fs):
+            peak = (k, d.copy())
+        Fs.append(f); its.append(simu._PhaseField__Niter); convd.append(bool(conv))
+        dmax.append(float(d.max())); secs.append(time.perf_counter() - ts)
+        if k % keep_every == 0 or k == steps:
+            kept[k] = d.copy()
+        print(name, "step", k, "F", f, "dmax", dmax[-1], "Niter", its[-1],
+              f"{secs[-1]:.1f}s total {time.perf_counter() - t0:.0f}s", flush=True)
+        if k % 10 == 0 or k == steps:
+            allk = dict(kept)
+            allk[peak[0]] = peak[1]
+            ks = sorted(allk)
+            res = dict(mesh_arrays(m), split="Miehe", regu="AT2", planeStress=False, E=210000.0,
+                       v=0.3, Gc=2.7, l0=0.01, dU=dU, tol=tol, maxIter=maxIter, convOption=0,
+                       F=np.array(Fs), Niter=np.array(its, np.int32), converged=np.array(convd),
+                       dmax=np.array(dmax), ref_seconds=np.array(secs),
+                       d_steps=np.array(ks, np.int32), d=np.array([allk[j] for j in ks]),
+                       bottom=bottom, top=top, notch=notch, top_dofs=top_dofs)
+            fn = f"{name}.npz" if k == steps else f"{name}.partial.npz"
+            np.savez_compressed(os.path.join(out, fn), **res)
+
+
 def pf_state_case(R, name, m, split, regu, out, seed=7):
     """Kd, Fd, Ku of the reference at a prescribed (u, d, committed history) state:
     pins r/f/k of both regularisations and the degraded stiffness without the
@@ -199,7 +300,10 @@ def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
     only = set(only[0]) if only else None
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("EASYFEA_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <path to EasyFEA sources> [--only=name,...] "
+                 "(or set EASYFEA_REFERENCE)")
     R = load_reference(ref)
     if only is not None:  # regenerate the named fixtures only
         for name, fn in CASES.items():
@@ -249,7 +353,8 @@ def _el_hexa8_hetero(R, out):
 
 
 # fixtures that can be regenerated alone (--only=name,...)
-CASES = {"el_hexa8_hetero": _el_hexa8_hetero}
+CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases,
+         "pf_curve_tri3_200x200": pf_curve_case}
 
 
 if __name__ == "__main__":

@@ -63,3 +63,27 @@ def test_staggered_loop_matches_reference(golden, case):
         # displacements: 1e-5 of max|u| (after full fracture the degraded system
         # is ill conditioned and the reference's direct solve itself moves at 1e-8)
         assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-5 * np.abs(g["u"][k - 1]).max(), f"step {k}"
+
+
+@pytest.mark.parametrize("opt", [1, 2, 3])
+def test_convergence_options_match_reference(golden, opt):
+    """Staggered loop with convOption 1 (crack energy), 2 (total energy) and 3
+    (summed relative increments) through fracture, against the reference's
+    own runs (EasyFEA/Simulations/_phasefield.py:347-405): the energy criteria
+    read the systems through the reference's lazy re-assembly, which decides
+    the displacement the committed History field comes from."""
+    g = golden(f"pf_tri3_conv{opt}")
+    m, simu = make_simu(g)
+    top_dofs = torch.as_tensor(g["top_dofs"], device="cuda")
+    for k in range(1, g["u"].shape[0] + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(g["notch"], [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(g["bottom"], [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(g["top"], [0.0, k * float(g["dU"])], ["x", "y"])
+        u, d, conv = simu.Solve(float(g["tol"]), int(g["maxIter"]), convOption=opt)
+        simu.Save_Iter()
+        F = simu.reaction_sum(top_dofs)
+        assert simu.Niter == g["Niter"][k - 1], f"step {k}: {simu.Niter} staggered iterations, reference {g['Niter'][k - 1]}"
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"
+        assert np.max(np.abs(d - g["d"][k - 1])) <= 1e-6, f"step {k}"
+        assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-5 * np.abs(g["u"][k - 1]).max(), f"step {k}"

@@ -131,6 +131,27 @@ def test_phasefield_oracle_matches_reference(golden, case):
     np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-7, atol=1e-12 * np.abs(g["Fd"]).max())
 
 
+@pytest.mark.parametrize("opt", [1, 2, 3])
+def test_phasefield_oracle_convergence_options_match_reference(golden, opt):
+    """convOption 1 (crack energy), 2 (total energy), 3 (summed relative
+    increments) through fracture on the 16x16 TRI3 plate."""
+    g = golden(f"pf_tri3_conv{opt}")
+    m = om(g)
+    pf = PhaseFieldOracle(m, float(g["E"]), float(g["v"]), bool(g["planeStress"]), 1.0,
+                          str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    for k in range(1, g["u"].shape[0] + 1):
+        pf.dir_d = [(g["notch"], [1.0], ["d"])]
+        pf.dir_u = [(g["bottom"], [0.0, 0.0], ["x", "y"]), (g["top"], [0.0, k * float(g["dU"])], ["x", "y"])]
+        u, d, conv = pf.solve(float(g["tol"]), int(g["maxIter"]), opt)
+        pf.save_iter()
+        F = np.sum(pf.reaction(g["top_dofs"]))
+        assert pf.Niter == g["Niter"][k - 1], (k, pf.Niter, g["Niter"][k - 1])
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), (k, F, g["F"][k - 1])
+        assert np.max(np.abs(d - g["d"][k - 1])) <= 1e-8
+        assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-8 * np.abs(g["u"][k - 1]).max()
+        assert abs(pf.convIter - g["convIter"][k - 1]) <= 1e-6 * abs(g["convIter"][k - 1])
+
+
 @pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2"])
 def test_phasefield_state_systems_match_reference(golden, case):
     g = golden(case)

@@ -26,8 +26,9 @@ Reported beside it, on the same requests:
 ``value`` is the served solves/s with solutions left on the device; ``e2e``
 replays the stream reading every solution back to pinned host memory.
 ``--impl reference`` times the CPU oracle (a numpy/scipy restatement of the
-reference's path) on small samples of each request kind and extrapolates to
-the stream by DOF.
+reference's path) solving the stream's own requests on all host cores, one
+single-threaded process per core (the requests too slow for one step's budget
+are excluded and listed).
 """
 
 from __future__ import annotations
@@ -72,77 +73,145 @@ def parse():
 
 
 # --------------------------------------------------------------------------
-# CPU oracle samples (reference arm and cpu_baseline)
+# CPU reference arm and cpu_baseline: the oracle timed on the stream's own
+# requests
 # --------------------------------------------------------------------------
 
-def _oracle_elastic(spec):
+# Requests the CPU runs within one step's time budget: every 2D elastic solve
+# up to 150k DOF, phase-field load steps on plates up to 80,000 elements and
+# HEXA8 solves up to 15k DOF (a 36.7k-DOF HEXA8 solve takes ~30 s in SuperLU,
+# a 500k-DOF 2D one ~20 s, a step of the 320,000-element plate ~40 s); the
+# others are reported as excluded and never counted in the value.
+REF_MAX_DOF = {"quad4": 150_000, "quad9": 150_000, "hexa8": 15_000, "tri3_sen": 81_000}
+
+_REF = {}  # per worker process: spec -> (OracleMesh, node sets) and phase-field sessions
+
+
+def _ref_spec(desc):
+    from easyfea_gb300 import serving
+
+    return serving.MeshSpec(*desc[1])
+
+
+def _ref_init(descs):
+    """Pool initializer: single-threaded numpy/BLAS, and every mesh of the
+    sample built once (the GPU arm's meshes are resident too)."""
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
     import numpy as np
 
-    from oracle.simulate import OracleMesh, elastic_solve
+    from oracle.simulate import OracleMesh
 
-    m = spec.build()
-    om = OracleMesh.from_mesh(m)
-    x = m.coord
-    left = np.where(x[:, 0] == 0)[0]
-    right = np.where(x[:, 0] == x[:, 0].max())[0]
+    for desc in descs:
+        spec = _ref_spec(desc)
+        if spec in _REF:
+            continue
+        m = spec.build()
+        x = m.coord
+        _REF[spec] = (OracleMesh.from_mesh(m), x)
+    _ = np  # noqa: F841
+
+
+def _ref_run(desc):
+    """One request of the stream on the oracle; returns its seconds."""
+    import numpy as np
+
+    from oracle.simulate import PhaseFieldOracle, elastic_solve
+
+    kind = desc[0]
+    spec = _ref_spec(desc)
+    om, x = _REF[spec]
     t0 = time.perf_counter()
-    if spec.dim == 2:
-        u, _, _ = elastic_solve(om, 210000.0, 0.3, True, 13.0, [(left, [0.0, 0.0], ["x", "y"])],
-                                [(right, [-800 / 13**2], ["y"])])
+    if kind == "phasefield":
+        key = ("pf", spec)
+        if key not in _REF:
+            pf = PhaseFieldOracle(om, 210e3, 0.3, False, 1.0, "Miehe", "AT2", 2.7, 0.01)
+            pf.dir_d = [(np.where((np.abs(x[:, 1] - 0.5) < 1e-12) & (x[:, 0] <= 0.5))[0], [1.0], ["d"])]
+            _REF[key] = [pf, 0]
+        sess = _REF[key]
+        sess[1] += 1
+        pf = sess[0]
+        pf.dir_u = [(np.where(x[:, 1] == 0)[0], [0.0, 0.0], ["x", "y"]),
+                    (np.where(x[:, 1] == 1.0)[0], [0.0, sess[1] * 1e-5], ["x", "y"])]
+        pf.solve(1e-3, 500, 0)
+        pf.save_iter()
     else:
-        u, _, _ = elastic_solve(om, 210000.0, 0.3, False, 1.0, [(left, [0.0, 0.0, 0.0], ["x", "y", "z"])],
-                                [(right, [-1.0], ["z"])])
-    dt = time.perf_counter() - t0
-    assert np.isfinite(u).all()
-    return dt
-
-
-def _oracle_pf_step(spec, step=1, dU=1e-5):
-    import numpy as np
-
-    from oracle.simulate import OracleMesh, PhaseFieldOracle
-
-    m = spec.build()
-    om = OracleMesh.from_mesh(m)
-    x = m.coord
-    pf = PhaseFieldOracle(om, 210e3, 0.3, False, 1.0, "Miehe", "AT2", 2.7, 0.01)
-    notch = np.where((np.abs(x[:, 1] - 0.5) < 1e-12) & (x[:, 0] <= 0.5))[0]
-    pf.dir_d = [(notch, [1.0], ["d"])]
-    pf.dir_u = [(np.where(x[:, 1] == 0)[0], [0.0, 0.0], ["x", "y"]),
-                (np.where(x[:, 1] == 1.0)[0], [0.0, step * dU], ["x", "y"])]
-    t0 = time.perf_counter()
-    pf.solve(1e-3, 500, 0)
-    pf.save_iter()
+        left = np.where(x[:, 0] == 0)[0]
+        right = np.where(x[:, 0] == x[:, 0].max())[0]
+        if spec.dim == 2:
+            u, _, _ = elastic_solve(om, 210000.0, 0.3, True, 13.0, [(left, [0.0, 0.0], ["x", "y"])],
+                                    [(right, [-800 / 13**2], ["y"])])
+        else:
+            u, _, _ = elastic_solve(om, 210000.0, 0.3, False, 1.0, [(left, [0.0, 0.0, 0.0], ["x", "y", "z"])],
+                                    [(right, [-1.0], ["z"])])
+        assert np.isfinite(u).all()
     return time.perf_counter() - t0
 
 
-def oracle_rates(budget_s=12.0):
-    """Seconds per DOF of the oracle for each request kind, from small
-    samples (about budget_s of CPU work in total)."""
+def _ref_desc(r):
+    s = r.spec
+    return ("phasefield" if r.kind == "phasefield" else "elastic", (s.kind, s.nx, s.ny, s.nz))
+
+
+def reference_sample(reqs):
+    """(descriptors of the stream requests the CPU runs, summary of the excluded ones)."""
+    run, excl = [], {}
+    for r in reqs:
+        if r.spec.dof <= REF_MAX_DOF[r.spec.kind]:
+            run.append(_ref_desc(r))
+        else:
+            k = f"{r.spec.kind} {r.spec.dof} DOF"
+            excl[k] = excl.get(k, 0) + 1
+    return run, excl
+
+
+def reference_measure(pool, sample, cores, steps, warmup):
+    """Solves/s of the oracle on the stream's requests: step k runs the next
+    ``cores`` requests of the sample (stream order, cyclic) at once, one per
+    worker process; value = requests / summed wall time of the timed steps."""
+    smallest = min(sample, key=lambda d: _ref_spec(d).dof)
+    for _ in range(warmup):
+        pool.map(_ref_run, [smallest] * cores)
+    pos, n_done, wall, cpu = 0, 0, 0.0, 0.0
+    for _ in range(steps):
+        chunk = [sample[(pos + i) % len(sample)] for i in range(cores)]
+        pos += cores
+        t0 = time.perf_counter()
+        secs = pool.map(_ref_run, chunk)
+        wall += time.perf_counter() - t0
+        cpu += sum(secs)
+        n_done += len(chunk)
+    return n_done / wall, wall, n_done, cpu
+
+
+def reference_line(args, steps, warmup):
+    """Runs the measurement on all host cores; returns (value, cpu_baseline dict, wall seconds)."""
     from easyfea_gb300 import serving
 
-    samples = {"quad4": serving.cantilever_spec("quad4", 8e3), "quad9": serving.cantilever_spec("quad9", 8e3),
-               "hexa8": serving.box_spec(2e4), "phasefield": serving.MeshSpec("tri3_sen", 40, 40)}
-    rates, desc = {}, []
-    t_end = time.perf_counter() + budget_s
-    for kind, spec in samples.items():
-        times = []
-        while not times or (time.perf_counter() < t_end - budget_s * 0.6 and len(times) < 3):
-            times.append(_oracle_pf_step(spec) if kind == "phasefield" else _oracle_elastic(spec))
-        t = statistics.median(times)
-        rates[kind] = t / spec.dof
-        desc.append(f"{kind} {spec.dof} DOF {t:.2f} s")
-    return rates, "; ".join(desc)
+    import multiprocessing as mp
 
-
-def oracle_stream_value(reqs, rates):
-    """Stream solves/s of the oracle, extrapolated linearly in DOF from the
-    samples (favours the CPU: a direct solve grows faster than linearly)."""
-    total = 0.0
-    for r in reqs:
-        kind = "phasefield" if r.kind == "phasefield" else r.spec.kind
-        total += rates[kind] * r.spec.dof
-    return len(reqs) / total
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+    cores = max(1, os.cpu_count() or 1)
+    _, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
+    sample, excl = reference_sample(reqs)
+    with mp.get_context("spawn").Pool(cores, initializer=_ref_init, initargs=(sorted(set(sample)),)) as pool:
+        value, wall, n_done, cpu = reference_measure(pool, sample, cores, steps, warmup)
+    base = {
+        "value": value, "unit": UNIT, "cores": cores, "kind": "port",
+        "sample": (f"oracle (numpy/scipy restatement of EasyFEA's path: einsum element matrices, bincount "
+                   f"assembly, SuperLU spsolve, staggered phase field) solving the stream's own requests, "
+                   f"{cores} at a time (one single-threaded process per host core): {n_done} requests in "
+                   f"{wall:.1f} s of wall time ({cpu:.1f} core-s); meshes prebuilt, phase-field sessions "
+                   f"resident and advanced one load step per request"),
+        "requests_in_sample": len(sample),
+        "excluded": {"requests": sum(excl.values()), "classes": excl,
+                     "why": "too slow for one step's budget on one core (a single solve of 20-40 s or more; "
+                            "the 2M-DOF box does not fit a direct solve); they are the stream's most "
+                            "expensive requests, so the value overstates the CPU's throughput on the full "
+                            "stream"},
+    }
+    return value, base, wall
 
 
 def cpu_threads():
@@ -154,52 +223,17 @@ def cpu_threads():
         return 1
 
 
-def _reference_worker(budget_s):
-    return oracle_rates(budget_s=budget_s)
-
-
-def reference_rates_all_cores(pool, workers, budget_s):
-    """Per-kind seconds per DOF of the oracle with one worker process per
-    host core, all timing their samples at once (so the rates include the
-    contention of a fully loaded host); the median over workers."""
-    results = pool.map(_reference_worker, [budget_s] * workers)
-    rates = {k: statistics.median(r[0][k] for r in results) for k in results[0][0]}
-    return rates, results[0][1]
-
-
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from easyfea_gb300 import serving
-
-    # the requests are independent: the host serves one per core, each
-    # oracle single-threaded (its BLAS included)
-    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[var] = "1"
-    import multiprocessing as mp
-
-    workers = max(1, os.cpu_count() or 1)
-    _, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
-    values, descs = [], []
-    with mp.get_context("spawn").Pool(workers) as pool:
-        for _ in range(args.warmup):
-            reference_rates_all_cores(pool, workers, 1.0)
-        for _ in range(args.steps):
-            rates, desc = reference_rates_all_cores(pool, workers, 4.0)
-            values.append(workers * oracle_stream_value(reqs, rates))
-            descs.append(desc)
-    value = statistics.median(values)
-    sample = (f"oracle (numpy/scipy restatement of EasyFEA's path: einsum element matrices, bincount assembly, "
-              f"SuperLU spsolve, staggered phase field) on one small request per kind ({descs[-1]}), "
-              f"{workers} worker processes at once, one per host core; stream time = sum over the "
-              f"{args.requests} requests of DOF x seconds-per-DOF of their kind, divided by {workers}")
+    value, base, wall = reference_line(args, args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.requests / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"serving_stream_poisson_{args.rate:g}rps_{args.requests}req_seed{SEED}"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample},
+        "cpu_baseline": base,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -589,12 +623,9 @@ def main():
         }
     line.update(extras)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rates, desc = oracle_rates(budget_s=12.0)
-        line["cpu_baseline"] = {
-            "value": oracle_stream_value(reqs, rates), "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-            "sample": f"oracle on one small request per kind ({desc}); stream time = sum of DOF x "
-                      f"seconds-per-DOF of each request's kind (linear in DOF, favours the CPU)",
-        }
+        # the reference arm's measurement, bounded: 2 steps of one request per host core
+        _, base, _ = reference_line(args, 2, 1)
+        line["cpu_baseline"] = base
     if rank == 0:
         print(json.dumps(line), flush=True)
     replicas.finish()

@@ -1,6 +1,7 @@
 """bench.py's reference arm (CPU only): one JSON line with the GPU arm's
-metric, unit and direction, the oracle timed with one worker process per
-host core, and no host<->device bytes."""
+metric, unit and direction, the oracle timed solving the stream's own
+requests with one worker process per host core (the excluded requests
+listed), and no host<->device bytes."""
 
 import json
 import os
@@ -29,6 +30,12 @@ def test_reference_arm_line():
     assert cb["cores"] == (os.cpu_count() or 1)
     assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("serving_stream_poisson")
+    # measured, not extrapolated: the timed requests and the wall time that
+    # gives the value are in the line, and the step time covers them
+    assert cb["requests_in_sample"] > 0
+    assert sum(cb["excluded"]["classes"].values()) == cb["excluded"]["requests"]
+    assert cb["requests_in_sample"] + cb["excluded"]["requests"] == 60
+    assert abs(d["ms_per_step"] * d["steps"] / 1000.0 - (os.cpu_count() or 1) / d["value"]) < 1e-6 * d["ms_per_step"]
 
 
 def test_non_zero_rank_prints_nothing():

@@ -183,26 +183,54 @@ class _Simu:
         self._neumann[problemType].append(_BC(problemType, nodes, dofs, vals.ravel(), unknowns, description))
 
     def _integrate_load(self, nodes, values, unknowns, problemType, factor, bdim):
+        """Boundary integral of a traction (EasyFEA/Simulations/_simu.py:2770-2842):
+        constants and functions of (x, y, z) at the mass Gauss points of the
+        boundary elements whose nodes all belong to ``nodes``; an array of one
+        value per node of ``nodes`` integrated as value(node) x integral of N_node."""
         problemType = self._check_pt(problemType)
-        for v in values:
-            if callable(v) or np.ndim(v) > 0:
-                raise NotImplementedError("surface / line loads take constant values on the GPU path")
         L = _lib.load()
         avail = self.Get_unknowns(problemType)
-        uidx = (ctypes_int32 * len(unknowns))(*[avail.index(u) for u in unknowns])
-        uval = (ctypes_double * len(unknowns))(*[float(v) for v in values])
+        nodes = np.asarray(nodes, dtype=np.int64)
         mask = torch.zeros(self.mesh.Nn, dtype=torch.uint8, device=_dev())
-        mask[torch.as_tensor(np.asarray(nodes, dtype=np.int64), device=_dev())] = 1
+        mask[torch.as_tensor(nodes, device=_dev())] = 1
         b = self._neumann_vec(problemType)
         groups = [g for g in self.dmesh.boundary if g.dim == bdim]
         if bdim == self.dim:
             groups = [self.dmesh.main]
-        for g in groups:
-            _lib.check(L.gfea_surface_load(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect), g.Ne,
-                                           _lib.ptr(mask), len(avail), len(unknowns), uidx, uval, float(factor),
-                                           _lib.ptr(b), _lib.stream()), "surface load")
-        self._neumann[problemType].append(_BC(problemType, np.asarray(nodes), None, np.asarray(values, float),
-                                              unknowns, "load"))
+        const = [i for i, v in enumerate(values) if isinstance(v, (int, float)) and not callable(v)]
+        if const:
+            uidx = (ctypes_int32 * len(const))(*[avail.index(unknowns[i]) for i in const])
+            uval = (ctypes_double * len(const))(*[float(values[i]) for i in const])
+            for g in groups:
+                _lib.check(L.gfea_surface_load(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect), g.Ne,
+                                               _lib.ptr(mask), len(avail), len(const), uidx, uval, float(factor),
+                                               _lib.ptr(b), _lib.stream()), "surface load")
+        for i, v in enumerate(values):
+            if i in const:
+                continue
+            ui = avail.index(unknowns[i])
+            for g in groups:
+                if g.Ne == 0:
+                    continue
+                if callable(v):
+                    npg = ctypes_int32()
+                    xyz = torch.empty((g.Ne, 8, 3), dtype=torch.float64, device=_dev())
+                    _lib.check(L.gfea_boundary_gauss_points(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect),
+                                                            g.Ne, _lib.ptr(xyz), __import__("ctypes").byref(npg),
+                                                            _lib.stream()), "gauss points")
+                    pts = xyz.view(-1)[:g.Ne * npg.value * 3].view(g.Ne, npg.value, 3).cpu().numpy()
+                    f = np.asarray(v(pts[:, :, 0], pts[:, :, 1], pts[:, :, 2]), dtype=np.float64)
+                    f = np.array(np.broadcast_to(f, (g.Ne, npg.value)), dtype=np.float64)
+                    vals, mode = torch.as_tensor(f, device=_dev()), 0
+                else:
+                    arr = np.asarray(v, dtype=np.float64)
+                    full = np.zeros(self.mesh.Nn)
+                    full[nodes] = arr
+                    vals, mode = torch.as_tensor(full, device=_dev()), 1
+                _lib.check(L.gfea_surface_load_field(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect), g.Ne,
+                                                     _lib.ptr(mask), len(avail), ui, mode, _lib.ptr(vals),
+                                                     float(factor), _lib.ptr(b), _lib.stream()), "surface load")
+        self._neumann[problemType].append(_BC(problemType, nodes, None, None, unknowns, "load"))
 
     def add_surfLoad(self, nodes, values: list, unknowns: list, problemType=None, description="") -> None:
         """Surface load: lines x thickness in 2D, faces in 3D (EasyFEA/Simulations/_simu.py:2572-2630)."""
@@ -504,6 +532,20 @@ class PhaseField(_Simu):
     @property
     def psiP_device(self) -> Optional[torch.Tensor]:
         return self.__psiP
+
+    def set_history(self, H: Optional[np.ndarray]) -> None:
+        """Replace the committed History field (psi+ at the mass Gauss points,
+        (Ne, nPg) or flat); None clears it, as before the first Save_Iter.
+        The damage system is re-assembled at its next use."""
+        self.__updatedDamage = False
+        if H is None:
+            self.__psiP_old = None
+            return
+        h = torch.as_tensor(np.ascontiguousarray(H, dtype=np.float64).ravel(), device=_dev())
+        if self.__psiP_old is not None and self.__psiP_old.numel() == h.numel():
+            self.__psiP_old.copy_(h)
+        else:
+            self.__psiP_old = h.clone()
 
     def _params(self) -> _lib.PfParams:
         m = self.phaseFieldModel

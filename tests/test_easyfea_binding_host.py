@@ -1,0 +1,67 @@
+"""The EasyFEA subclasses (easyfea_gb300/easyfea_binding.py) on the host:
+class hierarchy, mesh conversion and the models they reject (no GPU call).
+Skipped when EasyFEA is not installed (EASYFEA_PATH, else baseline/_ref)."""
+
+import os
+import sys
+import types
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def ref():
+    path = os.environ.get("EASYFEA_PATH") or os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(path, "EasyFEA")):
+        pytest.skip("EasyFEA is not installed")
+    try:
+        import gmsh  # noqa: F401
+    except ImportError:
+        sys.modules["gmsh"] = types.ModuleType("gmsh")
+    if path not in sys.path:
+        sys.path.insert(0, path)
+    from EasyFEA import Models, Simulations
+    from EasyFEA.FEM._group_elem import GroupElemFactory
+    from EasyFEA.FEM._mesh import Mesh
+    from EasyFEA.FEM._utils import ElemType
+
+    from easyfea_gb300 import easyfea_binding
+
+    return types.SimpleNamespace(Models=Models, Simulations=Simulations, GEF=GroupElemFactory, Mesh=Mesh,
+                                 ElemType=ElemType, B=easyfea_binding)
+
+
+def _mesh(R, g):
+    coord = np.asarray(g["coord"], float)
+    return R.Mesh({getattr(R.ElemType, str(g["belem"])): R.GEF.Create(getattr(R.ElemType, str(g["belem"])),
+                                                                       g["bconnect"].astype(np.int64), coord.copy()),
+                   getattr(R.ElemType, str(g["elem"])): R.GEF.Create(getattr(R.ElemType, str(g["elem"])),
+                                                                      g["connect"].astype(np.int64), coord.copy())})
+
+
+def test_subclasses_and_mesh_conversion(ref, golden):
+    R = ref
+    assert issubclass(R.B.GpuElastic, R.Simulations.Elastic)
+    assert issubclass(R.B.GpuPhaseField, R.Simulations.PhaseField)
+    g = golden("el_quad4")
+    mesh = _mesh(R, g)
+    m = R.B.to_gpu_mesh(mesh)
+    assert m.Nn == mesh.Nn and m.dim == 2
+    assert {e.value for e in m.dict_groupElem} == {"SEG2", "QUAD4"}
+    np.testing.assert_array_equal(m.groupElem.connect, mesh.groupElem.connect)
+    simu = R.B.GpuElastic(mesh, R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=True, thickness=13.0))
+    assert simu.dim == 2 and simu.rho == 1.0
+
+
+def test_unsupported_models_rejected(ref, golden):
+    R = ref
+    mesh = _mesh(R, golden("el_quad4"))
+    mat = R.Models.Elastic.TransverselyIsotropic(2, El=1e5, Et=1e4, Gl=1e4, vl=0.3, vt=0.2)
+    with pytest.raises(NotImplementedError):
+        R.B.GpuElastic(mesh, mat)
+    iso = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False)
+    with pytest.raises(NotImplementedError):
+        R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, "He", "AT2", 2.7, 0.01))

@@ -1,0 +1,123 @@
+"""The drop-in inside EasyFEA itself: the reference's own Mesh, Models,
+boundary-condition calls and Solve() loop, with ``GpuElastic`` /
+``GpuPhaseField`` (easyfea_gb300/easyfea_binding.py) in place of
+``Simulations.Elastic`` / ``Simulations.PhaseField``, against the fixtures the
+reference produced.
+
+EasyFEA is imported from an install of it (``EASYFEA_PATH``, else
+``baseline/_ref`` in this repository); gmsh, which it imports at start-up,
+is replaced by an empty module when absent (no mesher is used: meshes are
+built from the fixtures' arrays with GroupElemFactory + Mesh).
+"""
+
+import os
+import sys
+import types
+
+import numpy as np
+import pytest
+
+from helpers import csr, row_scaled_err, same_pattern
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def ref():
+    path = os.environ.get("EASYFEA_PATH") or os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(path, "EasyFEA")):
+        pytest.skip("EasyFEA is not installed (set EASYFEA_PATH or install it into baseline/_ref)")
+    try:
+        import gmsh  # noqa: F401
+    except ImportError:
+        sys.modules["gmsh"] = types.ModuleType("gmsh")
+    if path not in sys.path:
+        sys.path.insert(0, path)
+    import EasyFEA  # noqa: F401
+    from EasyFEA import Models, Simulations
+    from EasyFEA.FEM._group_elem import GroupElemFactory
+    from EasyFEA.FEM._mesh import Mesh
+    from EasyFEA.FEM._utils import ElemType
+
+    from easyfea_gb300 import easyfea_binding
+
+    assert issubclass(easyfea_binding.GpuElastic, Simulations.Elastic)
+    assert issubclass(easyfea_binding.GpuPhaseField, Simulations.PhaseField)
+    return types.SimpleNamespace(Models=Models, Simulations=Simulations, GEF=GroupElemFactory, Mesh=Mesh,
+                                 ElemType=ElemType, B=easyfea_binding)
+
+
+def ref_mesh(R, g):
+    coord = np.asarray(g["coord"], dtype=float)
+    groups = {}
+    for e, c in ((str(g["belem"]), g["bconnect"]), (str(g["elem"]), g["connect"])):
+        et = getattr(R.ElemType, e)
+        groups[et] = R.GEF.Create(et, np.asarray(c, dtype=np.int64), coord.copy())
+    return R.Mesh(groups)
+
+
+@pytest.mark.parametrize("case", ["el_cantilever_240x26", "el_quad4_hetero", "el_hexa8"])
+def test_gpu_elastic_inside_easyfea(ref, golden, case):
+    """EasyFEA's Elastic.Solve() on the GPU subclass: u within 1e-8 of the
+    reference's direct solve, K and M within 1e-12 (row-scaled) with the
+    reference's CSR pattern, reactions through the reference's Calc_Reaction."""
+    g = golden(case)
+    R = ref
+    mesh = ref_mesh(R, g)
+    dim = mesh.dim
+    E = np.asarray(g["E"], float)
+    mat = R.Models.Elastic.Isotropic(dim, E=float(E) if E.ndim == 0 else E, v=float(g["v"]),
+                                     planeStress=bool(g["planeStress"]), thickness=float(g["thickness"]))
+    simu = R.B.GpuElastic(mesh, mat, rtol=1e-12)
+    L = mesh.coord[:, 0].max()
+    left = mesh.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = mesh.Nodes_Conditions(lambda x, y, z: x == L)
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    simu.add_dirichlet(left, [0.0] * dim, unk)
+    simu.add_surfLoad(right, [float(g["loadval"])], [str(g["loaddir"])])
+    u = simu.Solve()
+    assert simu.last_solve is not None and simu.last_solve.status == 0  # the GPU solver ran
+    assert np.abs(u - g["u"]).max() <= 1e-8 * np.abs(g["u"]).max()
+    K, C, M, F = simu.Get_K_C_M_F()
+    Kref = csr(g, "K", u.size)
+    assert same_pattern(K, Kref) and row_scaled_err(K, Kref) <= 1e-12
+    assert row_scaled_err(M, csr(g, "M", u.size)) <= 1e-12
+    assert C.nnz == K.nnz and np.abs(C.data).max() == 0.0 and F.shape == (u.size, 1)
+    # the reference's own post-processing reads the GPU-assembled K
+    f = np.sum(simu.Calc_Reaction(simu.Bc_dofs_nodes(left, unk)))
+    f_ref = np.sum((Kref @ g["u"])[simu.Bc_dofs_nodes(left, unk)])
+    assert abs(f - f_ref) <= 1e-8 * np.abs(Kref @ g["u"]).max() * len(left)
+    # Rayleigh damping through the reference's own setter: C = coefK K + coefM M
+    simu.Set_Rayleigh_Damping_Coefs(coefM=0.5, coefK=2e-3)
+    K2, C2, M2, _ = simu.Get_K_C_M_F()
+    assert abs(C2 - (2e-3 * K2 + 0.5 * M2)).max() <= 1e-15 * abs(K2).max()
+
+
+@pytest.mark.parametrize("case,opt", [("pf_tri3_miehe_at2", 0), ("pf_tri3_conv2", 2)])
+def test_gpu_phasefield_inside_easyfea(ref, golden, case, opt):
+    """EasyFEA's staggered load loop (Bc_Init, add_dirichlet, Solve, Save_Iter,
+    Calc_Reaction) on the GPU subclass: iterations per step equal to the
+    reference's, force within 1e-6, damage within 1e-6."""
+    g = golden(case)
+    R = ref
+    mesh = ref_mesh(R, g)
+    mat = R.Models.Elastic.Isotropic(2, E=float(g["E"]), v=float(g["v"]), planeStress=bool(g["planeStress"]),
+                                     thickness=1.0)
+    pfm = R.Models.PhaseField(mat, str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    simu = R.B.GpuPhaseField(mesh, pfm)
+    top_dofs = simu.Bc_dofs_nodes(g["top"], ["y"])
+    for k in range(1, g["F"].shape[0] + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(g["notch"], [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(g["bottom"], [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(g["top"], [0.0, k * float(g["dU"])], ["x", "y"])
+        u, d, conv = simu.Solve(float(g["tol"]), int(g["maxIter"]), convOption=opt)
+        simu.Save_Iter()
+        F = np.sum(simu.Calc_Reaction(top_dofs, simu.ProblemTypes.elastic))
+        # staggered iterations as the reference's Save_Iter recorded them
+        niter = simu._Simu__list_results[-1]["Niter"]
+        assert niter == g["Niter"][k - 1], f"step {k}: {niter} vs {g['Niter'][k - 1]}"
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"
+        assert np.abs(d - g["d"][k - 1]).max() <= 1e-6

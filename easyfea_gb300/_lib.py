@@ -133,6 +133,10 @@ SIGNATURES = {
                                    c_double, c_int, c_void_p, c_int64, c_int, c_void_p]),
     "gfea_surface_load": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_int, c_int, POINTER(c_int32),
                                   POINTER(c_double), c_double, c_void_p, c_void_p]),
+    "gfea_boundary_gauss_points": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, POINTER(c_int32),
+                                           c_void_p]),
+    "gfea_surface_load_field": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_int, c_int, c_int,
+                                        c_void_p, c_double, c_void_p, c_void_p]),
     "gfea_pf_damage": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
                                POINTER(PfParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "gfea_pf_elastic": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,

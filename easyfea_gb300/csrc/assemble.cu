@@ -399,6 +399,89 @@ __global__ void surface_load_kernel(const double* __restrict__ coord, const int3
   }
 }
 
+// Jacobian measure of a boundary element at Gauss point g (length of the
+// tangent in 1D, norm of the cross product of the two tangents in 2D).
+template <int BELEM>
+__device__ double boundary_wj(const RefTables<BELEM, true>& ref, const double* __restrict__ coord,
+                              const int32_t (&nd)[Elem<BELEM>::nPe], int g) {
+  constexpr int nPe = Elem<BELEM>::nPe, BD = Elem<BELEM>::dim;
+  double T[BD][3];
+  for (int d = 0; d < BD; ++d)
+    for (int k = 0; k < 3; ++k) {
+      double s = 0;
+      for (int n = 0; n < nPe; ++n) s += ref.dN[g][d][n] * coord[(int64_t)nd[n] * 3 + k];
+      T[d][k] = s;
+    }
+  double J;
+  if (BD == 1) {
+    J = sqrt(T[0][0] * T[0][0] + T[0][1] * T[0][1] + T[0][2] * T[0][2]);
+  } else {
+    const double cx = T[0][1] * T[BD - 1][2] - T[0][2] * T[BD - 1][1];
+    const double cy = T[0][2] * T[BD - 1][0] - T[0][0] * T[BD - 1][2];
+    const double cz = T[0][0] * T[BD - 1][1] - T[0][1] * T[BD - 1][0];
+    J = sqrt(cx * cx + cy * cy + cz * cz);
+  }
+  return J * ref.w[g];
+}
+
+// Coordinates of the mass Gauss points of boundary elements: xyz[(e nPg + g) 3 + k].
+template <int BELEM>
+__global__ void boundary_gauss_kernel(const double* __restrict__ coord, const int32_t* __restrict__ bconnect,
+                                      int64_t Nbe, double* __restrict__ xyz) {
+  using E = Elem<BELEM>;
+  constexpr int nPe = E::nPe;
+  constexpr int nPg = RefTables<BELEM, true>::nPg;
+  __shared__ RefTables<BELEM, true> ref;
+  ref.fill();
+  __syncthreads();
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < Nbe; e += (int64_t)gridDim.x * blockDim.x) {
+    int32_t nd[nPe];
+    for (int p = 0; p < nPe; ++p) nd[p] = bconnect[e * nPe + p];
+    for (int g = 0; g < nPg; ++g)
+      for (int k = 0; k < 3; ++k) {
+        double s = 0;
+        for (int n = 0; n < nPe; ++n) s += ref.N[g][n] * coord[(int64_t)nd[n] * 3 + k];
+        xyz[((int64_t)e * nPg + g) * 3 + k] = s;
+      }
+  }
+}
+
+// Neumann load of one unknown with values varying over the boundary, on the
+// elements whose every node has mask set: mode 0, values at the mass Gauss
+// points (values[e nPg + g]): b_p += factor sum_g wJ f_g N_p(g); mode 1,
+// values per node: b_p += factor f_p sum_g wJ N_p(g).
+template <int BELEM>
+__global__ void surface_load_field_kernel(const double* __restrict__ coord, const int32_t* __restrict__ bconnect,
+                                          int64_t Nbe, const uint8_t* __restrict__ mask, int dof_n, int ui, int mode,
+                                          const double* __restrict__ vals, double factor, double* __restrict__ b) {
+  using E = Elem<BELEM>;
+  constexpr int nPe = E::nPe;
+  constexpr int nPg = RefTables<BELEM, true>::nPg;
+  __shared__ RefTables<BELEM, true> ref;
+  ref.fill();
+  __syncthreads();
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < Nbe; e += (int64_t)gridDim.x * blockDim.x) {
+    int32_t nd[nPe];
+    bool all = true;
+    for (int p = 0; p < nPe; ++p) {
+      nd[p] = bconnect[e * nPe + p];
+      all = all && mask[nd[p]];
+    }
+    if (!all) continue;
+    double acc[nPe];
+    for (int p = 0; p < nPe; ++p) acc[p] = 0;
+    for (int g = 0; g < nPg; ++g) {
+      const double wJ = boundary_wj<BELEM>(ref, coord, nd, g);
+      const double fg = mode == 0 ? vals[e * nPg + g] : 1.0;
+      for (int p = 0; p < nPe; ++p) acc[p] += wJ * fg * ref.N[g][p];
+    }
+    for (int p = 0; p < nPe; ++p) {
+      const double f = mode == 0 ? 1.0 : vals[nd[p]];
+      atomicAdd(&b[(int64_t)nd[p] * dof_n + ui], factor * f * acc[p]);
+    }
+  }
+}
+
 int64_t assemble_key(int elem, int value_type, int cpe, int64_t Ne) {
   return tune_key(kTuneAssemble, elem, value_type, cpe, tune_log2((double)Ne));
 }
@@ -609,6 +692,60 @@ extern "C" int gfea_surface_load(int belem, const double* coord, const int32_t* 
       break;
     case GFEA_TRI3:
       surface_load_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    default:
+      return GFEA_ERR_ARG;
+  }
+  GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+extern "C" int gfea_boundary_gauss_points(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                                          double* xyz, int32_t* npg_host, void* stream) {
+  if (!coord || !bconnect || !npg_host || n_belems < 0 || (n_belems > 0 && !xyz)) return GFEA_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int blocks = grid_for(n_belems > 0 ? n_belems : 1, 128);
+  switch (belem) {
+    case GFEA_SEG2:
+      *npg_host = RefTables<GFEA_SEG2, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_SEG2><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_QUAD4:
+      *npg_host = RefTables<GFEA_QUAD4, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_QUAD4><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_TRI3:
+      *npg_host = RefTables<GFEA_TRI3, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    default:
+      return GFEA_ERR_ARG;
+  }
+  if (n_belems) GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+extern "C" int gfea_surface_load_field(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                                       const uint8_t* node_mask, int dof_n, int unknown_idx, int mode,
+                                       const double* values, double factor, double* b, void* stream) {
+  if (!coord || !bconnect || !node_mask || !b || !values || n_belems < 0 || unknown_idx < 0 ||
+      unknown_idx >= dof_n || (mode != 0 && mode != 1))
+    return GFEA_ERR_ARG;
+  if (n_belems == 0) return GFEA_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int blocks = grid_for(n_belems, 128);
+  switch (belem) {
+    case GFEA_SEG2:
+      surface_load_field_kernel<GFEA_SEG2><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                                   unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_QUAD4:
+      surface_load_field_kernel<GFEA_QUAD4><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                                    unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_TRI3:
+      surface_load_field_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                                   unknown_idx, mode, values, factor, b);
       break;
     default:
       return GFEA_ERR_ARG;

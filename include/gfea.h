@@ -129,12 +129,32 @@ int gfea_assemble_mass(int elem, const double* coord, const int32_t* connect, in
 /* Neumann surface / line loads: b[dof] += factor * value_u * sum_pg wJ N
  * over boundary elements whose every node has node_mask set (mass Gauss
  * points).  Replaces _Simu.__Bc_Integration_Dim (EasyFEA/Simulations/
- * _simu.py:2770-2842) for constant values, and the COO summation of
+ * _simu.py:2770-2842) for constant values (gfea_surface_load_field below
+ * takes values that vary over the boundary), and the COO summation of
  * _Solver_Apply_Neumann (:1750-1756). */
 int gfea_surface_load(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
                       const uint8_t* node_mask, int dof_n, int n_unknowns,
                       const int32_t* unknown_idx_host, const double* values_host, double factor,
                       double* b, void* stream);
+
+/* Coordinates of the mass Gauss points of boundary elements,
+ * xyz[(e * nPg + g) * 3 + k] (n_belems * nPg * 3 doubles); *npg_host = nPg.
+ * The points where _Simu.__Bc_evaluate evaluates a load given as a function
+ * of position (EasyFEA/Simulations/_simu.py:2353-2385 with
+ * Get_GaussCoordinates_e_pg, :2803-2811). */
+int gfea_boundary_gauss_points(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                               double* xyz, int32_t* npg_host, void* stream);
+
+/* Neumann load of one unknown with values varying over the boundary, on the
+ * elements whose every node has node_mask set: mode 0, values at the mass
+ * Gauss points (values[e * nPg + g], a function evaluated at the points of
+ * gfea_boundary_gauss_points): b += factor * sum_g wJ f_g N(g); mode 1,
+ * values per node (values[node]): b_p += factor * f_p * sum_g wJ N_p(g).
+ * Replaces the callable and array branches of _Simu.__Bc_Integration_Dim
+ * (EasyFEA/Simulations/_simu.py:2811-2832). */
+int gfea_surface_load_field(int belem, const double* coord, const int32_t* bconnect, int64_t n_belems,
+                            const uint8_t* node_mask, int dof_n, int unknown_idx, int mode,
+                            const double* values, double factor, double* b, void* stream);
 
 /* ------------------------------------------------------------------------
  * Phase field.

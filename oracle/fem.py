@@ -434,11 +434,15 @@ def dofs_nodes(nodes, unknowns, available):
 
 def surf_load(elem, coord, connect, nodes, values, unknowns, available, thickness=1.0):
     """Neumann nodal loads -- _simu.py:2770-2842 (__Bc_Integration_Dim) with the
-    2D thickness factor of :2572-2630.  Constant ``values`` only.
+    2D thickness factor of :2572-2630.  A value is a constant or a function of
+    (x, y, z), evaluated at the mass Gauss points (__Bc_evaluate, :2353-2385),
+    or an array of one value per node of ``nodes``, integrated as
+    value(node) x sum_g wJ N_node(g) (:2820-2826).
 
     Returns (dofs, dofsValues) in the COO form the reference appends."""
+    nodes = np.asarray(nodes)
     mark = np.zeros(coord.shape[0], dtype=bool)
-    mark[np.asarray(nodes)] = True
+    mark[nodes] = True
     sel = np.nonzero(mark[connect].all(axis=1))[0]
     if sel.size == 0:
         return np.zeros(0, np.int64), np.zeros(0)
@@ -448,8 +452,19 @@ def surf_load(elem, coord, connect, nodes, values, unknowns, available, thicknes
     vals = np.zeros((Ne * nPe, len(unknowns)))
     dofs = np.zeros((Ne * nPe, len(unknowns)), dtype=np.int64)
     for u, name in enumerate(unknowns):
-        ev = np.full(geo.wJ.shape, float(values[u]))
-        ve = np.einsum("ep,ep,pn->epn", geo.wJ, ev, geo.N)
+        v = values[u]
+        if isinstance(v, (int, float)) or callable(v):
+            if callable(v):
+                xg = np.einsum("pn,enk->epk", geo.N, coord[con])
+                ev = np.zeros(geo.wJ.shape)
+                ev[:, :] = v(xg[:, :, 0], xg[:, :, 1], xg[:, :, 2])
+            else:
+                ev = np.full(geo.wJ.shape, float(v))
+            ve = np.einsum("ep,ep,pn->epn", geo.wJ, ev, geo.N)
+        else:
+            ev_n = np.zeros(coord.shape[0])
+            ev_n[nodes] = v
+            ve = np.einsum("ep,en,pn->epn", geo.wJ, ev_n[con], geo.N)
         vals[:, u] = ve.sum(1).ravel()
         dofs[:, u] = dofs_nodes(con.ravel(), [name], available)
     return dofs.ravel(), vals.ravel() * thickness

@@ -30,6 +30,9 @@ sys.path.insert(0, REPO)
 
 from easyfea_gb300 import mesh as gmesh  # noqa: E402
 
+sys.path.insert(0, os.path.dirname(HERE))
+from helpers import field_loads  # noqa: E402
+
 
 def load_reference(path):
     sys.modules.setdefault("gmsh", types.ModuleType("gmsh"))
@@ -162,6 +165,34 @@ def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, 
     res.update(csr_parts("Ku", Ku))
     res.update(csr_parts("Kd", Kd))
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+
+
+def field_load_case(R, name, m, E, v, planeStress, thickness, out):
+    dim = m.dim
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=thickness)
+    simu = R.Simulations.Elastic(rm, mat)
+    simu.solver = R.SolverType.scipy
+    L = m.coord[:, 0].max()
+    left = rm.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = rm.Nodes_Conditions(lambda x, y, z: x == L)
+    unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
+    simu.add_dirichlet(left, [0.0] * dim, unk)
+    for nodes, vals, un in field_loads(dim, m.coord, right):
+        simu.add_surfLoad(nodes, vals, un)
+    u = simu.Solve()
+    b = np.asarray(simu._Solver_Apply_Neumann(simu.problemType).todense()).ravel()
+    d = dict(mesh_arrays(m), E=E, v=v, planeStress=planeStress, thickness=thickness, u=u, b=b,
+             left=left, right=right)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **d)
+    print(name, "Ndof", u.size, "|b|", np.abs(b).sum())
+
+
+def _field_load_cases(R, out):
+    field_load_case(R, "el_quad4_field_load", gmesh.Mesh_Quad4_Rect(120.0, 13.0, 24, 4), 210000.0, 0.3, True,
+                    13.0, out)
+    field_load_case(R, "el_hexa8_field_load", gmesh.Mesh_Hexa8_Box(60.0, 10.0, 10.0, 6, 2, 2), 210000.0, 0.3,
+                    False, 1.0, out)
 
 
 def pf_conv_case(R, name, m, convOption, steps, dU, out, tol=1e-3, maxIter=100):
@@ -353,7 +384,7 @@ def _el_hexa8_hetero(R, out):
 
 
 # fixtures that can be regenerated alone (--only=name,...)
-CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases,
+CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "pf_curve_tri3_200x200": pf_curve_case}
 
 

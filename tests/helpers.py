@@ -34,3 +34,15 @@ def row_scaled_err(A, B):
 def same_pattern(A, B):
     return np.array_equal(np.asarray(A.indptr, np.int64), np.asarray(B.indptr, np.int64)) and \
         np.array_equal(np.asarray(A.indices, np.int64), np.asarray(B.indices, np.int64))
+
+
+def field_loads(dim, coord, right):
+    """Loads that vary over the boundary (the "el_*_field_load" fixtures):
+    [(nodes, values, unknowns)] of add_surfLoad -- a function of position on
+    the x = L face / edge and, in 2D, an array of one value per node."""
+    if dim == 2:
+        ramp = lambda x, y, z: -800 / 13**2 * (1.0 + y / 13.0)  # noqa: E731
+        per_node = 5.0 * (1.0 + np.arange(right.size, dtype=float) / right.size)
+        return [(right, [ramp], ["y"]), (right, [per_node], ["x"])]
+    ramp3 = lambda x, y, z: -1.0 * (1.0 + y / 10.0 + 0.5 * z / 10.0)  # noqa: E731
+    return [(right, [ramp3], ["z"])]

@@ -76,3 +76,28 @@ def test_reaction_balances_load(golden):
     R = np.sum(simu.Calc_Reaction(dofs))
     total = float(g["loadval"]) * 13.0 * float(g["thickness"])
     assert abs(R + total) <= 1e-8 * abs(total)
+
+
+@pytest.mark.parametrize("case", ["el_quad4_field_load", "el_hexa8_field_load"])
+def test_field_loads_match_reference(golden, case):
+    """Surface loads given as functions of position (evaluated at the
+    boundary Gauss points) and as per-node arrays (EasyFEA/Simulations/
+    _simu.py:2811-2832): Neumann vector within 1e-12, displacements 1e-8."""
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import simulations as Simulations
+    from helpers import field_loads
+
+    g = golden(case)
+    m = mesh_from_golden(g)
+    dim = m.dim
+    mat = Models.Elastic.Isotropic(dim, E=float(g["E"]), v=float(g["v"]), planeStress=bool(g["planeStress"]),
+                                   thickness=float(g["thickness"]))
+    simu = Simulations.Elastic(m, mat)
+    simu.rtol = 1e-12
+    simu.add_dirichlet(g["left"], [0.0] * dim, ["x", "y"] if dim == 2 else ["x", "y", "z"])
+    for nodes, vals, unk in field_loads(dim, g["coord"], g["right"]):
+        simu.add_surfLoad(nodes, vals, unk)
+    u = simu.Solve()
+    b = simu._neumann_vec("elastic").cpu().numpy()
+    np.testing.assert_allclose(b, g["b"], rtol=1e-12, atol=1e-13 * np.abs(g["b"]).max())
+    assert np.abs(u - g["u"]).max() <= 1e-8 * np.abs(g["u"]).max()

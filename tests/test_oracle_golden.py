@@ -5,7 +5,7 @@ import pytest
 import scipy.sparse as sp
 
 from oracle import fem
-from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve
+from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve, neumann
 
 ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26"]
 
@@ -129,6 +129,23 @@ def test_phasefield_oracle_matches_reference(golden, case):
     Kd, Fd = pf.damage_system()
     assert row_scaled_err(Kd, csr(g, "Kd", m.Nn)) <= 1e-7
     np.testing.assert_allclose(Fd, g["Fd"], rtol=1e-7, atol=1e-12 * np.abs(g["Fd"]).max())
+
+
+@pytest.mark.parametrize("case", ["el_quad4_field_load", "el_hexa8_field_load"])
+def test_field_loads_oracle_matches_reference(golden, case):
+    """Neumann loads given as functions of position and as per-node arrays."""
+    from helpers import field_loads
+
+    g = golden(case)
+    m = om(g)
+    dim = m.dim
+    loads = field_loads(dim, g["coord"], g["right"])
+    b = neumann(m, loads, dim, float(g["thickness"]))
+    np.testing.assert_allclose(b, g["b"], rtol=1e-12, atol=1e-13 * np.abs(g["b"]).max())
+    unk = fem.UNKNOWNS[dim]
+    u, _, _ = elastic_solve(m, float(g["E"]), float(g["v"]), bool(g["planeStress"]), float(g["thickness"]),
+                            [(g["left"], [0.0] * dim, unk)], loads)
+    assert np.abs(u - g["u"]).max() <= 1e-10 * np.abs(g["u"]).max()
 
 
 @pytest.mark.parametrize("opt", [1, 2, 3])

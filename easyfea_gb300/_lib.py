@@ -77,6 +77,23 @@ class PcgResult(ctypes.Structure):
     ]
 
 
+class CoarseLevel(ctypes.Structure):
+    _fields_ = [
+        ("n_agg", c_int32),
+        ("nr", c_int32),
+        ("nc", c_int32),
+        ("pad", c_int32),
+        ("agg", c_void_p),
+        ("off", c_void_p),
+        ("agg_ptr", c_void_p),
+        ("agg_nodes", c_void_p),
+        ("inv", c_void_p),
+        ("inv32", c_void_p),
+        ("rc", c_void_p),
+        ("ec", c_void_p),
+    ]
+
+
 class BatchInstance(ctypes.Structure):
     _fields_ = [
         ("version", c_int32),
@@ -95,6 +112,7 @@ class BatchInstance(ctypes.Structure):
         ("x", c_void_p),
         ("work", c_void_p),
         ("result", c_void_p),
+        ("coarse", CoarseLevel),
     ]
 
 
@@ -149,6 +167,9 @@ SIGNATURES = {
                                POINTER(PcgResult), c_void_p]),
     "gfea_pcg_solve_noalloc": (c_int, [POINTER(System), c_void_p, c_void_p, POINTER(PcgOpts), POINTER(PcgResult),
                                        c_void_p]),
+    "gfea_coarse_workspace_size": (c_int, [POINTER(System), POINTER(PcgOpts), POINTER(c_size_t)]),
+    "gfea_coarse_setup": (c_int, [POINTER(System), POINTER(PcgOpts), c_int, c_void_p, c_size_t, POINTER(CoarseLevel),
+                                  c_void_p]),
     "gfea_batch_workspace_size": (c_size_t, [c_int64, c_int, c_int]),
     "gfea_batch_scratch_size": (c_size_t, [c_int]),
     "gfea_batch_pcg": (c_int, [POINTER(BatchInstance), c_int, c_void_p, c_size_t, POINTER(PcgOpts), c_void_p]),

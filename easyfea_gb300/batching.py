@@ -48,22 +48,59 @@ class BatchSystem:
 RESULT_BYTES = ctypes.sizeof(_lib.PcgResult)
 
 
+class CoarseLevels:
+    """Coarse levels of the batched two-level preconditioner, one workspace
+    per system operator, kept between batches: the aggregation (which depends
+    only on the mesh) is built on a system's first setup and kept afterwards,
+    when only the coarse matrix and its inverse are rebuilt from the current
+    values (device work only, so that setup can be captured in a CUDA graph)."""
+
+    def __init__(self):
+        self._levels = {}  # id(op) -> (op, precision, workspace, CoarseLevel)
+
+    def setup(self, s: BatchSystem, precision: int, coarse: int = -1) -> _lib.CoarseLevel:
+        L = _lib.load()
+        sys_ = s.op.system(s.known)
+        opts = _lib.PcgOpts(_lib.ABI_VERSION, precision, 0, 0, 0.0, 0.0, 0, 0, int(coarse), 0)
+        key = id(s.op)
+        entry = self._levels.get(key)
+        keep = entry is not None and entry[0] is s.op and entry[1] == precision
+        if not keep:
+            nb = ctypes.c_size_t()
+            _lib.check(L.gfea_coarse_workspace_size(ctypes.byref(sys_), ctypes.byref(opts), ctypes.byref(nb)),
+                       "coarse workspace")
+            work = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=_dev())
+            entry = (s.op, precision, work, _lib.CoarseLevel())
+            self._levels[key] = entry
+        _, _, work, level = entry
+        _lib.check(L.gfea_coarse_setup(ctypes.byref(sys_), ctypes.byref(opts), int(keep), _lib.ptr(work),
+                                       work.numel(), ctypes.byref(level), _lib.stream()), "coarse setup")
+        return level
+
+
 class BatchSolver:
-    """Reusable buffers for repeated batches (workspace arena, descriptors, results)."""
+    """Reusable buffers for repeated batches (workspace arena, descriptors, results).
+
+    ``coarse`` (prepare / launch / solve): 0 solves with block-Jacobi PCG
+    alone; -1 (default) gives every system the two-level preconditioner's
+    coarse level (aggregate count chosen from its size, coarse dimension
+    capped at 512), built on the current stream before the launch."""
 
     def __init__(self):
         self._arena = None
         self._scratch = None
         self._results = None
+        self.coarse_levels = CoarseLevels()
 
     def _ensure(self, t: Optional[torch.Tensor], nbytes: int) -> torch.Tensor:
         if t is None or t.numel() < nbytes:
             t = torch.empty(max(nbytes, 1 << 16), dtype=torch.uint8, device=_dev())
         return t
 
-    def launch(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1):
+    def launch(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
+               coarse: int = -1):
         """Enqueue the batch on the current stream (asynchronous)."""
-        self.prepare(systems, precision, inner_rtol)
+        self.prepare(systems, precision, inner_rtol, coarse)
         self.launch_prepared()
 
     def launch_prepared(self):
@@ -71,8 +108,19 @@ class BatchSolver:
         _lib.check(_lib.load().gfea_batch_launch(_lib.ptr(self._scratch), self._n, ctypes.byref(self._opts),
                                                  _lib.stream()), "batch launch")
 
-    def prepare(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1):
-        """Validate the systems and upload their descriptors (largest first)."""
+    def setup_coarse(self, systems: List[BatchSystem], coarse: int = -1):
+        """(Re)build every system's coarse matrix and inverse from its current
+        values (device work only once the aggregations exist)."""
+        for s, lvl in zip(systems, self._levels):
+            if lvl is not None:
+                self.coarse_levels.setup(s, self._prec, coarse)
+
+    def prepare(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
+                coarse: int = -1):
+        """Validate the systems, build their coarse levels (unless ``coarse`` is
+        0) and upload their descriptors (largest first).  ``inner_rtol``: the
+        FP32 reliable-update trigger (0: 0.01 with the coarse level, 0.1
+        without)."""
         L = _lib.load()
         prec = _lib.F64 if precision == "fp64" else _lib.F32
         n = len(systems)
@@ -89,14 +137,19 @@ class BatchSolver:
         arr = (_lib.BatchInstance * n)()
         base = self._arena.data_ptr()
         rbase = self._results.data_ptr()
+        self._prec = prec
+        self._levels = [self.coarse_levels.setup(s, prec, coarse) if coarse != 0 and s.op.dmesh.coord is not None
+                        else None for s in systems]
         for i, s in enumerate(systems):
             d = s.op.dmesh
             arr[i] = _lib.BatchInstance(
                 _lib.ABI_VERSION, s.op.dof_n, d.Nn, d.n_pairs, _lib.ptr(d.node_ptr), _lib.ptr(d.nbr),
                 _lib.ptr(s.op.vals64), _lib.ptr(s.op.vals32) if prec == _lib.F32 else 0, _lib.ptr(s.known),
                 int(s.op.translation_invariant), int(s.max_iters), float(s.rtol), _lib.ptr(s.b), _lib.ptr(s.x),
-                base + int(offs[i]), rbase + i * RESULT_BYTES)
-        self._opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 0, 0, 0.0, float(inner_rtol), 0, 0)
+                base + int(offs[i]), rbase + i * RESULT_BYTES,
+                self._levels[i] if self._levels[i] is not None else _lib.CoarseLevel())
+        d_rtol = inner_rtol if 0 < inner_rtol < 1 else (0.01 if coarse != 0 else 0.1)
+        self._opts = _lib.PcgOpts(_lib.ABI_VERSION, prec, 0, 0, 0.0, float(d_rtol), 0, 0)
         _lib.check(L.gfea_batch_prepare(arr, n, _lib.ptr(self._scratch), self._scratch.numel(),
                                         ctypes.byref(self._opts), _lib.stream()), "batch prepare")
         self._n = n
@@ -111,9 +164,9 @@ class BatchSolver:
                                float(r.floor_rel)))
         return out
 
-    def solve(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
-              raise_on_fail: bool = True) -> List[PcgInfo]:
-        self.launch(systems, precision, inner_rtol)
+    def solve(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
+              raise_on_fail: bool = True, coarse: int = -1) -> List[PcgInfo]:
+        self.launch(systems, precision, inner_rtol, coarse)
         infos = self.results()
         if raise_on_fail:
             for i, info in enumerate(infos):
@@ -124,19 +177,20 @@ class BatchSolver:
 
 class GraphBatch:
     """A batch captured as one CUDA graph: optional device work ``pre`` (e.g.
-    re-assembling every instance's operator), the reset of each x to its
-    initial state and the persistent batched solve.  ``replay`` re-runs all of
+    re-assembling every instance's operator), the coarse matrices and their
+    inverses rebuilt from those values, the reset of each x to its initial
+    state and the persistent batched solve.  ``replay`` re-runs all of
     it with one graph launch; buffers (values, b, x) are read in place, so new
     values written into them between replays are picked up."""
 
-    def __init__(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
-                 pre=None):
+    def __init__(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
+                 pre=None, coarse: int = -1):
         from . import autotune
 
         self.systems = systems
         self.x0 = [s.x.clone() for s in systems]
         self.solver = BatchSolver()
-        self.solver.prepare(systems, precision, inner_rtol)
+        self.solver.prepare(systems, precision, inner_rtol, coarse)
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         stream = torch.cuda.Stream()
@@ -147,6 +201,8 @@ class GraphBatch:
             with torch.cuda.graph(self.graph, stream=stream):
                 if pre is not None:
                     pre()
+                # coarse matrices and inverses from the values 'pre' wrote
+                self.solver.setup_coarse(systems, coarse)
                 for s, x0 in zip(systems, self.x0):
                     s.x.copy_(x0)
                 self.solver.launch_prepared()
@@ -161,9 +217,9 @@ class GraphBatch:
         return self.solver.results()
 
 
-def solve_batch(systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.1,
-                raise_on_fail: bool = True) -> List[PcgInfo]:
-    return BatchSolver().solve(systems, precision, inner_rtol, raise_on_fail)
+def solve_batch(systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
+                raise_on_fail: bool = True, coarse: int = -1) -> List[PcgInfo]:
+    return BatchSolver().solve(systems, precision, inner_rtol, raise_on_fail, coarse)
 
 
 # ---------------------------------------------------------------------------

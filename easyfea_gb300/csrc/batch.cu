@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "coarse.cuh"
 #include "common.cuh"
 #include "rowops.cuh"
 
@@ -152,6 +153,105 @@ __device__ void restart_rz(const gfea_batch_instance& I, const BatchBuf<T>& w, i
   }
 }
 
+// Coarse correction of the two-level preconditioner, cluster-wide:
+// rc = R^T r (one warp per aggregate, its nodes in ascending order, fixed
+// butterfly), ec = A_c^-1 rc (one warp per row; FP32 inverse for the FP32
+// iteration).  Every thread of the cluster calls it; r must be written.
+template <int D, typename T>
+__device__ void coarse_correct(Ctx& c, const gfea_batch_instance& I, const T* r, int64_t gtid, int64_t nthr) {
+  constexpr int nr = Modes<D>::nr;
+  const gfea_coarse_level& L = I.coarse;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = gtid >> 5, nw = nthr >> 5;
+  const float4* off = reinterpret_cast<const float4*>(L.off);
+  c.cl.sync();  // r of every node written
+  for (int64_t g = gw; g < L.n_agg; g += nw) {
+    T v[nr];
+#pragma unroll
+    for (int m = 0; m < nr; ++m) v[m] = 0;
+    const int32_t k1 = L.agg_ptr[g + 1];
+    for (int32_t k = L.agg_ptr[g] + lane; k < k1; k += 32) {
+      const int64_t a = L.agg_nodes[k];
+      T R[D][nr];
+      node_modes<D, T>(off[a], I.known + a * D, R);
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        const T ri = ldcg(r + a * D + i);
+#pragma unroll
+        for (int m = 0; m < nr; ++m) v[m] += R[i][m] * ri;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < nr; ++m) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[m] += __shfl_xor_sync(0xffffffffu, v[m], o);
+      if (lane == 0) L.rc[g * nr + m] = (double)v[m];
+    }
+  }
+  c.cl.sync();  // rc complete
+  const int nc = L.nc;
+  for (int64_t i = gw; i < nc; i += nw) {
+    T acc = 0;
+    if (sizeof(T) == 4) {
+      const float* row = L.inv32 + i * nc;
+      for (int j = lane; j < nc; j += 32) acc += (T)__ldg(row + j) * (T)ldcg(L.rc + j);
+    } else {
+      const double* row = L.inv + i * nc;
+      for (int j = lane; j < nc; j += 32) acc += (T)(__ldg(row + j) * ldcg(L.rc + j));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) L.ec[i] = (double)acc;
+  }
+  c.cl.sync();  // ec complete
+}
+
+// z = D^-1 r + R ec[agg] (masked) for the nodes of this thread; partials r.z, r.r.
+template <int D, typename T>
+__device__ void z_two_level(const gfea_batch_instance& I, const BatchBuf<T>& w, int64_t gtid, int64_t nthr,
+                            DotAcc<T>& rz, DotAcc<T>& rr) {
+  constexpr int nr = Modes<D>::nr;
+  const gfea_coarse_level& L = I.coarse;
+  const float4* off = reinterpret_cast<const float4*>(L.off);
+  for (int64_t a = gtid; a < I.n_nodes; a += nthr) {
+    T rl[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) rl[i] = ldcg(w.r + a * D + i);
+    const int g = L.agg[a];
+    T R[D][nr];
+    node_modes<D, T>(off[a], I.known + a * D, R);
+    T e[nr];
+#pragma unroll
+    for (int m = 0; m < nr; ++m) e[m] = (T)ldcg(L.ec + g * nr + m);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      T zi = 0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) zi += w.dinv[a * D * D + i * D + j] * rl[j];
+#pragma unroll
+      for (int m = 0; m < nr; ++m) zi += R[i][m] * e[m];
+      if (I.known[a * D + i]) zi = 0;
+      w.z[a * D + i] = zi;
+      rz.add_prod(rl[i], zi);
+      rr.add_prod(rl[i], rl[i]);
+    }
+  }
+}
+
+// restart_rz with the coarse level: r = (T) r64, coarse correction, z.
+template <int D, typename T>
+__device__ void restart_rz_two_level(Ctx& c, const gfea_batch_instance& I, const BatchBuf<T>& w, int64_t gtid,
+                                     int64_t nthr, double (&v)[2]) {
+  for (int64_t a = gtid; a < I.n_nodes; a += nthr)
+#pragma unroll
+    for (int i = 0; i < D; ++i) w.r[a * D + i] = (T)ldcg(w.r64 + a * D + i);
+  coarse_correct<D, T>(c, I, w.r, gtid, nthr);
+  DotAcc<T> rz, rr;
+  z_two_level<D, T>(I, w, gtid, nthr, rz, rr);
+  v[0] = rz.value();
+  v[1] = rr.value();
+}
+
 template <int D, int G, typename T>
 __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delta2) {
   const int64_t Nn = I.n_nodes;
@@ -167,6 +267,7 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
   const int64_t grp = gtid / G, ngrp = nthr / G;
   const int64_t sub = grp % (32 / G);
   const double eps64 = 2.220446049250313e-16;
+  const bool two_level = I.coarse.n_agg > 0;
 
   // block-Jacobi inverses (thread per node)
   double bad = 0;
@@ -239,7 +340,10 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
         w.pa[a * D + i] = 0;
       }
     double v2[2] = {0, 0}, o2[2];
-    restart_rz<D, T>(I, w, gtid, nthr, v2);
+    if (two_level)
+      restart_rz_two_level<D, T>(c, I, w, gtid, nthr, v2);
+    else
+      restart_rz<D, T>(I, w, gtid, nthr, v2);
     csum<2>(c, v2, o2);
     double rz = o2[0];
     double beta = 0;
@@ -288,6 +392,17 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
       double vb[2] = {0, 0}, ob[2];
       DotAcc<T> rz_acc, rr_acc;
       const T al = (T)alpha;
+      if (two_level) {  // x, r; then the coarse correction; then z
+        for (int64_t a = gtid; a < Nn; a += nthr)
+#pragma unroll
+          for (int i = 0; i < D; ++i) {
+            const int64_t dof = a * D + i;
+            w.dx[dof] = ldcg(w.dx + dof) + al * ldcg(pb + dof);
+            w.r[dof] = ldcg(w.r + dof) - al * ldcg(w.Ap + dof);
+          }
+        coarse_correct<D, T>(c, I, w.r, gtid, nthr);
+        z_two_level<D, T>(I, w, gtid, nthr, rz_acc, rr_acc);
+      } else
       for (int64_t a = gtid; a < Nn; a += nthr) {
         T rl[D];
 #pragma unroll
@@ -352,7 +467,10 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
       rr_best = fmin(rr_best, rr_true);
       if (stall >= 8) break;
       double vz[2] = {0, 0}, oz[2];
-      restart_rz<D, T>(I, w, gtid, nthr, vz);
+      if (two_level)
+        restart_rz_two_level<D, T>(c, I, w, gtid, nthr, vz);
+      else
+        restart_rz<D, T>(I, w, gtid, nthr, vz);
       csum<2>(c, vz, oz);
       beta = oz[0] / rz;
       if (!(beta <= 1.0)) beta = 0;  // a replaced residual above the iterated one restarts
@@ -430,6 +548,14 @@ extern "C" int gfea_batch_prepare(const gfea_batch_instance* inst_host, int n, v
       return GFEA_ERR_ARG;
     if (prec == GFEA_F32 && !I.vals32) return GFEA_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(I.work) & 255) != 0) return GFEA_ERR_ARG;
+    const gfea_coarse_level& L = I.coarse;
+    if (L.n_agg < 0) return GFEA_ERR_ARG;
+    if (L.n_agg > 0) {
+      const int nr = I.dof_n == 1 ? 1 : (I.dof_n == 2 ? 3 : 6);
+      if (L.nr != nr || L.nc != nr * L.n_agg || L.nc > 512 || !L.agg || !L.off || !L.agg_ptr || !L.agg_nodes ||
+          !L.inv || !L.inv32 || !L.rc || !L.ec)
+        return GFEA_ERR_ARG;
+    }
   }
   if (n == 0) return GFEA_OK;
   // largest systems first (longest-processing-time order over the clusters)

@@ -32,6 +32,7 @@
 #include <chrono>
 #include <mutex>
 
+#include "coarse.cuh"
 #include "common.cuh"
 #include "rowops.cuh"
 #include "stage.cuh"
@@ -419,40 +420,6 @@ struct CoarseDev {
   double* ec = nullptr;    // nc: coarse correction
   float* ecf = nullptr;    // nc: its FP32 copy (read by the FP32 prolongation)
 };
-
-template <int D>
-struct Modes {
-  static constexpr int nr = D == 1 ? 1 : (D == 2 ? 3 : 6);
-};
-
-// Rigid-body modes at one node (D x nr), rows of known DOFs zeroed.
-// R holds exactly representable products of the float offsets, so the FP32
-// and FP64 iterations apply the same modes.
-template <int D, typename T = double>
-__device__ __forceinline__ void node_modes(float4 o, const uint8_t* kn, T (&R)[D][Modes<D>::nr]) {
-  if constexpr (D == 1) {
-    R[0][0] = kn[0] ? T(0) : T(1);
-  } else if constexpr (D == 2) {
-    const T dx = o.x, dy = o.y;
-    const T r0[3] = {1, 0, -dy}, r1[3] = {0, 1, dx};
-    const bool k0 = kn[0], k1 = kn[1];
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      R[0][m] = k0 ? T(0) : r0[m];
-      R[1][m] = k1 ? T(0) : r1[m];
-    }
-  } else {
-    const T dx = o.x, dy = o.y, dz = o.z;
-    const T r0[6] = {1, 0, 0, 0, dz, -dy}, r1[6] = {0, 1, 0, -dz, 0, dx}, r2[6] = {0, 0, 1, dy, -dx, 0};
-    const bool k0 = kn[0], k1 = kn[1], k2 = kn[2];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      R[0][m] = k0 ? T(0) : r0[m];
-      R[1][m] = k1 ? T(0) : r1[m];
-      R[2][m] = k2 ? T(0) : r2[m];
-    }
-  }
-}
 
 __global__ void bbox_kernel(const double* __restrict__ coord, int64_t Nn, double* partials) {
   double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -1728,28 +1695,12 @@ int coarse_aggregate(const gfea_system* s, int target, PcgWork& w, cudaStream_t 
 // extents get one cell), A_c = R^T A R from the FP64 values, inverted in place.
 // With 'reuse', an aggregation left in the workspace by an earlier call on the
 // same node count and target is kept.
+// A_c = R^T A R from the T-typed values, regularised and inverted in place
+// (the aggregation in C is given).
 template <typename T>
-int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaStream_t st, cudaEvent_t mark) {
-  CoarseDev& C = w.C;
+int coarse_matrix(const gfea_system* s, CoarseDev& C, cudaStream_t st, cudaEvent_t mark) {
   const int64_t Nn = s->n_nodes;
   const int D = s->dof_n;
-  bool have = false;
-  if (reuse) {
-    CoarseHdr h;
-    GFEA_CUDA_TRY(cudaMemcpyAsync(&h, C.hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
-    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
-    have = h.valid == kHdrValid && h.Nn == Nn && h.nr == coarse_nr(D) && h.n_agg >= 1 && h.n_agg <= target &&
-           h.nc == h.nr * h.n_agg;
-    if (have) {
-      C.nr = h.nr;
-      C.n_agg = h.n_agg;
-      C.nc = h.nc;
-    }
-  }
-  if (!have) {
-    const int e = coarse_aggregate(s, target, w, st);
-    if (e) return e;
-  }
   GFEA_CUDA_TRY(cudaMemsetAsync(C.Ac, 0, sizeof(double) * C.nc * C.nc, st));
   const SysT<T> S = sys_t<T>(s);
   GFEA_D_SWITCH(D, (coarse_assemble_kernel<DD, T><<<grid_elems(Nn), kThreads, 0, st>>>(S, C)));
@@ -1774,6 +1725,33 @@ int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaS
   }
   ff_merge_kernel<<<grid_elems(n2), kThreads, 0, st>>>(C.Ac, C.Ahi, C.Alo, n2);
   GFEA_LAUNCH_CHECK();
+  return GFEA_OK;
+}
+
+template <typename T>
+int coarse_setup(const gfea_system* s, int target, bool reuse, PcgWork& w, cudaStream_t st, cudaEvent_t mark) {
+  CoarseDev& C = w.C;
+  const int64_t Nn = s->n_nodes;
+  const int D = s->dof_n;
+  bool have = false;
+  if (reuse) {
+    CoarseHdr h;
+    GFEA_CUDA_TRY(cudaMemcpyAsync(&h, C.hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GFEA_CUDA_TRY(cudaStreamSynchronize(st));
+    have = h.valid == kHdrValid && h.Nn == Nn && h.nr == coarse_nr(D) && h.n_agg >= 1 && h.n_agg <= target &&
+           h.nc == h.nr * h.n_agg;
+    if (have) {
+      C.nr = h.nr;
+      C.n_agg = h.n_agg;
+      C.nc = h.nc;
+    }
+  }
+  if (!have) {
+    const int e = coarse_aggregate(s, target, w, st);
+    if (e) return e;
+  }
+  const int e = coarse_matrix<T>(s, C, st, mark);
+  if (e) return e;
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rc, 0, sizeof(double) * C.nc, st));
   GFEA_CUDA_TRY(cudaMemsetAsync(C.rcp, 0, sizeof(double) * C.nc * kRcCopies, st));
   return GFEA_OK;
@@ -2287,6 +2265,172 @@ extern "C" int gfea_pcg_solve(const gfea_system* s, const double* b, double* x, 
     return refine_solve<float>(s, b, x, o, work, work_bytes, res, st);
   }
   return GFEA_ERR_ARG;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse level for the batched PCG (gfea_batch_pcg): the same aggregation,
+// coarse matrix and inverse as the single-system two-level preconditioner,
+// built into a caller workspace, plus the nodes of each aggregate in
+// ascending order (the batched restriction gathers them in a fixed order) and
+// an FP32 copy of the inverse (the FP32 iteration's coarse GEMV).
+// ---------------------------------------------------------------------------
+
+// Coarse dimension cap of the batched solve: the whole inverse is read once
+// per iteration by the one cluster that owns the system.
+constexpr int kBatchCoarseMax = 512;
+
+struct CoarseLevelWork {
+  CoarseDev C;
+  double* partials = nullptr;
+  int32_t* agg_ptr = nullptr;
+  int32_t* agg_nodes = nullptr;
+  int32_t* counts = nullptr;
+  float* inv32 = nullptr;
+};
+
+int batch_coarse_target(const gfea_system* s, const gfea_pcg_opts* o) {
+  const int t = coarse_target(s, o);
+  const int cap = kBatchCoarseMax / coarse_nr(s->dof_n);
+  return t > cap ? cap : t;
+}
+
+size_t coarse_level_layout(int64_t Nn, int D, int n_agg_max, CoarseLevelWork* w, char* base) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  CoarseLevelWork t;
+  if (!w) w = &t;
+  const int64_t nc = (int64_t)n_agg_max * coarse_nr(D);
+  CoarseDev& C = w->C;
+  w->partials = reinterpret_cast<double*>(take(sizeof(double) * 4 * kMaxBlocks));
+  C.hdr = reinterpret_cast<CoarseHdr*>(take(sizeof(CoarseHdr)));
+  C.agg = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * Nn));
+  C.off = reinterpret_cast<float4*>(take(sizeof(float4) * Nn));
+  C.Ac = reinterpret_cast<double*>(take(sizeof(double) * nc * nc));
+  C.Ahi = reinterpret_cast<float*>(take(sizeof(float) * nc * nc));
+  C.Alo = reinterpret_cast<float*>(take(sizeof(float) * nc * nc));
+  C.rowph = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+  C.rowpl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+  C.colph = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+  C.colpl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * nc));
+  C.pinvh = reinterpret_cast<float*>(take(sizeof(float) * kGJB * kGJB));
+  C.pinvl = reinterpret_cast<float*>(take(sizeof(float) * kGJB * kGJB));
+  C.rc = reinterpret_cast<double*>(take(sizeof(double) * nc));
+  C.ec = reinterpret_cast<double*>(take(sizeof(double) * nc));
+  C.ecf = reinterpret_cast<float*>(take(sizeof(float) * nc));
+  w->agg_ptr = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * (n_agg_max + 1)));
+  w->counts = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * (n_agg_max + 1)));
+  w->agg_nodes = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * Nn));
+  w->inv32 = reinterpret_cast<float*>(take(sizeof(float) * nc * nc));
+  return off;
+}
+
+__global__ void agg_count_kernel(const int32_t* __restrict__ agg, int64_t Nn, int32_t* counts) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&counts[agg[a]], 1);
+}
+
+// ptr = exclusive scan of counts (one block; n_agg <= kBatchCoarseMax)
+__global__ void agg_scan_kernel(const int32_t* __restrict__ counts, int n, int32_t* ptr) {
+  if (threadIdx.x == 0) {
+    int32_t s = 0;
+    for (int g = 0; g < n; ++g) {
+      ptr[g] = s;
+      s += counts[g];
+    }
+    ptr[n] = s;
+  }
+}
+
+// Nodes of aggregate g in ascending order: warp g scans the node range in
+// order, placing its matches with a ballot prefix (no atomics, deterministic).
+__global__ void agg_fill_kernel(const int32_t* __restrict__ agg, int64_t Nn, int n_agg,
+                                const int32_t* __restrict__ ptr, int32_t* __restrict__ nodes) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g = warp; g < n_agg; g += nwarps) {
+    int32_t pos = ptr[g];
+    for (int64_t base = 0; base < Nn; base += 32) {
+      const int64_t a = base + lane;
+      const bool hit = a < Nn && agg[a] == (int32_t)g;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) nodes[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)a;
+      pos += __popc(m);
+    }
+  }
+}
+
+extern "C" int gfea_coarse_workspace_size(const gfea_system* s, const gfea_pcg_opts* o, size_t* bytes) {
+  if (!s || !o || !bytes || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3) return GFEA_ERR_ARG;
+  const int target = batch_coarse_target(s, o);
+  *bytes = target > 0 ? coarse_level_layout(s->n_nodes, s->dof_n, target, nullptr, nullptr) : 0;
+  return GFEA_OK;
+}
+
+extern "C" int gfea_coarse_setup(const gfea_system* s, const gfea_pcg_opts* o, int keep_aggregation, void* work,
+                                 size_t work_bytes, gfea_coarse_level* level, void* stream) {
+  if (!s || !o || !work || !level) return GFEA_ERR_ARG;
+  if (s->version != GFEA_ABI_VERSION || o->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
+  if (s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3 || !s->node_ptr || !s->nbr || !s->known || !s->coord)
+    return GFEA_ERR_ARG;
+  const bool f32 = o->precision == GFEA_F32;
+  if (!(f32 ? (const void*)s->vals32 : (const void*)s->vals64)) return GFEA_ERR_ARG;
+  const int target = batch_coarse_target(s, o);
+  if (target <= 0) return GFEA_ERR_ARG;
+  if (coarse_level_layout(s->n_nodes, s->dof_n, target, nullptr, nullptr) > work_bytes) return GFEA_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CoarseLevelWork cw;
+  coarse_level_layout(s->n_nodes, s->dof_n, target, &cw, static_cast<char*>(work));
+  CoarseDev& C = cw.C;
+  C.ncopies = 1;
+  const int64_t Nn = s->n_nodes;
+  if (keep_aggregation) {
+    // the aggregation of an earlier call on this mesh and workspace
+    if (level->n_agg < 1 || level->n_agg > target || level->nr != coarse_nr(s->dof_n) ||
+        level->nc != level->nr * level->n_agg || level->agg != C.agg)
+      return GFEA_ERR_ARG;
+    C.nr = level->nr;
+    C.n_agg = level->n_agg;
+    C.nc = level->nc;
+  } else {
+    PcgWork w;
+    w.partials = cw.partials;
+    w.C = C;
+    const int e = coarse_aggregate(s, target, w, st);
+    if (e) return e;
+    C = w.C;
+    GFEA_CUDA_TRY(cudaMemsetAsync(cw.counts, 0, sizeof(int32_t) * (C.n_agg + 1), st));
+    agg_count_kernel<<<grid_elems(Nn), kThreads, 0, st>>>(C.agg, Nn, cw.counts);
+    GFEA_LAUNCH_CHECK();
+    agg_scan_kernel<<<1, 32, 0, st>>>(cw.counts, C.n_agg, cw.agg_ptr);
+    GFEA_LAUNCH_CHECK();
+    const int warps_per_block = kThreads / 32;
+    agg_fill_kernel<<<(int)ceil_div(C.n_agg, warps_per_block), kThreads, 0, st>>>(C.agg, Nn, C.n_agg, cw.agg_ptr,
+                                                                                   cw.agg_nodes);
+    GFEA_LAUNCH_CHECK();
+  }
+  const int e = f32 ? coarse_matrix<float>(s, C, st, nullptr) : coarse_matrix<double>(s, C, st, nullptr);
+  if (e) return e;
+  const int64_t n2 = (int64_t)C.nc * C.nc;
+  cast_kernel<float><<<grid_elems(n2), kThreads, 0, st>>>(C.Ac, cw.inv32, n2);
+  GFEA_LAUNCH_CHECK();
+  level->n_agg = C.n_agg;
+  level->nr = C.nr;
+  level->nc = C.nc;
+  level->pad = 0;
+  level->agg = C.agg;
+  level->off = reinterpret_cast<const float*>(C.off);
+  level->agg_ptr = cw.agg_ptr;
+  level->agg_nodes = cw.agg_nodes;
+  level->inv = C.Ac;
+  level->inv32 = cw.inv32;
+  level->rc = C.rc;
+  level->ec = C.ec;
+  return GFEA_OK;
 }
 
 extern "C" size_t gfea_reduce_workspace_size(void) { return sizeof(double) * 4 * kMaxBlocks + 256; }

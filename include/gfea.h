@@ -262,6 +262,23 @@ typedef struct gfea_pcg_result {
  * is the batched driver behind the reference's per-instance loop of
  * Simulations.*.Solve calls (one SuperLU solve each, Solvers.py:361).
  * ---------------------------------------------------------------------- */
+/* Coarse level of the two-level preconditioner for one system of a batch
+ * (gfea_coarse_setup): pointers into the workspace it was built in. */
+typedef struct gfea_coarse_level {
+  int32_t n_agg;            /* aggregates (0: no coarse level, block-Jacobi only) */
+  int32_t nr;               /* rigid-body modes per aggregate (1, 3 or 6) */
+  int32_t nc;               /* coarse dimension nr * n_agg (<= 512) */
+  int32_t pad;
+  const int32_t* agg;       /* node -> aggregate */
+  const float* off;         /* 4 floats per node: offset from its cell centre, scaled */
+  const int32_t* agg_ptr;   /* n_agg + 1: ranges of agg_nodes */
+  const int32_t* agg_nodes; /* the nodes of each aggregate, ascending */
+  const double* inv;        /* nc x nc inverse of the coarse matrix R^T A R */
+  const float* inv32;       /* its FP32 copy */
+  double* rc;               /* nc: restriction scratch of the batched solve */
+  double* ec;               /* nc: coarse correction scratch */
+} gfea_coarse_level;
+
 typedef struct gfea_batch_instance {
   int32_t version;          /* GFEA_ABI_VERSION */
   int32_t dof_n;
@@ -279,9 +296,23 @@ typedef struct gfea_batch_instance {
   double* x;                /* in: known values + initial guess; out: solution */
   void* work;               /* gfea_batch_workspace_size() bytes, 256-byte aligned */
   gfea_pcg_result* result;  /* device pointer, written when the system's solve ends */
+  gfea_coarse_level coarse; /* two-level preconditioner (n_agg = 0: block-Jacobi only) */
 } gfea_batch_instance;
 
 size_t gfea_batch_workspace_size(int64_t n_nodes, int dof_n, int precision);
+/* Coarse level of one batch system: the aggregation, coarse matrix and
+ * inverse of gfea_pcg_solve's two-level preconditioner (aggregate count from
+ * opts.coarse, automatic when -1, capped at nc = 512), built into 'work'
+ * (gfea_coarse_workspace_size bytes, 256-byte aligned; FP32 coarse matrix for
+ * opts.precision GFEA_F32, FP64 otherwise).  keep_aggregation != 0 keeps the
+ * aggregation a previous call left in the same workspace for the same mesh
+ * ('level' as that call returned it) and rebuilds only the coarse matrix and
+ * its inverse, with device work only (capturable in a CUDA graph); without it
+ * the aggregation reads the mesh's bounding box back to the host once.  No
+ * reference counterpart (the reference solves each instance with SuperLU). */
+int gfea_coarse_workspace_size(const gfea_system* sys_host, const gfea_pcg_opts* opts_host, size_t* bytes_host);
+int gfea_coarse_setup(const gfea_system* sys_host, const gfea_pcg_opts* opts_host, int keep_aggregation,
+                      void* work, size_t work_bytes, gfea_coarse_level* level_host, void* stream);
 size_t gfea_batch_scratch_size(int n_instances);
 /* Enqueues the batch on the stream and returns; results are valid once the
  * stream has completed.  scratch: gfea_batch_scratch_size(n) device bytes

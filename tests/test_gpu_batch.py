@@ -35,14 +35,16 @@ def mixed_batch():
     return [elastic_system(m, 210000.0)[1] for m in ms]
 
 
+@pytest.mark.parametrize("coarse", [0, -1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_matches_single_solves(precision):
+def test_batch_matches_single_solves(precision, coarse):
+    """Block-Jacobi (coarse 0) and two-level (coarse -1) batched PCG."""
     from easyfea_gb300.batching import solve_batch
     from easyfea_gb300.device import pcg
 
     systems = mixed_batch()
     x0 = [s.x.clone() for s in systems]
-    infos = solve_batch(systems, precision=precision)
+    infos = solve_batch(systems, precision=precision, coarse=coarse)
     for s, x_init, info in zip(systems, x0, infos):
         assert info.status == 0
         assert info.rel_residual <= max(1e-10, info.floor_rel)
@@ -53,20 +55,46 @@ def test_batch_matches_single_solves(precision):
         assert err <= 1e-7, f"relative difference {err:.3e}"
 
 
+@pytest.mark.parametrize("coarse", [0, -1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_result_identical_alone_and_in_the_mix(precision):
-    """A system's solution does not depend on the other systems of the batch."""
+def test_result_identical_alone_and_in_the_mix(precision, coarse):
+    """A system's solution does not depend on the other systems of the batch:
+    bit for bit with block-Jacobi; with the coarse level within 1e-8 (its
+    coarse matrix is summed with FP64 atomics when it is rebuilt)."""
     from easyfea_gb300.batching import solve_batch
 
     systems = mixed_batch()
     x0 = [s.x.clone() for s in systems]
-    solve_batch(systems, precision=precision)
+    solve_batch(systems, precision=precision, coarse=coarse)
     mixed = [s.x.clone() for s in systems]
     for k in (0, 3, 4):
         s = systems[k]
         s.x.copy_(x0[k])
-        solve_batch([s], precision=precision)
-        assert np.array_equal(s.x.cpu().numpy(), mixed[k].cpu().numpy()), f"system {k} differs alone / in the mix"
+        solve_batch([s], precision=precision, coarse=coarse)
+        a, b = s.x.cpu().numpy(), mixed[k].cpu().numpy()
+        if coarse == 0:
+            assert np.array_equal(a, b), f"system {k} differs alone / in the mix"
+        else:
+            assert np.abs(a - b).max() <= 1e-8 * np.abs(b).max(), f"system {k} differs alone / in the mix"
+
+
+def test_two_level_batch_cuts_iterations():
+    """The coarse level inside the persistent kernel: same answer as
+    block-Jacobi with several times fewer iterations on the slender bars."""
+    from easyfea_gb300.batching import solve_batch
+
+    systems = mixed_batch()
+    x0 = [s.x.clone() for s in systems]
+    bj = solve_batch(systems, precision="mixed", coarse=0)
+    u_bj = [s.x.clone() for s in systems]
+    for s, x in zip(systems, x0):
+        s.x.copy_(x)
+    tl = solve_batch(systems, precision="mixed", coarse=-1)
+    for s, ub, i0, i1 in zip(systems, u_bj, bj, tl):
+        ref = ub.cpu().numpy()
+        assert np.abs(s.x.cpu().numpy() - ref).max() <= 1e-7 * np.abs(ref).max()
+    big = 4  # the 120 x 13 QUAD4 bar
+    assert tl[big].iterations * 3 < bj[big].iterations, (tl[big].iterations, bj[big].iterations)
 
 
 def test_random_material_batch_matches_oracle():
@@ -88,17 +116,20 @@ def test_random_material_batch_matches_oracle():
         assert np.abs(u - u_ref).max() <= 1e-8 * np.abs(u_ref).max()
 
 
+@pytest.mark.parametrize("coarse", [0, -1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_graph_captured_batch_replays(precision):
-    """Re-assembly of every operator, reset of x and the persistent solve
-    captured as one CUDA graph: each replay gives the direct batch's result."""
+def test_graph_captured_batch_replays(precision, coarse):
+    """Re-assembly of every operator, the coarse matrices and inverses, the
+    reset of x and the persistent solve captured as one CUDA graph: each
+    replay gives the direct batch's result (bit for bit with block-Jacobi,
+    within 1e-8 with the coarse level, whose matrix is summed with atomics)."""
     import torch
 
     from easyfea_gb300.batching import GraphBatch, solve_batch
 
     systems = mixed_batch()
     x0 = [s.x.clone() for s in systems]
-    solve_batch(systems, precision=precision)
+    solve_batch(systems, precision=precision, coarse=coarse)
     direct = [s.x.clone() for s in systems]
     for s, x in zip(systems, x0):
         s.x.copy_(x)
@@ -110,7 +141,7 @@ def test_graph_captured_batch_replays(precision):
             if s.op.vals32 is not None:
                 s.op.vals32.copy_(v)
 
-    gb = GraphBatch(systems, precision=precision, pre=pre)
+    gb = GraphBatch(systems, precision=precision, pre=pre, coarse=coarse)
     for _ in range(2):
         for s in systems:
             s.x.zero_()
@@ -118,4 +149,7 @@ def test_graph_captured_batch_replays(precision):
         infos = gb.results()
         assert all(i.status == 0 for i in infos)
         for s, d in zip(systems, direct):
-            assert torch.equal(s.x, d)
+            if coarse == 0:
+                assert torch.equal(s.x, d)
+            else:
+                assert (s.x - d).abs().max() <= 1e-8 * d.abs().max()

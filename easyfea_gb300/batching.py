@@ -253,3 +253,70 @@ def random_material_cantilevers(n: int = 256, seed: int = 0, dof_min: float = 2e
         E = 210000.0 * np.exp(0.3 * g)
         out.append((m, E))
     return out
+
+
+class RandomMaterialBatch:
+    """The random-material workload assembled and solved as one CUDA graph.
+
+    Per instance (a plane-stress cantilever with per-element E, clamped at
+    x = 0, surface load -800/13^2 in y at x = L, thickness 13): the device
+    mesh, the load vector, the Dirichlet mask and the stiffness operator are
+    built once.  The graph holds, for every instance, the element-stiffness
+    kernel (FP64, per-element moduli) and its FP32 copy, the coarse matrix
+    and inverse of its two-level preconditioner, the reset of x; then the
+    one persistent batched PCG launch for all instances.  ``replay`` runs the
+    whole thing with one graph launch."""
+
+    def __init__(self, instances, precision: str = "mixed", rtol: float = 1e-10, coarse: int = -1):
+        from . import models
+        from .device import DeviceMesh
+        from .simulations import isotropic_lame
+
+        L = _lib.load()
+        self.instances = instances
+        self.systems: List[BatchSystem] = []
+        self._assembly = []
+        lame = isotropic_lame(models.Elastic.Isotropic(2, E=1.0, v=0.3, planeStress=True).C)
+        for m, E in instances:
+            dm = DeviceMesh(m)
+            op = CsrOperator(dm, 2, with_f32=True, translation_invariant=True)
+            C = torch.as_tensor(np.concatenate([lame, np.asarray(E, dtype=np.float64)]), device=_dev())
+            Lx = m.coord[:, 0].max()
+            left = np.where(m.coord[:, 0] == 0)[0]
+            right = np.where(m.coord[:, 0] == Lx)[0]
+            b = torch.zeros(2 * m.Nn, dtype=torch.float64, device=_dev())
+            mask = torch.zeros(m.Nn, dtype=torch.uint8, device=_dev())
+            mask[torch.as_tensor(right, device=_dev())] = 1
+            seg = [g for g in dm.boundary if g.dim == 1][0]
+            _lib.check(L.gfea_surface_load(seg.code, _lib.ptr(dm.coord), _lib.ptr(seg.connect), seg.Ne,
+                                           _lib.ptr(mask), 2, 1, (ctypes.c_int32 * 1)(1),
+                                           (ctypes.c_double * 1)(-800 / 13**2), 13.0, _lib.ptr(b), _lib.stream()),
+                       "surface load")
+            known = torch.zeros(2 * m.Nn, dtype=torch.uint8, device=_dev())
+            kd = np.concatenate([2 * left, 2 * left + 1])
+            known[torch.as_tensor(kd, device=_dev())] = 1
+            x = torch.zeros(2 * m.Nn, dtype=torch.float64, device=_dev())
+            self.systems.append(BatchSystem(op, b, x, known, rtol=rtol))
+            self._assembly.append((dm, op, C))
+        self.assemble()  # values for the coarse aggregation and the capture's first pass
+        torch.cuda.synchronize()
+        self.graph = GraphBatch(self.systems, precision=precision, pre=self.assemble, coarse=coarse)
+
+    def assemble(self):
+        """Element stiffness (FP64, per-element E, thickness 13) and its FP32
+        copy for every instance: device work only."""
+        L = _lib.load()
+        for dm, op, C in self._assembly:
+            g = dm.main
+            _lib.check(L.gfea_assemble_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                               _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C), 4, 13.0,
+                                               _lib.F64, _lib.ptr(op.vals64), op.nnz, 0, _lib.stream()),
+                       "assemble elastic")
+            _lib.check(L.gfea_cast_f64_f32(_lib.ptr(op.vals64), _lib.ptr(op.vals32), op.nnz, _lib.stream()),
+                       "cast")
+
+    def replay(self):
+        self.graph.replay()
+
+    def results(self) -> List[PcgInfo]:
+        return self.graph.results()

@@ -170,6 +170,10 @@ SIGNATURES = {
     "gfea_coarse_workspace_size": (c_int, [POINTER(System), POINTER(PcgOpts), POINTER(c_size_t)]),
     "gfea_coarse_setup": (c_int, [POINTER(System), POINTER(PcgOpts), c_int, c_void_p, c_size_t, POINTER(CoarseLevel),
                                   c_void_p]),
+    "gfea_coarse_batch_scratch_size": (c_size_t, [c_int]),
+    "gfea_coarse_batch_prepare": (c_int, [POINTER(System), POINTER(PcgOpts), c_int, POINTER(c_void_p),
+                                          POINTER(CoarseLevel), c_void_p, c_size_t, c_void_p]),
+    "gfea_coarse_batch_build": (c_int, [c_void_p, c_int, POINTER(c_int32), c_int, c_int, c_void_p]),
     "gfea_batch_workspace_size": (c_size_t, [c_int64, c_int, c_int]),
     "gfea_batch_scratch_size": (c_size_t, [c_int]),
     "gfea_batch_pcg": (c_int, [POINTER(BatchInstance), c_int, c_void_p, c_size_t, POINTER(PcgOpts), c_void_p]),

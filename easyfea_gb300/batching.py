@@ -51,31 +51,74 @@ RESULT_BYTES = ctypes.sizeof(_lib.PcgResult)
 class CoarseLevels:
     """Coarse levels of the batched two-level preconditioner, one workspace
     per system operator, kept between batches: the aggregation (which depends
-    only on the mesh) is built on a system's first setup and kept afterwards,
-    when only the coarse matrix and its inverse are rebuilt from the current
-    values (device work only, so that setup can be captured in a CUDA graph)."""
+    only on the mesh) is built on a system's first sight; afterwards the
+    coarse matrices and inverses of a whole batch are rebuilt from the current
+    values by ``build`` -- device work only, one launch per stage for all
+    systems, so that it can be captured in a CUDA graph."""
 
     def __init__(self):
         self._levels = {}  # id(op) -> (op, precision, workspace, CoarseLevel)
+        self._scratch = None
+        self._n = 0
 
-    def setup(self, s: BatchSystem, precision: int, coarse: int = -1) -> _lib.CoarseLevel:
+    def level(self, s: BatchSystem, precision: int, coarse: int = -1) -> _lib.CoarseLevel:
+        """The system's level; its first call builds the aggregation (and a first matrix)."""
         L = _lib.load()
-        sys_ = s.op.system(s.known)
-        opts = _lib.PcgOpts(_lib.ABI_VERSION, precision, 0, 0, 0.0, 0.0, 0, 0, int(coarse), 0)
         key = id(s.op)
         entry = self._levels.get(key)
-        keep = entry is not None and entry[0] is s.op and entry[1] == precision
-        if not keep:
+        if entry is None or entry[0] is not s.op or entry[1] != precision:
+            sys_ = s.op.system(s.known)
+            opts = _lib.PcgOpts(_lib.ABI_VERSION, precision, 0, 0, 0.0, 0.0, 0, 0, int(coarse), 0)
             nb = ctypes.c_size_t()
             _lib.check(L.gfea_coarse_workspace_size(ctypes.byref(sys_), ctypes.byref(opts), ctypes.byref(nb)),
                        "coarse workspace")
             work = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=_dev())
-            entry = (s.op, precision, work, _lib.CoarseLevel())
+            level = _lib.CoarseLevel()
+            _lib.check(L.gfea_coarse_setup(ctypes.byref(sys_), ctypes.byref(opts), 0, _lib.ptr(work), work.numel(),
+                                           ctypes.byref(level), _lib.stream()), "coarse setup")
+            entry = (s.op, precision, work, level)
             self._levels[key] = entry
-        _, _, work, level = entry
-        _lib.check(L.gfea_coarse_setup(ctypes.byref(sys_), ctypes.byref(opts), int(keep), _lib.ptr(work),
-                                       work.numel(), ctypes.byref(level), _lib.stream()), "coarse setup")
-        return level
+        return entry[3]
+
+    def prepare(self, systems: List[BatchSystem], precision: int, coarse: int = -1):
+        """Levels of every system and the descriptors of the batched rebuild."""
+        L = _lib.load()
+        order = sorted(range(len(systems)), key=lambda i: systems[i].op.dof_n)
+        n = len(order)
+        sys_arr = (_lib.System * max(n, 1))()
+        works = (ctypes.c_void_p * max(n, 1))()
+        lvls = (_lib.CoarseLevel * max(n, 1))()
+        keep = []  # the System structures hold raw pointers into these tensors
+        for k, i in enumerate(order):
+            s = systems[i]
+            lvl = self.level(s, precision, coarse)
+            sys_arr[k] = s.op.system(s.known)
+            works[k] = self._levels[id(s.op)][2].data_ptr()
+            lvls[k] = lvl
+            keep.append(s)
+        first = [n, n, n, n]
+        for k, i in enumerate(order):
+            d = systems[i].op.dof_n
+            first[d - 1] = min(first[d - 1], k)
+        for d in (2, 1, 0):  # no system of dof_n = d + 1: its range is empty at the next start
+            if first[d] == n:
+                first[d] = first[d + 1]
+        self._first = (ctypes.c_int32 * 4)(*first)
+        self._max_nc = max([lvls[k].nc for k in range(n)] + [0])
+        nb = int(L.gfea_coarse_batch_scratch_size(n))
+        if self._scratch is None or self._scratch.numel() < nb:
+            self._scratch = torch.empty(max(nb, 256), dtype=torch.uint8, device=_dev())
+        opts = _lib.PcgOpts(_lib.ABI_VERSION, precision, 0, 0, 0.0, 0.0, 0, 0, int(coarse), 0)
+        _lib.check(L.gfea_coarse_batch_prepare(sys_arr, ctypes.byref(opts), n, works, lvls, _lib.ptr(self._scratch),
+                                               self._scratch.numel(), _lib.stream()), "coarse batch prepare")
+        self._n = n
+        self._prec = precision
+        return [self._levels[id(s.op)][3] for s in systems]
+
+    def build(self):
+        """Rebuild the prepared batch's coarse matrices and inverses (device work only)."""
+        _lib.check(_lib.load().gfea_coarse_batch_build(_lib.ptr(self._scratch), self._n, self._first, self._max_nc,
+                                                       self._prec, _lib.stream()), "coarse batch build")
 
 
 class BatchSolver:
@@ -109,11 +152,10 @@ class BatchSolver:
                                                  _lib.stream()), "batch launch")
 
     def setup_coarse(self, systems: List[BatchSystem], coarse: int = -1):
-        """(Re)build every system's coarse matrix and inverse from its current
-        values (device work only once the aggregations exist)."""
-        for s, lvl in zip(systems, self._levels):
-            if lvl is not None:
-                self.coarse_levels.setup(s, self._prec, coarse)
+        """Rebuild every system's coarse matrix and inverse from its current
+        values (device work only, one launch per stage for the batch)."""
+        if coarse != 0 and self._levels and self._levels[0] is not None:
+            self.coarse_levels.build()
 
     def prepare(self, systems: List[BatchSystem], precision: str = "mixed", inner_rtol: float = 0.0,
                 coarse: int = -1):
@@ -138,8 +180,11 @@ class BatchSolver:
         base = self._arena.data_ptr()
         rbase = self._results.data_ptr()
         self._prec = prec
-        self._levels = [self.coarse_levels.setup(s, prec, coarse) if coarse != 0 and s.op.dmesh.coord is not None
-                        else None for s in systems]
+        if coarse != 0:
+            self._levels = self.coarse_levels.prepare(systems, prec, coarse)
+            self.coarse_levels.build()
+        else:
+            self._levels = [None] * n
         for i, s in enumerate(systems):
             d = s.op.dmesh
             arr[i] = _lib.BatchInstance(

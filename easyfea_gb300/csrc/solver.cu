@@ -31,6 +31,7 @@
 #include <atomic>
 #include <chrono>
 #include <mutex>
+#include <vector>
 
 #include "coarse.cuh"
 #include "common.cuh"
@@ -470,10 +471,10 @@ __global__ void aggregate_kernel(const double* __restrict__ coord, int64_t Nn, d
 // a coarse matrix accurate to ~1e-6, plenty for a preconditioner, on the FP32
 // pipe; sums go to A_c in FP64).
 template <int D, typename T>
-__global__ void coarse_assemble_kernel(SysT<T> S, CoarseDev C) {
+__device__ __forceinline__ void coarse_assemble_body(const SysT<T>& S, const CoarseDev& C, int64_t bx, int64_t gx) {
   constexpr int nr = Modes<D>::nr;
   constexpr int kSlots = 8;
-  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < S.Nn; a += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t a = bx * (int64_t)blockDim.x + threadIdx.x; a < S.Nn; a += gx * blockDim.x) {
     const int ga = C.agg[a];
     T Ra[D][nr];
     node_modes<D, T>(C.off[a], S.known + a * D, Ra);
@@ -525,12 +526,17 @@ __global__ void coarse_assemble_kernel(SysT<T> S, CoarseDev C) {
   }
 }
 
+template <int D, typename T>
+__global__ void coarse_assemble_kernel(SysT<T> S, CoarseDev C) {
+  coarse_assemble_body<D, T>(S, C, blockIdx.x, gridDim.x);
+}
+
 // Unit diagonal for empty or fully constrained coarse DOFs, a 1e-10 relative
 // shift elsewhere (rotation modes of degenerate aggregates), identity in inv.
 // (zero_tol, shift): (1e-14, 1e-10) for a coarse matrix built in FP64,
 // (1e-6, 1e-6) for one built from FP32 values, whose rounding can reach the
 // 1e-6 level in nearly degenerate modes.
-__global__ void coarse_regularize_kernel(CoarseDev C, double zero_tol, double shift) {
+__device__ __forceinline__ void coarse_regularize_body(const CoarseDev& C, double zero_tol, double shift) {
   __shared__ double smax[256];
   double m = 0;
   for (int i = threadIdx.x; i < C.nc; i += blockDim.x) m = fmax(m, fabs(C.Ac[(int64_t)i * C.nc + i]));
@@ -545,6 +551,10 @@ __global__ void coarse_regularize_kernel(CoarseDev C, double zero_tol, double sh
     double& d = C.Ac[(int64_t)i * C.nc + i];
     d = d > zero_tol * dmax ? d + shift * dmax : dmax;
   }
+}
+
+__global__ void coarse_regularize_kernel(CoarseDev C, double zero_tol, double shift) {
+  coarse_regularize_body(C, zero_tol, shift);
 }
 
 // In-place blocked Gauss-Jordan inversion of the SPD coarse matrix (no
@@ -597,12 +607,11 @@ __global__ void ff_merge_kernel(double* __restrict__ a, const float* __restrict_
     a[i] = (double)hi[i] + (double)lo[i];
 }
 
-__global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int b) {
-  // block (bx, l): row l of the transformed row panel for columns bx * 128 ..;
-  // every block inverts the b x b pivot block itself (b steps in shared
-  // memory, FP64), so the panel's work spreads over n / 128 x b blocks
+// block (bx, l): row l of the transformed row panel for columns bx * 128 ..;
+// every block inverts the b x b pivot block itself (b steps in shared
+// memory, FP64), so the panel's work spreads over n / 128 x b blocks
+__device__ __forceinline__ void gj_panel_body(const CoarseDev& C, int k0, int b, int bx, int l) {
   const int n = C.nc;
-  const int l = blockIdx.y;
   __shared__ double M[kGJB][kGJB + 1], M2[kGJB][kGJB + 1];
   for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
     const int64_t q = (int64_t)(k0 + t / b) * n + k0 + t % b;
@@ -619,9 +628,9 @@ __global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int 
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) M[t / b][t % b] = M2[t / b][t % b];
     __syncthreads();
   }
-  if (blockIdx.x == 0 && l == 0)
+  if (bx == 0 && l == 0)
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) ff_split(M[t / b][t % b], C.pinvh[t], C.pinvl[t]);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = bx * blockDim.x + threadIdx.x;
   if (j >= n) return;
   double s = 0;
 #pragma unroll
@@ -641,10 +650,14 @@ __global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int 
   }
 }
 
+__global__ void __launch_bounds__(128) gj_panel_kernel(CoarseDev C, int k0, int b) {
+  gj_panel_body(C, k0, b, blockIdx.x, blockIdx.y);
+}
+
 // Block (bx, by) owns column j = bx * blockDim + tid and rows by, by + gridDim.y, ...
-__global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int b) {
+__device__ __forceinline__ void gj_update_body(const CoarseDev& C, int k0, int b, int bx, int by, int gy) {
   const int n = C.nc;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = bx * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const bool jk = j >= k0 && j < k0 + b;
   float rh[kGJB], rl[kGJB];
@@ -654,7 +667,7 @@ __global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int
     rh[l] = l < b ? (jk ? C.pinvh[q] : C.rowph[q]) : 0.f;
     rl[l] = l < b ? (jk ? C.pinvl[q] : C.rowpl[q]) : 0.f;
   }
-  for (int i = blockIdx.y; i < n; i += gridDim.y) {
+  for (int i = by; i < n; i += gy) {
     const int64_t q = (int64_t)i * n + j;
     float vh, vl;
     if (i >= k0 && i < k0 + b) {
@@ -672,6 +685,10 @@ __global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int
     C.Ahi[q] = vh;
     C.Alo[q] = vl;
   }
+}
+
+__global__ void __launch_bounds__(128) gj_update_kernel(CoarseDev C, int k0, int b) {
+  gj_update_body(C, k0, b, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 template <int nr, typename T>
@@ -2430,6 +2447,171 @@ extern "C" int gfea_coarse_setup(const gfea_system* s, const gfea_pcg_opts* o, i
   level->inv32 = cw.inv32;
   level->rc = C.rc;
   level->ec = C.ec;
+  return GFEA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse matrices and inverses of a whole batch with one launch per stage:
+// the single-system stages above, with blockIdx.y (elementwise and assembly
+// stages) or blockIdx.z (Gauss-Jordan panels) selecting the system.  A batch
+// of 256 systems otherwise records ~15,000 launches, each a few microseconds.
+// ---------------------------------------------------------------------------
+
+struct CoarseJob {
+  CoarseDev C;
+  int64_t Nn;
+  const int32_t* node_ptr;
+  const int32_t* nbr;
+  const void* vals;  // the iteration's value type
+  const uint8_t* known;
+  float* inv32;
+  int32_t dof_n;
+  int32_t diff;
+};
+
+__global__ void cb_zero_kernel(const CoarseJob* __restrict__ jobs) {
+  const CoarseDev C = jobs[blockIdx.y].C;
+  const int64_t n2 = (int64_t)C.nc * C.nc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+    C.Ac[i] = 0.0;
+}
+
+template <int D, typename T>
+__global__ void cb_assemble_kernel(const CoarseJob* __restrict__ jobs, int first) {
+  const CoarseJob& J = jobs[first + blockIdx.y];
+  if (J.dof_n != D) return;
+  const SysT<T> S{J.Nn, J.node_ptr, J.nbr, static_cast<const T*>(J.vals), J.known, J.diff};
+  coarse_assemble_body<D, T>(S, J.C, blockIdx.x, gridDim.x);
+}
+
+__global__ void cb_regularize_kernel(const CoarseJob* __restrict__ jobs, double zero_tol, double shift) {
+  coarse_regularize_body(jobs[blockIdx.x].C, zero_tol, shift);
+}
+
+__global__ void cb_split_kernel(const CoarseJob* __restrict__ jobs) {
+  const CoarseDev C = jobs[blockIdx.y].C;
+  const int64_t n2 = (int64_t)C.nc * C.nc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+    ff_split(C.Ac[i], C.Ahi[i], C.Alo[i]);
+}
+
+// merge the float-float pairs back into A_c^-1 and write its FP32 copy
+__global__ void cb_merge_kernel(const CoarseJob* __restrict__ jobs) {
+  const CoarseJob& J = jobs[blockIdx.y];
+  const CoarseDev C = J.C;
+  const int64_t n2 = (int64_t)C.nc * C.nc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (double)C.Ahi[i] + (double)C.Alo[i];
+    C.Ac[i] = v;
+    J.inv32[i] = (float)v;
+  }
+}
+
+__global__ void __launch_bounds__(128) cb_gj_panel_kernel(const CoarseJob* __restrict__ jobs, int k0) {
+  const CoarseDev C = jobs[blockIdx.z].C;
+  if (k0 >= C.nc) return;
+  const int b = C.nc - k0 < kGJB ? C.nc - k0 : kGJB;
+  if ((int)blockIdx.y >= b || (int)(blockIdx.x * blockDim.x) >= C.nc) return;
+  gj_panel_body(C, k0, b, blockIdx.x, blockIdx.y);
+}
+
+__global__ void __launch_bounds__(128) cb_gj_update_kernel(const CoarseJob* __restrict__ jobs, int k0) {
+  const CoarseDev C = jobs[blockIdx.z].C;
+  if (k0 >= C.nc) return;
+  const int b = C.nc - k0 < kGJB ? C.nc - k0 : kGJB;
+  gj_update_body(C, k0, b, blockIdx.x, blockIdx.y, gridDim.y);
+}
+
+extern "C" size_t gfea_coarse_batch_scratch_size(int n) {
+  return n < 0 ? 0 : align256(sizeof(CoarseJob) * (size_t)(n > 0 ? n : 1));
+}
+
+extern "C" int gfea_coarse_batch_prepare(const gfea_system* systems, const gfea_pcg_opts* o, int n,
+                                         void* const* works, const gfea_coarse_level* levels, void* scratch,
+                                         size_t scratch_bytes, void* stream) {
+  if (!systems || !o || n < 0 || (n > 0 && (!works || !levels)) || !scratch) return GFEA_ERR_ARG;
+  if (o->version != GFEA_ABI_VERSION || (o->precision != GFEA_F32 && o->precision != GFEA_F64)) return GFEA_ERR_ARG;
+  if (scratch_bytes < gfea_coarse_batch_scratch_size(n)) return GFEA_ERR_WORKSPACE;
+  if (n == 0) return GFEA_OK;
+  const bool f32 = o->precision == GFEA_F32;
+  std::vector<CoarseJob> jobs((size_t)n);
+  // systems of one dof_n are contiguous (the assembly stage runs per dof_n)
+  for (int i = 0; i < n; ++i) {
+    const gfea_system* s = &systems[i];
+    const gfea_coarse_level& L = levels[i];
+    if (s->version != GFEA_ABI_VERSION || s->n_nodes <= 0 || s->dof_n < 1 || s->dof_n > 3 || !works[i])
+      return GFEA_ERR_ARG;
+    if (i > 0 && s->dof_n < systems[i - 1].dof_n) return GFEA_ERR_ARG;
+    if (!(f32 ? (const void*)s->vals32 : (const void*)s->vals64)) return GFEA_ERR_ARG;
+    const int target = batch_coarse_target(s, o);
+    CoarseLevelWork cw;
+    coarse_level_layout(s->n_nodes, s->dof_n, target, &cw, static_cast<char*>(works[i]));
+    // the aggregation a gfea_coarse_setup call left in this workspace
+    if (target <= 0 || L.n_agg < 1 || L.n_agg > target || L.nr != coarse_nr(s->dof_n) || L.nc != L.nr * L.n_agg ||
+        L.agg != cw.C.agg)
+      return GFEA_ERR_ARG;
+    CoarseJob& J = jobs[(size_t)i];
+    J.C = cw.C;
+    J.C.nr = L.nr;
+    J.C.n_agg = L.n_agg;
+    J.C.nc = L.nc;
+    J.C.ncopies = 1;
+    J.Nn = s->n_nodes;
+    J.node_ptr = s->node_ptr;
+    J.nbr = s->nbr;
+    J.vals = f32 ? (const void*)s->vals32 : (const void*)s->vals64;
+    J.known = s->known;
+    J.inv32 = cw.inv32;
+    J.dof_n = s->dof_n;
+    J.diff = s->translation_invariant;
+  }
+  GFEA_CUDA_TRY(cudaMemcpyAsync(scratch, jobs.data(), sizeof(CoarseJob) * (size_t)n, cudaMemcpyHostToDevice,
+                                static_cast<cudaStream_t>(stream)));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));  // jobs leaves scope
+  return GFEA_OK;
+}
+
+extern "C" int gfea_coarse_batch_build(const void* scratch, int n, const int32_t* dof_n_first_host, int max_nc,
+                                       int precision, void* stream) {
+  if (!scratch || n < 0 || !dof_n_first_host || max_nc < 0 || max_nc > kBatchCoarseMax) return GFEA_ERR_ARG;
+  if (precision != GFEA_F32 && precision != GFEA_F64) return GFEA_ERR_ARG;
+  if (n == 0 || max_nc == 0) return GFEA_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const auto* jobs = static_cast<const CoarseJob*>(scratch);
+  const int64_t n2 = (int64_t)max_nc * max_nc;
+  const int ge = (int)std::min<int64_t>(ceil_div(n2, kThreads), 64);
+  cb_zero_kernel<<<dim3(ge, n), kThreads, 0, st>>>(jobs);
+  GFEA_LAUNCH_CHECK();
+  // dof_n_first_host[d - 1] = first system with dof_n = d (n if none), d = 1..3; [3] = n
+  for (int d = 1; d <= 3; ++d) {
+    const int first = dof_n_first_host[d - 1], last = dof_n_first_host[d];
+    if (first < 0 || last > n || first > last) return GFEA_ERR_ARG;
+    if (first == last) continue;
+    const dim3 grid(kSMs, last - first);
+    if (precision == GFEA_F32) {
+      GFEA_D_SWITCH(d, (cb_assemble_kernel<DD, float><<<grid, kThreads, 0, st>>>(jobs, first)));
+    } else {
+      GFEA_D_SWITCH(d, (cb_assemble_kernel<DD, double><<<grid, kThreads, 0, st>>>(jobs, first)));
+    }
+    GFEA_LAUNCH_CHECK();
+  }
+  if (precision == GFEA_F32)
+    cb_regularize_kernel<<<n, 256, 0, st>>>(jobs, 1e-6, 1e-6);
+  else
+    cb_regularize_kernel<<<n, 256, 0, st>>>(jobs, 1e-14, 1e-10);
+  GFEA_LAUNCH_CHECK();
+  cb_split_kernel<<<dim3(ge, n), kThreads, 0, st>>>(jobs);
+  GFEA_LAUNCH_CHECK();
+  const int gx = (int)ceil_div(max_nc, 128);
+  const int gy = (int)std::min<int64_t>(max_nc, 16);
+  for (int k0 = 0; k0 < max_nc; k0 += kGJB) {
+    cb_gj_panel_kernel<<<dim3(gx, kGJB, n), 128, 0, st>>>(jobs, k0);
+    GFEA_LAUNCH_CHECK();
+    cb_gj_update_kernel<<<dim3(gx, gy, n), 128, 0, st>>>(jobs, k0);
+    GFEA_LAUNCH_CHECK();
+  }
+  cb_merge_kernel<<<dim3(ge, n), kThreads, 0, st>>>(jobs);
+  GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
 

@@ -313,6 +313,20 @@ size_t gfea_batch_workspace_size(int64_t n_nodes, int dof_n, int precision);
 int gfea_coarse_workspace_size(const gfea_system* sys_host, const gfea_pcg_opts* opts_host, size_t* bytes_host);
 int gfea_coarse_setup(const gfea_system* sys_host, const gfea_pcg_opts* opts_host, int keep_aggregation,
                       void* work, size_t work_bytes, gfea_coarse_level* level_host, void* stream);
+/* The coarse matrices and inverses of a whole batch rebuilt from the current
+ * values with one launch per stage (instead of ~60 per system): prepare
+ * uploads one descriptor per system into scratch
+ * (gfea_coarse_batch_scratch_size(n) bytes) from systems[i], works[i] and
+ * levels[i] as gfea_coarse_setup returned them (its aggregation is kept;
+ * systems ordered by dof_n); build enqueues device work only (capturable):
+ * dof_n_first[d - 1] = index of the first system with dof_n = d (d = 1..3,
+ * n when there is none), dof_n_first[3] = n; max_nc = the largest level's nc. */
+size_t gfea_coarse_batch_scratch_size(int n);
+int gfea_coarse_batch_prepare(const gfea_system* systems_host, const gfea_pcg_opts* opts_host, int n,
+                              void* const* works_host, const gfea_coarse_level* levels_host, void* scratch,
+                              size_t scratch_bytes, void* stream);
+int gfea_coarse_batch_build(const void* scratch, int n, const int32_t* dof_n_first_host, int max_nc,
+                            int precision, void* stream);
 size_t gfea_batch_scratch_size(int n_instances);
 /* Enqueues the batch on the stream and returns; results are valid once the
  * stream has completed.  scratch: gfea_batch_scratch_size(n) device bytes

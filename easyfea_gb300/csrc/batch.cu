@@ -153,6 +153,62 @@ __device__ void restart_rz(const gfea_batch_instance& I, const BatchBuf<T>& w, i
   }
 }
 
+// node_rows for R nodes at once (one G-lane group): the index, value and
+// gathered-vector loads of the R rows in a pass are independent and issued
+// together.  A cluster runs 16 warps per SM, too few to hide the three
+// dependent L2 round trips of a row (row pointer, neighbour index, gather)
+// one row at a time.
+template <int D, int G, typename T, bool DIFF, int R, typename XF>
+__device__ __forceinline__ void node_rows_multi(const int64_t (&a)[R], int lane, const SysT<T>& S, XF xf,
+                                                T (&acc)[R][D]) {
+  constexpr int LA = G - G % D;
+  constexpr int NPP = LA / D;
+  const int j = lane % D;
+  int32_t p0[R], nb[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    p0[r] = S.node_ptr[a[r]];
+    nb[r] = S.node_ptr[a[r] + 1] - p0[r];
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int i = 0; i < D; ++i) acc[r][i] = 0;
+  if (lane < LA) {
+    T self[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) self[r] = DIFF ? xf(a[r] * D + j) : (T)0;
+    int32_t maxnb = nb[0];
+#pragma unroll
+    for (int r = 1; r < R; ++r) maxnb = nb[r] > maxnb ? nb[r] : maxnb;
+    for (int32_t k = lane / D, t = lane; k < maxnb; k += NPP, t += LA) {
+      int32_t c[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) c[r] = k < nb[r] ? __ldg(S.nbr + p0[r] + k) : -1;
+      T v[R][D];
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+          v[r][i] = c[r] >= 0 ? __ldg(S.vals + (int64_t)D * D * p0[r] + (int64_t)i * D * nb[r] + t) : (T)0;
+      T xv[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const T x = c[r] >= 0 ? xf((int64_t)c[r] * D + j) : (T)0;
+        xv[r] = DIFF && c[r] >= 0 ? x - self[r] : x;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int i = 0; i < D; ++i) acc[r][i] += v[r][i] * xv[r];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int i = 0; i < D; ++i) acc[r][i] = group_sum<G, T>(acc[r][i]);
+}
+
 // Coarse correction of the two-level preconditioner, cluster-wide:
 // rc = R^T r (one warp per aggregate, its nodes in ascending order, fixed
 // butterfly), ec = A_c^-1 rc (one warp per row; FP32 inverse for the FP32
@@ -358,26 +414,34 @@ __device__ void solve_instance(Ctx& c, const gfea_batch_instance& I, double delt
       double va[1] = {0}, oa[1];
       DotAcc<T> pap_acc;
       const T bt = (T)beta;
-      for (int64_t a0 = grp - sub; a0 < Nn; a0 += ngrp) {
-        const int64_t a = a0 + sub;
-        const int64_t ac = a < Nn ? a : Nn - 1;
-        T acc[D];
+      constexpr int R = 4;  // rows per group per round
+      for (int64_t a0 = grp - sub; a0 < Nn; a0 += (int64_t)R * ngrp) {
+        int64_t an[R], ac[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          an[r] = a0 + sub + (int64_t)r * ngrp;
+          ac[r] = an[r] < Nn ? an[r] : Nn - 1;
+        }
+        T acc[R][D];
         auto dir = [&](int64_t cc) { return ldcg(w.z + cc) + bt * ldcg(pa + cc); };
         if (diff)
-          node_rows<D, G, T, T, false, true>(ac, lane, S, dir, acc);
+          node_rows_multi<D, G, T, true, R>(ac, lane, S, dir, acc);
         else
-          node_rows<D, G, T, T>(ac, lane, S, dir, acc);
-        if (a < Nn && lane < D) {
-          T av = acc[0];
+          node_rows_multi<D, G, T, false, R>(ac, lane, S, dir, acc);
 #pragma unroll
-          for (int i = 1; i < D; ++i)
-            if (lane == i) av = acc[i];
-          const int64_t dof = a * D + lane;
-          const T pn = ldcg(w.z + dof) + bt * ldcg(pa + dof);
-          if (S.known[dof]) av = 0;
-          pb[dof] = pn;
-          w.Ap[dof] = av;
-          pap_acc.add_prod(pn, av);
+        for (int r = 0; r < R; ++r) {
+          if (an[r] < Nn && lane < D) {
+            T av = acc[r][0];
+#pragma unroll
+            for (int i = 1; i < D; ++i)
+              if (lane == i) av = acc[r][i];
+            const int64_t dof = an[r] * D + lane;
+            const T pn = ldcg(w.z + dof) + bt * ldcg(pa + dof);
+            if (S.known[dof]) av = 0;
+            pb[dof] = pn;
+            w.Ap[dof] = av;
+            pap_acc.add_prod(pn, av);
+          }
         }
       }
       va[0] = pap_acc.value();
@@ -498,7 +562,7 @@ __device__ void dispatch(Ctx& c, const gfea_batch_instance& I, double delta2) {
   }
 }
 
-__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kBT)
+__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kBT, 2)
     batch_pcg_kernel(const gfea_batch_instance* __restrict__ insts, int n, int* next, int fp64, double delta2) {
   __shared__ double slots[8];
   __shared__ double sh[32];

@@ -304,6 +304,168 @@ def run_elastic(req: ElasticRequest, cache: MeshCache, precision: str, rtol: flo
 
 
 # ---------------------------------------------------------------------------
+# batched small solves
+# ---------------------------------------------------------------------------
+
+class _Slot:
+    """Device state of one batch position on one mesh: stiffness operator
+    (FP64 + FP32), load vector, Dirichlet mask and initial x, kept across
+    batches so that the coarse aggregation is built once per slot."""
+
+    def __init__(self, spec: MeshSpec, cache: MeshCache):
+        from . import _lib
+        from .batching import BatchSystem
+        from .device import CsrOperator
+        from .simulations import isotropic_lame
+
+        m, dm, nodes = cache.get(spec)
+        D = spec.dim
+        self.dm = dm
+        self.op = CsrOperator(dm, D, with_f32=True, translation_invariant=True)
+        if D == 2:
+            ref = ElasticModels.Isotropic(2, E=1.0, v=0.3, planeStress=True, thickness=13.0)
+        else:
+            ref = ElasticModels.Isotropic(3, E=1.0, v=0.3, planeStress=False)
+        self.lame = isotropic_lame(ref.C)
+        self.thickness = 13.0 if D == 2 else 1.0
+        self.C_hom = torch.as_tensor(self.lame * 210000.0)
+        L = _lib.load()
+        b = torch.zeros(D * m.Nn, dtype=torch.float64)
+        b = b.cuda()
+        mask = torch.zeros(m.Nn, dtype=torch.uint8, device=b.device)
+        mask[torch.as_tensor(nodes["right"], device=b.device)] = 1
+        for g in dm.boundary:
+            if g.dim != D - 1:
+                continue
+            comp, val = (1, -800 / 13**2) if D == 2 else (2, -1.0)
+            _lib.check(L.gfea_surface_load(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne, _lib.ptr(mask), D,
+                                           1, (__import__("ctypes").c_int32 * 1)(comp),
+                                           (__import__("ctypes").c_double * 1)(val), self.thickness, _lib.ptr(b),
+                                           _lib.stream()), "surface load")
+        known = torch.zeros(D * m.Nn, dtype=torch.uint8, device=b.device)
+        left = nodes["left"]
+        known[torch.as_tensor(np.concatenate([D * left + c for c in range(D)]), device=b.device)] = 1
+        self.C_hom = self.C_hom.to(b.device)
+        self.system = BatchSystem(self.op, b, torch.zeros(D * m.Nn, dtype=torch.float64, device=b.device), known)
+
+    def assemble(self, E: Optional[np.ndarray]):
+        """K of this request (homogeneous E = 210000, or per element) in FP64 and FP32; x reset."""
+        from . import _lib
+
+        L = _lib.load()
+        g = self.dm.main
+        if E is None:
+            C, mode = self.C_hom, 3
+        else:
+            C = torch.as_tensor(np.concatenate([self.lame, np.asarray(E, dtype=np.float64)]), device=self.op.vals64.device)
+            mode = 4
+        _lib.check(L.gfea_assemble_elastic(g.code, _lib.ptr(self.dm.coord), _lib.ptr(g.connect), g.Ne,
+                                           _lib.ptr(self.dm.node_ptr), _lib.ptr(self.dm.rank), _lib.ptr(C), mode,
+                                           self.thickness, _lib.F64, _lib.ptr(self.op.vals64), self.op.nnz, 0,
+                                           _lib.stream()), "assemble elastic")
+        _lib.check(L.gfea_cast_f64_f32(_lib.ptr(self.op.vals64), _lib.ptr(self.op.vals32), self.op.nnz,
+                                       _lib.stream()), "cast")
+        self.system.x.zero_()
+        return C  # kept alive until the batch has run
+
+
+class SmallBatcher:
+    """Serves small elastic requests (at most ``max_dof`` DOF) by batching
+    their PCG iterations: requests admitted within ``window_s`` of the first
+    one waiting (at most ``max_batch``) are assembled on the batcher's stream
+    and solved together by one persistent launch of the batched two-level PCG
+    (gfea_batch_pcg), each system with its own convergence test (its cluster
+    stops when its residual does), so a result does not depend on the rest of
+    the batch beyond rounding."""
+
+    def __init__(self, server: "Server", max_dof: int, window_s: float, max_batch: int):
+        from .batching import BatchSolver
+
+        self.server = server
+        self.max_dof = max_dof
+        self.window_s = window_s
+        self.max_batch = max_batch
+        self.queue: "queue.Queue" = queue.Queue()
+        self.solver = BatchSolver()
+        self.slots: Dict[Tuple[MeshSpec, int], _Slot] = {}
+        self.batches = 0
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def accepts(self, req) -> bool:
+        return req.kind == "elastic" and req.spec.dof <= self.max_dof
+
+    def _run(self):
+        torch.cuda.set_device(self.server.device)
+        stream = torch.cuda.Stream()
+        while True:
+            item = self.queue.get()
+            if item is None:
+                return
+            items = [item]
+            t_end = time.perf_counter() + self.window_s
+            while len(items) < self.max_batch:
+                left = t_end - time.perf_counter()
+                try:
+                    nxt = self.queue.get(timeout=max(left, 0.0)) if left > 0 else self.queue.get_nowait()
+                except queue.Empty:
+                    break
+                if nxt is None:
+                    self.queue.put(None)
+                    break
+                items.append(nxt)
+            self._execute(items, stream)
+
+    def _execute(self, items, stream):
+        srv = self.server
+        results = []
+        start = time.perf_counter()
+        try:
+            with torch.cuda.stream(stream):
+                count: Dict[MeshSpec, int] = {}
+                systems, keep = [], []
+                for req, arrival, fp in items:
+                    k = count.get(req.spec, 0)
+                    count[req.spec] = k + 1
+                    key = (req.spec, k)
+                    if key not in self.slots:
+                        self.slots[key] = _Slot(req.spec, srv.cache)
+                    slot = self.slots[key]
+                    keep.append(slot.assemble(req.E))
+                    slot.system.rtol = srv.rtol
+                    systems.append(slot.system)
+                infos = self.solver.solve(systems, precision="fp64" if srv.precision == "fp64" else "mixed",
+                                          raise_on_fail=False)
+                self.batches += 1
+                for (req, arrival, fp), s, info in zip(items, systems, infos):
+                    res = Result(req.rid, req.kind, req.spec.dof, arrival=arrival, start=start)
+                    res.iterations, res.rel_residual, res.status = info.iterations, info.rel_residual, info.status
+                    if req.keep_solution:
+                        res.u = s.x.cpu().numpy()
+                    results.append((res, fp))
+                stream.synchronize()
+        except Exception as e:  # reported per request, the server keeps running
+            results = []
+            for req, arrival, fp in items:
+                res = Result(req.rid, req.kind, req.spec.dof, arrival=arrival, start=start)
+                res.error = f"{type(e).__name__}: {e}"
+                res.status = -1
+                results.append((res, fp))
+        end = time.perf_counter()
+        with srv._cv:
+            for res, fp in results:
+                res.end = end
+                srv.results[res.rid] = res
+                srv.in_use -= fp
+                srv._outstanding -= 1
+            srv._cv.notify_all()
+
+    def close(self):
+        self.queue.put(None)
+        self.thread.join()
+
+
+# ---------------------------------------------------------------------------
 # server
 # ---------------------------------------------------------------------------
 
@@ -312,11 +474,16 @@ class Server:
 
     def __init__(self, workers: int = 8, hbm_budget: Optional[int] = None, precision: str = "mixed",
                  rtol: float = 1e-10, max_bypass: int = 8, cache: Optional[MeshCache] = None,
-                 executor=None, tune: bool = True):
+                 executor=None, tune: bool = True, batch_max_dof: int = 0, batch_window_s: float = 0.002,
+                 batch_max: int = 64):
         """``executor(request, result)``: runs one request (default: the GPU
         path on the worker's stream); replaceable to test the scheduling.
         ``tune``: the first request of each problem class tunes the SpMV and
-        element-kernel schedules (process-wide autotuner mode 2)."""
+        element-kernel schedules (process-wide autotuner mode 2).
+        ``batch_max_dof`` > 0: elastic requests up to that many DOF skip the
+        workers and are solved in batches (``SmallBatcher``: one persistent
+        batched PCG launch per batch, ``batch_window_s`` to gather one, at
+        most ``batch_max`` requests)."""
         if executor is None and tune:
             from . import autotune
 
@@ -342,6 +509,8 @@ class Server:
         self._workers = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(workers)]
         self._dispatcher = threading.Thread(target=self._dispatch, daemon=True)
         self.device = torch.cuda.current_device() if executor is None else None
+        self.batcher = (SmallBatcher(self, batch_max_dof, batch_window_s, batch_max)
+                        if batch_max_dof > 0 and executor is None else None)
         for t in self._workers:
             t.start()
         self._dispatcher.start()
@@ -366,7 +535,7 @@ class Server:
             with self._cv:
                 item = None
                 while not self._stop:
-                    item = self._take() if self._free_workers > 0 else None
+                    item = self._take(self._free_workers > 0)
                     if item is not None:
                         break
                     self._cv.wait(timeout=0.05)
@@ -375,15 +544,28 @@ class Server:
                 _, req, arrival, fp = item
                 self.in_use += fp
                 self.peak_in_use = max(self.peak_in_use, self.in_use)
-                self._free_workers -= 1
-            self._ready.put((req, arrival, fp))
+                batched = self.batcher is not None and self.batcher.accepts(req)
+                if not batched:
+                    self._free_workers -= 1
+            if batched:
+                self.batcher.queue.put((req, arrival, fp))
+            else:
+                self._ready.put((req, arrival, fp))
 
-    def _take(self):
+    def _take(self, worker_free: bool = True):
+        """The next admissible request in arrival order: its footprint fits,
+        and a worker is free unless the batcher takes it (requests waiting for
+        a worker do not hold back batched ones).  A request that does not fit
+        may be passed by later ones at most max_bypass times."""
         room = self.budget - self.in_use
         for i, p in enumerate(self._pending):
+            needs_worker = self.batcher is None or not self.batcher.accepts(p[1])
+            if needs_worker and not worker_free:
+                continue
             if p[3] <= room:
                 for q in self._pending[:i]:
-                    q[0] += 1
+                    if q[3] > room:
+                        q[0] += 1
                 return self._pending.pop(i)
             if p[0] >= self.max_bypass:  # the head has waited long enough: hold the rest
                 return None
@@ -453,6 +635,8 @@ class Server:
         for t in self._workers:
             t.join()
         self._dispatcher.join()
+        if self.batcher is not None:
+            self.batcher.close()
 
     def __enter__(self):
         return self

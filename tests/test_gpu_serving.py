@@ -87,3 +87,38 @@ def _nx_ny(m):
     nx = len(np.unique(x[:, 0])) - 1
     ny = len(np.unique(x[:, 1])) - 1
     return nx, ny
+
+
+@pytest.mark.parametrize("batch_max_dof", [40_000])
+def test_batched_small_requests(batch_max_dof):
+    """Small elastic requests served through the batcher (one persistent
+    batched two-level PCG launch per batch, per-system convergence): every
+    result against one-at-a-time FP64 solves within 1e-8, the same alone (a
+    batch of one) and in the mix within 1e-8, and the large requests and
+    phase-field steps still served by the workers."""
+    from easyfea_gb300 import serving
+
+    cache = serving.MeshCache()
+    t, reqs, _ = small_stream(n=24, seed=13)
+    with serving.Server(workers=4, precision="mixed", cache=cache, batch_max_dof=batch_max_dof,
+                        batch_window_s=0.005) as srv:
+        served = serving.run_stream(srv, np.zeros(len(reqs)), reqs)
+        assert srv.batcher.batches >= 1
+    assert all(r.error is None for r in served), [r.error for r in served if r.error]
+    n_small = sum(1 for r in reqs if r.kind == "elastic" and r.spec.dof <= batch_max_dof)
+    assert n_small >= 4
+    t2, reqs2, _ = small_stream(n=24, seed=13)
+    plain = serving.run_plain(reqs2, cache, precision="fp64")
+    for r, a, b in zip(reqs, served, plain):
+        if a.kind == "elastic":
+            assert a.status == 0
+            assert rel(a.u, b.u) <= 1e-8, (a.rid, a.dof, rel(a.u, b.u))
+    for r, m in zip(reqs, served):
+        if r.kind != "elastic" or r.spec.dof > batch_max_dof:
+            continue
+        with serving.Server(workers=1, precision="mixed", cache=cache, batch_max_dof=batch_max_dof) as srv:
+            srv.submit(r)
+            srv.drain()
+            alone = srv.results[r.rid]
+        assert alone.status == 0
+        assert rel(m.u, alone.u) <= 1e-8, (r.rid, rel(m.u, alone.u))

@@ -71,9 +71,10 @@ def parse():
                    help="elastic requests up to this size are solved in cross-request batches (0: off)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the single-solve and batch measurements")
-    p.add_argument("--workload", default="stream", choices=["stream", "single", "batch"],
-                   help="stream: the full benchmark; single / batch: only that measurement, printed as "
-                        "its own JSON object (for profiling)")
+    p.add_argument("--workload", default="stream",
+                   choices=["stream", "single", "batch", "batch_one_launch", "assembly", "phasefield"],
+                   help="stream: the full benchmark; the others: only that measurement, printed as its own "
+                        "JSON object (for profiling)")
     return p.parse_args()
 
 
@@ -414,13 +415,15 @@ def rate_sweep(server, sessions, rates=(10, 30, 100, 300, 1000, 2000), seconds=3
     return out
 
 
-def assembly_roofline(lib):
-    """FP64 stiffness assembly of the 400x40x40 box, timed with CUDA events:
-    compulsory bytes (coordinates, connectivity, CSR values written once) and
+def assembly_roofline(lib, peak=6782.1, reps=3):
+    """Stiffness assembly of the 400x40x40 box, timed with CUDA events, in
+    FP64 (the values the mixed solve's reliable updates need) and FP32 (the
+    element path that writes the FP32 operator directly): compulsory bytes
+    (coordinates, connectivity, CSR values written once) and the reference's
     generic element flops (8 Gauss points x (24x6x6 + 24x24x6) FMA)."""
     import torch
 
-    from easyfea_gb300 import Models
+    from easyfea_gb300 import Models, _lib
     from easyfea_gb300 import mesh as gmesh
     from easyfea_gb300 import simulations as Simulations
 
@@ -429,7 +432,6 @@ def assembly_roofline(lib):
     simu.Assembly()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 3
     e0.record()
     for _ in range(reps):
         simu.Assembly()
@@ -439,13 +441,46 @@ def assembly_roofline(lib):
     nnz = simu.dmesh.nnz(3)
     byts = m.Nn * 3 * 8 + m.Ne * 8 * 4 + nnz * 8
     flops = 2.0 * m.Ne * 8 * (24 * 6 * 6 + 24 * 24 * 6)
+    # FP32 element path into the FP32 operator
+    op = simu.K_device
+    op.ensure_f32()
+    C, mode = simu._C_device()
+    dm, g = simu.dmesh, simu.dmesh.main
+
+    def f32():
+        _lib.check(lib.gfea_assemble_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                             _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C), int(mode), 1.0,
+                                             _lib.F32, _lib.ptr(op.vals32), op.nnz, 0, _lib.stream()), "assemble f32")
+    f32()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        f32()
+    e1.record()
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / reps
+    byts32 = m.Nn * 3 * 8 + m.Ne * 8 * 4 + nnz * 4
     return {"kernel": "elastic_kernel<HEXA8, double, isotropic> (FP64 element stiffness in the (lambda, mu) "
                       "form + CSR scatter)", "ms": ms,
-            "algorithmic_bytes": byts, "achieved_gbs": byts / ms / 1e6, "hbm_frac_of_measured": byts / ms / 1e6 / 6782.1,
+            "algorithmic_bytes": byts, "achieved_gbs": byts / ms / 1e6, "hbm_frac_of_measured": byts / ms / 1e6 / peak,
             "algorithmic_flops": flops, "reference_flops_rate_tflops": flops / ms / 1e9,
             "bound": "FP64 pipe: the flops above are the reference's B^T C B; the kernel computes each symmetric "
                      "block pair once and, for an isotropic law, accumulates grad N_p (x) grad N_q per Gauss "
-                     "point (D^2 FMAs per block) instead of B^T C B"}
+                     "point (D^2 FMAs per block) instead of B^T C B",
+            "f32": {"kernel": "elastic_kernel<HEXA8, float, isotropic> (FP32 values, FP32 atomics into the CSR "
+                              "slots)", "ms": ms32, "algorithmic_bytes": byts32,
+                    "achieved_gbs": byts32 / ms32 / 1e6, "hbm_frac_of_measured": byts32 / ms32 / 1e6 / peak}}
+
+
+def phasefield_kernels(steps=3):
+    """A few load steps of the 80,000-element notched plate (profiling)."""
+    from easyfea_gb300 import serving
+
+    cache = serving.MeshCache()
+    sess = serving.PhaseFieldSession(serving.MeshSpec("tri3_sen", 200, 200))
+    for _ in range(steps):
+        sess.run_step(cache, "fp64")
+    return {"workload": "notched plate load steps", "steps": steps}
 
 
 def batch_measure(workers):
@@ -560,6 +595,17 @@ def main():
     if args.workload == "batch":
         print(json.dumps(batch_measure(args.workers)), flush=True)
         return
+    if args.workload == "batch_one_launch":
+        from easyfea_gb300.batching import random_material_cantilevers
+
+        print(json.dumps(one_launch_batch(random_material_cantilevers(n=256, seed=0), reps=1)), flush=True)
+        return
+    if args.workload == "assembly":
+        print(json.dumps(assembly_roofline(lib, reps=1)), flush=True)
+        return
+    if args.workload == "phasefield":
+        print(json.dumps(phasefield_kernels()), flush=True)
+        return
     cache = serving.MeshCache()
     offsets, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
     cache.prebuild({r.spec for r in reqs})
@@ -659,7 +705,7 @@ def main():
         peak_src = "measured"
     if not args.no_extras:
         extras["single_solve"], roof = single_solve(lib, peak)
-        extras["assembly"] = assembly_roofline(lib)
+        extras["assembly"] = assembly_roofline(lib, peak)
         extras["phasefield"] = phasefield_measure()
         extras["batch"] = batch_measure(args.workers)
     traffic = None

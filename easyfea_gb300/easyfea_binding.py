@@ -17,14 +17,17 @@ What runs on the GPU:
   ``gfea_assemble_elastic`` / ``gfea_assemble_mass``, returned as scipy CSR
   matrices with the reference's exact layout, so every reference path that
   reads ``Get_K_C_M_F`` (reactions, energies, time schemes) sees them.
-* ``_Solver_Solve_problemType`` for a static linear problem (elliptic
-  algorithm, no Lagrange conditions): the reference's own Neumann and
-  Dirichlet conditions (``Bc_dofs_Neumann`` / ``Bc_values_Neumann``, summed as
+* ``_Solver_Solve_problemType`` for linear problems without Lagrange
+  conditions: the static solve (the reference's own Neumann and Dirichlet
+  conditions, ``Bc_dofs_Neumann`` / ``Bc_values_Neumann`` summed as
   ``_Solver_Apply_Neumann`` sums them, and ``Bc_dofs_Dirichlet`` /
-  ``Bc_values_Dirichlet``) are solved with the library's PCG on the device
-  operator, with the previous solution as the initial guess (``Get_x0``).
-  Other algorithms (dynamics, Newton, Lagrange multipliers) go to the
-  reference's solver with the GPU-assembled matrices.
+  ``Bc_values_Dirichlet``) and the time-stepping solves of the parabolic and
+  hyperbolic schemes (Newmark, HHT, midpoint, Euler; ``_simu.py:1291-1456``,
+  ``Solvers.py:69-182``: the operator coefK K + coefC C + coefM M formed on
+  the device, the right-hand side from the reference's own
+  ``_Solver_Apply_Neumann``), all with the library's PCG and the previous
+  solution as the initial guess (``Get_x0``).  Newton and Lagrange
+  multipliers go to the reference's solver with the GPU-assembled matrices.
 * ``GpuPhaseField.Solve``: the staggered loop on the device (split, history,
   damage and degraded elastic systems, both solves), started from the
   reference's current u, d and committed history field and written back to
@@ -164,19 +167,54 @@ class GpuElastic(_RefSimulations.Elastic):
         return K, C, M, F
 
     def _gpu_solvable(self, problemType) -> bool:
-        return (self.algo == _AlgoType.elliptic and not self.isNonLinear and len(self.Bc_Lagrange) == 0)
+        return not self.isNonLinear and len(self.Bc_Lagrange) == 0
+
+    def _time_operator(self, eng):
+        """A = coefK K + coefC C + coefM M of the time scheme
+        (_simu.py:1399-1456, Solvers.py:69-182) on the device, with the
+        Rayleigh C = rK K + rM M: one linear combination of the K and M values,
+        which share the CSR pattern."""
+        from .device import CsrOperator
+
+        cK, cC, cM = self._Solver_Get_K_C_M_coefs_for_time_scheme()
+        rK = getattr(self, "_Elastic__coefK", 0.0)
+        rM = getattr(self, "_Elastic__coefM", 0.0)
+        a, m = cK + cC * rK, cM + cC * rM
+        K, M = eng.K_device, eng._mass()
+        if getattr(self, "_gpu_A", None) is None or self._gpu_A.dmesh is not K.dmesh:
+            self._gpu_A = CsrOperator(K.dmesh, K.dof_n)
+        A = self._gpu_A
+        torch.mul(K.vals64, a, out=A.vals64)
+        A.vals64.add_(M.vals64, alpha=m)
+        # node block rows of A sum to zero only without the mass term
+        A.translation_invariant = m == 0.0
+        return A
 
     def _Solver_Solve_problemType(self, problemType):
+        """The static and time-stepping linear solves on the GPU (elliptic,
+        parabolic and every hyperbolic scheme): the right-hand side is the
+        reference's own (_Solver_Apply_Neumann, which adds the scheme's
+        history terms with the GPU-assembled matrices), the operator
+        coefK K + coefC C + coefM M is formed on the device, the velocity and
+        acceleration are updated by the reference's _Solver_Update_solutions."""
         if not self._gpu_solvable(problemType):
             return super()._Solver_Solve_problemType(problemType)
         eng = self._engine()
-        b_host = _neumann(self, problemType)
-        eng._dirichlet[eng.problemType] = [_DirichletBC(self.Bc_dofs_Dirichlet(problemType),
-                                                        self.Bc_values_Dirichlet(problemType))]
+        dofs = self.Bc_dofs_Dirichlet(problemType)
+        vals = self.Bc_values_Dirichlet(problemType)
+        if self.algo == _AlgoType.elliptic:
+            b_host = _neumann(self, problemType)
+            op = eng.K_device
+        else:
+            b_host = np.asarray(self._Solver_Apply_Neumann(problemType).toarray(), dtype=np.float64).ravel()
+            op = self._time_operator(eng)
+            if self.algo == _AlgoType.euler_explicit:  # the unknown is a^n: zero on constrained DOFs
+                vals = np.zeros_like(np.asarray(vals, dtype=np.float64))
+        eng._dirichlet[eng.problemType] = [_DirichletBC(dofs, vals)]
         b = torch.as_tensor(b_host, device=_engine._dev())
         x0 = torch.as_tensor(np.ascontiguousarray(self.Get_x0(problemType), dtype=np.float64),
                              device=_engine._dev())
-        u = eng._solve_system(eng.K_device, b, eng.problemType, x0=x0).cpu().numpy()
+        u = eng._solve_system(op, b, eng.problemType, x0=x0).cpu().numpy()
         self.last_solve = eng.last_solve
         solutions = self._Solver_Update_solutions(problemType, u)
         self._Set_solutions(problemType, *solutions)

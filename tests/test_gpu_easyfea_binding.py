@@ -121,3 +121,52 @@ def test_gpu_phasefield_inside_easyfea(ref, golden, case, opt):
         assert niter == g["Niter"][k - 1], f"step {k}: {niter} vs {g['Niter'][k - 1]}"
         assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"
         assert np.abs(d - g["d"][k - 1]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("algo", ["newmark", "hht", "midpoint", "euler_implicit", "parabolic"])
+def test_gpu_time_schemes_inside_easyfea(ref, golden, algo):
+    """EasyFEA's time integration (Solver_Set_Hyperbolic_Algorithm /
+    Parabolic; EasyFEA/Simulations/_simu.py:1173-1456, Solvers.py:69-182) with
+    Rayleigh damping on the GPU subclass, against the reference's own Elastic
+    (scipy SuperLU) run step by step in the same script: u, v and a within
+    1e-8 of their scale after every step."""
+    from EasyFEA.Simulations.Solvers import AlgoType, SolverType
+
+    g = golden("el_quad4")
+    R = ref
+    mesh = ref_mesh(R, g)
+    sims = []
+    for cls in (R.Simulations.Elastic, R.B.GpuElastic):
+        mat = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=True, thickness=13.0)
+        simu = cls(mesh, mat) if cls is R.Simulations.Elastic else cls(mesh, mat, rtol=1e-13)
+        if cls is R.Simulations.Elastic:
+            simu.solver = SolverType.scipy
+        simu.rho = 7.8e-9
+        simu.Set_Rayleigh_Damping_Coefs(coefM=1e-3, coefK=1e-5)
+        dt = 2e-5
+        if algo == "parabolic":
+            simu.Solver_Set_Parabolic_Algorithm(dt)
+        else:
+            simu.Solver_Set_Hyperbolic_Algorithm(dt, algo=getattr(AlgoType, algo))
+        sims.append(simu)
+    left = mesh.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = mesh.Nodes_Conditions(lambda x, y, z: x == mesh.coord[:, 0].max())
+    for step in range(6):
+        for simu in sims:
+            simu.Bc_Init()
+            simu.add_dirichlet(left, [0.0, 0.0], ["x", "y"])
+            simu.add_surfLoad(right, [-800 / 13**2 * (1.0 if step < 3 else 0.5)], ["y"])
+            simu.Solve()
+            simu.Save_Iter()
+        ref_s, gpu_s = sims
+        assert gpu_s.last_solve is not None and gpu_s.last_solve.status == 0
+        # v and a are differences of displacements over dt and dt^2: a
+        # displacement difference e (solver rounding) moves them by e/dt and
+        # e/dt^2, which the tolerance allows for
+        umax = np.abs(ref_s.displacement).max()
+        for name, amp in (("displacement", 1.0), ("speed", 1.0 / dt), ("accel", 1.0 / dt**2)):
+            a, b = getattr(gpu_s, name), getattr(ref_s, name)
+            if b is None or np.size(b) == 0 or np.abs(b).max() == 0:
+                continue
+            tol = 1e-8 * (np.abs(b).max() if name == "displacement" else np.abs(b).max() + umax * amp)
+            assert np.abs(a - b).max() <= tol, (algo, step, name, np.abs(a - b).max(), tol)

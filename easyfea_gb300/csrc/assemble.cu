@@ -106,11 +106,56 @@ __device__ __forceinline__ void group8_sum9(const double (&v)[9], double (&F)[9]
   F[8] = __shfl_sync(0xffffffffu, k3[1], 0, 8);
 }
 
+// FP32 values: the whole geometry on the FP32 pipe, from coordinates taken
+// relative to the element's first node (so the Jacobian's entries keep
+// FP32 precision however far the element is from the origin): F by group
+// sums of dN_p (x) X_p, det and adjugate in FP32, one FP32 division.
+template <int D, int G>
+__device__ __forceinline__ float lane_geometry_f32(const float (&dn)[D], const float (&X)[D], float w,
+                                                   float (&grad)[D]) {
+  float F[D][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d)
+#pragma unroll
+    for (int k = 0; k < D; ++k) F[d][k] = group_sum<G, float>(dn[d] * X[k]);
+  if constexpr (D == 2) {
+    const float det = F[0][0] * F[1][1] - F[1][0] * F[0][1];
+    const float id = 1.0f / det;
+    grad[0] = id * (F[1][1] * dn[0] - F[0][1] * dn[1]);
+    grad[1] = id * (-F[1][0] * dn[0] + F[0][0] * dn[1]);
+    return fabsf(det) * w;
+  } else {
+    const float a11 = F[0][0], a12 = F[0][1], a13 = F[0][2], a21 = F[1][0], a22 = F[1][1], a23 = F[1][2],
+                a31 = F[2][0], a32 = F[2][1], a33 = F[2][2];
+    const float c11 = a22 * a33 - a32 * a23, c21 = -(a21 * a33 - a31 * a23), c31 = a21 * a32 - a31 * a22;
+    const float det = a11 * c11 + a12 * c21 + a13 * c31;
+    const float id = 1.0f / det;
+    const float adj[3][3] = {{c11, -(a12 * a33 - a32 * a13), a12 * a23 - a22 * a13},
+                             {c21, a11 * a33 - a31 * a13, -(a11 * a23 - a21 * a13)},
+                             {c31, -(a11 * a32 - a31 * a12), a11 * a22 - a21 * a12}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) grad[i] = id * (adj[i][0] * dn[0] + adj[i][1] * dn[1] + adj[i][2] * dn[2]);
+    return fabsf(det) * w;
+  }
+}
+
 template <int ELEM, bool MASS, int G, typename R>
 __device__ __forceinline__ R lane_geometry(const RefTables<ELEM, MASS>& ref, int g, int lane, bool node_lane,
                                            const R (&X)[Elem<ELEM>::dim], R (&grad)[Elem<ELEM>::dim]) {
   constexpr int D = Elem<ELEM>::dim;
-  if constexpr (D == 3 && G == 8) {
+  if constexpr (sizeof(R) == 4 && D >= 2) {
+    float dn[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dn[d] = node_lane ? (float)ref.dN[g][d][lane] : 0.f;
+    float Xf[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) Xf[k] = (float)X[k];
+    float gf[D];
+    const float wJ = lane_geometry_f32<D, G>(dn, Xf, (float)ref.w[g], gf);
+#pragma unroll
+    for (int k = 0; k < D; ++k) grad[k] = (R)gf[k];
+    return (R)wJ;
+  } else if constexpr (D == 3 && G == 8) {
     // F[d][k] = sum_p dN_d(p) X_p[k]; grad = F^-1 dN = adj(F) dN / det(F)
     double dn[3], v[9], F[9];
 #pragma unroll
@@ -189,7 +234,12 @@ __global__ void __launch_bounds__(128) elastic_kernel(const double* __restrict__
     const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
     R X[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) X[k] = node_lane ? (R)coord[(int64_t)a * 3 + k] : (R)0;
+    for (int k = 0; k < D; ++k) {
+      const double xa = node_lane ? coord[(int64_t)a * 3 + k] : 0.0;
+      // FP32 values: coordinates relative to the element's first node
+      const double x0 = sizeof(R) == 4 ? group_bcast<G, double>(xa, 0) : 0.0;
+      X[k] = node_lane ? (R)(xa - x0) : (R)0;
+    }
     R Cl[NS * NS];
     const R* C = Csh;
     if (CMODE == 1) {
@@ -323,7 +373,12 @@ __global__ void __launch_bounds__(128) mass_kernel(const double* __restrict__ co
     const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
     R X[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) X[k] = node_lane ? (R)coord[(int64_t)a * 3 + k] : (R)0;
+    for (int k = 0; k < D; ++k) {
+      const double xa = node_lane ? coord[(int64_t)a * 3 + k] : 0.0;
+      // FP32 values: coordinates relative to the element's first node
+      const double x0 = sizeof(R) == 4 ? group_bcast<G, double>(xa, 0) : 0.0;
+      X[k] = node_lane ? (R)(xa - x0) : (R)0;
+    }
     R acc[nPe];
 #pragma unroll
     for (int q = 0; q < nPe; ++q) acc[q] = 0;

@@ -101,3 +101,38 @@ def test_field_loads_match_reference(golden, case):
     b = simu._neumann_vec("elastic").cpu().numpy()
     np.testing.assert_allclose(b, g["b"], rtol=1e-12, atol=1e-13 * np.abs(g["b"]).max())
     assert np.abs(u - g["u"]).max() <= 1e-8 * np.abs(g["u"]).max()
+
+
+@pytest.mark.parametrize("case", ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero",
+                                  "el_cantilever_240x26"])
+def test_f32_element_path_matches_reference(golden, case):
+    """The FP32 element path (gfea_assemble_elastic / gfea_assemble_mass with
+    GFEA_F32: geometry on the FP32 pipe from coordinates relative to each
+    element's first node) against the reference's K and M, row-scaled,
+    within 1e-6 (FP32 values)."""
+    import torch
+
+    from easyfea_gb300 import _lib
+
+    g = golden(case)
+    simu, u = run_case(g)
+    n = u.size
+    op = simu.K_device
+    op.ensure_f32()
+    C, mode = simu._C_device()
+    dm, grp = simu.dmesh, simu.dmesh.main
+    L = _lib.load()
+    t = float(g["thickness"]) if simu.dim == 2 else 1.0
+    _lib.check(L.gfea_assemble_elastic(grp.code, _lib.ptr(dm.coord), _lib.ptr(grp.connect), grp.Ne,
+                                       _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C), int(mode), t,
+                                       _lib.F32, _lib.ptr(op.vals32), op.nnz, 0, _lib.stream()), "assemble f32")
+    K32 = simu.K_device.to_scipy()
+    K32.data = op.vals32.double().cpu().numpy()
+    assert row_scaled_err(K32, csr(g, "K", n)) <= 1e-6
+    m32 = torch.zeros(op.nnz, dtype=torch.float32, device="cuda")
+    _lib.check(L.gfea_assemble_mass(grp.code, _lib.ptr(dm.coord), _lib.ptr(grp.connect), grp.Ne, _lib.ptr(dm.node_ptr),
+                                    _lib.ptr(dm.rank), simu.dim, 1.0, t, _lib.F32, _lib.ptr(m32), op.nnz, 0,
+                                    _lib.stream()), "mass f32")
+    M32 = simu.K_device.to_scipy()
+    M32.data = m32.double().cpu().numpy()
+    assert row_scaled_err(M32, csr(g, "M", n)) <= 1e-6

@@ -132,3 +132,41 @@ def test_notched_plate_first_steps_match_oracle(precision):
         assert abs(F - F_ref) <= 1e-6 * abs(F_ref), (k, F, F_ref)
         assert np.abs(d - d_ref).max() <= 1e-6, k
         assert np.abs(u - u_ref).max() <= 1e-6 * np.abs(u_ref).max(), k
+
+
+def test_notched_plate_load_curve_matches_reference(golden):
+    """The phase-field benchmark through its whole load history: the
+    reference's own run of the 200x200 notched plate (80,000 TRI3, AT2,
+    Miehe, top displacement k x 1e-5 mm, Solve(1e-3, 500, convOption=0) and
+    Save_Iter per step; make_golden.py pf_curve_tri3_200x200) against the
+    GPU staggered loop in FP64: the same staggered iteration count at every
+    step, the top reaction within 1e-6 relative, the damage field within 1e-6
+    at the stored steps (every 50th, the force peak, the last)."""
+    import torch
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    g = golden("pf_curve_tri3_200x200")
+    m = gmesh.Mesh_Tri3_Rect(1.0, 1.0, 200, 200)
+    mat = Models.Elastic.Isotropic(2, E=210e3, v=0.3, planeStress=False)
+    simu = Simulations.PhaseField(m, Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.01))
+    simu.precision = "fp64"
+    simu.rtol = 1e-12
+    top_dofs = torch.as_tensor(g["top_dofs"], device="cuda")
+    kept = {int(k): i for i, k in enumerate(g["d_steps"])}
+    dU, tol, maxIter = float(g["dU"]), float(g["tol"]), int(g["maxIter"])
+    for k in range(1, len(g["F"]) + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(g["notch"], [1.0], ["d"], problemType="damage")
+        simu.add_dirichlet(g["bottom"], [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(g["top"], [0.0, k * dU], ["x", "y"])
+        u, d, conv = simu.Solve(tol, maxIter, convOption=0)
+        simu.Save_Iter()
+        F = simu.reaction_sum(top_dofs)
+        assert simu.Niter == g["Niter"][k - 1], f"step {k}: {simu.Niter} staggered iterations, reference {g['Niter'][k - 1]}"
+        assert bool(conv) == bool(g["converged"][k - 1]), f"step {k}"
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"
+        if k in kept:
+            assert np.abs(d - g["d"][kept[k]]).max() <= 1e-6, f"step {k}"

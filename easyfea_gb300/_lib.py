@@ -23,7 +23,7 @@ F64 = 0
 F32 = 1
 
 ELEM_CODE = {"SEG2": 0, "TRI3": 1, "QUAD4": 2, "QUAD9": 3, "HEXA8": 4}
-SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2}
+SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2, "Zhang": 3, "Stress": 4, "He": 5}
 REGU_CODE = {"AT1": 0, "AT2": 1}
 
 
@@ -130,6 +130,8 @@ class PfParams(ctypes.Structure):
         ("A", c_double * 9),
         ("C", c_double * 36),
         ("k_res", c_double),
+        ("plane_stress", c_int32),
+        ("pad", c_int32),
     ]
 
 

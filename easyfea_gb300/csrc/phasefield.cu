@@ -32,7 +32,7 @@ constexpr double kEigTolArg = 1e-12;
 constexpr double kEigTolZero = 1e-12;
 
 struct PF {
-  int split, regu, dim;
+  int split, regu, dim, plane_stress;
   double lambda, mu, Gc, l0, thickness, k_res;
   double A[9];
   double C[36];
@@ -41,40 +41,16 @@ struct PF {
 __host__ __device__ __forceinline__ double heav(double v) { return v > 0 ? 1.0 : (v == 0 ? 0.5 : 0.0); }
 __host__ __device__ __forceinline__ double sgn(double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); }
 
-// c = gP * cP + cM  (n x n, row-major); gP = 1 gives cP + cM.
-// With want_parts, cP and cM are also returned separately.
+// Spectral projector P+ of a second-order tensor given as a Kelvin-Mandel
+// vector (the strain for Miehe, the stress for the stress-based splits, the
+// transformed strain of He): its positive part is P+ : vec and P- = I - P+
+// (Models/_phasefield.py:751-1243).
 template <int D>
-__host__ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
-  constexpr int n = D == 2 ? 3 : 6;
-  const double tr = D == 2 ? eps[0] + eps[1] : eps[0] + eps[1] + eps[2];
-  const double Rp = (1 + sgn(tr)) / 2, Rm = (1 + sgn(-tr)) / 2;
-  auto IxI = [](int i, int j) { return (i < D && j < D) ? 1.0 : 0.0; };
-  if (P.split == GFEA_SPLIT_BOURDIN) {
-    for (int i = 0; i < n * n; ++i) {
-      c[i] = gP * P.C[i];
-      if (cPo) cPo[i] = P.C[i];
-      if (cMo) cMo[i] = 0.0;
-    }
-    return;
-  }
-  if (P.split == GFEA_SPLIT_AMOR) {
-    const double bulk = P.lambda + 2 * P.mu / D;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) {
-        const double cp = bulk * (Rp * IxI(i, j)) + 2 * P.mu * ((i == j ? 1.0 : 0.0) - 1.0 / D * IxI(i, j));
-        const double cm = bulk * (Rm * IxI(i, j));
-        c[i * n + j] = gP * cp + cm;
-        if (cPo) cPo[i * n + j] = cp;
-        if (cMo) cMo[i * n + j] = cm;
-      }
-    return;
-  }
-  // Miehe: projP from the eigen decomposition of the strain tensor
-  double projP[n * n];
+__host__ __device__ void spectral_proj(const double* vec, double* projP) {
   if constexpr (D == 2) {
     // eigenvalues m -+ rad with m = tr/2 and rad^2 = ((M00 - M11)/2)^2 + M01^2,
     // i.e. the reference's (tr -+ sqrt(tr^2 - 4 det))/2 without its cancellation
-    const double M00 = eps[0], M11 = eps[1], M01 = eps[2] / kSqrt2;
+    const double M00 = vec[0], M11 = vec[1], M01 = vec[2] / kSqrt2;
     const double trM = M00 + M11;
     const double h = (M00 - M11) / 2;
     double rad2 = h * h + M01 * M01;
@@ -103,10 +79,10 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
         projP[i * 3 + j] = (i == j ? beta : 0.0) + g1 * m1[i] * m1[j] + g2 * m2[i] * m2[j];
   } else {
     double M[3][3];
-    M[0][0] = eps[0]; M[1][1] = eps[1]; M[2][2] = eps[2];
-    M[1][2] = M[2][1] = eps[3] / kSqrt2;
-    M[0][2] = M[2][0] = eps[4] / kSqrt2;
-    M[0][1] = M[1][0] = eps[5] / kSqrt2;
+    M[0][0] = vec[0]; M[1][1] = vec[1]; M[2][2] = vec[2];
+    M[1][2] = M[2][1] = vec[3] / kSqrt2;
+    M[0][2] = M[2][0] = vec[4] / kSqrt2;
+    M[0][1] = M[1][0] = vec[5] / kSqrt2;
     // Invariants of the deviator s = M - I1/3 I: g = I1^2 - 3 I2 = 3/2 tr(s^2)
     // and 2 I1^3 - 9 I1 I2 + 27 I3 = 27 det(s), the reference's quantities
     // without their cancellation when the eigenvalues cluster.
@@ -228,6 +204,151 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
         projP[I * 6 + K] = s + gs;
       }
   }
+}
+
+// c = gP * cP + cM  (n x n, row-major); gP = 1 gives cP + cM.
+// With want_parts, cP and cM are also returned separately.
+template <int D>
+__host__ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
+  constexpr int n = D == 2 ? 3 : 6;
+  const double tr = D == 2 ? eps[0] + eps[1] : eps[0] + eps[1] + eps[2];
+  const double Rp = (1 + sgn(tr)) / 2, Rm = (1 + sgn(-tr)) / 2;
+  auto IxI = [](int i, int j) { return (i < D && j < D) ? 1.0 : 0.0; };
+  if (P.split == GFEA_SPLIT_BOURDIN) {
+    for (int i = 0; i < n * n; ++i) {
+      c[i] = gP * P.C[i];
+      if (cPo) cPo[i] = P.C[i];
+      if (cMo) cMo[i] = 0.0;
+    }
+    return;
+  }
+  if (P.split == GFEA_SPLIT_AMOR) {
+    const double bulk = P.lambda + 2 * P.mu / D;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        const double cp = bulk * (Rp * IxI(i, j)) + 2 * P.mu * ((i == j ? 1.0 : 0.0) - 1.0 / D * IxI(i, j));
+        const double cm = bulk * (Rm * IxI(i, j));
+        c[i * n + j] = gP * cp + cm;
+        if (cPo) cPo[i * n + j] = cp;
+        if (cMo) cMo[i * n + j] = cm;
+      }
+    return;
+  }
+  if (P.split == GFEA_SPLIT_ZHANG || P.split == GFEA_SPLIT_STRESS || P.split == GFEA_SPLIT_HE) {
+    // stress-based splits (Models/_phasefield.py:573-687): projectors of
+    // sigma = C eps; He (:689-749): projectors of C^1/2 eps mapped back with
+    // C^-1/2 (.) C^1/2, where C^1/2 of the isotropic law is
+    // sqrt(2 mu) (I - Pv) + sqrt(D lambda + 2 mu) Pv, Pv = IxI / D
+    const double* C = P.C;
+    double pp[n * n], cp[n * n], cm[n * n];
+    if (P.split == GFEA_SPLIT_HE) {
+      const double a = sqrt(2 * P.mu), b = sqrt(D * P.lambda + 2 * P.mu);
+      double sq[n * n], si[n * n];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          const double pv = IxI(i, j) / D, id = i == j ? 1.0 : 0.0;
+          sq[i * n + j] = a * (id - pv) + b * pv;
+          si[i * n + j] = (id - pv) / a + pv / b;
+        }
+      double et[n];
+      for (int i = 0; i < n; ++i) {
+        double t = 0;
+        for (int j = 0; j < n; ++j) t += sq[i * n + j] * eps[j];
+        et[i] = t;
+      }
+      double ppt[n * n];
+      spectral_proj<D>(et, ppt);
+      // P+ = S^1/2 Pt+ C^1/2, P- = S^1/2 (I - Pt+) C^1/2 = I - P+
+      double tmp[n * n];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0;
+          for (int k = 0; k < n; ++k) t += ppt[i * n + k] * sq[k * n + j];
+          tmp[i * n + j] = t;
+        }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0;
+          for (int k = 0; k < n; ++k) t += si[i * n + k] * tmp[k * n + j];
+          pp[i * n + j] = t;
+        }
+      // cP = C P+, cM = C P-
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double tp = 0, tm = 0;
+          for (int k = 0; k < n; ++k) {
+            tp += C[i * n + k] * pp[k * n + j];
+            tm += C[i * n + k] * ((k == j ? 1.0 : 0.0) - pp[k * n + j]);
+          }
+          cp[i * n + j] = tp;
+          cm[i * n + j] = tm;
+        }
+    } else {
+      double sig[n];
+      for (int i = 0; i < n; ++i) {
+        double t = 0;
+        for (int j = 0; j < n; ++j) t += C[i * n + j] * eps[j];
+        sig[i] = t;
+      }
+      spectral_proj<D>(sig, pp);
+      if (P.split == GFEA_SPLIT_ZHANG) {  // cP = P+ C, cM = P- C
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            double tp = 0, tm = 0;
+            for (int k = 0; k < n; ++k) {
+              tp += pp[i * n + k] * C[k * n + j];
+              tm += ((i == k ? 1.0 : 0.0) - pp[i * n + k]) * C[k * n + j];
+            }
+            cp[i * n + j] = tp;
+            cm[i * n + j] = tm;
+          }
+      } else {  // Stress: s+- = a1 P+- - a2 R+- IxI (isotropic compliance), c+- = C s+- C
+        const double trs = D == 2 ? sig[0] + sig[1] : sig[0] + sig[1] + sig[2];
+        const double Rps = (1 + sgn(trs)) / 2, Rms = (1 + sgn(-trs)) / 2;
+        const double nu = P.plane_stress ? P.lambda / (P.lambda + 2 * P.mu) : P.lambda / (2 * (P.lambda + P.mu));
+        const double E = 2 * P.mu * (1 + nu);
+        const double a1 = D == 2 ? (1 + nu) / E : 1 / (2 * P.mu);
+        const double a2 = D == 2 ? (P.plane_stress ? nu / E : nu * (1 + nu) / E) : nu / E;
+        double sp[n * n], sm[n * n];
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            const double id = i == j ? 1.0 : 0.0;
+            sp[i * n + j] = a1 * pp[i * n + j] - a2 * Rps * IxI(i, j);
+            sm[i * n + j] = a1 * (id - pp[i * n + j]) - a2 * Rms * IxI(i, j);
+          }
+        double tp[n * n], tm[n * n];
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            double a = 0, b = 0;
+            for (int k = 0; k < n; ++k) {
+              a += C[k * n + i] * sp[k * n + j];  // C^T s
+              b += C[k * n + i] * sm[k * n + j];
+            }
+            tp[i * n + j] = a;
+            tm[i * n + j] = b;
+          }
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            double a = 0, b = 0;
+            for (int k = 0; k < n; ++k) {
+              a += tp[i * n + k] * C[k * n + j];
+              b += tm[i * n + k] * C[k * n + j];
+            }
+            cp[i * n + j] = a;
+            cm[i * n + j] = b;
+          }
+      }
+    }
+    for (int i = 0; i < n * n; ++i) {
+      c[i] = gP * cp[i] + cm[i];
+      if (cPo) cPo[i] = cp[i];
+      if (cMo) cMo[i] = cm[i];
+    }
+    return;
+  }
+  // Miehe: projP from the eigen decomposition of the strain tensor
+  double projP[n * n];
+  spectral_proj<D>(eps, projP);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       const double pp = projP[i * n + j];
@@ -518,9 +639,10 @@ __global__ void split_kernel(const double* __restrict__ eps, int64_t n, PF P, do
 int to_pf(const gfea_pf_params* p, PF* o) {
   if (!p || p->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
   if (p->dim != 2 && p->dim != 3) return GFEA_ERR_ARG;
-  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_MIEHE) return GFEA_ERR_ARG;
+  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_HE) return GFEA_ERR_ARG;
   if (p->regularization != GFEA_AT1 && p->regularization != GFEA_AT2) return GFEA_ERR_ARG;
   o->split = p->split;
+  o->plane_stress = p->plane_stress;
   o->regu = p->regularization;
   o->dim = p->dim;
   o->lambda = p->lambda_;

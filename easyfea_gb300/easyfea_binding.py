@@ -36,7 +36,7 @@ What runs on the GPU:
 
 Materials: isotropic elastic laws (homogeneous or with a per-element Young's
 modulus) and, for the phase field, a homogeneous isotropic material with the
-Bourdin / Amor / Miehe splits, AT1 / AT2 and the History / HistoryDamage
+Bourdin / Amor / Miehe / He splits, AT1 / AT2 and the History / HistoryDamage
 solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9 and HEXA8.  Other
 models raise ``NotImplementedError`` at construction.
 
@@ -246,7 +246,7 @@ class GpuPhaseField(_RefSimulations.PhaseField):
         split = str(getattr(pfm.split, "value", pfm.split))
         regu = str(getattr(pfm.regularization, "value", pfm.regularization))
         solver = str(getattr(pfm.solver, "value", pfm.solver))
-        if split not in ("Bourdin", "Amor", "Miehe") or regu not in ("AT1", "AT2") or \
+        if split not in ("Bourdin", "Amor", "Miehe", "He") or regu not in ("AT1", "AT2") or \
                 solver not in ("History", "HistoryDamage"):
             raise NotImplementedError(f"GPU phase field: split {split}, {regu}, solver {solver}")
         A = getattr(pfm, "A", None)

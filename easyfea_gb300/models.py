@@ -164,6 +164,9 @@ class PhaseField(_Observable):
         Bourdin = "Bourdin"
         Amor = "Amor"
         Miehe = "Miehe"
+        Zhang = "Zhang"
+        Stress = "Stress"
+        He = "He"
 
     class SolverType(str, Enum):
         History = "History"

@@ -449,6 +449,14 @@ class PhaseField(_Simu):
 
     def __init__(self, mesh: Mesh, model: PhaseFieldModel, folder: str = "", verbosity: bool = False):
         assert isinstance(model, PhaseFieldModel), "model must be a phase field model"
+        if model.split in ("Zhang", "Stress"):
+            # Zhang: c+ = P+(sigma) C is not symmetric; Stress: c+ = C s+ C
+            # with s+ = a P+ - b R+ IxI is not positive semi-definite, so the
+            # degraded stiffness g c+ + c- can be indefinite.  The staggered
+            # loop's PCG needs SPD systems (the reference factorises them with
+            # a direct solver); both splits are available through gfea_pf_split
+            raise NotImplementedError(f"the {model.split} split does not give an SPD degraded stiffness; the GPU "
+                                      "staggered loop solves SPD systems")
         assert model.dim == mesh.dim, "the material and the mesh must have the same dimension"
         self.__u = None
         self.__d = None
@@ -567,6 +575,7 @@ class PhaseField(_Simu):
         for i in range(C.size):
             p.C[i] = C[i]
         p.k_res = 1e-12
+        p.plane_stress = int(bool(getattr(mat, "planeStress", False)) and self.dim == 2)
         return p
 
     # ---- assembly ----------------------------------------------------------

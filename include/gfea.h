@@ -63,6 +63,9 @@ extern "C" {
 #define GFEA_SPLIT_BOURDIN 0
 #define GFEA_SPLIT_AMOR 1
 #define GFEA_SPLIT_MIEHE 2
+#define GFEA_SPLIT_ZHANG 3
+#define GFEA_SPLIT_STRESS 4
+#define GFEA_SPLIT_HE 5
 #define GFEA_AT1 0
 #define GFEA_AT2 1
 
@@ -168,8 +171,10 @@ typedef struct gfea_pf_params {
   double Gc, l0;
   double thickness;      /* factor applied to Kd, Fd, Ku (1 in 3D) */
   double A[9];           /* diffusion tensor, row-major dim x dim (identity by default) */
-  double C[36];          /* Kelvin-Mandel C, row-major n x n (used by the Bourdin split) */
+  double C[36];          /* Kelvin-Mandel C, row-major n x n (Bourdin, Zhang, Stress, He splits) */
   double k_res;          /* residual stiffness of g(d), 1e-12 in the reference */
+  int32_t plane_stress;  /* 2D: 1 plane stress, 0 plane strain (the Stress split's compliance) */
+  int32_t pad;
 } gfea_pf_params;
 
 /* Damage system at the current displacement: strain at mass Gauss points,

@@ -755,11 +755,15 @@ def IxI(dim):
     return np.outer(I, I)
 
 
-def split_C(eps, split, lmbda, mu, dim, C=None, robust=False):
+def split_C(eps, split, lmbda, mu, dim, C=None, robust=False, E=None, v=None, planeStress=False):
     """cP, cM -- Models/_phasefield.py:396-571 (Calc_C, Bourdin :433-449,
-    Amor :451-483, Rp/Rm :485-501, Miehe :503-540).
+    Amor :451-483, Rp/Rm :485-501, Miehe :503-540), and the stress-based
+    splits :573-687 (Zhang: projectors of sigma = C eps, cP = P+ C; Stress:
+    cP = C s+ C with s+ from the isotropic compliance of sigma's positive
+    part) and He :689-749 (projectors of C^1/2 eps mapped back, cP = C P+).
 
-    ``lmbda``/``mu`` scalars or (Ne,) arrays; eps (Ne, nPg, 3|6)."""
+    ``lmbda``/``mu`` scalars or (Ne,) arrays; eps (Ne, nPg, 3|6); ``E``,
+    ``v``, ``planeStress``: the isotropic material of the Stress split."""
     Ne, nPg = eps.shape[:2]
     lm = np.broadcast_to(np.asarray(lmbda, float).reshape(-1, 1) if np.ndim(lmbda) else lmbda, (Ne, nPg))
     mm = np.broadcast_to(np.asarray(mu, float).reshape(-1, 1) if np.ndim(mu) else mu, (Ne, nPg))
@@ -781,6 +785,34 @@ def split_C(eps, split, lmbda, mu, dim, C=None, robust=False):
         cP = lm[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * projP
         cM = lm[..., None, None] * (Rm[..., None, None] * II) + 2 * mm[..., None, None] * projM
         return cP, cM
+    Cm = np.asarray(C, float)
+    if split in ("Zhang", "Stress"):
+        sig = np.einsum("ij,epj->epi", Cm, eps)
+        projP, projM = spectral_projectors(sig, robust)
+        if split == "Zhang":
+            return projP @ Cm, projM @ Cm
+        trs = sig[..., 0] + sig[..., 1] + (sig[..., 2] if dim == 3 else 0)
+        Rp = ((1 + np.sign(trs)) / 2)[..., None, None]
+        Rm = ((1 + np.sign(-trs)) / 2)[..., None, None]
+        mu0 = float(np.ravel(mu)[0])
+        if dim == 2:
+            a1 = (1 + v) / E
+            a2 = v / E if planeStress else v * (1 + v) / E
+        else:
+            a1 = 1 / (2 * mu0)
+            a2 = v / E
+        sP = a1 * projP - a2 * Rp * II
+        sM = a1 * projM - a2 * Rm * II
+        return Cm.T @ sP @ Cm, Cm.T @ sM @ Cm
+    if split == "He":
+        lam, Q = np.linalg.eigh(Cm)
+        sqrtC = (Q * np.sqrt(lam)) @ Q.T
+        sqrtS = (Q / np.sqrt(lam)) @ Q.T
+        epst = np.einsum("ij,epj->epi", sqrtC, eps)
+        pPt, pMt = spectral_projectors(epst, robust)
+        projP = sqrtS @ pPt @ sqrtC
+        projM = sqrtS @ pMt @ sqrtC
+        return Cm @ projP, Cm @ projM
     raise NotImplementedError(split)
 
 

@@ -143,7 +143,8 @@ class PhaseFieldOracle:
     def damage_system(self):
         """__Construct_Damage_Matrix, _phasefield.py:540-573."""
         eps = self.strain(self.geo_m)
-        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C)
+        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v,
+                              planeStress=self.planeStress)
         psiP, _ = fem.psi_split(eps, cP, cM)
         if self.H_old is not None and self.H_old.shape == psiP.shape:
             psiP = np.where(psiP - self.H_old < 0, self.H_old, psiP)
@@ -162,7 +163,8 @@ class PhaseFieldOracle:
     def elastic_system(self):
         """__Construct_Elastic_Matrix, _phasefield.py:444-482 (g = (1-d)^2 + 1e-12)."""
         eps = self.strain(self.geo_r)
-        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C)
+        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v,
+                              planeStress=self.planeStress)
         d_e = self.d[self.mesh.connect]
         d_pg = np.einsum("pn,en->ep", self.geo_r.N, d_e)
         g = (1 - d_pg) ** 2 + 1e-12

@@ -115,7 +115,7 @@ def split_case(R, out, seed=0):
         eps = np.concatenate([eps, np.array(special)], 0)[:, None, :]  # (Ne, 1, n)
         for planeStress in ((True, False) if dim == 2 else (False,)):
             mat = R.Models.Elastic.Isotropic(dim, E=210000.0, v=0.3, planeStress=planeStress)
-            for split in ("Bourdin", "Amor", "Miehe"):
+            for split in ("Bourdin", "Amor", "Miehe", "Zhang", "Stress", "He"):
                 pfm = R.Models.PhaseField(mat, split, "AT2", 2.7, 0.01)
                 cP, cM = pfm.Calc_C(FeArray.asfearray(eps.copy()))
                 psiP, psiM = pfm.Calc_psi_e_pg(FeArray.asfearray(eps.copy()))
@@ -229,6 +229,13 @@ def pf_conv_case(R, name, m, convOption, steps, dU, out, tol=1e-3, maxIter=100):
                u=np.array(us), d=np.array(ds), F=np.array(Fs), Niter=np.array(its),
                convIter=np.array(convs), bottom=bottom, top=top, notch=notch, top_dofs=top_dofs)
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+
+
+def _pf_split_cases(R, out):
+    """Staggered loops with the stress-based and He splits on the 16x16 plate."""
+    for split in ("Zhang", "Stress", "He"):
+        pf_case(R, f"pf_tri3_{split.lower()}_at2", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16), split, "AT2", False,
+                210000.0, 0.3, 2.7, 0.1, 3, 4e-3, out)
 
 
 def _pf_conv_cases(R, out):
@@ -385,6 +392,7 @@ def _el_hexa8_hetero(R, out):
 
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
+         "split": split_case, "pf_splits": _pf_split_cases,
          "pf_curve_tri3_200x200": pf_curve_case}
 
 

@@ -64,4 +64,4 @@ def test_unsupported_models_rejected(ref, golden):
         R.B.GpuElastic(mesh, mat)
     iso = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False)
     with pytest.raises(NotImplementedError):
-        R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, "He", "AT2", 2.7, 0.01))
+        R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, "AnisotStress", "AT2", 2.7, 0.01))

@@ -41,7 +41,7 @@ def test_state_systems_match_reference(golden, case):
     assert row_scaled_err(Ku, Kuref) <= 1e-12
 
 
-@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2"])
+@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2", "pf_tri3_he_at2"])
 def test_staggered_loop_matches_reference(golden, case):
     g = golden(case)
     m, simu = make_simu(g)
@@ -87,3 +87,18 @@ def test_convergence_options_match_reference(golden, opt):
         assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), f"step {k}: F {F} vs {g['F'][k - 1]}"
         assert np.max(np.abs(d - g["d"][k - 1])) <= 1e-6, f"step {k}"
         assert np.max(np.abs(u - g["u"][k - 1])) <= 1e-5 * np.abs(g["u"][k - 1]).max(), f"step {k}"
+
+
+@pytest.mark.parametrize("split", ["Zhang", "Stress"])
+def test_non_spd_splits_rejected_by_the_staggered_loop(split):
+    """The Zhang split's degraded stiffness is not symmetric and the Stress
+    split's can be indefinite: the GPU staggered loop (PCG, SPD systems)
+    refuses them rather than solve them badly."""
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    m = gmesh.Mesh_Tri3_Rect(1.0, 1.0, 4, 4)
+    mat = Models.Elastic.Isotropic(2, E=210e3, v=0.3, planeStress=False)
+    with pytest.raises(NotImplementedError):
+        Simulations.PhaseField(m, Models.PhaseField(mat, split, "AT2", 2.7, 0.1))

@@ -26,6 +26,7 @@ def gpu_split(eps, split, dim, planeStress):
     p.lambda_ = float(lmbda)
     p.mu = float(mu)
     p.Gc, p.l0, p.thickness, p.k_res = 2.7, 0.01, 1.0, 1e-12
+    p.plane_stress = int(planeStress)
     for i, v in enumerate(C.ravel()):
         p.C[i] = v
     n = 3 if dim == 2 else 6
@@ -41,7 +42,7 @@ def gpu_split(eps, split, dim, planeStress):
 
 
 @pytest.mark.parametrize("dim,ps", [(2, 1), (2, 0), (3, 0)])
-@pytest.mark.parametrize("split", ["Bourdin", "Amor", "Miehe"])
+@pytest.mark.parametrize("split", ["Bourdin", "Amor", "Miehe", "Zhang", "Stress", "He"])
 def test_split_matches_reference(golden, dim, ps, split):
     g = golden("split")
     eps = g[f"d{dim}_eps"]
@@ -52,13 +53,16 @@ def test_split_matches_reference(golden, dim, ps, split):
     refM = np.broadcast_to(g[key + "_cM"].reshape(-1, n, n), cM.shape)
     scale = np.abs(C).max()
     lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
-    fP, _ = fem.split_C(eps, split, lmbda, mu, dim, C, robust=False)
-    rP, rM = fem.split_C(eps, split, lmbda, mu, dim, C, robust=True)
+    kw = dict(E=210000.0, v=0.3, planeStress=bool(ps))
+    fP, _ = fem.split_C(eps, split, lmbda, mu, dim, C, robust=False, **kw)
+    rP, rM = fem.split_C(eps, split, lmbda, mu, dim, C, robust=True, **kw)
     # degenerate rows (exactly repeated or zero eigenvalues): the reference
     # returns NaN, or its result depends on the last bit of a rounding residue
     bad = np.isnan(refP.reshape(len(cP), -1)).any(1) | \
         (np.abs(np.nan_to_num(fP, nan=1e300) - rP).reshape(len(cP), -1).max(1) > 1e-9 * scale)
-    assert bad.sum() <= 6
+    # only the special strains appended to the seeded ones can be degenerate
+    n_special = 9 if dim == 3 else 6
+    assert not bad[:-n_special].any()
     ok = ~bad
     assert np.max(np.abs(cP[ok] - refP[ok])) <= 1e-12 * scale
     assert np.max(np.abs(cM[ok] - refM[ok])) <= 1e-12 * scale

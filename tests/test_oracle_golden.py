@@ -59,14 +59,14 @@ def test_mass_matrix_matches_reference(golden):
 
 
 @pytest.mark.parametrize("dim,ps", [(2, 1), (2, 0), (3, 0)])
-@pytest.mark.parametrize("split", ["Bourdin", "Amor", "Miehe"])
+@pytest.mark.parametrize("split", ["Bourdin", "Amor", "Miehe", "Zhang", "Stress", "He"])
 def test_split_oracle_matches_reference(golden, dim, ps, split):
     g = golden("split")
     eps = g[f"d{dim}_eps"]
     key = f"d{dim}_ps{ps}_{split}"
     lmbda, mu = fem.lame(210000.0, 0.3, dim, bool(ps))
     C = fem.isotropic_C(210000.0, 0.3, dim, bool(ps))
-    cP, cM = fem.split_C(eps, split, lmbda, mu, dim, C)
+    cP, cM = fem.split_C(eps, split, lmbda, mu, dim, C, E=210000.0, v=0.3, planeStress=bool(ps))
     psiP, psiM = fem.psi_split(eps, cP, cM)
     refP = np.broadcast_to(g[key + "_cP"].reshape((-1,) + cP.shape[1:]) if g[key + "_cP"].size != cP.size
                            else g[key + "_cP"].reshape(cP.shape), cP.shape)
@@ -101,7 +101,8 @@ def test_split_robust_fixes_reference_nan(golden):
     np.testing.assert_allclose(psiP + psiM, psi, rtol=1e-10, atol=1e-14)
 
 
-@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2"])
+@pytest.mark.parametrize("case", ["pf_tri3_miehe_at2", "pf_quad4_amor_at2", "pf_hexa8_miehe_at2", "pf_tri3_zhang_at2",
+                                  "pf_tri3_stress_at2", "pf_tri3_he_at2"])
 def test_phasefield_oracle_matches_reference(golden, case):
     g = golden(case)
     m = om(g)

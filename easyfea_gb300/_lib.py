@@ -22,7 +22,7 @@ ERR_TIMEOUT = 9
 F64 = 0
 F32 = 1
 
-ELEM_CODE = {"SEG2": 0, "TRI3": 1, "QUAD4": 2, "QUAD9": 3, "HEXA8": 4}
+ELEM_CODE = {"SEG2": 0, "TRI3": 1, "QUAD4": 2, "QUAD9": 3, "HEXA8": 4, "TETRA4": 5}
 SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2, "Zhang": 3, "Stress": 4, "He": 5}
 REGU_CODE = {"AT1": 0, "AT2": 1}
 

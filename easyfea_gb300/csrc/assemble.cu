@@ -626,6 +626,7 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
     GFEA_ELASTIC_CASE(GFEA_QUAD4)
     GFEA_ELASTIC_CASE(GFEA_QUAD9)
     GFEA_ELASTIC_CASE(GFEA_HEXA8)
+    GFEA_ELASTIC_CASE(GFEA_TETRA4)
     default: return GFEA_ERR_ARG;
   }
 #undef GFEA_ELASTIC_CASE
@@ -634,7 +635,7 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
 int elem_dim(int elem) {
   switch (elem) {
     case GFEA_SEG2: return 1;
-    case GFEA_HEXA8: return 3;
+    case GFEA_HEXA8: case GFEA_TETRA4: return 3;
     case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: return 2;
     default: return -1;
   }
@@ -704,6 +705,7 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_QUAD4: return launch_mass<GFEA_QUAD4, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TETRA4: return launch_mass<GFEA_TETRA4, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   } else if (value_type == GFEA_F32) {
@@ -713,6 +715,7 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_QUAD4: return launch_mass<GFEA_QUAD4, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TETRA4: return launch_mass<GFEA_TETRA4, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   }

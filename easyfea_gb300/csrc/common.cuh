@@ -45,7 +45,7 @@ __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + 
 
 // ---------------------------------------------------------------------------
 // Element reference data.  Gauss tables follow EasyFEA/FEM/_gauss.py:364-480
-// and the shape functions EasyFEA/FEM/Elems/{_seg,_tri,_quad,_hexa}.py; they
+// and the shape functions EasyFEA/FEM/Elems/{_seg,_tri,_quad,_hexa,_tetra}.py; they
 // are evaluated on the device into shared memory by each kernel's prologue.
 // ---------------------------------------------------------------------------
 
@@ -206,6 +206,27 @@ template <> struct Elem<GFEA_HEXA8> {
     if (d == 0) return a * (1 + b * s) * (1 + c * t) / 8;
     if (d == 1) return b * (1 + a * r) * (1 + c * t) / 8;
     return c * (1 + a * r) * (1 + b * s) / 8;
+  }
+};
+
+template <> struct Elem<GFEA_TETRA4> {
+  static constexpr int nPe = 4, dim = 3, nPg_rigi = 1, nPg_mass = 4;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (!mass) { xi[0] = xi[1] = xi[2] = 0.25; *w = 1.0 / 6; return; }
+    // EasyFEA/FEM/_gauss.py:155-163: a = (5 - sqrt 5)/20, b = (5 + 3 sqrt 5)/20,
+    // x = [a, a, a, b], y = [a, a, b, a], z = [a, b, a, a], weights 1/24
+    const double a = (5 - sqrt(5.0)) / 20, b = (5 + 3 * sqrt(5.0)) / 20;
+    xi[0] = g == 3 ? b : a;
+    xi[1] = g == 2 ? b : a;
+    xi[2] = g == 1 ? b : a;
+    *w = 1.0 / 24;
+  }
+  __device__ static double N(const double* p, int n) {
+    return n == 0 ? 1 - p[0] - p[1] - p[2] : p[n - 1];
+  }
+  __device__ static double dN(const double*, int d, int n) {
+    if (n == 0) return -1.0;
+    return d == n - 1 ? 1.0 : 0.0;
   }
 };
 

@@ -698,6 +698,7 @@ extern "C" int gfea_pf_damage(int elem, const double* coord, const int32_t* conn
     case GFEA_QUAD4: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD4>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     case GFEA_QUAD9: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD9>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     case GFEA_HEXA8: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_HEXA8>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_TETRA4: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_TETRA4>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     default: return GFEA_ERR_ARG;
   }
 }
@@ -717,6 +718,7 @@ extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* con
       case GFEA_QUAD4: return launch_pfel<GFEA_QUAD4, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TETRA4: return launch_pfel<GFEA_TETRA4, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       default: return GFEA_ERR_ARG;
     }
   } else if (value_type == GFEA_F32) {
@@ -726,6 +728,7 @@ extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* con
       case GFEA_QUAD4: return launch_pfel<GFEA_QUAD4, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TETRA4: return launch_pfel<GFEA_TETRA4, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       default: return GFEA_ERR_ARG;
     }
   }

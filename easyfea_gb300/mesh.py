@@ -32,6 +32,7 @@ class ElemType(str, Enum):
     QUAD4 = "QUAD4"
     QUAD9 = "QUAD9"
     HEXA8 = "HEXA8"
+    TETRA4 = "TETRA4"
 
 
 class MatrixType(str, Enum):
@@ -48,6 +49,7 @@ ELEM_INFO = {
     ElemType.QUAD4: (4, 2, 2),
     ElemType.QUAD9: (9, 2, 3),
     ElemType.HEXA8: (8, 3, 4),
+    ElemType.TETRA4: (4, 3, 5),
 }
 
 # Gauss points per (element, matrixType), as chosen by
@@ -64,6 +66,8 @@ NPG = {
     (ElemType.QUAD9, MatrixType.mass): 9,
     (ElemType.HEXA8, MatrixType.rigi): 8,
     (ElemType.HEXA8, MatrixType.mass): 8,
+    (ElemType.TETRA4, MatrixType.rigi): 1,
+    (ElemType.TETRA4, MatrixType.mass): 4,
 }
 
 
@@ -339,6 +343,43 @@ def Mesh_Hexa8_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -
     groups = {
         ElemType.QUAD4: GroupElem(ElemType.QUAD4, faces, coord),
         ElemType.HEXA8: GroupElem(ElemType.HEXA8, connect, coord),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Tetra4_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised TETRA4 mesh of [0,Lx]x[0,Ly]x[0,Lz]: every cell of the
+    HEXA8 grid (same node numbering) split into the six tetrahedra of its
+    main diagonal (conforming: each cell face is cut along its diagonal from
+    the corner of lowest to highest coordinates); the TRI3 boundary faces
+    are the tetrahedra's faces that belong to one tetrahedron only."""
+    xs = np.linspace(0.0, Lx, nx + 1)
+    ys = np.linspace(0.0, Ly, ny + 1)
+    zs = np.linspace(0.0, Lz, nz + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    coord = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    nid = lambda i, j, k: (k * (ny + 1) + j) * (nx + 1) + i  # noqa: E731
+    K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    I, J, K = I.ravel(), J.ravel(), K.ravel()
+    corner = lambda a, b, c: nid(I + a, J + b, K + c)  # noqa: E731
+    tets = []
+    # a path 000 -> 111 through the cell's corners for each order of the axes
+    for order in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+        p = [0, 0, 0]
+        path = [corner(*p)]
+        for ax in order:
+            p[ax] = 1
+            path.append(corner(*p))
+        tets.append(np.stack(path, axis=1))
+    connect = np.concatenate(tets, 0)
+    faces = np.concatenate([connect[:, [0, 2, 1]], connect[:, [0, 3, 2]], connect[:, [0, 1, 3]],
+                            connect[:, [1, 2, 3]]], 0)
+    key = np.sort(faces, axis=1)
+    _, inv, counts = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    boundary = faces[counts[inv.ravel()] == 1]
+    groups = {
+        ElemType.TRI3: GroupElem(ElemType.TRI3, boundary, coord),
+        ElemType.TETRA4: GroupElem(ElemType.TETRA4, connect, coord),
     }
     return Mesh(groups)
 

@@ -54,6 +54,7 @@ extern "C" {
 #define GFEA_QUAD4 2
 #define GFEA_QUAD9 3
 #define GFEA_HEXA8 4
+#define GFEA_TETRA4 5
 
 /* value types */
 #define GFEA_F64 0

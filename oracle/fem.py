@@ -57,6 +57,12 @@ def gauss(elem: str, matrixType: str):
         y = [-a, -a, a, a, -a, -a, a, a]
         z = [-a, a, -a, a, -a, a, -a, a]
         return np.array([x, y, z]).T, np.ones(8)
+    if elem == "TETRA4":  # _gauss.py:142-163 (rigi 1 point, mass 4)
+        if matrixType == "rigi":
+            return np.array([[1 / 4, 1 / 4, 1 / 4]]), np.array([1 / 6])
+        a = (5 - np.sqrt(5)) / 20
+        b = (5 + 3 * np.sqrt(5)) / 20
+        return np.array([[a, a, a, b], [a, a, b, a], [a, b, a, a]]).T, np.full(4, 1 / 24)
     raise NotImplementedError(elem)
 
 
@@ -93,6 +99,9 @@ def shape_N(elem: str, p: np.ndarray) -> np.ndarray:
             -(r + 1) * (s + 1) * (t - 1) / 8, (r - 1) * (s + 1) * (t - 1) / 8,
             (r - 1) * (s - 1) * (t + 1) / 8, -(r + 1) * (s - 1) * (t + 1) / 8,
             (r + 1) * (s + 1) * (t + 1) / 8, -(r - 1) * (s + 1) * (t + 1) / 8])
+    if elem == "TETRA4":  # Elems/_tetra.py TETRA4._N
+        r, s, t = p
+        return np.array([-r - s - t + 1, r, s, t])
     raise NotImplementedError(elem)
 
 
@@ -142,10 +151,12 @@ def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
             [-(r - 1) * (s - 1) / 8, (r + 1) * (s - 1) / 8, -(r + 1) * (s + 1) / 8, (r - 1) * (s + 1) / 8,
              (r - 1) * (s - 1) / 8, -(r + 1) * (s - 1) / 8, (r + 1) * (s + 1) / 8, -(r - 1) * (s + 1) / 8],
         ])
+    if elem == "TETRA4":  # Elems/_tetra.py TETRA4._dN
+        return np.array([[-1.0, 1.0, 0.0, 0.0], [-1.0, 0.0, 1.0, 0.0], [-1.0, 0.0, 0.0, 1.0]])
     raise NotImplementedError(elem)
 
 
-ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3}
+ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3, "TETRA4": 3}
 
 
 def N_pg(elem, matrixType):

@@ -231,6 +231,13 @@ def pf_conv_case(R, name, m, convOption, steps, dU, out, tol=1e-3, maxIter=100):
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
 
 
+def _tetra4_cases(R, out):
+    """TETRA4: the 3D cantilever box and a phase-field system at a prescribed state."""
+    elastic_case(R, "el_tetra4", gmesh.Mesh_Tetra4_Box(60.0, 10.0, 10.0, 6, 2, 2), 210000.0, 0.3, False, 1.0,
+                 -1.0, "z", out)
+    pf_state_case(R, "pfsys_tetra4_miehe_at2", gmesh.Mesh_Tetra4_Box(1.0, 1.0, 0.5, 4, 4, 2), "Miehe", "AT2", out)
+
+
 def _pf_split_cases(R, out):
     """Staggered loops with the stress-based and He splits on the 16x16 plate."""
     for split in ("Zhang", "Stress", "He"):
@@ -392,7 +399,7 @@ def _el_hexa8_hetero(R, out):
 
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
-         "split": split_case, "pf_splits": _pf_split_cases,
+         "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
          "pf_curve_tri3_200x200": pf_curve_case}
 
 

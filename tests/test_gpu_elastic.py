@@ -7,7 +7,8 @@ from helpers import csr, mesh_from_golden, row_scaled_err, same_pattern
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26"]
+CASES = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26",
+         "el_tetra4"]
 
 
 def run_case(g, precision="fp64", rtol=1e-12):
@@ -104,7 +105,7 @@ def test_field_loads_match_reference(golden, case):
 
 
 @pytest.mark.parametrize("case", ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero",
-                                  "el_cantilever_240x26"])
+                                  "el_cantilever_240x26", "el_tetra4"])
 def test_f32_element_path_matches_reference(golden, case):
     """The FP32 element path (gfea_assemble_elastic / gfea_assemble_mass with
     GFEA_F32: geometry on the FP32 pipe from coordinates relative to each

@@ -7,7 +7,8 @@ import scipy.sparse as sp
 from oracle import fem
 from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve, neumann
 
-ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26"]
+ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26",
+           "el_tetra4"]
 
 
 def row_scaled_err(A, B):
@@ -170,7 +171,8 @@ def test_phasefield_oracle_convergence_options_match_reference(golden, opt):
         assert abs(pf.convIter - g["convIter"][k - 1]) <= 1e-6 * abs(g["convIter"][k - 1])
 
 
-@pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2"])
+@pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2",
+                                  "pfsys_tetra4_miehe_at2"])
 def test_phasefield_state_systems_match_reference(golden, case):
     g = golden(case)
     m = om(g)

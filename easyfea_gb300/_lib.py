@@ -135,6 +135,29 @@ class PfParams(ctypes.Structure):
     ]
 
 
+class Fields(ctypes.Structure):
+    """gfea_fields: inputs and outputs of gfea_element_fields."""
+
+    _fields_ = [
+        ("version", c_int32),
+        ("gauss", c_int32),
+        ("coef", c_double),
+        ("thickness", c_double),
+        ("C", c_void_p),
+        ("c_per_elem", c_int32),
+        ("pad", c_int32),
+        ("pf", POINTER(PfParams)),
+        ("d", c_void_p),
+        ("H_old", c_void_p),
+        ("sigma_n", c_void_p),
+        ("strain_e", c_void_p),
+        ("stress_e", c_void_p),
+        ("vm_e", c_void_p),
+        ("energy_e", c_void_p),
+        ("psiP_e", c_void_p),
+    ]
+
+
 _LIB = None
 
 # name -> (restype, argtypes); the complete list of exported entry points
@@ -163,6 +186,10 @@ SIGNATURES = {
                                 POINTER(PfParams), c_int, c_void_p, c_void_p]),
     "gfea_pf_split": (c_int, [c_void_p, c_int64, POINTER(PfParams), c_void_p, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
+    "gfea_element_fields": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, POINTER(Fields), c_void_p]),
+    "gfea_node_incidence": (c_int, [c_void_p, c_int64, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_size_t,
+                                    c_void_p]),
+    "gfea_node_average": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_void_p]),
     "gfea_spmv": (c_int, [POINTER(System), c_int, c_void_p, c_void_p, c_void_p]),
     "gfea_pcg_workspace_size": (c_int, [POINTER(System), POINTER(PcgOpts), POINTER(c_size_t)]),
     "gfea_pcg_solve": (c_int, [POINTER(System), c_void_p, c_void_p, POINTER(PcgOpts), c_void_p, c_size_t,

@@ -234,6 +234,23 @@ __global__ void csr_pattern_kernel(const int32_t* node_ptr, const int32_t* nbr, 
   }
 }
 
+// Each node's incident elements in ascending order (insertion sort in place:
+// a node of a conforming mesh has a few tens of elements at most).
+__global__ void inc_sort(const int32_t* inc_ptr, int64_t Nn, int32_t* list) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < Nn; a += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t lo = inc_ptr[a], hi = inc_ptr[a + 1];
+    for (int32_t i = lo + 1; i < hi; ++i) {
+      const int32_t v = list[i];
+      int32_t j = i;
+      while (j > lo && list[j - 1] > v) {
+        list[j] = list[j - 1];
+        --j;
+      }
+      list[j] = v;
+    }
+  }
+}
+
 }  // namespace
 }  // namespace gfea
 
@@ -305,4 +322,31 @@ extern "C" int gfea_csr_pattern(const int32_t* node_ptr, const int32_t* nbr, int
   csr_pattern_kernel<<<grid_for(n_nodes * 32, 256), 256, 0, s>>>(node_ptr, nbr, n_nodes, dof_n, indptr, indices);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
+}
+
+extern "C" int gfea_node_incidence(const int32_t* connect, int64_t n_elems, int nPe, int64_t n_nodes,
+                                   int32_t* inc_ptr, int32_t* inc_list, void* work, size_t work_bytes,
+                                   void* stream) {
+  if (!connect || !inc_ptr || !inc_list || !work || n_nodes <= 0 || n_elems <= 0 || nPe < 1 || nPe > 32)
+    return GFEA_ERR_ARG;
+  if (n_elems * nPe >= ((int64_t)1 << 31) || n_nodes >= ((int64_t)1 << 31) - 1) return GFEA_ERR_ARG;
+  GraphWork w;
+  if (graph_ws(n_nodes, n_elems, nPe, &w, static_cast<char*>(work)) > work_bytes) return GFEA_ERR_WORKSPACE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GFEA_CUDA_TRY(cudaMemsetAsync(inc_ptr, 0, sizeof(int32_t) * (n_nodes + 1), s));
+  GFEA_CUDA_TRY(cudaMemsetAsync(w.flag, 0, sizeof(int32_t), s));
+  const int64_t nent = n_elems * nPe;
+  inc_count<<<grid_for(nent, 256), 256, 0, s>>>(connect, nent, n_nodes, inc_ptr, w.flag);
+  GFEA_LAUNCH_CHECK();
+  int st = exclusive_scan(inc_ptr, inc_ptr, n_nodes + 1, w.sums, s);
+  if (st) return st;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(w.cursor, inc_ptr, sizeof(int32_t) * n_nodes, cudaMemcpyDeviceToDevice, s));
+  inc_fill<<<grid_for(nent, 256), 256, 0, s>>>(connect, n_elems, nPe, n_nodes, w.cursor, inc_list);
+  GFEA_LAUNCH_CHECK();
+  inc_sort<<<grid_for(n_nodes, 128), 128, 0, s>>>(inc_ptr, n_nodes, inc_list);
+  GFEA_LAUNCH_CHECK();
+  int32_t flag = 0;
+  GFEA_CUDA_TRY(cudaMemcpyAsync(&flag, w.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GFEA_CUDA_TRY(cudaStreamSynchronize(s));
+  return flag ? GFEA_ERR_ARG : GFEA_OK;
 }

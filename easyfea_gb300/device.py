@@ -77,6 +77,34 @@ class DeviceMesh:
     def nnz(self, dof_n: int) -> int:
         return dof_n * dof_n * self.n_pairs
 
+    def incidence(self):
+        """(inc_ptr, inc_list) int32 device tensors: each node's elements of the
+        main group, ascending (built once)."""
+        if getattr(self, "_incidence", None) is None:
+            L = _lib.load()
+            g = self.main
+            ws = ctypes.c_size_t()
+            _lib.check(L.gfea_graph_workspace_size(self.Nn, g.Ne, g.nPe, ctypes.byref(ws)), "graph workspace")
+            work = torch.empty(int(ws.value), dtype=torch.uint8, device=_dev())
+            inc_ptr = torch.empty(self.Nn + 1, dtype=torch.int32, device=_dev())
+            inc_list = torch.empty(g.Ne * g.nPe, dtype=torch.int32, device=_dev())
+            _lib.check(L.gfea_node_incidence(_lib.ptr(g.connect), g.Ne, g.nPe, self.Nn, _lib.ptr(inc_ptr),
+                                             _lib.ptr(inc_list), _lib.ptr(work), work.numel(), _lib.stream()),
+                       "node incidence")
+            self._incidence = (inc_ptr, inc_list)
+        return self._incidence
+
+    def node_values(self, values_e: torch.Tensor) -> torch.Tensor:
+        """Mean of element values (Ne,) or (Ne, k) around each node, on the
+        device (Mesh.Get_Node_Values)."""
+        ve = values_e.contiguous()
+        k = 1 if ve.dim() == 1 else ve.shape[1]
+        out = torch.empty((self.Nn,) if ve.dim() == 1 else (self.Nn, k), dtype=torch.float64, device=_dev())
+        inc_ptr, inc_list = self.incidence()
+        _lib.check(_lib.load().gfea_node_average(_lib.ptr(inc_ptr), _lib.ptr(inc_list), self.Nn, _lib.ptr(ve), k,
+                                                 _lib.ptr(out), _lib.stream()), "node average")
+        return out
+
     def pattern(self, dof_n: int):
         """(indptr int64, indices int32) device tensors of the dof_n CSR pattern."""
         if dof_n not in self._patterns:

@@ -301,6 +301,111 @@ class _Simu:
     def results(self) -> list:
         return self._results
 
+    # ---- post-processing on the device (_simu.py:3067-3151) -------------------
+    def Results_Available(self) -> list:
+        return []
+
+    def Result(self, result: str, nodeValues: bool = True):
+        """The reference's Result(result, nodeValues): a host array (nodes or
+        elements) or a float; computed on the device by Result_device."""
+        v = self.Result_device(result, nodeValues)
+        return v if isinstance(v, float) or v is None else v.cpu().numpy()
+
+    def Result_device(self, result: str, nodeValues: bool = True):
+        raise NotImplementedError
+
+    def _check_result(self, result: str) -> None:
+        if result not in self.Results_Available():
+            raise ValueError(f"For a {self.problemType} problem result must be in: {self.Results_Available()}")
+
+    def _reshape_values(self, values: torch.Tensor, nodeValues: bool) -> torch.Tensor:
+        """Results_Reshape_values (_simu.py:3095-3151): element values to the
+        nodes (node average) or node values to the elements (mean over each
+        element's nodes); a node-sized array counts as node values first, as
+        in the reference."""
+        dm = self.dmesh
+        Nn, Ne = dm.Nn, dm.main.Ne
+        is1d = values.dim() == 1
+        if nodeValues:
+            if values.numel() % Nn == 0:
+                return values.reshape(-1) if is1d else values.reshape(Nn, -1)
+            vn = dm.node_values(values.reshape(Ne, -1))
+            return vn.reshape(-1) if is1d else vn
+        if values.numel() % Ne == 0:
+            return values.reshape(-1) if is1d else values.reshape(Ne, -1)
+        ve = values.reshape(Nn, -1)[dm.main.connect.long()].mean(1)
+        return ve.reshape(-1) if is1d else ve
+
+    def _element_fields(self, u: torch.Tensor, gauss: int = 0, coef: float = float(np.sqrt(2)), strain=False,
+                        stress=False, vm=False, energy=False, psiP=False, sigma_n=None, pf=None, d=None,
+                        H_old=None) -> dict:
+        """One gfea_element_fields launch; returns the requested (Ne, ...) device tensors."""
+        import ctypes
+
+        dm = self.dmesh
+        g = dm.main
+        n = 3 if self.dim == 2 else 6
+        out = {}
+
+        def take(key, want, shape):
+            if not want:
+                return 0
+            out[key] = torch.empty(shape, dtype=torch.float64, device=_dev())
+            return _lib.ptr(out[key])
+
+        f = _lib.Fields()
+        f.version = _lib.ABI_VERSION
+        f.gauss = gauss
+        f.coef = coef
+        f.thickness = self.model_thickness if self.dim == 2 else 1.0
+        keep = []
+        if pf is None:
+            C, mode = self._C_device()
+            keep.append(C)
+            f.C = _lib.ptr(C)
+            f.c_per_elem = int(mode)
+        else:
+            f.pf = ctypes.pointer(pf)
+            f.d = _lib.ptr(d)
+            f.H_old = _lib.ptr(H_old)
+        if sigma_n is not None:
+            sigma_n = sigma_n.contiguous()
+            keep.append(sigma_n)
+            f.sigma_n = _lib.ptr(sigma_n)
+        f.strain_e = take("strain", strain, (g.Ne, n))
+        f.stress_e = take("stress", stress, (g.Ne, n))
+        f.vm_e = take("vm", vm, (g.Ne, 2))
+        f.energy_e = take("energy", energy, (g.Ne,))
+        f.psiP_e = take("psiP", psiP, (g.Ne,))
+        _lib.check(_lib.load().gfea_element_fields(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                                   _lib.ptr(u), ctypes.byref(f), _lib.stream()), "element fields")
+        return out
+
+    def _displacement_result(self, u: torch.Tensor, result: str):
+        Nn = self.mesh.Nn
+        if result in ("ux", "uy", "uz"):
+            return u.reshape(Nn, -1)[:, "xyz".index(result[1])]
+        if result == "displacement":
+            return u
+        return torch.linalg.norm(u.reshape(Nn, -1), dim=1)  # displacement_norm
+
+    def _strain_stress_result(self, result: str, fields) -> torch.Tensor:
+        """The strain / stress branch of Result (_elastic.py:296-320,
+        _phasefield.py:733-754); ``fields(strain, stress, vm)`` launches the
+        element kernel."""
+        isStrain = "E" in result or result == "Strain"
+        isStress = "S" in result and result != "Strain"
+        if not (isStrain or isStress):
+            raise ValueError("Wrong option")
+        res = result if result in ("Strain", "Stress") else result[-2:]
+        if res == "vm":
+            return fields(False, False, True)["vm"][:, 1 if isStress else 0]
+        out = fields(not isStress, isStress, False)["stress" if isStress else "strain"]
+        if res in ("Strain", "Stress"):
+            return out
+        names = ("xx", "yy", "xy") if self.dim == 2 else ("xx", "yy", "zz", "yz", "xz", "xy")
+        return out[:, names.index(res)]
+
 
 ctypes_int32 = __import__("ctypes").c_int32
 ctypes_double = __import__("ctypes").c_double
@@ -418,6 +523,11 @@ class Elastic(_Simu):
     def u_device(self) -> Optional[torch.Tensor]:
         return self.__u
 
+    def _Set_solutions(self, problemType, u) -> None:
+        """Set the displacement (_simu.py:1517-1530)."""
+        self._check_pt(problemType)
+        self.__u = torch.as_tensor(np.ascontiguousarray(u, dtype=np.float64), device=_dev()).reshape(-1).clone()
+
     @property
     def displacement(self) -> np.ndarray:
         if self.__u is None:
@@ -436,6 +546,48 @@ class Elastic(_Simu):
         it = {} if iter is None else iter
         it["displacement"] = self.displacement
         return super().Save_Iter(it)
+
+    # ---- results (_elastic.py:201-418) ---------------------------------------
+    def Results_Available(self) -> list:
+        comps = ["x", "y"] if self.dim == 2 else ["x", "y", "z"]
+        tens = ["xx", "yy", "xy"] if self.dim == 2 else ["xx", "yy", "zz", "yz", "xz", "xy"]
+        return (["displacement", "displacement_norm"] + [f"u{c}" for c in comps] + [f"S{t}" for t in tens] +
+                [f"E{t}" for t in tens] + ["Svm", "Stress", "Evm", "Strain", "Wdef", "Wdef_e", "ZZ1", "ZZ1_e"])
+
+    def Result_device(self, result: str, nodeValues: bool = True):
+        """Elastic.Result on the device: displacement results, strain / stress
+        components and von Mises (element means of the Gauss-point values),
+        the strain energy and the ZZ1 error estimator."""
+        self._check_result(result)
+        u = self.__u if self.__u is not None else torch.zeros(self.Ndof(), dtype=torch.float64, device=_dev())
+        if result in ("ux", "uy", "uz", "displacement", "displacement_norm"):
+            values = self._displacement_result(u, result)
+        elif result in ("Wdef", "Wdef_e"):
+            W_e = self._element_fields(u, energy=True)["energy"]
+            if result == "Wdef":
+                return float(W_e.sum())
+            values = W_e
+        elif result in ("ZZ1", "ZZ1_e"):
+            err, err_e = self._zz1(u)
+            if result == "ZZ1":
+                return err
+            values = err_e
+        else:
+            values = self._strain_stress_result(
+                result, lambda e, s, v: self._element_fields(u, strain=e, stress=s, vm=v))
+        return self._reshape_values(values, nodeValues)
+
+    def _zz1(self, u: torch.Tensor):
+        """ZZ1 error (_elastic.py:397-418): the plain element energies, the
+        Kelvin-Mandel element-mean stress averaged at the nodes, and the
+        energies of that smoothed stress interpolated back with N."""
+        first = self._element_fields(u, coef=1.0, stress=True, energy=True)
+        sigma_n = self.dmesh.node_values(first["stress"])
+        Ws_e = self._element_fields(u, energy=True, sigma_n=sigma_n)["energy"]
+        W_e = first["energy"]
+        Welas = W_e.sum()
+        err = float(torch.abs(Welas - Ws_e.sum()) / Welas)
+        return err, torch.abs(Ws_e - W_e) / Welas
 
 
 class PhaseField(_Simu):
@@ -540,6 +692,15 @@ class PhaseField(_Simu):
     @property
     def psiP_device(self) -> Optional[torch.Tensor]:
         return self.__psiP
+
+    def _Set_solutions(self, problemType, x) -> None:
+        """Set the displacement or the damage (_simu.py:1517-1530); the
+        operators that depend on it are re-assembled at their next use."""
+        pt = self._check_pt_raw(problemType)
+        u, d = self._state()
+        (u if pt == "elastic" else d).copy_(torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64)).reshape(-1))
+        self.__updatedDamage = False
+        self.__updatedDisplacement = False
 
     def set_history(self, H: Optional[np.ndarray]) -> None:
         """Replace the committed History field (psi+ at the mass Gauss points,
@@ -744,3 +905,40 @@ class PhaseField(_Simu):
     def reaction_sum(self, dofs: torch.Tensor) -> float:
         """sum Ku[dofs] @ u reduced on the device (no host copy of the vector)."""
         return reaction_energy(self.__Ku, self._state()[0], dofs)[0]
+
+    # ---- results (_phasefield.py:659-760) ------------------------------------
+    def Results_Available(self) -> list:
+        comps = ["x", "y"] if self.dim == 2 else ["x", "y", "z"]
+        tens = ["xx", "yy", "xy"] if self.dim == 2 else ["xx", "yy", "zz", "yz", "xz", "xy"]
+        return (["displacement", "displacement_norm"] + [f"u{c}" for c in comps] + [f"S{t}" for t in tens] +
+                [f"E{t}" for t in tens] + ["Svm", "Stress", "Evm", "Strain", "damage", "psiP", "Psi_Crack", "Wdef"])
+
+    def Result_device(self, result: str, nodeValues: bool = True):
+        """PhaseField.Result on the device: the degraded stress g(d) sig+ +
+        sig- results, the strains, psiP (the History-max'ed psi+ at the mass
+        Gauss points), the damage and the two energies."""
+        self._check_result(result)
+        u, d = self._state()
+        if result == "Psi_Crack":
+            return 0.0 if float(torch.linalg.norm(d)) == 0 else self._psi_crack()
+        if result == "Wdef":
+            return 0.0 if float(torch.linalg.norm(u)) == 0 else self._psi_elas()
+        if result == "damage":
+            values = d
+        elif result in ("ux", "uy", "uz", "displacement", "displacement_norm"):
+            values = self._displacement_result(u, result)
+        elif result == "psiP":
+            H = None
+            if self.phaseFieldModel.solver == "History":
+                from .mesh import NPG, MatrixType
+
+                g = self.dmesh.main
+                H = self.__psiP_old
+                if H is None:  # nothing committed yet: the reference's zero history
+                    H = torch.zeros(g.Ne * NPG[(g.elemType, MatrixType.mass)], dtype=torch.float64, device=_dev())
+            values = self._element_fields(u, gauss=1, psiP=True, pf=self._params(), d=d, H_old=H)["psiP"]
+        else:
+            p = self._params()
+            values = self._strain_stress_result(
+                result, lambda e, s, v: self._element_fields(u, strain=e, stress=s, vm=v, pf=p, d=d))
+        return self._reshape_values(values, nodeValues)

@@ -207,6 +207,51 @@ int gfea_pf_split(const double* eps, int64_t n_points, const gfea_pf_params* par
                   double* cP, double* cM, double* psiP, double* psiM, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Post-processing: element results of a displacement field and their node
+ * averages, computed where the field lives.
+ * ---------------------------------------------------------------------- */
+typedef struct gfea_fields {
+  int32_t version;          /* GFEA_ABI_VERSION */
+  int32_t gauss;            /* 0: rigi Gauss points, 1: mass Gauss points */
+  double coef;              /* strain_e / stress_e shear components are the Kelvin-Mandel
+                               ones times 1/coef (sqrt(2): tensor components, as the
+                               reference's results; 1: Kelvin-Mandel) */
+  double thickness;         /* factor of energy_e (2D thickness, 1 in 3D) */
+  const double* C;          /* elastic law, as gfea_assemble_elastic's C / c_per_elem */
+  int32_t c_per_elem;
+  int32_t pad;
+  const gfea_pf_params* pf; /* non-NULL: phase-field stress g(d) cP eps + cM eps, and psiP_e */
+  const double* d;          /* nodal damage (pf) */
+  const double* H_old;      /* pf: History field at this Gauss family (Ne x nPg), max'ed into psiP_e; may be NULL */
+  const double* sigma_n;    /* non-NULL: energy_e integrates 1/2 (N sigma_n) . eps, sigma_n the nodal
+                               Kelvin-Mandel stress (Nn x n) -- the ZZ1 smoothed energy */
+  double* strain_e;         /* Ne x n: mean over the Gauss points of eps (scaled shear) */
+  double* stress_e;         /* Ne x n: same for sigma */
+  double* vm_e;             /* Ne x 2: mean of the von Mises equivalent of eps, of sigma */
+  double* energy_e;         /* Ne: thickness * sum_pg wJ 1/2 sigma . eps */
+  double* psiP_e;           /* Ne: mean of psi+ (pf) */
+} gfea_fields;
+/* Replaces Elastic.Result's strain and stress results (EasyFEA/Simulations/
+ * _elastic.py:296-320) through Result_strain_or_stress_field_e and
+ * __Result_in_Strain_or_Stress_field (EasyFEA/Models/_utils.py:302-430),
+ * Elastic._Calc_Psi_Elas with and without smoothing (_elastic.py:322-395),
+ * PhaseField._Calc_Sigma_e_pg (EasyFEA/Simulations/_phasefield.py:868-915)
+ * and its psiP result (:494-530, :706-714).  Any output may be NULL. */
+int gfea_element_fields(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                        const double* u, const gfea_fields* fields_host, void* stream);
+/* Node -> incident elements, each list ascending: inc_ptr[Nn+1], inc_list[Ne*nPe]
+ * (the rows of _GroupElem.Get_connect_n_e, EasyFEA/FEM/_group_elem.py:322-345).
+ * Workspace: gfea_graph_workspace_size. */
+int gfea_node_incidence(const int32_t* connect, int64_t n_elems, int nPe, int64_t n_nodes,
+                        int32_t* inc_ptr, int32_t* inc_list, void* work, size_t work_bytes,
+                        void* stream);
+/* values_n[a, c] = (sum over the elements e of node a of values_e[e, c]) / (their
+ * number), summed in ascending e:
+ * Mesh.Get_Node_Values (EasyFEA/FEM/_mesh.py:822-873). */
+int gfea_node_average(const int32_t* inc_ptr, const int32_t* inc_list, int64_t n_nodes,
+                      const double* values_e, int n_cols, double* values_n, void* stream);
+
+/* ------------------------------------------------------------------------
  * Sparse SPD solve.  Replaces Solvers.__Solver_1 (EasyFEA/Simulations/
  * Solvers.py:502-553: Dirichlet elimination) and _Solve_Axb's spsolve
  * (Solvers.py:361-362) by block-Jacobi PCG on the masked operator

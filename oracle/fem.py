@@ -846,3 +846,180 @@ def pf_r_f_k(psiP, regu, Gc, l0):
         r = 2 * psiP + Gc / l0
         f = 2 * psiP
     return r, f, k
+
+
+# ---------------------------------------------------------------------------
+# post-processing (EasyFEA/Models/_utils.py:302-430, Simulations/_elastic.py:
+# 229-418, Simulations/_phasefield.py:682-915, FEM/_mesh.py:822-873,
+# Simulations/_simu.py:3095-3151)
+# ---------------------------------------------------------------------------
+
+STRESS_COMPONENTS = {2: ("xx", "yy", "xy"), 3: ("xx", "yy", "zz", "yz", "xz", "xy")}
+
+
+def strain_e_pg(geo: Geometry, connect, u):
+    """eps = B u_e (Kelvin-Mandel) -- Models/Elastic/_laws.py:127-157."""
+    dim = geo.dim
+    u_e = np.asarray(u, float).reshape(-1, dim)[connect].reshape(len(connect), -1)
+    return np.einsum("epij,ej->epi", B_e_pg(geo.dNx), u_e)
+
+
+def stress_e_pg(C, eps):
+    """sigma = C eps; C (n,n) or per element (Ne,n,n) -- Elastic/_laws.py:159-185."""
+    C = np.asarray(C, float)
+    if C.ndim == 2:
+        return np.einsum("ij,epj->epi", C, eps)
+    return np.einsum("eij,epj->epi", C, eps)
+
+
+def result_in_field(field_e_pg, result, coef=SQRT2):
+    """One result of a Kelvin-Mandel strain / stress field (Ne, nPg, n): a
+    component with the shear ones times 1/coef, the von Mises equivalent, or
+    the whole scaled field -- Models/_utils.py:302-392."""
+    f = np.array(field_e_pg, dtype=float, copy=True)
+    dim = 2 if f.shape[-1] == 3 else 3
+    f[..., dim:] *= 1 / coef
+    names = STRESS_COMPONENTS[dim]
+    for i, nm in enumerate(names):
+        if nm in result:
+            return f[..., i]
+    if "vm" in result:
+        if dim == 2:
+            xx, yy, xy = (f[..., i] for i in range(3))
+            return np.sqrt(xx**2 + yy**2 - xx * yy + 3 * xy**2)
+        xx, yy, zz, yz, xz, xy = (f[..., i] for i in range(6))
+        return np.sqrt(0.5 * ((xx - yy) ** 2 + (yy - zz) ** 2 + (zz - xx) ** 2 + 6 * (xy**2 + yz**2 + xz**2)))
+    if result in ("Strain", "Stress"):
+        return f
+    raise ValueError(result)
+
+
+def node_values(connect, Nn, values_e):
+    """Mean of the element values around each node -- FEM/_mesh.py:822-873
+    (connect_n_e @ values_e * 1 / elements_n, _group_elem.py:322-345)."""
+    values_e = np.asarray(values_e, float)
+    is1d = values_e.ndim == 1
+    ve = values_e.reshape(len(connect), -1)
+    nPe = connect.shape[1]
+    cne = sp.csr_matrix((np.ones(connect.size), (connect.ravel(), np.repeat(np.arange(len(connect)), nPe))),
+                        shape=(Nn, len(connect)))
+    cnt = np.asarray(cne.sum(axis=1)).reshape(-1, 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = (cne @ ve) * 1 / cnt
+    return out.ravel() if is1d else out
+
+
+def reshape_values(values, nodeValues, connect, Nn):
+    """Simulations/_simu.py:3095-3151: element values to nodes (node_values)
+    or node values to elements (mean over the element's nodes); the size
+    tests come first in the reference's order (a node-sized array is taken as
+    node values)."""
+    values = np.asarray(values, float)
+    Ne = len(connect)
+    is1d = values.ndim == 1
+    if nodeValues:
+        if values.size % Nn == 0:
+            return values.ravel() if is1d else values.reshape(Nn, -1)
+        vn = node_values(connect, Nn, values.reshape(Ne, -1))
+        return vn.ravel() if is1d else vn.reshape(Nn, -1)
+    if values.size % Ne == 0:
+        return values.ravel() if is1d else values.reshape(Ne, -1)
+    ve = np.mean(values.reshape(Nn, -1)[connect], axis=1)
+    return ve.ravel() if is1d else ve.reshape(Ne, -1)
+
+
+def psi_elas_e(geo: Geometry, eps, sig, thickness):
+    """W_e = sum_pg thickness wJ 1/2 sig . eps -- Simulations/_elastic.py:322-395
+    with Elastic/_laws.py:187-213."""
+    psi = 0.5 * np.sum(sig * eps, -1)
+    return (thickness * geo.wJ * psi).sum(1)
+
+
+def zz1(geo: Geometry, connect, Nn, eps, sig, thickness):
+    """ZZ1 error (global, per element) -- Simulations/_elastic.py:397-418:
+    the energy of the node-averaged element-mean stress interpolated back
+    with N against the plain energy."""
+    W_e = psi_elas_e(geo, eps, sig, thickness)
+    sig_n = node_values(connect, Nn, np.mean(sig, 1))
+    sig_s = np.einsum("eni,pn->epi", sig_n[connect], geo.N)
+    Ws_e = psi_elas_e(geo, eps, sig_s, thickness)
+    Welas = W_e.sum()
+    return abs(Welas - Ws_e.sum()) / Welas, np.abs(Ws_e - W_e).ravel() / Welas
+
+
+def elastic_result(elem, coord, connect, u, C, result, thickness=1.0, nodeValues=True, coef=SQRT2):
+    """Elastic.Result for the displacement, strain, stress and energy results
+    (Simulations/_elastic.py:229-320)."""
+    Nn = len(coord)
+    dim = ELEM_DIM[elem]
+    un = np.asarray(u, float).reshape(Nn, dim)
+    if result in ("ux", "uy", "uz"):
+        values = un[:, "xyz".index(result[1])]
+    elif result == "displacement":
+        values = np.asarray(u, float)
+    elif result == "displacement_norm":
+        values = np.linalg.norm(un, axis=1)
+    elif result in ("Wdef", "Wdef_e", "ZZ1", "ZZ1_e"):
+        geo = Geometry(elem, coord, connect, "rigi")
+        eps = strain_e_pg(geo, connect, u)
+        sig = stress_e_pg(C, eps)
+        if result == "Wdef":
+            return float(psi_elas_e(geo, eps, sig, thickness).sum())
+        if result == "Wdef_e":
+            values = psi_elas_e(geo, eps, sig, thickness)
+        else:
+            err, err_e = zz1(geo, connect, Nn, eps, sig, thickness)
+            if result == "ZZ1":
+                return err
+            values = err_e
+    else:
+        geo = Geometry(elem, coord, connect, "rigi")
+        eps = strain_e_pg(geo, connect, u)
+        isStress = "S" in result and result != "Strain"
+        field = stress_e_pg(C, eps) if isStress else eps
+        res = result if result in ("Strain", "Stress") else result[-2:]
+        values = result_in_field(field, res, coef).mean(1)
+    return reshape_values(values, nodeValues, connect, Nn)
+
+
+def degradation_e_pg(d, N, connect, k_res=1e-12):
+    """g = (1 - N d_e)^2 + k_res -- Models/_phasefield.py:295-317."""
+    d_pg = np.einsum("pn,en->ep", N, np.asarray(d, float)[connect])
+    return (1 - d_pg) ** 2 + k_res
+
+
+def pf_result(elem, coord, connect, u, d, split, lmbda, mu, C, result, thickness=1.0, nodeValues=True,
+              H_old=None, coef=SQRT2, **split_kw):
+    """PhaseField.Result for the strain, stress, damage and psiP results
+    (Simulations/_phasefield.py:682-760): sigma = g(d) cP eps + cM eps at the
+    rigi Gauss points (:868-915), psiP the mean of psi+ at the mass Gauss
+    points, max'ed with the committed History field (:494-530, :706-714)."""
+    Nn = len(coord)
+    dim = ELEM_DIM[elem]
+    if result == "damage":
+        values = np.asarray(d, float)
+    elif result in ("ux", "uy", "uz", "displacement", "displacement_norm"):
+        return elastic_result(elem, coord, connect, u, C, result, thickness, nodeValues, coef)
+    elif result == "psiP":
+        geo = Geometry(elem, coord, connect, "mass")
+        eps = strain_e_pg(geo, connect, u)
+        cP, cM = split_C(eps, split, lmbda, mu, dim, C, **split_kw)
+        psiP, _ = psi_split(eps, cP, cM)
+        if H_old is not None:
+            psiP = np.where(psiP - H_old.reshape(psiP.shape) < 0, H_old.reshape(psiP.shape), psiP)
+        values = psiP.mean(1)
+    else:
+        geo = Geometry(elem, coord, connect, "rigi")
+        eps = strain_e_pg(geo, connect, u)
+        isStress = "S" in result and result != "Strain"
+        if isStress:
+            cP, cM = split_C(eps, split, lmbda, mu, dim, C, **split_kw)
+            g = degradation_e_pg(d, geo.N, connect)
+            sP = np.einsum("epij,epj->epi", cP, eps)
+            sM = np.einsum("epij,epj->epi", cM, eps)
+            field = g[..., None] * sP + sM
+        else:
+            field = eps
+        res = result if result in ("Strain", "Stress") else result[-2:]
+        values = result_in_field(field, res, coef).mean(1)
+    return reshape_values(values, nodeValues, connect, Nn)

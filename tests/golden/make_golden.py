@@ -341,6 +341,95 @@ def pf_state_case(R, name, m, split, regu, out, seed=7):
     print(name, "Kd nnz", Kd.nnz, "Ku nnz", Ku.nnz)
 
 
+ELASTIC_RESULTS = {2: ["ux", "uy", "displacement", "displacement_norm", "Sxx", "Syy", "Sxy", "Exx", "Eyy", "Exy"],
+                   3: ["ux", "uy", "uz", "displacement", "displacement_norm", "Sxx", "Syy", "Szz", "Syz", "Sxz",
+                       "Sxy", "Exx", "Eyy", "Ezz", "Eyz", "Exz", "Exy"]}
+FIELD_RESULTS = ["Svm", "Stress", "Evm", "Strain"]
+
+
+def _smooth_u(m, scale=1e-3):
+    """A displacement field with strains that vary inside each element."""
+    x = m.coord
+    L = max(x[:, 0].max(), 1e-12)
+    u = np.zeros((m.Nn, m.dim))
+    u[:, 0] = scale * (np.sin(2.1 * x[:, 1] / L * 3) + 0.3 * (x[:, 0] / L) ** 2)
+    u[:, 1] = scale * (0.7 * (x[:, 1] / L) ** 2 - 0.4 * x[:, 0] / L + 0.2 * np.cos(3 * x[:, 0] / L))
+    if m.dim == 3:
+        u[:, 2] = scale * (0.5 * x[:, 0] * x[:, 2] / L**2 + 0.1 * np.sin(4 * x[:, 1] / L))
+    return u.ravel()
+
+
+def results_case(R, name, m, E, v, planeStress, thickness, out):
+    """Elastic.Result (Simulations/_elastic.py:229-320) on a prescribed
+    displacement: every strain / stress / energy result at the nodes and on
+    the elements."""
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(m.dim, E=E, v=v, planeStress=planeStress, thickness=thickness)
+    simu = R.Simulations.Elastic(rm, mat)
+    u = _smooth_u(m)
+    simu._Set_solutions(simu.problemType, u)
+    res = dict(mesh_arrays(m), E=np.asarray(E, float), v=v, planeStress=planeStress, thickness=thickness, u=u)
+    names = ELASTIC_RESULTS[m.dim] + FIELD_RESULTS + ["Wdef_e", "ZZ1_e"]
+    for r in names:
+        res[f"{r}_n"] = np.asarray(simu.Result(r, nodeValues=True))
+        res[f"{r}_e"] = np.asarray(simu.Result(r, nodeValues=False))
+    for r in ("Wdef", "ZZ1"):
+        res[r] = float(simu.Result(r))
+    res["names"] = np.array(names)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+    print(name, "Wdef", res["Wdef"], "ZZ1", res["ZZ1"])
+
+
+def pf_results_case(R, name, m, split, regu, out, seed=11):
+    """PhaseField.Result (Simulations/_phasefield.py:682-760) at a prescribed
+    (u, d, committed History) state: the degraded stress results, psiP and the
+    energies."""
+    dim = m.dim
+    rng = np.random.default_rng(seed)
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(dim, E=210000.0, v=0.3, planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, split, regu, 2.7, 0.05)
+    simu = R.Simulations.PhaseField(rm, pfm)
+    u = _smooth_u(m)
+    x = m.coord
+    d = np.clip(0.5 + 0.45 * np.sin(3 * x[:, 0]) * np.cos(2 * x[:, 1]), 0, 1)
+    simu._Set_solutions(simu.ProblemTypes.elastic, u)
+    simu._Set_solutions(simu.ProblemTypes.damage, d)
+    simu.Need_Update()
+    # a committed History field that is above psi+ at part of the Gauss points
+    simu.Get_K_C_M_F("damage")
+    psiP = np.asarray(simu._PhaseField__psiP_e_pg).copy()
+    H_old = psiP * rng.uniform(0.5, 1.5, psiP.shape)
+    from EasyFEA.FEM import FeArray
+    simu._PhaseField__old_psiP_e_pg = FeArray.asfearray(H_old.copy())
+    simu.Need_Update()
+    res = dict(mesh_arrays(m), split=split, regu=regu, E=210000.0, v=0.3, Gc=2.7, l0=0.05, u=u, d=d, H_old=H_old)
+    names = ELASTIC_RESULTS[dim][:2] + ELASTIC_RESULTS[dim][5:] + FIELD_RESULTS + ["damage", "psiP"]
+    for r in names:
+        res[f"{r}_n"] = np.asarray(simu.Result(r, nodeValues=True))
+        res[f"{r}_e"] = np.asarray(simu.Result(r, nodeValues=False))
+    for r in ("Wdef", "Psi_Crack"):
+        res[r] = float(simu.Result(r))
+    res["names"] = np.array(names)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+    print(name, "Wdef", res["Wdef"], "Psi_Crack", res["Psi_Crack"])
+
+
+def _results_cases(R, out):
+    rng = np.random.default_rng(21)
+    results_case(R, "res_quad4", gmesh.Mesh_Quad4_Rect(12.0, 3.0, 8, 3), 210000.0, 0.3, True, 13.0, out)
+    mq = gmesh.Mesh_Quad4_Rect(12.0, 3.0, 7, 3)
+    results_case(R, "res_quad4_hetero", mq, 210000.0 * np.exp(0.3 * rng.standard_normal(mq.Ne)), 0.3, True, 2.0,
+                 out)
+    results_case(R, "res_tri3", gmesh.Mesh_Tri3_Rect(12.0, 3.0, 6, 3), 210000.0, 0.25, False, 1.0, out)
+    results_case(R, "res_quad9", gmesh.Mesh_Quad9_Rect(12.0, 3.0, 4, 2), 210000.0, 0.3, True, 1.0, out)
+    results_case(R, "res_hexa8", gmesh.Mesh_Hexa8_Box(6.0, 2.0, 2.0, 4, 2, 2), 210000.0, 0.3, False, 1.0, out)
+    results_case(R, "res_tetra4", gmesh.Mesh_Tetra4_Box(6.0, 2.0, 2.0, 3, 2, 2), 210000.0, 0.3, False, 1.0, out)
+    pf_results_case(R, "res_pf_tri3_miehe", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 6, 6), "Miehe", "AT2", out)
+    pf_results_case(R, "res_pf_quad4_amor", gmesh.Mesh_Quad4_Rect(1.0, 1.0, 5, 5), "Amor", "AT1", out)
+    pf_results_case(R, "res_pf_hexa8_miehe", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.5, 3, 3, 2), "Miehe", "AT2", out)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
@@ -388,6 +477,7 @@ def main():
         pf_state_case(R, f"pfsys_{m.elemType.value.lower()}_{split.lower()}_{regu.lower()}", m, split, regu, out)
     pf_case(R, "pf_hexa8_miehe_at2", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.25, 6, 6, 1), "Miehe", "AT2", False,
             210000.0, 0.3, 2.7, 0.2, 2, 4e-3, out)
+    _results_cases(R, out)
 
 
 def _el_hexa8_hetero(R, out):
@@ -400,7 +490,7 @@ def _el_hexa8_hetero(R, out):
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
-         "pf_curve_tri3_200x200": pf_curve_case}
+         "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases}
 
 
 if __name__ == "__main__":

@@ -6,10 +6,11 @@ override the seams the reference documents for new simulations
 (``docs/howto/new_simulation.md:92-130``): ``Assembly``
 (``EasyFEA/Simulations/_simu.py:1104-1144``), ``_Solver_Solve_problemType``
 (``_simu.py:1532-1550``) and, for the phase field, ``Solve`` and
-``Get_K_C_M_F`` (``EasyFEA/Simulations/_phasefield.py:248-269, 303-432``).  Everything else -- meshes, materials, boundary
-conditions, results, post-processing -- is the reference's code, so an
-EasyFEA script switches by replacing ``Simulations.Elastic(mesh, mat)`` with
-``GpuElastic(mesh, mat)``.
+``Get_K_C_M_F`` (``EasyFEA/Simulations/_phasefield.py:248-269, 303-432``);
+``Result`` computes the strain, stress and energy results on the device.
+Everything else -- meshes, materials, boundary conditions, the remaining
+results -- is the reference's code, so an EasyFEA script switches by
+replacing ``Simulations.Elastic(mesh, mat)`` with ``GpuElastic(mesh, mat)``.
 
 What runs on the GPU:
 
@@ -37,7 +38,7 @@ What runs on the GPU:
 Materials: isotropic elastic laws (homogeneous or with a per-element Young's
 modulus) and, for the phase field, a homogeneous isotropic material with the
 Bourdin / Amor / Miehe / He splits, AT1 / AT2 and the History / HistoryDamage
-solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9 and HEXA8.  Other
+solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
 models raise ``NotImplementedError`` at construction.
 
 EasyFEA must be importable (it imports gmsh at start-up).
@@ -221,6 +222,26 @@ class GpuElastic(_RefSimulations.Elastic):
         return solutions[0]
 
 
+    def Result(self, result: str, nodeValues: bool = True, iter=None):
+        """Elastic.Result (_elastic.py:229-320) with the strain, stress, von
+        Mises, energy and ZZ1 results computed on the device from the current
+        displacement; the velocity, acceleration and displacement-matrix
+        results are the reference's own."""
+        if iter is not None:
+            self.Set_Iter(iter)
+        eng = self._engine()
+        if result not in _DEVICE_RESULTS or result not in self.Results_Available():
+            return super().Result(result, nodeValues)
+        eng._Set_solutions(eng.problemType, self.displacement)
+        return eng.Result(result, nodeValues)
+
+
+# the results the device computes (the displacement ones stay on the host)
+_DEVICE_RESULTS = frozenset(["Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy", "Exx", "Eyy", "Ezz", "Eyz", "Exz", "Exy",
+                             "Svm", "Stress", "Evm", "Strain", "Wdef", "Wdef_e", "ZZ1", "ZZ1_e", "psiP",
+                             "Psi_Crack"])
+
+
 class GpuPhaseField(_RefSimulations.PhaseField):
     """``EasyFEA.Simulations.PhaseField`` with the staggered scheme on the GPU.
 
@@ -316,7 +337,7 @@ class GpuPhaseField(_RefSimulations.PhaseField):
         self._Set_solutions(pts.damage, d)
         self._gpu_state = (np.array(u, dtype=np.float64), np.array(d, dtype=np.float64))
         # the reference's per-solve record, read by its Save_Iter
-        self._PhaseField__Niter = eng.Niter
+        self._PhaseField__Niter = eng.staggered_iterations
         self._PhaseField__convIter = eng._PhaseField__convIter
         self._PhaseField__timeIter = time.perf_counter() - t0
         self._PhaseField__tolConv = tolConv
@@ -330,6 +351,18 @@ class GpuPhaseField(_RefSimulations.PhaseField):
         self._PhaseField__updatedDamage = False
         self._PhaseField__updatedDisplacement = False
         return u, d, converged
+
+    def Result(self, result: str, nodeValues: bool = True, iter=None):
+        """PhaseField.Result (_phasefield.py:682-760) with the degraded
+        stress, strain, von Mises, psiP and energy results computed on the
+        device from the reference's current u, d and committed history."""
+        if iter is not None:
+            self.Set_Iter(iter)
+        if result not in _DEVICE_RESULTS or result not in self.Results_Available():
+            return super().Result(result, nodeValues)
+        eng = self._engine()
+        self._push_state(eng)
+        return eng.Result(result, nodeValues)
 
     def Get_K_C_M_F(self, problemType=None):
         """The damage system (Kd, Fd) or the degraded stiffness at the current

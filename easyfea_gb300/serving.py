@@ -274,7 +274,7 @@ class PhaseFieldSession:
         simu.add_dirichlet(n["top"], [0.0, k * self.dU], ["x", "y"])
         u, d, conv = simu.Solve(self.tol, self.max_iter, convOption=0)
         simu.Save_Iter()
-        return u, d, simu.Niter
+        return u, d, simu.staggered_iterations
 
 
 def run_elastic(req: ElasticRequest, cache: MeshCache, precision: str, rtol: float = 1e-10, coarse: int = -1):

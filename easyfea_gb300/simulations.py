@@ -84,6 +84,7 @@ class _Simu:
         self.last_solve = None
         self._dmesh: Optional[DeviceMesh] = None
         self._results: list = []
+        self.folder = ""
         model._Add_observer(self)
         self.Bc_Init()
         self.Need_Update()
@@ -291,15 +292,52 @@ class _Simu:
         self.last_solve = info
         return x
 
-    # ---- results -----------------------------------------------------------
+    # ---- iterations (_simu.py:288-471) ---------------------------------------
     def Save_Iter(self, iter: Optional[dict] = None) -> dict:
-        it = {} if iter is None else iter
-        self._results.append(it)
+        """Store one iteration dict, in memory (folder == "") or as
+        ``folder/Results/results{Niter}.pickle``: the reference's
+        single-process layout and keys, so either side reads the other's."""
+        it = {} if iter is None else dict(iter)
+        it["indexMesh"] = 0
+        if self.folder == "":
+            self._results.append(it)
+        else:
+            import os
+            import pickle
+
+            d = os.path.join(self.folder, "Results")
+            os.makedirs(d, exist_ok=True)
+            path = os.path.join(d, f"results{self.Niter}.pickle")
+            with open(path, "wb") as f:
+                pickle.dump(it, f)
+            self._results.append(path)
         return it
 
     @property
+    def Niter(self) -> int:
+        """Number of saved iterations."""
+        return len(self._results)
+
+    def Get_results(self, iter: int = -1) -> dict:
+        """The iteration dict at index ``iter`` (read from its pickle in folder mode)."""
+        iter = int(iter)
+        if iter < 0:
+            iter += self.Niter
+        assert 0 <= iter < self.Niter, f"`iter` must be in [0, {self.Niter})"
+        entry = self._results[iter]
+        if isinstance(entry, str):
+            import pickle
+
+            with open(entry, "rb") as f:
+                return pickle.load(f)
+        return dict(entry)
+
+    def Set_Iter(self, iter: int = -1, resetAll: bool = False) -> dict:
+        raise NotImplementedError
+
+    @property
     def results(self) -> list:
-        return self._results
+        return [self.Get_results(i) for i in range(self.Niter)]
 
     # ---- post-processing on the device (_simu.py:3067-3151) -------------------
     def Results_Available(self) -> list:
@@ -547,6 +585,12 @@ class Elastic(_Simu):
         it["displacement"] = self.displacement
         return super().Save_Iter(it)
 
+    def Set_Iter(self, iter: int = -1, resetAll: bool = False) -> dict:
+        """Restore the displacement of a saved iteration (_elastic.py:178-205)."""
+        results = self.Get_results(iter)
+        self._Set_solutions(self.problemType, results["displacement"])
+        return results
+
     # ---- results (_elastic.py:201-418) ---------------------------------------
     def Results_Available(self) -> list:
         comps = ["x", "y"] if self.dim == 2 else ["x", "y", "z"]
@@ -621,6 +665,7 @@ class PhaseField(_Simu):
         self.__updatedDisplacement = False
         self.__Niter = 0
         self.__convIter = 0.0
+        self.__timeIter = 0.0
         super().__init__(mesh, model, verbosity)
 
     @property
@@ -801,6 +846,9 @@ class PhaseField(_Simu):
         assert 0 < tolConv <= 1, "tolConv must be between 0 and 1."
         assert maxIter > 1, "Must be > 1."
         assert convOption in (0, 1, 2, 3), "convOption must be 0, 1, 2 or 3"
+        import time
+
+        tic = time.perf_counter()
         u, d = self._state()
         old_damage = d.clone()
         Niter = 0
@@ -854,6 +902,7 @@ class PhaseField(_Simu):
             torch.maximum(d, old_damage, out=d)
         self.__Niter = Niter
         self.__convIter = convIter
+        self.__timeIter = time.perf_counter() - tic
         return u.cpu().numpy(), d.cpu().numpy(), converged
 
     def _psi_crack(self) -> float:
@@ -870,13 +919,16 @@ class PhaseField(_Simu):
         return float(torch.dot(self._state()[0], fu))
 
     @property
-    def Niter(self) -> int:
+    def staggered_iterations(self) -> int:
+        """Staggered iterations of the last Solve (the "Niter" of its saved
+        iteration dict)."""
         return self.__Niter
 
     def Save_Iter(self, iter: Optional[dict] = None) -> dict:
         """Commit the History field (_phasefield.py:613-630) and store u, d."""
         it = {} if iter is None else iter
         it["Niter"] = self.__Niter
+        it["timeIter"] = self.__timeIter
         it["convIter"] = self.__convIter
         if self.phaseFieldModel.solver == "History" and self.__psiP is not None:
             if self.__psiP_old is None:
@@ -886,6 +938,19 @@ class PhaseField(_Simu):
         it["displacement"] = self.displacement
         it["damage"] = self.damage
         return super().Save_Iter(it)
+
+    def Set_Iter(self, iter: int = -1, resetAll: bool = False) -> dict:
+        """Restore u and d of a saved iteration (_phasefield.py:632-657); with
+        resetAll the History field restarts from psi+ of that state."""
+        results = self.Get_results(iter)
+        self._Set_solutions("damage", results["damage"])
+        self._Set_solutions("elastic", results["displacement"])
+        if resetAll and self.phaseFieldModel.solver == "History":
+            self.__psiP_old = None
+            self._assemble_damage()
+            self.__psiP_old = self.__psiP.clone()
+            self.__updatedDamage = False
+        return results
 
     def Calc_Reaction(self, dofs=None, problemType=None) -> np.ndarray:
         """Ku[dofs] @ u on the current degraded stiffness (_simu.py:212-260)."""

@@ -65,3 +65,39 @@ def test_unsupported_models_rejected(ref, golden):
     iso = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False)
     with pytest.raises(NotImplementedError):
         R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, "AnisotStress", "AT2", 2.7, 0.01))
+
+
+def test_save_iter_pickles_read_both_ways(ref, golden, tmp_path):
+    """Save_Iter in folder mode writes the reference's single-process layout
+    (Results/results{i}.pickle holding the iteration dict): the library's
+    simulation and the reference read each other's files (no GPU call)."""
+    import pickle
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import simulations as Simulations
+    from easyfea_gb300.mesh import Mesh_Quad4_Rect
+
+    R = ref
+    g = golden("el_quad4")
+    m = Mesh_Quad4_Rect(120.0, 13.0, 24, 4)
+    ours = Simulations.Elastic(m, Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=True, thickness=13.0))
+    ours.folder = str(tmp_path / "ours")
+    ours.Save_Iter()
+    ours.Save_Iter()
+    assert ours.Niter == 2
+    assert sorted(os.listdir(tmp_path / "ours" / "Results")) == ["results0.pickle", "results1.pickle"]
+    theirs = R.Simulations.Elastic(_mesh(R, g), R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=True,
+                                                                            thickness=13.0),
+                                   folder=str(tmp_path / "theirs"))
+    theirs._Set_solutions(theirs.problemType, g["u"])
+    theirs.Save_Iter()
+    with open(tmp_path / "theirs" / "Results" / "results0.pickle", "rb") as f:
+        ref_iter = pickle.load(f)
+    assert set(ref_iter) == set(ours.Get_results(0))
+    # ours reads the reference's file, the reference reads ours
+    ours._results.append(str(tmp_path / "theirs" / "Results" / "results0.pickle"))
+    np.testing.assert_array_equal(ours.Get_results(-1)["displacement"], g["u"])
+    theirs._Simu__list_results.append(str(tmp_path / "ours" / "Results" / "results0.pickle"))
+    theirs._Simu__Niter += 1
+    theirs.Set_Iter(-1)
+    assert np.abs(theirs.displacement).max() == 0.0

@@ -170,3 +170,45 @@ def test_gpu_time_schemes_inside_easyfea(ref, golden, algo):
                 continue
             tol = 1e-8 * (np.abs(b).max() if name == "displacement" else np.abs(b).max() + umax * amp)
             assert np.abs(a - b).max() <= tol, (algo, step, name, np.abs(a - b).max(), tol)
+
+
+@pytest.mark.parametrize("case", ["res_quad4_hetero", "res_hexa8", "res_tetra4"])
+def test_gpu_results_inside_easyfea(ref, golden, case):
+    """The reference's Result() on the GPU subclass: strain, stress, von Mises,
+    energy and ZZ1 results from the device against the reference's own."""
+    g = golden(case)
+    R = ref
+    mesh = ref_mesh(R, g)
+    E = np.asarray(g["E"], float)
+    mat = R.Models.Elastic.Isotropic(mesh.dim, E=float(E) if E.ndim == 0 else E, v=float(g["v"]),
+                                     planeStress=bool(g["planeStress"]), thickness=float(g["thickness"]))
+    simu = R.B.GpuElastic(mesh, mat)
+    simu._Set_solutions(simu.problemType, g["u"])
+    for r in [str(n) for n in g["names"]]:
+        for suffix, nodeValues in (("_n", True), ("_e", False)):
+            got = np.asarray(simu.Result(r, nodeValues=nodeValues))
+            want = g[r + suffix]
+            tol = 1e-10 if r.startswith("ZZ1") else 1e-12
+            assert np.abs(got - want).max() <= tol * np.abs(want).max(), (case, r, suffix)
+    assert abs(simu.Result("ZZ1") - float(g["ZZ1"])) <= 1e-10 * float(g["ZZ1"])
+
+
+def test_gpu_phasefield_results_inside_easyfea(ref, golden):
+    """PhaseField.Result on the GPU subclass at a prescribed (u, d, History) state."""
+    from EasyFEA.FEM import FeArray
+
+    g = golden("res_pf_hexa8_miehe")
+    R = ref
+    mesh = ref_mesh(R, g)
+    mat = R.Models.Elastic.Isotropic(mesh.dim, E=float(g["E"]), v=float(g["v"]), planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, str(g["split"]), str(g["regu"]), float(g["Gc"]), float(g["l0"]))
+    simu = R.B.GpuPhaseField(mesh, pfm)
+    simu._Set_solutions(simu.ProblemTypes.elastic, g["u"])
+    simu._Set_solutions(simu.ProblemTypes.damage, g["d"])
+    simu._PhaseField__old_psiP_e_pg = FeArray.asfearray(np.array(g["H_old"]))
+    for r in [str(n) for n in g["names"]]:
+        for suffix, nodeValues in (("_n", True), ("_e", False)):
+            got = np.asarray(simu.Result(r, nodeValues=nodeValues))
+            want = g[r + suffix]
+            assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max(), (r, suffix)
+    assert abs(simu.Result("Wdef") - float(g["Wdef"])) <= 1e-11 * float(g["Wdef"])

@@ -72,7 +72,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the single-solve and batch measurements")
     p.add_argument("--workload", default="stream",
-                   choices=["stream", "single", "batch", "batch_one_launch", "assembly", "phasefield"],
+                   choices=["stream", "single", "batch", "batch_one_launch", "assembly", "phasefield", "results"],
                    help="stream: the full benchmark; the others: only that measurement, printed as its own "
                         "JSON object (for profiling)")
     return p.parse_args()
@@ -472,6 +472,54 @@ def assembly_roofline(lib, peak=6782.1, reps=3):
                     "achieved_gbs": byts32 / ms32 / 1e6, "hbm_frac_of_measured": byts32 / ms32 / 1e6 / peak}}
 
 
+def results_roofline(lib, peak=6782.1, reps=5):
+    """Post-processing of the 400x40x40 box's displacement on the device:
+    the element kernel (von Mises of the stress, element means) and the node
+    average, timed with CUDA events; compulsory bytes: coordinates and
+    displacement read once, connectivity, the element output written once;
+    for the node average the incidence lists, the gathered element values and
+    the node output."""
+    import torch
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    m = gmesh.Mesh_Hexa8_Box(1000.0, 100.0, 100.0, *C1)
+    simu = Simulations.Elastic(m, Models.Elastic.Isotropic(3, E=210000.0, v=0.3, planeStress=False))
+    rng = np.random.default_rng(SEED)
+    simu._Set_solutions("elastic", 1e-3 * rng.standard_normal(m.Nn * 3))
+    u = simu.u_device
+    dm = simu.dmesh
+    dm.incidence()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    ms_f, vm = timed(lambda: simu._element_fields(u, vm=True)["vm"])
+    ms_n, _ = timed(lambda: dm.node_values(vm[:, 1].contiguous()))
+    ms_svm, _ = timed(lambda: simu.Result_device("Svm"))
+    ms_zz1, _ = timed(lambda: simu._zz1(u))
+    b_f = m.Nn * 3 * 8 * 2 + m.Ne * 8 * 4 + m.Ne * 2 * 8
+    b_n = (m.Nn + 1) * 4 + m.Ne * 8 * 4 + m.Ne * 8 + m.Nn * 8
+    return {"workload": f"HEXA8 box {C1[0]}x{C1[1]}x{C1[2]} ({m.Ne} elements, {m.Nn * 3} DOF), random displacement",
+            "element_kernel": {"kernel": "fields_kernel<HEXA8, rigi> (8 Gauss points: strain, stress, von Mises, "
+                                         "element means)", "ms": ms_f, "algorithmic_bytes": b_f,
+                               "achieved_gbs": b_f / ms_f / 1e6, "hbm_frac_of_measured": b_f / ms_f / 1e6 / peak},
+            "node_average": {"kernel": "node_average_kernel (ascending incidence lists)", "ms": ms_n,
+                             "algorithmic_bytes": b_n, "achieved_gbs": b_n / ms_n / 1e6,
+                             "hbm_frac_of_measured": b_n / ms_n / 1e6 / peak},
+            "Result_Svm_nodes_ms": ms_svm, "Result_ZZ1_ms": ms_zz1}
+
+
 def phasefield_kernels(steps=3):
     """A few load steps of the 80,000-element notched plate (profiling)."""
     from easyfea_gb300 import serving
@@ -606,6 +654,9 @@ def main():
     if args.workload == "phasefield":
         print(json.dumps(phasefield_kernels()), flush=True)
         return
+    if args.workload == "results":
+        print(json.dumps(results_roofline(lib, reps=1)), flush=True)
+        return
     cache = serving.MeshCache()
     offsets, reqs, _ = serving.poisson_stream(args.rate, args.requests, seed=SEED)
     cache.prebuild({r.spec for r in reqs})
@@ -706,6 +757,7 @@ def main():
     if not args.no_extras:
         extras["single_solve"], roof = single_solve(lib, peak)
         extras["assembly"] = assembly_roofline(lib, peak)
+        extras["results"] = results_roofline(lib, peak)
         extras["phasefield"] = phasefield_measure()
         extras["batch"] = batch_measure(args.workers)
     traffic = None

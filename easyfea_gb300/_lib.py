@@ -158,6 +158,24 @@ class Fields(ctypes.Structure):
     ]
 
 
+class PartPlan(ctypes.Structure):
+    """gfea_part_plan: the row-owned assembly's parts and visit lists (device arrays)."""
+
+    _fields_ = [
+        ("version", c_int32),
+        ("n_parts", c_int32),
+        ("max_part_values", c_int32),
+        ("threads", c_int32),
+        ("node_off", c_void_p),
+        ("part_node_ptr", c_void_p),
+        ("part_nodes", c_void_p),
+        ("part_nvals", c_void_p),
+        ("visit_ptr", c_void_p),
+        ("visit_elem", c_void_p),
+        ("visit_mask", c_void_p),
+    ]
+
+
 _LIB = None
 
 # name -> (restype, argtypes); the complete list of exported entry points
@@ -186,6 +204,12 @@ SIGNATURES = {
                                 POINTER(PfParams), c_int, c_void_p, c_void_p]),
     "gfea_pf_split": (c_int, [c_void_p, c_int64, POINTER(PfParams), c_void_p, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
+    "gfea_part_plan_host": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int64, c_void_p, c_int, c_int32,
+                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    POINTER(c_int32), POINTER(c_int64)]),
+    "gfea_part_smem_bytes": (c_size_t, [c_int, c_int, c_int32, c_int]),
+    "gfea_assemble_elastic_parts": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                                            c_double, c_int, c_void_p, POINTER(PartPlan), c_void_p]),
     "gfea_element_fields": (c_int, [c_int, c_void_p, c_void_p, c_int64, c_void_p, POINTER(Fields), c_void_p]),
     "gfea_node_incidence": (c_int, [c_void_p, c_int64, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_size_t,
                                     c_void_p]),

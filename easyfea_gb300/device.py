@@ -42,6 +42,41 @@ class DeviceGroup:
         self.coord = coord_d
 
 
+# values of one part of the row-owned assembly: 76 KiB of shared memory in
+# either value type (two blocks per SM with their scratch)
+PART_VALUES = {_lib.F32: 19456, _lib.F64: 9728}
+
+
+def part_plan_host(coord: np.ndarray, connect: np.ndarray, node_ptr: np.ndarray, dof_n: int, max_values: int):
+    """The row-owned assembly's plan (gfea_part_plan_host) as host arrays:
+    dict of node_off, part_node_ptr, part_nodes, part_nvals, visit_ptr,
+    visit_elem, visit_mask."""
+    coord = np.ascontiguousarray(coord, dtype=np.float64)
+    connect = np.ascontiguousarray(connect, dtype=np.int32)
+    node_ptr = np.ascontiguousarray(node_ptr, dtype=np.int32)
+    Nn = coord.shape[0]
+    Ne, nPe = connect.shape
+    out = {"node_off": np.empty(Nn, np.int32), "part_node_ptr": np.empty(Nn + 1, np.int32),
+           "part_nodes": np.empty(Nn, np.int32), "part_nvals": np.empty(Nn, np.int32),
+           "visit_ptr": np.empty(Nn + 1, np.int32), "visit_elem": np.empty(Ne * nPe, np.int32),
+           "visit_mask": np.empty(Ne * nPe, np.uint32)}
+    n_parts = ctypes.c_int32()
+    n_visits = ctypes.c_int64()
+    h = lambda a: a.ctypes.data  # noqa: E731
+    _lib.check(_lib.load().gfea_part_plan_host(h(coord), h(connect), Ne, nPe, Nn, h(node_ptr), dof_n, int(max_values),
+                                               h(out["node_off"]), h(out["part_node_ptr"]), h(out["part_nodes"]),
+                                               h(out["part_nvals"]), h(out["visit_ptr"]), h(out["visit_elem"]),
+                                               h(out["visit_mask"]), ctypes.byref(n_parts), ctypes.byref(n_visits)),
+               "part plan")
+    P, V = n_parts.value, n_visits.value
+    for k in ("part_node_ptr", "visit_ptr"):
+        out[k] = out[k][:P + 1]
+    out["part_nvals"] = out["part_nvals"][:P]
+    out["visit_elem"] = out["visit_elem"][:V]
+    out["visit_mask"] = out["visit_mask"][:V]
+    return out
+
+
 class DeviceMesh:
     """Mesh arrays on the GPU plus the node graph of the main element group."""
 
@@ -76,6 +111,22 @@ class DeviceMesh:
 
     def nnz(self, dof_n: int) -> int:
         return dof_n * dof_n * self.n_pairs
+
+    def part_plan(self, dof_n: int, value_type: int, max_values: int | None = None, threads: int = 0):
+        """The row-owned assembly's plan on the device (built once per dof_n,
+        value type and part size; ``threads`` per block, 0 for the default):
+        (gfea_part_plan struct, its tensors)."""
+        mv = int(max_values or PART_VALUES[value_type])
+        key = ("parts", dof_n, value_type, mv, threads)
+        if key not in self._patterns:
+            h = part_plan_host(self.mesh.coord, self.mesh.groupElem.connect, self.node_ptr.cpu().numpy(), dof_n, mv)
+            t = {k: torch.as_tensor(v.view(np.int32) if v.dtype == np.uint32 else v, device=_dev())
+                 for k, v in h.items()}
+            plan = _lib.PartPlan(_lib.ABI_VERSION, len(h["part_nvals"]), mv, int(threads), _lib.ptr(t["node_off"]),
+                                 _lib.ptr(t["part_node_ptr"]), _lib.ptr(t["part_nodes"]), _lib.ptr(t["part_nvals"]),
+                                 _lib.ptr(t["visit_ptr"]), _lib.ptr(t["visit_elem"]), _lib.ptr(t["visit_mask"]))
+            self._patterns[key] = (plan, t)
+        return self._patterns[key]
 
     def incidence(self):
         """(inc_ptr, inc_list) int32 device tensors: each node's elements of the

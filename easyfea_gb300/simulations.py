@@ -80,6 +80,9 @@ class _Simu:
         # 0 block-Jacobi only
         self.coarse = -1
         self.coarse_scalar = 0
+        # stiffness assembly schedule: "atomic" (element kernel with global
+        # atomic adds) or "parts" (row-owned parts in shared memory)
+        self.assembly_schedule = "atomic"
         self._workspaces: dict = {}
         self.last_solve = None
         self._dmesh: Optional[DeviceMesh] = None
@@ -509,10 +512,19 @@ class Elastic(_Simu):
         C, per_elem = self._C_device()
         g = dm.main
         factor = self.material.thickness if self.dim == 2 else 1.0
-        _lib.check(_lib.load().gfea_assemble_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
-                                                     _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C),
-                                                     int(per_elem), factor, _lib.F64, _lib.ptr(op.vals64),
-                                                     op.nnz, 0, _lib.stream()), "assemble elastic")
+        if self.assembly_schedule == "parts":
+            import ctypes
+
+            plan, _ = dm.part_plan(self.dim, _lib.F64)
+            _lib.check(_lib.load().gfea_assemble_elastic_parts(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                                               _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C),
+                                                               int(per_elem), factor, _lib.F64, _lib.ptr(op.vals64),
+                                                               ctypes.byref(plan), _lib.stream()), "assemble parts")
+        else:
+            _lib.check(_lib.load().gfea_assemble_elastic(g.code, _lib.ptr(dm.coord), _lib.ptr(g.connect), g.Ne,
+                                                         _lib.ptr(dm.node_ptr), _lib.ptr(dm.rank), _lib.ptr(C),
+                                                         int(per_elem), factor, _lib.F64, _lib.ptr(op.vals64),
+                                                         op.nnz, 0, _lib.stream()), "assemble elastic")
         self.__K = op
         return op
 

@@ -122,6 +122,45 @@ int gfea_assemble_elastic(int elem, const double* coord, const int32_t* connect,
                           int c_per_elem, double factor, int value_type, void* values,
                           int64_t n_values, int accumulate, void* stream);
 
+/* Row-owned assembly: the same K as gfea_assemble_elastic (accumulate = 0)
+ * without global atomics.  The nodes are cut into parts whose CSR rows fit in
+ * shared memory (max_part_values values each, nodes in Morton order of their
+ * coordinates); one thread block per part adds the element blocks of its own
+ * rows in shared memory and writes them once.  The plan is built on the host
+ * once per mesh (and dof_n, and max_part_values):
+ *   node_off[Nn]          offset of the node's rows within its part
+ *   part_node_ptr[P+1], part_nodes[Nn]   the nodes of each part
+ *   part_nvals[P]         values of each part
+ *   visit_ptr[P+1], visit_elem[V], visit_mask[V]   the elements touching each
+ *                         part, with the bitmask of their local nodes it owns
+ * The host arrays must hold Nn, Nn + 1, Nn, Nn, Nn + 1, Ne*nPe and Ne*nPe
+ * entries (upper bounds of P and V); *n_parts_host and *n_visits_host get
+ * the sizes.  gfea_part_smem_bytes gives the dynamic shared memory a block
+ * takes for parts of max_part_values values (at most 200 KiB is accepted). */
+typedef struct gfea_part_plan {
+  int32_t version;          /* GFEA_ABI_VERSION */
+  int32_t n_parts;
+  int32_t max_part_values;  /* the value the plan was built with */
+  int32_t threads;          /* threads per block: a multiple of 32 up to 256; 0: 256 (FP32), 128 (FP64) */
+  const int32_t* node_off;
+  const int32_t* part_node_ptr;
+  const int32_t* part_nodes;
+  const int32_t* part_nvals;
+  const int32_t* visit_ptr;
+  const int32_t* visit_elem;
+  const uint32_t* visit_mask;
+} gfea_part_plan;
+int gfea_part_plan_host(const double* coord_host, const int32_t* connect_host, int64_t n_elems, int nPe,
+                        int64_t n_nodes, const int32_t* node_ptr_host, int dof_n, int32_t max_part_values,
+                        int32_t* node_off_host, int32_t* part_node_ptr_host, int32_t* part_nodes_host,
+                        int32_t* part_nvals_host, int32_t* visit_ptr_host, int32_t* visit_elem_host,
+                        uint32_t* visit_mask_host, int32_t* n_parts_host, int64_t* n_visits_host);
+size_t gfea_part_smem_bytes(int elem, int value_type, int32_t max_part_values, int threads);
+int gfea_assemble_elastic_parts(int elem, const double* coord, const int32_t* connect, int64_t n_elems,
+                                const int32_t* node_ptr, const uint8_t* rank, const double* C,
+                                int c_per_elem, double factor, int value_type, void* values,
+                                const gfea_part_plan* plan, void* stream);
+
 /* M = sum_e sum_pg rho wJ N^T N * factor (mass Gauss points, dof_n components).
  * Replaces Bilinear.UV (EasyFEA/FEM/Operators/Bilinear.py:42-59) as used by
  * EasyFEA/Simulations/_elastic.py:137. */

@@ -16,10 +16,11 @@
 // Models/_phasefield.py:295-317) and psiP the History-max'ed psi+ at the mass
 // Gauss points (_phasefield.py:494-530, :706-714).
 //
-// One lane group of G lanes per element, one lane per node (as the assembly
-// kernels): each lane loads its node's coordinates and displacement, the
-// Gauss-point strain is a group sum, every lane of the group then holds the
-// element's Gauss-point values and lane 0 writes the element's results.
+// One lane group of G lanes per element: lane p stages node p's coordinates
+// and displacement in shared memory, lane g then computes Gauss point g
+// (Jacobian, gradients, strain, stress and its results; FP64, the FP64 work
+// done once per point), the group sums the points' contributions and lane 0
+// writes the element's results.
 
 #include "split.cuh"
 
@@ -59,28 +60,40 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
   constexpr int nPe = E::nPe, D = E::dim, G = NextPow2<nPe>::value, EPW = 32 / G, NS = D == 2 ? 3 : 6;
   using Ref = RefTables<ELEM, MASS>;
   constexpr int nPg = Ref::nPg;
+  constexpr int GPB = 128 / G;                      // lane groups per block
+  constexpr int SC = 2 * nPe * D + nPe + nPe * NS;  // per group: X, u, d, nodal stress
   __shared__ Ref ref;
+  __shared__ double scr[GPB][SC];
   ref.fill();
   __syncthreads();
   const int lane = threadIdx.x % G;
   const int sub = (threadIdx.x & 31) / G;
+  double* sX = scr[threadIdx.x / G];
+  double* sU = sX + nPe * D;
+  double* sD = sU + nPe * D;
+  double* sS = sD + nPe;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const bool node_lane = lane < nPe;
   const bool iso = A.cmode == 3 || A.cmode == 4;
 
   for (int64_t e0 = warp * EPW; e0 < Ne; e0 += nwarp * EPW) {
     const int64_t e = e0 + sub;
     const bool valid = e < Ne;
     const int64_t ec = valid ? e : Ne - 1;
-    const int32_t a = node_lane ? connect[ec * nPe + lane] : 0;
-    double X[D], ul[D];
+    // the element's nodes into the group's scratch
+    if (lane < nPe) {
+      const int32_t a = connect[ec * nPe + lane];
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      X[k] = node_lane ? coord[(int64_t)a * 3 + k] : 0.0;
-      ul[k] = node_lane ? u[(int64_t)a * D + k] : 0.0;
+      for (int k = 0; k < D; ++k) {
+        sX[lane * D + k] = coord[(int64_t)a * 3 + k];
+        sU[lane * D + k] = u[(int64_t)a * D + k];
+      }
+      if (PFM) sD[lane] = A.d[a];
+      if (A.sigma_n)
+#pragma unroll
+        for (int i = 0; i < NS; ++i) sS[lane * NS + i] = A.sigma_n[(int64_t)a * NS + i];
     }
-    const double dl = (PFM && node_lane) ? A.d[a] : 0.0;
+    __syncwarp();
     // the element's elastic law
     double C[NS * NS];
     double lam = 0, mu = 0;
@@ -100,13 +113,43 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
 #pragma unroll
     for (int i = 0; i < NS; ++i) se[i] = ss[i] = 0;
     double vme = 0, vms = 0, W = 0, pp = 0;
-    for (int g = 0; g < nPg; ++g) {
-      double grad[D];
-      const double wJ = lane_geo<ELEM, MASS, G>(ref, g, lane, node_lane, X, grad);
+    // lane g: Gauss point g (and g + G, ...)
+    for (int g = lane; g < nPg; g += G) {
+      double F[D][D];
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          double t = 0;
+#pragma unroll
+          for (int n = 0; n < nPe; ++n) t += ref.dN[g][d][n] * sX[n * D + k];
+          F[d][k] = t;
+        }
+      double iF[D][D];
+      const double det = det_inv<D>(F, iF);
+      const double wJ = fabs(det) * ref.w[g];
       double eps[NS], sig[NS];
-      group_strain<ELEM, G>(grad, ul, node_lane, eps);
+#pragma unroll
+      for (int i = 0; i < NS; ++i) eps[i] = 0;
+#pragma unroll
+      for (int n = 0; n < nPe; ++n) {
+        double gr[D], un[D], en[NS];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          double t = 0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) t += iF[i][d] * ref.dN[g][d][n];
+          gr[i] = t;
+          un[i] = sU[n * D + i];
+        }
+        node_strain<D>(gr, un, en);
+#pragma unroll
+        for (int i = 0; i < NS; ++i) eps[i] += en[i];
+      }
       if constexpr (PFM) {
-        const double dg = group_sum<G, double>(node_lane ? ref.N[g][lane] * dl : 0.0);
+        double dg = 0;
+#pragma unroll
+        for (int n = 0; n < nPe; ++n) dg += ref.N[g][n] * sD[n];
         const double gd = (1 - dg) * (1 - dg) + P.k_res;
         double c[NS * NS];
         split_c<D>(P, eps, gd, c, nullptr, nullptr);
@@ -147,14 +190,18 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
         se[i] += te[i];
         ss[i] += ts[i];
       }
-      vme += von_mises<D>(te);
-      vms += von_mises<D>(ts);
+      if (A.vm_e) {
+        vme += von_mises<D>(te);
+        vms += von_mises<D>(ts);
+      }
       // energy density 1/2 sigma . eps, sigma either C eps or the smoothed nodal stress
       double psi = 0;
       if (A.sigma_n) {
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          const double sn = group_sum<G, double>(node_lane ? ref.N[g][lane] * A.sigma_n[(int64_t)a * NS + i] : 0.0);
+          double sn = 0;
+#pragma unroll
+          for (int n = 0; n < nPe; ++n) sn += ref.N[g][n] * sS[n * NS + i];
           psi += sn * eps[i];
         }
       } else {
@@ -163,6 +210,16 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
       }
       W += A.thickness * wJ * (0.5 * psi);
     }
+    // sums over the Gauss points (each lane holds its own points' share)
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      se[i] = group_sum<G, double>(se[i]);
+      ss[i] = group_sum<G, double>(ss[i]);
+    }
+    vme = group_sum<G, double>(vme);
+    vms = group_sum<G, double>(vms);
+    W = group_sum<G, double>(W);
+    pp = group_sum<G, double>(pp);
     if (valid && lane == 0) {
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
@@ -176,6 +233,7 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
       if (A.energy_e) A.energy_e[e] = W;
       if (A.psiP_e) A.psiP_e[e] = pp / nPg;
     }
+    __syncwarp();  // the scratch is overwritten by the next element
   }
 }
 

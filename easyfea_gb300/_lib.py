@@ -23,7 +23,9 @@ F64 = 0
 F32 = 1
 
 ELEM_CODE = {"SEG2": 0, "TRI3": 1, "QUAD4": 2, "QUAD9": 3, "HEXA8": 4, "TETRA4": 5}
-SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2, "Zhang": 3, "Stress": 4, "He": 5}
+SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2, "Zhang": 3, "Stress": 4, "He": 5, "AnisotStrain": 6,
+              "AnisotStrain_PM": 7, "AnisotStrain_MP": 8, "AnisotStrain_NoCross": 9, "AnisotStress": 10,
+              "AnisotStress_PM": 11, "AnisotStress_MP": 12, "AnisotStress_NoCross": 13}
 REGU_CODE = {"AT1": 0, "AT2": 1}
 
 
@@ -132,6 +134,7 @@ class PfParams(ctypes.Structure):
         ("k_res", c_double),
         ("plane_stress", c_int32),
         ("pad", c_int32),
+        ("S", c_double * 36),
     ]
 
 

@@ -10,7 +10,7 @@ namespace gfea {
 namespace {
 
 
-template <int ELEM>
+template <int ELEM, bool ANI>
 __global__ void __launch_bounds__(128) damage_kernel(const double* __restrict__ coord, const int32_t* __restrict__ connect,
                                                      int64_t Ne, const int32_t* __restrict__ node_ptr,
                                                      const uint8_t* __restrict__ rank, const double* __restrict__ u,
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(128) damage_kernel(const double* __restrict__ 
       const double wJ = lane_geo<ELEM, true, G>(refm, g, lane, node_lane, X, grad);
       double eps[D == 2 ? 3 : 6];
       group_strain<ELEM, G>(grad, ul, node_lane, eps);
-      double psi = psi_plus<D>(P, eps);
+      double psi = psi_plus<D, ANI>(P, eps);
       if (H_old) {
         const double ho = H_old[ec * nPgM + g];
         if (psi - ho < 0) psi = ho;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) damage_kernel(const double* __restrict__ 
   }
 }
 
-template <int ELEM, typename T>
+template <int ELEM, typename T, bool ANI>
 __global__ void __launch_bounds__(128) pf_elastic_kernel(const double* __restrict__ coord,
                                                          const int32_t* __restrict__ connect, int64_t Ne,
                                                          const int32_t* __restrict__ node_ptr,
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(128) pf_elastic_kernel(const double* __restric
       const double dpg = group_sum<G, double>(node_lane ? ref.N[g][lane] * dl : 0.0);
       const double gd = (1 - dpg) * (1 - dpg) + P.k_res;
       double c[NS * NS];
-      split_c<D>(P, eps, gd, c, nullptr, nullptr);
+      split_c<D, ANI>(P, eps, gd, c, nullptr, nullptr);
       // BtC and accumulation as in the elastic kernel (KM B of _group_elem.py:1242-1312)
       double BtC[D][NS];
       if constexpr (D == 2) {
@@ -195,14 +195,14 @@ __global__ void __launch_bounds__(128) pf_elastic_kernel(const double* __restric
   }
 }
 
-template <int D>
+template <int D, bool ANI>
 __global__ void split_kernel(const double* __restrict__ eps, int64_t n, PF P, double* cP, double* cM, double* psiP,
                              double* psiM) {
   constexpr int ns = D == 2 ? 3 : 6;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double e[ns], c[ns * ns], p[ns * ns], m[ns * ns];
     for (int k = 0; k < ns; ++k) e[k] = eps[i * ns + k];
-    split_c<D>(P, e, 1.0, c, p, m);
+    split_c<D, ANI>(P, e, 1.0, c, p, m);
     double sp = 0, sm = 0;
     for (int a = 0; a < ns; ++a) {
       double tp = 0, tm = 0;
@@ -223,7 +223,7 @@ __global__ void split_kernel(const double* __restrict__ eps, int64_t n, PF P, do
 int to_pf(const gfea_pf_params* p, PF* o) {
   if (!p || p->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
   if (p->dim != 2 && p->dim != 3) return GFEA_ERR_ARG;
-  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_HE) return GFEA_ERR_ARG;
+  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_ANISOT_STRESS_NOCROSS) return GFEA_ERR_ARG;
   if (p->regularization != GFEA_AT1 && p->regularization != GFEA_AT2) return GFEA_ERR_ARG;
   o->split = p->split;
   o->plane_stress = p->plane_stress;
@@ -237,6 +237,7 @@ int to_pf(const gfea_pf_params* p, PF* o) {
   o->k_res = p->k_res;
   for (int i = 0; i < 9; ++i) o->A[i] = p->A[i];
   for (int i = 0; i < 36; ++i) o->C[i] = p->C[i];
+  for (int i = 0; i < 36; ++i) o->S[i] = p->S[i];
   return GFEA_OK;
 }
 
@@ -247,7 +248,10 @@ int launch_damage(const double* coord, const int32_t* connect, int64_t Ne, const
   constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
   int blocks = grid_for(ceil_div(Ne, 32 / G) * 32, 128);
   if (blocks > kSMs * 64) blocks = kSMs * 64;
-  damage_kernel<ELEM><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, P, H_old, H_new, Kd, Fd);
+  if (pf_anisot(P.split))
+    damage_kernel<ELEM, true><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, P, H_old, H_new, Kd, Fd);
+  else
+    damage_kernel<ELEM, false><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, P, H_old, H_new, Kd, Fd);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -258,7 +262,10 @@ int launch_pfel(const double* coord, const int32_t* connect, int64_t Ne, const i
   constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
   int blocks = grid_for(ceil_div(Ne, 32 / G) * 32, 128);
   if (blocks > kSMs * 64) blocks = kSMs * 64;
-  pf_elastic_kernel<ELEM, T><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, d, P, vals);
+  if (pf_anisot(P.split))
+    pf_elastic_kernel<ELEM, T, true><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, d, P, vals);
+  else
+    pf_elastic_kernel<ELEM, T, false><<<blocks, 128, 0, s>>>(coord, connect, Ne, node_ptr, rank, u, d, P, vals);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -328,9 +335,11 @@ extern "C" int gfea_pf_split(const double* eps, int64_t n_points, const gfea_pf_
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int blocks = grid_for(n_points, 128);
   if (P.dim == 2)
-    split_kernel<2><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
+    pf_anisot(P.split) ? split_kernel<2, true><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM)
+                       : split_kernel<2, false><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
   else
-    split_kernel<3><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
+    pf_anisot(P.split) ? split_kernel<3, true><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM)
+                       : split_kernel<3, false><<<blocks, 128, 0, s>>>(eps, n_points, P, cP, cM, psiP, psiM);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }

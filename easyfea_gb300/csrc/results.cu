@@ -52,7 +52,7 @@ __device__ __forceinline__ double von_mises(const double* t) {
   }
 }
 
-template <int ELEM, bool MASS, bool PFM>
+template <int ELEM, bool MASS, bool PFM, bool ANI>
 __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ coord,
                                                      const int32_t* __restrict__ connect, int64_t Ne,
                                                      const double* __restrict__ u, FieldArgs A, PF P) {
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
         for (int n = 0; n < nPe; ++n) dg += ref.N[g][n] * sD[n];
         const double gd = (1 - dg) * (1 - dg) + P.k_res;
         double c[NS * NS];
-        split_c<D>(P, eps, gd, c, nullptr, nullptr);
+        split_c<D, ANI>(P, eps, gd, c, nullptr, nullptr);
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
           double t = 0;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(128) fields_kernel(const double* __restrict__ 
           sig[i] = t;
         }
         if (A.psiP_e) {
-          double psi = psi_plus<D>(P, eps);
+          double psi = psi_plus<D, ANI>(P, eps);
           if (A.H_old) {
             const double ho = A.H_old[ec * nPg + g];
             if (psi - ho < 0) psi = ho;
@@ -250,13 +250,13 @@ __global__ void node_average_kernel(const int32_t* __restrict__ inc_ptr, const i
   }
 }
 
-template <int ELEM, bool MASS, bool PFM>
+template <int ELEM, bool MASS, bool PFM, bool ANI>
 int launch_fields(const double* coord, const int32_t* connect, int64_t Ne, const double* u, const FieldArgs& A,
                   const PF& P, cudaStream_t s) {
   constexpr int G = NextPow2<Elem<ELEM>::nPe>::value;
   int blocks = grid_for(ceil_div(Ne, 32 / G) * 32, 128);
   if (blocks > kSMs * 32) blocks = kSMs * 32;
-  fields_kernel<ELEM, MASS, PFM><<<blocks, 128, 0, s>>>(coord, connect, Ne, u, A, P);
+  fields_kernel<ELEM, MASS, PFM, ANI><<<blocks, 128, 0, s>>>(coord, connect, Ne, u, A, P);
   GFEA_LAUNCH_CHECK();
   return GFEA_OK;
 }
@@ -264,17 +264,20 @@ int launch_fields(const double* coord, const int32_t* connect, int64_t Ne, const
 template <int ELEM>
 int dispatch_fields(bool mass, const double* coord, const int32_t* connect, int64_t Ne, const double* u,
                     const FieldArgs& A, const PF& P, cudaStream_t s) {
+  if (A.pf && pf_anisot(P.split))
+    return mass ? launch_fields<ELEM, true, true, true>(coord, connect, Ne, u, A, P, s)
+                : launch_fields<ELEM, false, true, true>(coord, connect, Ne, u, A, P, s);
   if (A.pf)
-    return mass ? launch_fields<ELEM, true, true>(coord, connect, Ne, u, A, P, s)
-                : launch_fields<ELEM, false, true>(coord, connect, Ne, u, A, P, s);
-  return mass ? launch_fields<ELEM, true, false>(coord, connect, Ne, u, A, P, s)
-              : launch_fields<ELEM, false, false>(coord, connect, Ne, u, A, P, s);
+    return mass ? launch_fields<ELEM, true, true, false>(coord, connect, Ne, u, A, P, s)
+                : launch_fields<ELEM, false, true, false>(coord, connect, Ne, u, A, P, s);
+  return mass ? launch_fields<ELEM, true, false, false>(coord, connect, Ne, u, A, P, s)
+              : launch_fields<ELEM, false, false, false>(coord, connect, Ne, u, A, P, s);
 }
 
 int to_pf_params(const gfea_pf_params* p, PF* o) {
   if (!p || p->version != GFEA_ABI_VERSION) return GFEA_ERR_ARG;
   if (p->dim != 2 && p->dim != 3) return GFEA_ERR_ARG;
-  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_HE) return GFEA_ERR_ARG;
+  if (p->split < GFEA_SPLIT_BOURDIN || p->split > GFEA_SPLIT_ANISOT_STRESS_NOCROSS) return GFEA_ERR_ARG;
   o->split = p->split;
   o->plane_stress = p->plane_stress;
   o->regu = p->regularization;
@@ -287,6 +290,7 @@ int to_pf_params(const gfea_pf_params* p, PF* o) {
   o->k_res = p->k_res;
   for (int i = 0; i < 9; ++i) o->A[i] = p->A[i];
   for (int i = 0; i < 36; ++i) o->C[i] = p->C[i];
+  for (int i = 0; i < 36; ++i) o->S[i] = p->S[i];
   return GFEA_OK;
 }
 

@@ -33,11 +33,17 @@ constexpr double kEigTolArg = 1e-12;
 // eigenvalues within kEigTolZero * ||eps|| of zero are zero (Heaviside(0) = 1/2)
 constexpr double kEigTolZero = 1e-12;
 
+// anisotropic splits (compiled into the ANI instantiations only)
+__host__ __device__ inline bool pf_anisot(int split) {
+  return split >= GFEA_SPLIT_ANISOT_STRAIN && split <= GFEA_SPLIT_ANISOT_STRESS_NOCROSS;
+}
+
 struct PF {
   int split, regu, dim, plane_stress;
   double lambda, mu, Gc, l0, thickness, k_res;
   double A[9];
   double C[36];
+  double S[36];
 };
 
 __host__ __device__ __forceinline__ double heav(double v) { return v > 0 ? 1.0 : (v == 0 ? 0.5 : 0.0); }
@@ -208,9 +214,88 @@ __host__ __device__ void spectral_proj(const double* vec, double* projP) {
   }
 }
 
+// Anisotropic splits (Models/_phasefield.py:541-567, 646-676): with the
+// projectors P+- of eps (strain) or of sigma = C eps (stress),
+//   strain: Cab = Pa^T C Pb;   stress: Cab = (Pa C)^T S (Pb C)
+// and cP / cM from the four blocks by variant (full: cP = Cpp + Cpm + Cmp;
+// PM: Cpp + Cpm; MP: Cpp + Cmp; NoCross: Cpp; cM takes the rest).  Compiled
+// only into the kernels instantiated for them (split_c's ANI): its 6x6
+// temporaries would otherwise weigh on the registers of every split.
+template <int D>
+__host__ __device__ __forceinline__ void split_anisot(const PF& P, const double* eps, double gP, double* c, double* cPo,
+                                                   double* cMo) {
+  constexpr int n = D == 2 ? 3 : 6;
+
+    const double* C = P.C;
+    const bool strain = P.split <= GFEA_SPLIT_ANISOT_STRAIN_NOCROSS;
+    const int variant = (P.split - GFEA_SPLIT_ANISOT_STRAIN) % 4;
+    double pp[n * n], ap[n * n], am[n * n], bp[n * n], bm[n * n];
+    if (strain) {
+      spectral_proj<D>(eps, pp);
+      // ap = C P+, am = C P-; blocks Cab = Pa^T (C Pb): bp/bm are P+^T, P-^T
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0;
+          for (int k = 0; k < n; ++k) t += C[i * n + k] * pp[k * n + j];
+          ap[i * n + j] = t;
+          am[i * n + j] = C[i * n + j] - t;
+          bp[i * n + j] = pp[j * n + i];
+          bm[i * n + j] = (i == j ? 1.0 : 0.0) - pp[j * n + i];
+        }
+    } else {
+      double sig[n];
+      for (int i = 0; i < n; ++i) {
+        double t = 0;
+        for (int j = 0; j < n; ++j) t += C[i * n + j] * eps[j];
+        sig[i] = t;
+      }
+      spectral_proj<D>(sig, pp);
+      // Cp = P+ C, Cm = C - Cp; ap = S Cp, am = S Cm; bp = Cp^T, bm = Cm^T
+      double cpm[n * n];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double t = 0;
+          for (int k = 0; k < n; ++k) t += pp[i * n + k] * C[k * n + j];
+          cpm[i * n + j] = t;
+        }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double tp = 0, tm = 0;
+          for (int k = 0; k < n; ++k) {
+            tp += P.S[i * n + k] * cpm[k * n + j];
+            tm += P.S[i * n + k] * (C[k * n + j] - cpm[k * n + j]);
+          }
+          ap[i * n + j] = tp;
+          am[i * n + j] = tm;
+          bp[i * n + j] = cpm[j * n + i];
+          bm[i * n + j] = C[j * n + i] - cpm[j * n + i];
+        }
+    }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double cpp = 0, cpmm = 0, cmp = 0, cmm = 0;  // Cpp, Cpm, Cmp, Cmm
+        for (int k = 0; k < n; ++k) {
+          cpp += bp[i * n + k] * ap[k * n + j];
+          cpmm += bp[i * n + k] * am[k * n + j];
+          cmp += bm[i * n + k] * ap[k * n + j];
+          cmm += bm[i * n + k] * am[k * n + j];
+        }
+        double cp, cm;
+        switch (variant) {
+          case 0: cp = cpp + cpmm + cmp; cm = cmm; break;
+          case 1: cp = cpp + cpmm; cm = cmm + cmp; break;
+          case 2: cp = cpp + cmp; cm = cmm + cpmm; break;
+          default: cp = cpp; cm = cmm + cpmm + cmp; break;
+        }
+        c[i * n + j] = gP * cp + cm;
+        if (cPo) cPo[i * n + j] = cp;
+        if (cMo) cMo[i * n + j] = cm;
+      }
+}
+
 // c = gP * cP + cM  (n x n, row-major); gP = 1 gives cP + cM.
 // With want_parts, cP and cM are also returned separately.
-template <int D>
+template <int D, bool ANI = false>
 __host__ __device__ void split_c(const PF& P, const double* eps, double gP, double* c, double* cPo, double* cMo) {
   constexpr int n = D == 2 ? 3 : 6;
   const double tr = D == 2 ? eps[0] + eps[1] : eps[0] + eps[1] + eps[2];
@@ -234,6 +319,10 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
         if (cPo) cPo[i * n + j] = cp;
         if (cMo) cMo[i * n + j] = cm;
       }
+    return;
+  }
+  if constexpr (ANI) {
+    split_anisot<D>(P, eps, gP, c, cPo, cMo);
     return;
   }
   if (P.split == GFEA_SPLIT_ZHANG || P.split == GFEA_SPLIT_STRESS || P.split == GFEA_SPLIT_HE) {
@@ -363,11 +452,11 @@ __host__ __device__ void split_c(const PF& P, const double* eps, double gP, doub
     }
 }
 
-template <int D>
+template <int D, bool ANI = false>
 __device__ double psi_plus(const PF& P, const double* eps) {
   constexpr int n = D == 2 ? 3 : 6;
   double c[n * n], cP[n * n];
-  split_c<D>(P, eps, 1.0, c, cP, nullptr);
+  split_c<D, ANI>(P, eps, 1.0, c, cP, nullptr);
   double s = 0;
   for (int i = 0; i < n; ++i) {
     double sig = 0;

@@ -36,9 +36,10 @@ What runs on the GPU:
   meaning.
 
 Materials: isotropic elastic laws (homogeneous or with a per-element Young's
-modulus) and, for the phase field, a homogeneous isotropic material with the
-Bourdin / Amor / Miehe / He splits, AT1 / AT2 and the History / HistoryDamage
-solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
+modulus), homogeneous transversely isotropic and anisotropic laws and, for the
+phase field, a homogeneous material with the Bourdin / Amor / Miehe / He
+(isotropic) and AnisotStrain / AnisotStress splits, AT1 / AT2 and the
+History / HistoryDamage solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
 models raise ``NotImplementedError`` at construction.
 
 EasyFEA must be importable (it imports gmsh at start-up).
@@ -83,9 +84,26 @@ def to_gpu_mesh(ref_mesh) -> _gmesh.Mesh:
 
 
 def _gpu_material(mat):
-    """The library's isotropic law for an EasyFEA isotropic material."""
+    """The library's law for an EasyFEA elastic material: isotropic
+    (homogeneous or per-element E), transversely isotropic or anisotropic
+    (homogeneous)."""
+    thickness = float(getattr(mat, "thickness", 1.0))
+    if isinstance(mat, _RefModels.Elastic.TransverselyIsotropic):
+        if np.ndim(mat.El) or np.ndim(mat.Et) or np.ndim(mat.Gl):
+            raise NotImplementedError("the GPU path takes a homogeneous transversely isotropic law")
+        return _ElasticModels.TransverselyIsotropic(mat.dim, float(mat.El), float(mat.Et), float(mat.Gl),
+                                                    float(mat.vl), float(mat.vt), axis_l=mat.axis_l,
+                                                    axis_t=mat.axis_t, planeStress=bool(mat.planeStress),
+                                                    thickness=thickness)
+    if isinstance(mat, _RefModels.Elastic.Anisotropic):
+        C = np.asarray(mat.C, dtype=np.float64)
+        if C.ndim != 2:
+            raise NotImplementedError("the GPU path takes a homogeneous anisotropic law")
+        # the reference's C is already Kelvin-Mandel in x, y, z
+        return _ElasticModels.Anisotropic(mat.dim, C, False, thickness=thickness)
     if not isinstance(mat, _RefModels.Elastic.Isotropic):
-        raise NotImplementedError(f"the GPU path takes isotropic elastic laws, not {type(mat).__name__}")
+        raise NotImplementedError(f"the GPU path takes isotropic, transversely isotropic and anisotropic "
+                                  f"elastic laws, not {type(mat).__name__}")
     E = mat.E
     E = float(E) if np.ndim(E) == 0 else np.asarray(E, dtype=np.float64)
     thickness = float(getattr(mat, "thickness", 1.0))
@@ -262,14 +280,17 @@ class GpuPhaseField(_RefSimulations.PhaseField):
     @staticmethod
     def _gpu_model(pfm):
         mat = pfm.material
-        if not isinstance(mat, _RefModels.Elastic.Isotropic) or np.ndim(mat.E) != 0:
-            raise NotImplementedError("the GPU phase field takes a homogeneous isotropic material")
         split = str(getattr(pfm.split, "value", pfm.split))
         regu = str(getattr(pfm.regularization, "value", pfm.regularization))
         solver = str(getattr(pfm.solver, "value", pfm.solver))
-        if split not in ("Bourdin", "Amor", "Miehe", "He") or regu not in ("AT1", "AT2") or \
-                solver not in ("History", "HistoryDamage"):
-            raise NotImplementedError(f"GPU phase field: split {split}, {regu}, solver {solver}")
+        if isinstance(mat, _RefModels.Elastic.Isotropic):
+            if np.ndim(mat.E) != 0:
+                raise NotImplementedError("the GPU phase field takes a homogeneous material")
+            splits = ("Bourdin", "Amor", "Miehe", "He", "AnisotStrain", "AnisotStress")
+        else:
+            splits = ("Bourdin", "AnisotStrain", "AnisotStress")
+        if split not in splits or regu not in ("AT1", "AT2") or solver not in ("History", "HistoryDamage"):
+            raise NotImplementedError(f"GPU phase field: {type(mat).__name__}, split {split}, {regu}, solver {solver}")
         A = getattr(pfm, "A", None)
         return _PhaseFieldModel(_gpu_material(mat), split, regu, float(pfm.Gc), float(pfm.l0), solver=solver,
                                 A=None if A is None else np.asarray(A, dtype=np.float64))

@@ -657,12 +657,16 @@ class PhaseField(_Simu):
 
     def __init__(self, mesh: Mesh, model: PhaseFieldModel, folder: str = "", verbosity: bool = False):
         assert isinstance(model, PhaseFieldModel), "model must be a phase field model"
-        if model.split in ("Zhang", "Stress"):
+        if model.split in ("Zhang", "Stress") or model.split.endswith(("_PM", "_MP", "_NoCross")):
             # Zhang: c+ = P+(sigma) C is not symmetric; Stress: c+ = C s+ C
             # with s+ = a P+ - b R+ IxI is not positive semi-definite, so the
-            # degraded stiffness g c+ + c- can be indefinite.  The staggered
+            # degraded stiffness g c+ + c- can be indefinite; the PM / MP
+            # anisotropic variants put one cross block (Cpm or Cmp, transposes
+            # of each other) on each side, which is not symmetric, and NoCross
+            # leaves C - (1 - g) Cpp, which can be indefinite.  The staggered
             # loop's PCG needs SPD systems (the reference factorises them with
-            # a direct solver); both splits are available through gfea_pf_split
+            # a direct solver); these splits are available through
+            # gfea_pf_split.  AnisotStrain / AnisotStress give g C + (1 - g) Cmm.
             raise NotImplementedError(f"the {model.split} split does not give an SPD degraded stiffness; the GPU "
                                       "staggered loop solves SPD systems")
         assert model.dim == mesh.dim, "the material and the mesh must have the same dimension"
@@ -781,8 +785,9 @@ class PhaseField(_Simu):
         p.split = _lib.SPLIT_CODE[m.split]
         p.regularization = _lib.REGU_CODE[m.regularization]
         p.dim = self.dim
-        p.lambda_ = float(mat.get_lambda())
-        p.mu = float(mat.get_mu())
+        if isinstance(mat, ElasticModels.Isotropic):
+            p.lambda_ = float(mat.get_lambda())
+            p.mu = float(mat.get_mu())
         p.Gc = m.Gc
         p.l0 = m.l0
         p.thickness = m.thickness if self.dim == 2 else 1.0
@@ -792,6 +797,9 @@ class PhaseField(_Simu):
         C = mat.C.ravel()
         for i in range(C.size):
             p.C[i] = C[i]
+        S = np.asarray(mat.S, dtype=float).ravel()
+        for i in range(S.size):
+            p.S[i] = S[i]
         p.k_res = 1e-12
         p.plane_stress = int(bool(getattr(mat, "planeStress", False)) and self.dim == 2)
         return p

@@ -67,6 +67,14 @@ extern "C" {
 #define GFEA_SPLIT_ZHANG 3
 #define GFEA_SPLIT_STRESS 4
 #define GFEA_SPLIT_HE 5
+#define GFEA_SPLIT_ANISOT_STRAIN 6
+#define GFEA_SPLIT_ANISOT_STRAIN_PM 7
+#define GFEA_SPLIT_ANISOT_STRAIN_MP 8
+#define GFEA_SPLIT_ANISOT_STRAIN_NOCROSS 9
+#define GFEA_SPLIT_ANISOT_STRESS 10
+#define GFEA_SPLIT_ANISOT_STRESS_PM 11
+#define GFEA_SPLIT_ANISOT_STRESS_MP 12
+#define GFEA_SPLIT_ANISOT_STRESS_NOCROSS 13
 #define GFEA_AT1 0
 #define GFEA_AT2 1
 
@@ -215,6 +223,7 @@ typedef struct gfea_pf_params {
   double k_res;          /* residual stiffness of g(d), 1e-12 in the reference */
   int32_t plane_stress;  /* 2D: 1 plane stress, 0 plane strain (the Stress split's compliance) */
   int32_t pad;
+  double S[36];          /* Kelvin-Mandel compliance C^-1 (AnisotStress splits) */
 } gfea_pf_params;
 
 /* Damage system at the current displacement: strain at mass Gauss points,

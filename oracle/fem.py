@@ -766,7 +766,7 @@ def IxI(dim):
     return np.outer(I, I)
 
 
-def split_C(eps, split, lmbda, mu, dim, C=None, robust=False, E=None, v=None, planeStress=False):
+def split_C(eps, split, lmbda, mu, dim, C=None, robust=False, E=None, v=None, planeStress=False, S=None):
     """cP, cM -- Models/_phasefield.py:396-571 (Calc_C, Bourdin :433-449,
     Amor :451-483, Rp/Rm :485-501, Miehe :503-540), and the stress-based
     splits :573-687 (Zhang: projectors of sigma = C eps, cP = P+ C; Stress:
@@ -774,7 +774,11 @@ def split_C(eps, split, lmbda, mu, dim, C=None, robust=False, E=None, v=None, pl
     part) and He :689-749 (projectors of C^1/2 eps mapped back, cP = C P+).
 
     ``lmbda``/``mu`` scalars or (Ne,) arrays; eps (Ne, nPg, 3|6); ``E``,
-    ``v``, ``planeStress``: the isotropic material of the Stress split."""
+    ``v``, ``planeStress``: the isotropic material of the Stress split.
+
+    Anisotropic splits (:541-567, 646-676): P+- of eps (AnisotStrain*) or of
+    sigma = C eps (AnisotStress*, with the compliance ``S``), blocks
+    Cab = Pa^T C Pb or (Pa C)^T S (Pb C), combined by variant."""
     Ne, nPg = eps.shape[:2]
     lm = np.broadcast_to(np.asarray(lmbda, float).reshape(-1, 1) if np.ndim(lmbda) else lmbda, (Ne, nPg))
     mm = np.broadcast_to(np.asarray(mu, float).reshape(-1, 1) if np.ndim(mu) else mu, (Ne, nPg))
@@ -791,6 +795,29 @@ def split_C(eps, split, lmbda, mu, dim, C=None, robust=False, E=None, v=None, pl
         cP = bulk[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * (np.eye(n) - II / dim)
         cM = bulk[..., None, None] * (Rm[..., None, None] * II)
         return cP, cM
+    if split.startswith("Anisot"):
+        Cm = np.asarray(C, float)
+        if split.startswith("AnisotStrain"):
+            projP, projM = spectral_projectors(eps, robust)
+            T = lambda X: np.swapaxes(X, -1, -2)  # noqa: E731
+            Cpp, Cpm = T(projP) @ Cm @ projP, T(projP) @ Cm @ projM
+            Cmp, Cmm = T(projM) @ Cm @ projP, T(projM) @ Cm @ projM
+        else:
+            sig = np.einsum("ij,epj->epi", Cm, eps)
+            projP, projM = spectral_projectors(sig, robust)
+            Cp, Cn = projP @ Cm, projM @ Cm
+            T = lambda X: np.swapaxes(X, -1, -2)  # noqa: E731
+            Sm = np.asarray(S, float)
+            Cpp, Cpm = T(Cp) @ Sm @ Cp, T(Cp) @ Sm @ Cn
+            Cmp, Cmm = T(Cn) @ Sm @ Cp, T(Cn) @ Sm @ Cn
+        variant = split.split("_")[1] if "_" in split else ""
+        if variant == "":
+            return Cpp + Cpm + Cmp, Cmm
+        if variant == "PM":
+            return Cpp + Cpm, Cmm + Cmp
+        if variant == "MP":
+            return Cpp + Cmp, Cmm + Cpm
+        return Cpp, Cmm + Cpm + Cmp
     if split == "Miehe":
         projP, projM = spectral_projectors(eps, robust)
         cP = lm[..., None, None] * (Rp[..., None, None] * II) + 2 * mm[..., None, None] * projP

@@ -77,10 +77,11 @@ def dirichlet(mesh: OracleMesh, conds, dof_n):
     return np.concatenate(dofs), np.concatenate(vals)
 
 
-def elastic_system(mesh: OracleMesh, E, v, planeStress=True, thickness=1.0, rho=1.0):
-    """K, M (CSR) -- _elastic.py:123-152 (K_e, M_e x thickness in 2D) + assembly."""
+def elastic_system(mesh: OracleMesh, E, v, planeStress=True, thickness=1.0, rho=1.0, C=None):
+    """K, M (CSR) -- _elastic.py:123-152 (K_e, M_e x thickness in 2D) + assembly.
+    ``C``: a Kelvin-Mandel law in place of the isotropic (E, v) one."""
     dim = mesh.dim
-    C = fem.isotropic_C(E, v, dim, planeStress)
+    C = fem.isotropic_C(E, v, dim, planeStress) if C is None else np.asarray(C, float)
     geo = fem.Geometry(mesh.elem, mesh.coord, mesh.connect, "rigi")
     K_e = fem.K_elastic_e(geo, C)
     geom = fem.Geometry(mesh.elem, mesh.coord, mesh.connect, "mass")
@@ -95,10 +96,10 @@ def elastic_system(mesh: OracleMesh, E, v, planeStress=True, thickness=1.0, rho=
     return K, M
 
 
-def elastic_solve(mesh: OracleMesh, E, v, planeStress, thickness, dir_conds, loads):
+def elastic_solve(mesh: OracleMesh, E, v, planeStress, thickness, dir_conds, loads, C=None):
     """Simulations.Elastic.Solve() restated: returns (u, K, b)."""
     dim = mesh.dim
-    K, _ = elastic_system(mesh, E, v, planeStress, thickness)
+    K, _ = elastic_system(mesh, E, v, planeStress, thickness, C=C)
     b = neumann(mesh, loads, dim, thickness)
     dk, dv = dirichlet(mesh, dir_conds, dim)
     orphan = fem.dofs_nodes(mesh.orphans, fem.UNKNOWNS[dim], fem.UNKNOWNS[dim])
@@ -111,7 +112,9 @@ class PhaseFieldOracle:
     History solver (psi+ max against the committed field, :494-538, committed in
     Save_Iter :613-630)."""
 
-    def __init__(self, mesh: OracleMesh, E, v, planeStress, thickness, split, regu, Gc, l0, A=None):
+    def __init__(self, mesh: OracleMesh, E, v, planeStress, thickness, split, regu, Gc, l0, A=None, C=None, S=None):
+        """``C``, ``S``: a Kelvin-Mandel law and its compliance in place of the
+        isotropic (E, v) one (the Bourdin and anisotropic splits)."""
         self.mesh = mesh
         self.dim = dim = mesh.dim
         self.E, self.v = E, v
@@ -119,8 +122,9 @@ class PhaseFieldOracle:
         self.thickness = thickness if dim == 2 else 1.0
         self.split, self.regu, self.Gc, self.l0 = split, regu, Gc, l0
         self.A = np.eye(dim) if A is None else np.asarray(A, float)
-        self.lmbda, self.mu = fem.lame(E, v, dim, planeStress)
-        self.C = fem.isotropic_C(E, v, dim, planeStress)
+        self.lmbda, self.mu = fem.lame(E, v, dim, planeStress) if C is None else (0.0, 0.0)
+        self.C = fem.isotropic_C(E, v, dim, planeStress) if C is None else np.asarray(C, float)
+        self.S = None if S is None else np.asarray(S, float)
         self.u = np.zeros(mesh.Nn * dim)
         self.d = np.zeros(mesh.Nn)
         self.H_old = None
@@ -143,7 +147,7 @@ class PhaseFieldOracle:
     def damage_system(self):
         """__Construct_Damage_Matrix, _phasefield.py:540-573."""
         eps = self.strain(self.geo_m)
-        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v,
+        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v, S=self.S,
                               planeStress=self.planeStress)
         psiP, _ = fem.psi_split(eps, cP, cM)
         if self.H_old is not None and self.H_old.shape == psiP.shape:
@@ -163,7 +167,7 @@ class PhaseFieldOracle:
     def elastic_system(self):
         """__Construct_Elastic_Matrix, _phasefield.py:444-482 (g = (1-d)^2 + 1e-12)."""
         eps = self.strain(self.geo_r)
-        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v,
+        cP, cM = fem.split_C(eps, self.split, self.lmbda, self.mu, self.dim, self.C, E=self.E, v=self.v, S=self.S,
                               planeStress=self.planeStress)
         d_e = self.d[self.mesh.connect]
         d_pg = np.einsum("pn,en->ep", self.geo_r.N, d_e)

@@ -69,10 +69,15 @@ def csr_parts(prefix, A):
             f"{prefix}_indptr": A.indptr.astype(np.int64)}
 
 
-def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out):
+def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out, law=None):
+    """``law``: None (isotropic E, v) or a dict of transversely isotropic
+    parameters (El, Et, Gl, vl, vt, axis_l, axis_t)."""
     dim = m.dim
     rm = to_ref_mesh(R, m)
-    mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=thickness)
+    if law is None:
+        mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=thickness)
+    else:
+        mat = R.Models.Elastic.TransverselyIsotropic(dim, **law, planeStress=planeStress, thickness=thickness)
     simu = R.Simulations.Elastic(rm, mat)
     simu.solver = R.SolverType.scipy
     L = m.coord[:, 0].max()
@@ -87,6 +92,8 @@ def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out
     d = dict(mesh_arrays(m), E=np.asarray(E, float), v=v, planeStress=planeStress,
              thickness=thickness, loadval=loadval, loaddir=loaddir, u=u, b=b,
              left=left, right=right)
+    if law is not None:
+        d.update({f"ti_{k}": np.asarray(val, float) for k, val in law.items()}, C=mat.C, S=mat.S)
     d.update(csr_parts("K", K))
     d.update(csr_parts("M", M))
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **d)
@@ -129,10 +136,13 @@ def split_case(R, out, seed=0):
     print("split", len(res))
 
 
-def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, tol=1e-3, maxIter=100):
+def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, tol=1e-3, maxIter=100, law=None):
     dim = m.dim
     rm = to_ref_mesh(R, m)
-    mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=1.0)
+    if law is None:
+        mat = R.Models.Elastic.Isotropic(dim, E=E, v=v, planeStress=planeStress, thickness=1.0)
+    else:
+        mat = R.Models.Elastic.TransverselyIsotropic(dim, **law, planeStress=planeStress, thickness=1.0)
     pfm = R.Models.PhaseField(mat, split, regu, Gc, l0)
     simu = R.Simulations.PhaseField(rm, pfm)
     simu.solver = R.SolverType.scipy
@@ -157,8 +167,9 @@ def pf_case(R, name, m, split, regu, planeStress, E, v, Gc, l0, steps, dU, out, 
         print(name, "step", k, "F", f, "dmax", d.max(), "Niter", its[-1])
     Ku = simu.Get_K_C_M_F("elastic")[0]
     Kd, _, _, Fd = simu.Get_K_C_M_F("damage")
+    extra = {} if law is None else {f"ti_{k}": np.asarray(val, float) for k, val in law.items()}
     res = dict(mesh_arrays(m), split=split, regu=regu, planeStress=planeStress, E=E, v=v,
-               Gc=Gc, l0=l0, dU=dU, tol=tol, maxIter=maxIter,
+               Gc=Gc, l0=l0, dU=dU, tol=tol, maxIter=maxIter, **extra,
                u=np.array(us), d=np.array(ds), H=np.array(Hs), F=np.array(Fs), Niter=np.array(its),
                bottom=bottom, top=top, notch=notch, top_dofs=top_dofs,
                Fd=np.asarray(Fd.todense()).ravel())
@@ -430,6 +441,60 @@ def _results_cases(R, out):
     pf_results_case(R, "res_pf_hexa8_miehe", gmesh.Mesh_Hexa8_Box(1.0, 1.0, 0.5, 3, 3, 2), "Miehe", "AT2", out)
 
 
+# a transversely isotropic law (moduli of a wood-like fibre material), its
+# fibre at 30 degrees in the plane, and a 3D orientation out of the axes
+TI = dict(El=11580.0, Et=500.0, Gl=450.0, vl=0.02, vt=0.44)
+TI_2D = dict(TI, axis_l=(np.cos(np.pi / 6), np.sin(np.pi / 6), 0.0), axis_t=(-np.sin(np.pi / 6), np.cos(np.pi / 6), 0.0))
+TI_3D = dict(TI, axis_l=(1.0, 1.0, 1.0), axis_t=(1.0, -1.0, 0.0))
+ANISOT_SPLITS = ("AnisotStrain", "AnisotStrain_PM", "AnisotStrain_MP", "AnisotStrain_NoCross", "AnisotStress",
+                 "AnisotStress_PM", "AnisotStress_MP", "AnisotStress_NoCross")
+
+
+def anisot_case(R, out, seed=3):
+    """Transversely isotropic and anisotropic laws (Models/Elastic/_laws.py:
+    513-717, 1111-1270): C and S; the anisotropic splits' cP, cM, psi+, psi-
+    (Models/_phasefield.py:541-567, 646-676) on seeded strains."""
+    from EasyFEA.FEM._linalg import FeArray
+    rng = np.random.default_rng(seed)
+    res = {}
+    for dim, ps in ((2, True), (2, False), (3, False)):
+        law = TI_2D if dim == 2 else TI_3D
+        mat = R.Models.Elastic.TransverselyIsotropic(dim, **law, planeStress=ps)
+        key = f"ti_d{dim}_ps{int(ps)}"
+        res[key + "_C"], res[key + "_S"] = mat.C, mat.S
+        n = 3 if dim == 2 else 6
+        eps = rng.standard_normal((48, 1, n)) * 1e-3
+        res[key + "_eps"] = eps
+        for split in ANISOT_SPLITS:
+            pfm = R.Models.PhaseField(mat, split, "AT2", 2.7, 0.01)
+            cP, cM = pfm.Calc_C(FeArray.asfearray(eps.copy()))
+            psiP, psiM = pfm.Calc_psi_e_pg(FeArray.asfearray(eps.copy()))
+            res[f"{key}_{split}_cP"], res[f"{key}_{split}_cM"] = np.asarray(cP), np.asarray(cM)
+            res[f"{key}_{split}_psiP"], res[f"{key}_{split}_psiM"] = np.asarray(psiP), np.asarray(psiM)
+    for dim in (2, 3):
+        n = 3 if dim == 2 else 6
+        A = rng.standard_normal((n, n))
+        Cin = A @ A.T + n * np.eye(n)
+        res[f"an_d{dim}_Cin"] = Cin
+        for voigt in (True, False):
+            mat = R.Models.Elastic.Anisotropic(dim, Cin.copy(), voigt, axis1=(1.0, 2.0, 0.0), axis2=(-2.0, 1.0, 0.0))
+            res[f"an_d{dim}_v{int(voigt)}_C"], res[f"an_d{dim}_v{int(voigt)}_S"] = mat.C, mat.S
+    for k, val in TI.items():
+        res["TI_" + k] = val
+    for k in ("axis_l", "axis_t"):
+        res["TI_2D_" + k] = np.asarray(TI_2D[k])
+        res["TI_3D_" + k] = np.asarray(TI_3D[k])
+    np.savez_compressed(os.path.join(out, "anisot.npz"), **res)
+    print("anisot", len(res))
+    elastic_case(R, "el_quad4_ti", gmesh.Mesh_Quad4_Rect(120.0, 13.0, 24, 4), 0.0, 0.0, True, 13.0, -8 / 13**2,
+                 "y", out, law=TI_2D)
+    elastic_case(R, "el_hexa8_ti", gmesh.Mesh_Hexa8_Box(60.0, 10.0, 10.0, 6, 2, 2), 0.0, 0.0, False, 1.0, -0.05, "z",
+                 out, law=TI_3D)
+    for split in ("AnisotStrain", "AnisotStress"):
+        pf_case(R, f"pf_tri3_ti_{split.lower()}", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16), split, "AT2", False,
+                0.0, 0.0, 2.7, 0.1, 4, 1.6e-2, out, law=TI_2D)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
@@ -490,7 +555,7 @@ def _el_hexa8_hetero(R, out):
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
-         "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases}
+         "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases, "anisot": anisot_case}
 
 
 if __name__ == "__main__":

@@ -58,13 +58,16 @@ def test_subclasses_and_mesh_conversion(ref, golden):
 
 def test_unsupported_models_rejected(ref, golden):
     R = ref
-    mesh = _mesh(R, golden("el_quad4"))
-    mat = R.Models.Elastic.TransverselyIsotropic(2, El=1e5, Et=1e4, Gl=1e4, vl=0.3, vt=0.2)
+    g = golden("el_quad4")
+    mesh = _mesh(R, g)
+    Ne = len(g["connect"])
+    mat = R.Models.Elastic.TransverselyIsotropic(2, El=1e5 * np.ones(Ne), Et=1e4, Gl=1e4, vl=0.3, vt=0.2)
     with pytest.raises(NotImplementedError):
-        R.B.GpuElastic(mesh, mat)
+        R.B.GpuElastic(mesh, mat)  # a per-element transversely isotropic law
     iso = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False)
-    with pytest.raises(NotImplementedError):
-        R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, "AnisotStress", "AT2", 2.7, 0.01))
+    for split in ("Zhang", "AnisotStrain_PM", "AnisotStress_NoCross"):
+        with pytest.raises(NotImplementedError):
+            R.B.GpuPhaseField(mesh, R.Models.PhaseField(iso, split, "AT2", 2.7, 0.01))
 
 
 def test_save_iter_pickles_read_both_ways(ref, golden, tmp_path):

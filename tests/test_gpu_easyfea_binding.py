@@ -212,3 +212,25 @@ def test_gpu_phasefield_results_inside_easyfea(ref, golden):
             want = g[r + suffix]
             assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max(), (r, suffix)
     assert abs(simu.Result("Wdef") - float(g["Wdef"])) <= 1e-11 * float(g["Wdef"])
+
+
+def test_gpu_transversely_isotropic_inside_easyfea(ref, golden):
+    """A transversely isotropic law of EasyFEA's own through GpuElastic."""
+    g = golden("el_quad4_ti")
+    R = ref
+    mesh = ref_mesh(R, g)
+    law = {k: (float(g["ti_" + k]) if g["ti_" + k].ndim == 0 else g["ti_" + k])
+           for k in ("El", "Et", "Gl", "vl", "vt", "axis_l", "axis_t")}
+    mat = R.Models.Elastic.TransverselyIsotropic(2, **law, planeStress=bool(g["planeStress"]),
+                                                 thickness=float(g["thickness"]))
+    simu = R.B.GpuElastic(mesh, mat, rtol=1e-12)
+    L = mesh.coord[:, 0].max()
+    left = mesh.Nodes_Conditions(lambda x, y, z: x == 0)
+    right = mesh.Nodes_Conditions(lambda x, y, z: x == L)
+    simu.add_dirichlet(left, [0.0, 0.0], ["x", "y"])
+    simu.add_surfLoad(right, [float(g["loadval"])], [str(g["loaddir"])])
+    u = simu.Solve()
+    assert simu.last_solve is not None and simu.last_solve.status == 0
+    assert np.abs(u - g["u"]).max() <= 1e-8 * np.abs(g["u"]).max()
+    K = simu.Get_K_C_M_F()[0]
+    assert row_scaled_err(K, csr(g, "K", u.size)) <= 1e-12

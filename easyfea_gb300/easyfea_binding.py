@@ -39,7 +39,7 @@ Materials: isotropic elastic laws (homogeneous or with a per-element Young's
 modulus), homogeneous transversely isotropic and anisotropic laws and, for the
 phase field, a homogeneous material with the Bourdin / Amor / Miehe / He
 (isotropic) and AnisotStrain / AnisotStress splits, AT1 / AT2 and the
-History / HistoryDamage solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
+History / HistoryDamage / BoundConstrain solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
 models raise ``NotImplementedError`` at construction.
 
 EasyFEA must be importable (it imports gmsh at start-up).
@@ -289,7 +289,7 @@ class GpuPhaseField(_RefSimulations.PhaseField):
             splits = ("Bourdin", "Amor", "Miehe", "He", "AnisotStrain", "AnisotStress")
         else:
             splits = ("Bourdin", "AnisotStrain", "AnisotStress")
-        if split not in splits or regu not in ("AT1", "AT2") or solver not in ("History", "HistoryDamage"):
+        if split not in splits or regu not in ("AT1", "AT2") or solver not in ("History", "HistoryDamage", "BoundConstrain"):
             raise NotImplementedError(f"GPU phase field: {type(mat).__name__}, split {split}, {regu}, solver {solver}")
         A = getattr(pfm, "A", None)
         return _PhaseFieldModel(_gpu_material(mat), split, regu, float(pfm.Gc), float(pfm.l0), solver=solver,

@@ -333,6 +333,7 @@ class PhaseField(_Observable):
     class SolverType(str, Enum):
         History = "History"
         HistoryDamage = "HistoryDamage"
+        BoundConstrain = "BoundConstrain"
 
     def __init__(self, material: _Elastic, split: Union[str, SplitType], regularization: Union[str, ReguType],
                  Gc: float, l0: float, solver: Union[str, SolverType] = "History",

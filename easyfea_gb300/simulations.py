@@ -295,6 +295,75 @@ class _Simu:
         self.last_solve = info
         return x
 
+    def _solve_bounded(self, op: CsrOperator, b: torch.Tensor, problemType, lb: torch.Tensor, ub: torch.Tensor,
+                       x0: Optional[torch.Tensor] = None, tol: float = 1e-12, max_outer: int = 100):
+        """min ||A_uu x_u - (b_u - A_uk x_k)|| with lb <= x_u <= ub on the
+        unknown DOFs u, the known ones x_k fixed: the reference's bounded
+        least-squares damage solve (scipy.optimize.lsq_linear on the r1
+        system, Solvers.py:376-383, bounds of _phasefield.py:148-163).
+
+        Projected Newton on the strictly convex cost: the gradient
+        g = A^T (A x - b) (A symmetric) fixes the binding set (at lb with
+        g > 0, at ub with g < 0); the step on the other unknowns solves their
+        least-squares problem by CGLS (two products with A per iteration);
+        the step is projected on the box and halved until the cost decreases
+        (Armijo); the loop ends when the projected gradient is below
+        ``tol`` times its start value."""
+        known, xk = self._dirichlet_state(problemType, b)
+        unk = known == 0
+        zero = torch.zeros_like(b)
+
+        def A_u(v):  # rows and columns of the unknown DOFs
+            return torch.where(unk, op.matvec(torch.where(unk, v, zero)), zero)
+
+        bi = torch.where(unk, b - op.matvec(torch.where(unk, zero, xk)), zero)
+        lo = torch.where(unk, lb, zero)
+        hi = torch.where(unk, ub, zero)
+        x = torch.where(unk, x0 if x0 is not None else zero, zero)
+        x = torch.minimum(torch.maximum(x, lo), hi)
+        g0 = None
+        for _ in range(max_outer):
+            r = A_u(x) - bi
+            g = A_u(r)
+            free = unk & ~(((x <= lo) & (g > 0)) | ((x >= hi) & (g < 0)))
+            pg = float(torch.linalg.norm(torch.where(free, g, zero)))
+            if g0 is None:
+                g0 = max(float(torch.linalg.norm(A_u(bi))), 1e-300)
+            if pg <= tol * g0:
+                break
+            # CGLS on the free unknowns: min ||A_F d + r||
+            d = torch.zeros_like(b)
+            rr = -r
+            sv = torch.where(free, A_u(rr), zero)
+            p = sv.clone()
+            gam = float(sv @ sv)
+            gam0 = gam
+            for _k in range(20 * int(free.sum()) + 10):
+                q = A_u(p)
+                qq = float(q @ q)
+                if qq <= 0:
+                    break
+                a = gam / qq
+                d += a * p
+                rr -= a * q
+                sv = torch.where(free, A_u(rr), zero)
+                gn = float(sv @ sv)
+                if gn <= (1e-14) ** 2 * gam0:
+                    break
+                p = sv + (gn / gam) * p
+                gam = gn
+            f0 = 0.5 * float(r @ r)
+            alpha = 1.0
+            while True:
+                xn = torch.minimum(torch.maximum(x + alpha * d, lo), hi)
+                rn = A_u(xn) - bi
+                fn = 0.5 * float(rn @ rn)
+                if fn <= f0 + 1e-4 * float(g @ (xn - x)) or alpha < 1e-12:
+                    break
+                alpha *= 0.5
+            x = xn
+        return torch.where(unk, x, xk)
+
     # ---- iterations (_simu.py:288-471) ---------------------------------------
     def Save_Iter(self, iter: Optional[dict] = None) -> dict:
         """Store one iteration dict, in memory (folder == "") or as
@@ -886,7 +955,12 @@ class PhaseField(_Simu):
             # damage
             self._assemble_damage()
             bd = self.__Fd + self._neumann_vec("damage")
-            d_new = self._solve_system(self.__Kd, bd, "damage", x0=d)
+            if self.phaseFieldModel.solver == "BoundConstrain":
+                # d_n <= d <= 1 (1 - eps where d_n reached 1), _phasefield.py:148-163
+                lb = torch.where(d >= 1, torch.full_like(d, 1 - np.finfo(float).eps), d)
+                d_new = self._solve_bounded(self.__Kd, bd, "damage", lb, torch.ones_like(d), x0=d)
+            else:
+                d_new = self._solve_system(self.__Kd, bd, "damage", x0=d)
             d.copy_(d_new)
             self.__updatedDisplacement = False
             # displacement

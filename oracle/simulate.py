@@ -107,6 +107,35 @@ def elastic_solve(mesh: OracleMesh, E, v, planeStress, thickness, dir_conds, loa
     return u, K, b
 
 
+def bounded_lsq_exact(A, b, lb, ub, tol=1e-14, max_outer=200):
+    """The minimiser of ||A x - b|| over lb <= x <= ub (A nonsingular, so the
+    cost is strictly convex): projected Newton -- the binding set from the
+    gradient A^T (A x - b), a least-squares step (LSQR) on the other
+    unknowns, projection on the box and step halving until the cost drops --
+    until the projected gradient is below tol times its start value."""
+    import scipy.sparse.linalg as sla
+
+    x = np.clip(np.asarray(lb, float), lb, ub)
+    g0 = max(np.linalg.norm(A.T @ b), 1e-300)
+    for _ in range(max_outer):
+        r = A @ x - b
+        g = A.T @ r
+        free = ~(((x <= lb) & (g > 0)) | ((x >= ub) & (g < 0)))
+        if np.linalg.norm(g[free]) <= tol * g0:
+            break
+        dx = np.zeros_like(x)
+        dx[free] = sla.lsqr(A[:, free], -r, atol=1e-15, btol=1e-15, iter_lim=100000)[0]
+        f0, a = 0.5 * r @ r, 1.0
+        while True:
+            xn = np.clip(x + a * dx, lb, ub)
+            rn = A @ xn - b
+            if 0.5 * rn @ rn <= f0 + 1e-4 * g @ (xn - x) or a < 1e-12:
+                break
+            a *= 0.5
+        x = xn
+    return x
+
+
 class PhaseFieldOracle:
     """Staggered phase-field scheme (Simulations/_phasefield.py:303-432) with the
     History solver (psi+ max against the committed field, :494-538, committed in
@@ -129,6 +158,11 @@ class PhaseFieldOracle:
         self.d = np.zeros(mesh.Nn)
         self.H_old = None
         self.psiP = None
+        self.solver = "History"  # History, HistoryDamage or BoundConstrain (_phasefield.py:105-110)
+        # BoundConstrain: "lsq_linear" (the reference's scipy call, which stops
+        # at a 1e-10 relative change of the cost: about 1e-5 from the
+        # minimiser where bounds are active) or "exact" (the minimiser itself)
+        self.bounded_solver = "lsq_linear"
         self.geo_r = fem.Geometry(mesh.elem, mesh.coord, mesh.connect, "rigi")
         self.geo_m = fem.Geometry(mesh.elem, mesh.coord, mesh.connect, "mass")
         self.map_u = fem.csr_map(mesh.connect, dim, mesh.Nn * dim)
@@ -199,7 +233,22 @@ class PhaseFieldOracle:
     def solve_damage(self):
         Kd, Fd = self._kd(), self.Fd
         dk, dv = dirichlet(self.mesh, self.dir_d, 1)
-        self.d = fem.solve_r1(Kd, Fd, dk, dv)
+        if self.solver == "BoundConstrain":
+            # scipy.optimize.lsq_linear on the r1 system with d_n <= d <= 1
+            # (Solvers.py:376-383, _phasefield.py:148-163; the reference takes
+            # these full-length bounds, so its damage problem has no Dirichlet DOF)
+            from scipy import optimize
+
+            assert len(dk) == 0, "bounded damage solve without damage Dirichlet conditions"
+            lb = self.d.copy()
+            lb[lb >= 1] = 1 - np.finfo(float).eps
+            ub = np.ones(lb.shape)
+            if self.bounded_solver == "lsq_linear":
+                self.d = optimize.lsq_linear(Kd.tocsr(), Fd, bounds=(lb, ub), tol=1e-10, method="trf", verbose=0)["x"]
+            else:
+                self.d = bounded_lsq_exact(Kd.tocsr(), Fd, lb, ub)
+        else:
+            self.d = fem.solve_r1(Kd, Fd, dk, dv)
         return self.d
 
     def solve_elastic(self):
@@ -223,6 +272,7 @@ class PhaseFieldOracle:
         """Staggered loop, _phasefield.py:303-432 (no external forces: the work
         of f_u in convOption 2 is zero)."""
         assert convOption in (0, 1, 2, 3)
+        old_damage = self.d.copy()
         Niter = 0
         converged = False
         convIter = 0.0
@@ -258,12 +308,15 @@ class PhaseFieldOracle:
                 converged = (convD <= tolConv) and (convU <= tolConv * 0.999)
             else:
                 converged = convIter <= tolConv
+        if self.solver == "HistoryDamage":  # _phasefield.py:412-416
+            self.d = np.maximum(self.d, old_damage)
         self.Niter = Niter
         self.convIter = convIter
         return self.u, self.d, converged
 
     def save_iter(self):
-        self.H_old = self.psiP
+        if self.solver == "History":
+            self.H_old = self.psiP
 
     def reaction(self, dofs):
         """Calc_Reaction, _simu.py:212-260: Ku[dofs] @ u."""

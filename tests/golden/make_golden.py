@@ -495,6 +495,48 @@ def anisot_case(R, out, seed=3):
                 0.0, 0.0, 2.7, 0.1, 4, 1.6e-2, out, law=TI_2D)
 
 
+def pf_solver_case(R, name, m, solver, steps, dU, out, tol=1e-3, maxIter=100):
+    """The staggered loop with the HistoryDamage or BoundConstrain
+    irreversibility solver (Simulations/_phasefield.py:148-163, 409-419;
+    BoundConstrain solves the damage by scipy.optimize.lsq_linear with
+    d_n <= d <= 1): the 16x16 TRI3 plate pulled at the top, no notch (the
+    reference's bounds are full length, so no damage Dirichlet condition)."""
+    rm = to_ref_mesh(R, m)
+    mat = R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=False, thickness=1.0)
+    pfm = R.Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.1, solver=getattr(R.Models.PhaseField.SolverType, solver))
+    simu = R.Simulations.PhaseField(rm, pfm)
+    simu.solver = R.SolverType.scipy
+    H = m.coord[:, 1].max()
+    bottom = rm.Nodes_Conditions(lambda x, y, z: y == 0)
+    top = rm.Nodes_Conditions(lambda x, y, z: y == H)
+    top_dofs = simu.Bc_dofs_nodes(top, ["y"])
+    us, ds, Fs, its = [], [], [], []
+    for k in range(1, steps + 1):
+        simu.Bc_Init()
+        simu.add_dirichlet(bottom, [0.0, 0.0], ["x", "y"])
+        simu.add_dirichlet(top, [0.0, k * dU], ["x", "y"])
+        u, d, conv = simu.Solve(tol, maxIter, convOption=0)
+        simu.Save_Iter()
+        f = np.sum(simu.Calc_Reaction(top_dofs, simu.ProblemTypes.elastic))
+        us.append(u.copy()); ds.append(d.copy()); Fs.append(f)
+        its.append(simu._PhaseField__Niter)
+        print(name, "step", k, "F", f, "dmax", d.max(), "Niter", its[-1])
+    res = dict(mesh_arrays(m), split="Miehe", regu="AT2", solver=solver, planeStress=False, E=210000.0, v=0.3,
+               Gc=2.7, l0=0.1, dU=dU, tol=tol, maxIter=maxIter, u=np.array(us), d=np.array(ds), F=np.array(Fs),
+               Niter=np.array(its), bottom=bottom, top=top, top_dofs=top_dofs)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+
+
+def _pf_solver_cases(R, out):
+    pf_solver_case(R, "pf_tri3_boundconstrain", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16), "BoundConstrain", 4, 4e-3,
+                   out)
+    # HistoryDamage: load steps small enough that the crack grows over several
+    # steps (a larger step breaks the plate within one step in dozens of
+    # staggered iterations, a path that rounding can change)
+    pf_solver_case(R, "pf_tri3_historydamage", gmesh.Mesh_Tri3_Rect(1.0, 1.0, 16, 16), "HistoryDamage", 6,
+                   1.5e-3, out)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
@@ -555,7 +597,8 @@ def _el_hexa8_hetero(R, out):
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
-         "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases, "anisot": anisot_case}
+         "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases, "anisot": anisot_case,
+         "pf_solvers": _pf_solver_cases}
 
 
 if __name__ == "__main__":

@@ -206,3 +206,25 @@ def test_robust_split_differs_from_reference_only_at_degenerate_points(golden):
         for r in expected:
             w = np.linalg.eigvalsh(fem.vec_to_mat(eps[r, 0]))
             assert min(np.min(np.abs(np.diff(w))), np.min(np.abs(w))) < 1e-12 * np.abs(w).max()
+
+
+@pytest.mark.parametrize("solver", ["BoundConstrain", "HistoryDamage"])
+def test_phasefield_oracle_solvers_match_reference(golden, solver):
+    """The HistoryDamage and BoundConstrain irreversibility solvers
+    (Simulations/_phasefield.py:148-163, 409-419) on the un-notched plate."""
+    g = golden(f"pf_tri3_{solver.lower()}")
+    m = om(g)
+    pf = PhaseFieldOracle(m, float(g["E"]), float(g["v"]), False, 1.0, "Miehe", "AT2", float(g["Gc"]), float(g["l0"]))
+    pf.solver = solver
+    for k in range(1, g["u"].shape[0] + 1):
+        pf.dir_u = [(g["bottom"], [0.0, 0.0], ["x", "y"]), (g["top"], [0.0, k * float(g["dU"])], ["x", "y"])]
+        u, d, conv = pf.solve(float(g["tol"]), int(g["maxIter"]), 0)
+        pf.save_iter()
+        F = np.sum(pf.reaction(g["top_dofs"]))
+        assert pf.Niter == g["Niter"][k - 1], (k, pf.Niter, g["Niter"][k - 1])
+        assert abs(F - g["F"][k - 1]) <= 1e-6 * abs(g["F"][k - 1]), (k, F, g["F"][k - 1])
+        # the step that breaks the plate (25 staggered iterations, d past 1
+        # without the bounds): the same iterations and force, the damage at
+        # the crack within 1e-3 (the path through those iterations amplifies
+        # rounding); 1e-6 elsewhere
+        assert np.max(np.abs(d - g["d"][k - 1])) <= (1e-6 if g["Niter"][k - 1] < 20 else 1e-3), k

@@ -580,6 +580,9 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
     GFEA_ELASTIC_CASE(GFEA_QUAD9)
     GFEA_ELASTIC_CASE(GFEA_HEXA8)
     GFEA_ELASTIC_CASE(GFEA_TETRA4)
+    GFEA_ELASTIC_CASE(GFEA_TRI6)
+    GFEA_ELASTIC_CASE(GFEA_QUAD8)
+    GFEA_ELASTIC_CASE(GFEA_TETRA10)
     default: return GFEA_ERR_ARG;
   }
 #undef GFEA_ELASTIC_CASE
@@ -587,9 +590,9 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
 
 int elem_dim(int elem) {
   switch (elem) {
-    case GFEA_SEG2: return 1;
-    case GFEA_HEXA8: case GFEA_TETRA4: return 3;
-    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: return 2;
+    case GFEA_SEG2: case GFEA_SEG3: return 1;
+    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: return 3;
+    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: case GFEA_TRI6: case GFEA_QUAD8: return 2;
     default: return -1;
   }
 }
@@ -659,6 +662,9 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_TETRA4: return launch_mass<GFEA_TETRA4, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TRI6: return launch_mass<GFEA_TRI6, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD8: return launch_mass<GFEA_QUAD8, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TETRA10: return launch_mass<GFEA_TETRA10, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   } else if (value_type == GFEA_F32) {
@@ -669,6 +675,9 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_QUAD9: return launch_mass<GFEA_QUAD9, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_HEXA8: return launch_mass<GFEA_HEXA8, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_TETRA4: return launch_mass<GFEA_TETRA4, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TRI6: return launch_mass<GFEA_TRI6, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_QUAD8: return launch_mass<GFEA_QUAD8, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_TETRA10: return launch_mass<GFEA_TETRA10, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   }
@@ -704,6 +713,12 @@ extern "C" int gfea_surface_load(int belem, const double* coord, const int32_t* 
     case GFEA_TRI3:
       surface_load_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
       break;
+    case GFEA_SEG3:
+      surface_load_kernel<GFEA_SEG3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    case GFEA_TRI6:
+      surface_load_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
     default:
       return GFEA_ERR_ARG;
   }
@@ -728,6 +743,14 @@ extern "C" int gfea_boundary_gauss_points(int belem, const double* coord, const 
     case GFEA_TRI3:
       *npg_host = RefTables<GFEA_TRI3, true>::nPg;
       if (n_belems) boundary_gauss_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_SEG3:
+      *npg_host = RefTables<GFEA_SEG3, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_SEG3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_TRI6:
+      *npg_host = RefTables<GFEA_TRI6, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
       break;
     default:
       return GFEA_ERR_ARG;
@@ -757,6 +780,14 @@ extern "C" int gfea_surface_load_field(int belem, const double* coord, const int
     case GFEA_TRI3:
       surface_load_field_kernel<GFEA_TRI3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
                                                                    unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_SEG3:
+      surface_load_field_kernel<GFEA_SEG3><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                           unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_TRI6:
+      surface_load_field_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                           unknown_idx, mode, values, factor, b);
       break;
     default:
       return GFEA_ERR_ARG;

@@ -230,6 +230,148 @@ template <> struct Elem<GFEA_TETRA4> {
   }
 };
 
+// Quadratic elements (EasyFEA/FEM/Elems/_seg.py SEG3, _tri.py TRI6, _quad.py
+// QUAD8, _tetra.py TETRA10; Gauss rules of EasyFEA/FEM/_gauss.py:55-108 and
+// :364-480: SEG3 1 / 3 points, TRI6 3 / 6, QUAD8 4 / 9, TETRA10 4 / 4).
+template <> struct Elem<GFEA_SEG3> {
+  static constexpr int nPe = 3, dim = 1, nPg_rigi = 1, nPg_mass = 3;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (!mass) { xi[0] = 0.0; *w = 2.0; return; }
+    const double a = sqrt(3.0 / 5.0);
+    xi[0] = g == 0 ? -a : (g == 1 ? 0.0 : a);
+    *w = g == 1 ? 8.0 / 9 : 5.0 / 9;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0];
+    return n == 0 ? r * (r - 1) / 2 : (n == 1 ? r * (r + 1) / 2 : -(r - 1) * (r + 1));
+  }
+  __device__ static double dN(const double* p, int, int n) {
+    const double r = p[0];
+    return n == 0 ? r - 0.5 : (n == 1 ? r + 0.5 : -2 * r);
+  }
+};
+
+template <> struct Elem<GFEA_TRI6> {
+  static constexpr int nPe = 6, dim = 2, nPg_rigi = 3, nPg_mass = 6;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (!mass) {
+      const double xs[3] = {1.0 / 6, 2.0 / 3, 1.0 / 6};
+      const double ys[3] = {1.0 / 6, 1.0 / 6, 2.0 / 3};
+      xi[0] = xs[g]; xi[1] = ys[g]; *w = 1.0 / 6;
+      return;
+    }
+    // literals of EasyFEA/FEM/_gauss.py:71-74
+    const double a = 0.445948490915965, b = 0.091576213509771;
+    const double p1 = 0.11169079483905, p2 = 0.0549758718227661;
+    const double xs[6] = {b, 1 - 2 * b, b, a, a, 1 - 2 * a};
+    const double ys[6] = {b, b, 1 - 2 * b, 1 - 2 * a, a, a};
+    xi[0] = xs[g]; xi[1] = ys[g]; *w = g < 3 ? p2 : p1;
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1];
+    switch (n) {
+      case 0: return (r + s - 1) * (2 * r + 2 * s - 1);
+      case 1: return r * (2 * r - 1);
+      case 2: return s * (2 * s - 1);
+      case 3: return -4 * r * (r + s - 1);
+      case 4: return 4 * r * s;
+      default: return -4 * s * (r + s - 1);
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1];
+    switch (n) {
+      case 0: return 4 * r + 4 * s - 3;
+      case 1: return d == 0 ? 4 * r - 1 : 0.0;
+      case 2: return d == 0 ? 0.0 : 4 * s - 1;
+      case 3: return d == 0 ? -8 * r - 4 * s + 4 : -4 * r;
+      case 4: return d == 0 ? 4 * s : 4 * r;
+      default: return d == 0 ? -4 * s : -4 * r - 8 * s + 4;
+    }
+  }
+};
+
+template <> struct Elem<GFEA_QUAD8> {
+  static constexpr int nPe = 8, dim = 2, nPg_rigi = 4, nPg_mass = 9;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) {
+    if (mass) { Elem<GFEA_QUAD9>::gauss(true, g, xi, w); return; }
+    Elem<GFEA_QUAD4>::gauss(false, g, xi, w);
+  }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1];
+    switch (n) {
+      case 0: return -(r - 1) * (s - 1) * (r + s + 1) / 4;
+      case 1: return -(r + 1) * (s - 1) * (r - s - 1) / 4;
+      case 2: return (r + 1) * (s + 1) * (r + s - 1) / 4;
+      case 3: return (r - 1) * (s + 1) * (r - s + 1) / 4;
+      case 4: return (r - 1) * (r + 1) * (s - 1) / 2;
+      case 5: return -(r + 1) * (s - 1) * (s + 1) / 2;
+      case 6: return -(r - 1) * (r + 1) * (s + 1) / 2;
+      default: return (r - 1) * (s - 1) * (s + 1) / 2;
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1];
+    if (d == 0) {
+      switch (n) {
+        case 0: return -(r - 1) * (s - 1) / 4 - (s - 1) * (r + s + 1) / 4;
+        case 1: return -(r + 1) * (s - 1) / 4 - (s - 1) * (r - s - 1) / 4;
+        case 2: return (r + 1) * (s + 1) / 4 + (s + 1) * (r + s - 1) / 4;
+        case 3: return (r - 1) * (s + 1) / 4 + (s + 1) * (r - s + 1) / 4;
+        case 4: return (r - 1) * (s - 1) / 2 + (r + 1) * (s - 1) / 2;
+        case 5: return -(s - 1) * (s + 1) / 2;
+        case 6: return -(r - 1) * (s + 1) / 2 - (r + 1) * (s + 1) / 2;
+        default: return (s - 1) * (s + 1) / 2;
+      }
+    }
+    switch (n) {
+      case 0: return -(r - 1) * (s - 1) / 4 - (r - 1) * (r + s + 1) / 4;
+      case 1: return (r + 1) * (s - 1) / 4 - (r + 1) * (r - s - 1) / 4;
+      case 2: return (r + 1) * (s + 1) / 4 + (r + 1) * (r + s - 1) / 4;
+      case 3: return -(r - 1) * (s + 1) / 4 + (r - 1) * (r - s + 1) / 4;
+      case 4: return (r - 1) * (r + 1) / 2;
+      case 5: return -(r + 1) * (s - 1) / 2 - (r + 1) * (s + 1) / 2;
+      case 6: return -(r - 1) * (r + 1) / 2;
+      default: return (r - 1) * (s - 1) / 2 + (r - 1) * (s + 1) / 2;
+    }
+  }
+};
+
+template <> struct Elem<GFEA_TETRA10> {
+  static constexpr int nPe = 10, dim = 3, nPg_rigi = 4, nPg_mass = 4;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { Elem<GFEA_TETRA4>::gauss(true, g, xi, w); }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1], t = p[2];
+    switch (n) {
+      case 0: return (r + s + t - 1) * (2 * r + 2 * s + 2 * t - 1);
+      case 1: return r * (2 * r - 1);
+      case 2: return s * (2 * s - 1);
+      case 3: return t * (2 * t - 1);
+      case 4: return -4 * r * (r + s + t - 1);
+      case 5: return 4 * r * s;
+      case 6: return -4 * s * (r + s + t - 1);
+      case 7: return -4 * t * (r + s + t - 1);
+      case 8: return 4 * s * t;
+      default: return 4 * r * t;
+    }
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double r = p[0], s = p[1], t = p[2];
+    switch (n) {
+      case 0: return 4 * r + 4 * s + 4 * t - 3;
+      case 1: return d == 0 ? 4 * r - 1 : 0.0;
+      case 2: return d == 1 ? 4 * s - 1 : 0.0;
+      case 3: return d == 2 ? 4 * t - 1 : 0.0;
+      case 4: return d == 0 ? -8 * r - 4 * s - 4 * t + 4 : -4 * r;
+      case 5: return d == 0 ? 4 * s : (d == 1 ? 4 * r : 0.0);
+      case 6: return d == 1 ? -4 * r - 8 * s - 4 * t + 4 : -4 * s;
+      case 7: return d == 2 ? -4 * r - 4 * s - 8 * t + 4 : -4 * t;
+      case 8: return d == 0 ? 0.0 : (d == 1 ? 4 * t : 4 * s);
+      default: return d == 0 ? 4 * t : (d == 1 ? 0.0 : 4 * r);
+    }
+  }
+};
+
 // Shared-memory reference tables of one element type and Gauss family.
 template <int ELEM, bool MASS>
 struct RefTables {

@@ -439,6 +439,9 @@ int dispatch_parts(int elem, const double* coord, const int32_t* connect, const 
     case GFEA_QUAD9: return launch_parts<GFEA_QUAD9, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     case GFEA_HEXA8: return launch_parts<GFEA_HEXA8, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     case GFEA_TETRA4: return launch_parts<GFEA_TETRA4, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
+    case GFEA_TRI6: return launch_parts<GFEA_TRI6, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
+    case GFEA_QUAD8: return launch_parts<GFEA_QUAD8, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
+    case GFEA_TETRA10: return launch_parts<GFEA_TETRA10, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     default: return GFEA_ERR_ARG;
   }
 }
@@ -471,6 +474,9 @@ extern "C" size_t gfea_part_smem_bytes(int elem, int value_type, int32_t max_par
     GFEA_PART_SMEM(GFEA_QUAD9)
     GFEA_PART_SMEM(GFEA_HEXA8)
     GFEA_PART_SMEM(GFEA_TETRA4)
+    GFEA_PART_SMEM(GFEA_TRI6)
+    GFEA_PART_SMEM(GFEA_QUAD8)
+    GFEA_PART_SMEM(GFEA_TETRA10)
 #undef GFEA_PART_SMEM
     default: return 0;
   }

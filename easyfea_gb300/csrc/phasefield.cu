@@ -290,6 +290,9 @@ extern "C" int gfea_pf_damage(int elem, const double* coord, const int32_t* conn
     case GFEA_QUAD9: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD9>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     case GFEA_HEXA8: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_HEXA8>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     case GFEA_TETRA4: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_TETRA4>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_TRI6: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_TRI6>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_QUAD8: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD8>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
+    case GFEA_TETRA10: if (P.dim != 3) return GFEA_ERR_ARG; return launch_damage<GFEA_TETRA10>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     default: return GFEA_ERR_ARG;
   }
 }
@@ -310,6 +313,9 @@ extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* con
       case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_TETRA4: return launch_pfel<GFEA_TETRA4, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TRI6: return launch_pfel<GFEA_TRI6, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD8: return launch_pfel<GFEA_QUAD8, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TETRA10: return launch_pfel<GFEA_TETRA10, double>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       default: return GFEA_ERR_ARG;
     }
   } else if (value_type == GFEA_F32) {
@@ -320,6 +326,9 @@ extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* con
       case GFEA_QUAD9: return launch_pfel<GFEA_QUAD9, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_HEXA8: return launch_pfel<GFEA_HEXA8, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       case GFEA_TETRA4: return launch_pfel<GFEA_TETRA4, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TRI6: return launch_pfel<GFEA_TRI6, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_QUAD8: return launch_pfel<GFEA_QUAD8, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
+      case GFEA_TETRA10: return launch_pfel<GFEA_TETRA10, float>(coord, connect, n_elems, node_ptr, rank, u, d, P, v, s);
       default: return GFEA_ERR_ARG;
     }
   }

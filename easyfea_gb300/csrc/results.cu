@@ -321,8 +321,8 @@ extern "C" int gfea_element_fields(int elem, const double* coord, const int32_t*
   A.psiP_e = f->psiP_e;
   int dim = 0;
   switch (elem) {
-    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: dim = 2; break;
-    case GFEA_HEXA8: case GFEA_TETRA4: dim = 3; break;
+    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: case GFEA_TRI6: case GFEA_QUAD8: dim = 2; break;
+    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: dim = 3; break;
     default: return GFEA_ERR_ARG;
   }
   if (A.pf) {
@@ -338,6 +338,9 @@ extern "C" int gfea_element_fields(int elem, const double* coord, const int32_t*
     case GFEA_QUAD4: return dispatch_fields<GFEA_QUAD4>(mass, coord, connect, n_elems, u, A, P, s);
     case GFEA_QUAD9: return dispatch_fields<GFEA_QUAD9>(mass, coord, connect, n_elems, u, A, P, s);
     case GFEA_HEXA8: return dispatch_fields<GFEA_HEXA8>(mass, coord, connect, n_elems, u, A, P, s);
+    case GFEA_TRI6: return dispatch_fields<GFEA_TRI6>(mass, coord, connect, n_elems, u, A, P, s);
+    case GFEA_QUAD8: return dispatch_fields<GFEA_QUAD8>(mass, coord, connect, n_elems, u, A, P, s);
+    case GFEA_TETRA10: return dispatch_fields<GFEA_TETRA10>(mass, coord, connect, n_elems, u, A, P, s);
     default: return dispatch_fields<GFEA_TETRA4>(mass, coord, connect, n_elems, u, A, P, s);
   }
 }

@@ -33,6 +33,10 @@ class ElemType(str, Enum):
     QUAD9 = "QUAD9"
     HEXA8 = "HEXA8"
     TETRA4 = "TETRA4"
+    SEG3 = "SEG3"
+    TRI6 = "TRI6"
+    QUAD8 = "QUAD8"
+    TETRA10 = "TETRA10"
 
 
 class MatrixType(str, Enum):
@@ -50,6 +54,10 @@ ELEM_INFO = {
     ElemType.QUAD9: (9, 2, 3),
     ElemType.HEXA8: (8, 3, 4),
     ElemType.TETRA4: (4, 3, 5),
+    ElemType.TRI6: (6, 2, 6),
+    ElemType.QUAD8: (8, 2, 7),
+    ElemType.TETRA10: (10, 3, 8),
+    ElemType.SEG3: (3, 1, 9),
 }
 
 # Gauss points per (element, matrixType), as chosen by
@@ -68,6 +76,14 @@ NPG = {
     (ElemType.HEXA8, MatrixType.mass): 8,
     (ElemType.TETRA4, MatrixType.rigi): 1,
     (ElemType.TETRA4, MatrixType.mass): 4,
+    (ElemType.SEG3, MatrixType.rigi): 1,
+    (ElemType.SEG3, MatrixType.mass): 3,
+    (ElemType.TRI6, MatrixType.rigi): 3,
+    (ElemType.TRI6, MatrixType.mass): 6,
+    (ElemType.QUAD8, MatrixType.rigi): 4,
+    (ElemType.QUAD8, MatrixType.mass): 9,
+    (ElemType.TETRA10, MatrixType.rigi): 4,
+    (ElemType.TETRA10, MatrixType.mass): 4,
 }
 
 
@@ -384,6 +400,49 @@ def Mesh_Tetra4_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) 
     return Mesh(groups)
 
 
+def _quadratic(m: Mesh, elem: ElemType, edges, belem: ElemType, bedges) -> Mesh:
+    """The quadratic version of a linear mesh: one node at the middle of
+    every edge, appended after the vertices; ``edges`` / ``bedges`` list the
+    local vertex pairs whose middle nodes follow the vertices, in the
+    reference's node order (EasyFEA/FEM/Elems: TRI6 01 12 20; QUAD8 01 12 23
+    30; TETRA10 01 12 20 03 23 13; SEG3 01; boundary TRI6 as TRI6)."""
+    coord = m.coord
+    lin = m.groupElem.connect
+    blin = m.Get_list_groupElem(m.dim - 1)[0].connect
+    pairs = np.concatenate([np.sort(lin[:, list(e)], axis=1) for e in edges] +
+                           [np.sort(blin[:, list(e)], axis=1) for e in bedges])
+    uniq, inv = np.unique(pairs, axis=0, return_inverse=True)
+    inv = inv.ravel()
+    Nn = len(coord)
+    mids = (coord[uniq[:, 0]] + coord[uniq[:, 1]]) / 2
+    coord2 = np.concatenate([coord, mids])
+    n_e = len(lin) * len(edges)
+    emid = (Nn + inv[:n_e]).reshape(len(edges), -1).T
+    bmid = (Nn + inv[n_e:]).reshape(len(bedges), -1).T
+    groups = {
+        belem: GroupElem(belem, np.concatenate([blin, bmid], axis=1), coord2),
+        elem: GroupElem(elem, np.concatenate([lin, emid], axis=1), coord2),
+    }
+    return Mesh(groups)
+
+
+def Mesh_Tri6_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised TRI6 mesh (the TRI3 mesh with mid-edge nodes) with SEG3 boundary edges."""
+    return _quadratic(Mesh_Tri3_Rect(L, h, nx, ny), ElemType.TRI6, [(0, 1), (1, 2), (2, 0)], ElemType.SEG3, [(0, 1)])
+
+
+def Mesh_Quad8_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised QUAD8 mesh (the QUAD4 mesh with mid-edge nodes) with SEG3 boundary edges."""
+    return _quadratic(Mesh_Quad4_Rect(L, h, nx, ny), ElemType.QUAD8, [(0, 1), (1, 2), (2, 3), (3, 0)], ElemType.SEG3,
+                      [(0, 1)])
+
+
+def Mesh_Tetra10_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised TETRA10 mesh (the TETRA4 mesh with mid-edge nodes) with TRI6 boundary faces."""
+    return _quadratic(Mesh_Tetra4_Box(Lx, Ly, Lz, nx, ny, nz), ElemType.TETRA10,
+                      [(0, 1), (1, 2), (2, 0), (0, 3), (2, 3), (1, 3)], ElemType.TRI6, [(0, 1), (1, 2), (2, 0)])
+
+
 def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
     elemType = ElemType(elemType)
     if elemType == ElemType.QUAD4:
@@ -392,4 +451,8 @@ def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
         return Mesh_Tri3_Rect(L, h, nx, ny)
     if elemType == ElemType.QUAD9:
         return Mesh_Quad9_Rect(L, h, nx, ny)
+    if elemType == ElemType.TRI6:
+        return Mesh_Tri6_Rect(L, h, nx, ny)
+    if elemType == ElemType.QUAD8:
+        return Mesh_Quad8_Rect(L, h, nx, ny)
     raise NotImplementedError(elemType)

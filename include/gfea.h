@@ -55,6 +55,10 @@ extern "C" {
 #define GFEA_QUAD9 3
 #define GFEA_HEXA8 4
 #define GFEA_TETRA4 5
+#define GFEA_TRI6 6
+#define GFEA_QUAD8 7
+#define GFEA_TETRA10 8
+#define GFEA_SEG3 9
 
 /* value types */
 #define GFEA_F64 0

@@ -57,6 +57,22 @@ def gauss(elem: str, matrixType: str):
         y = [-a, -a, a, a, -a, -a, a, a]
         z = [-a, a, -a, a, -a, a, -a, a]
         return np.array([x, y, z]).T, np.ones(8)
+    if elem == "SEG3":  # Gauss-Legendre, rigi 1 / mass 3 (_gauss.py:384-394)
+        n = 1 if matrixType == "rigi" else 3
+        x, w = np.polynomial.legendre.leggauss(n)
+        return x.reshape(-1, 1), w
+    if elem == "TRI6":  # rigi 3 / mass 6 (_gauss.py:64-79, :431-438)
+        if matrixType == "rigi":
+            return gauss("TRI3", "mass")
+        a, b = 0.445948490915965, 0.091576213509771
+        p1, p2 = 0.11169079483905, 0.0549758718227661
+        xi = [b, 1 - 2 * b, b, a, a, 1 - 2 * a]
+        eta = [b, b, 1 - 2 * b, 1 - 2 * a, a, a]
+        return np.array([xi, eta]).T, np.array([p2, p2, p2, p1, p1, p1])
+    if elem == "QUAD8":  # rigi 4 / mass 9 (_gauss.py:452-459)
+        return gauss("QUAD4" if matrixType == "rigi" else "QUAD9", matrixType)
+    if elem == "TETRA10":  # 4 points for both (_gauss.py:470-472)
+        return gauss("TETRA4", "mass")
     if elem == "TETRA4":  # _gauss.py:142-163 (rigi 1 point, mass 4)
         if matrixType == "rigi":
             return np.array([[1 / 4, 1 / 4, 1 / 4]]), np.array([1 / 6])
@@ -102,6 +118,24 @@ def shape_N(elem: str, p: np.ndarray) -> np.ndarray:
     if elem == "TETRA4":  # Elems/_tetra.py TETRA4._N
         r, s, t = p
         return np.array([-r - s - t + 1, r, s, t])
+    if elem == "SEG3":  # Elems/_seg.py SEG3._N
+        (r,) = p
+        return np.array([r * (r - 1) / 2, r * (r + 1) / 2, -(r - 1) * (r + 1)])
+    if elem == "TRI6":  # Elems/_tri.py TRI6._N
+        r, s = p
+        return np.array([(r + s - 1) * (2 * r + 2 * s - 1), r * (2 * r - 1), s * (2 * s - 1), -4 * r * (r + s - 1),
+                         4 * r * s, -4 * s * (r + s - 1)])
+    if elem == "QUAD8":  # Elems/_quad.py QUAD8._N
+        r, s = p
+        return np.array([-(r - 1) * (s - 1) * (r + s + 1) / 4, -(r + 1) * (s - 1) * (r - s - 1) / 4,
+                         (r + 1) * (s + 1) * (r + s - 1) / 4, (r - 1) * (s + 1) * (r - s + 1) / 4,
+                         (r - 1) * (r + 1) * (s - 1) / 2, -(r + 1) * (s - 1) * (s + 1) / 2,
+                         -(r - 1) * (r + 1) * (s + 1) / 2, (r - 1) * (s - 1) * (s + 1) / 2])
+    if elem == "TETRA10":  # Elems/_tetra.py TETRA10._N
+        r, s, t = p
+        return np.array([(r + s + t - 1) * (2 * r + 2 * s + 2 * t - 1), r * (2 * r - 1), s * (2 * s - 1),
+                         t * (2 * t - 1), -4 * r * (r + s + t - 1), 4 * r * s, -4 * s * (r + s + t - 1),
+                         -4 * t * (r + s + t - 1), 4 * s * t, 4 * r * t])
     raise NotImplementedError(elem)
 
 
@@ -153,10 +187,36 @@ def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
         ])
     if elem == "TETRA4":  # Elems/_tetra.py TETRA4._dN
         return np.array([[-1.0, 1.0, 0.0, 0.0], [-1.0, 0.0, 1.0, 0.0], [-1.0, 0.0, 0.0, 1.0]])
+    if elem == "SEG3":  # Elems/_seg.py SEG3._dN
+        (r,) = p
+        return np.array([[r - 1 / 2, r + 1 / 2, -2 * r]])
+    if elem == "TRI6":  # Elems/_tri.py TRI6._dN
+        r, s = p
+        return np.array([[4 * r + 4 * s - 3, 4 * r - 1, 0.0, -8 * r - 4 * s + 4, 4 * s, -4 * s],
+                         [4 * r + 4 * s - 3, 0.0, 4 * s - 1, -4 * r, 4 * r, -4 * r - 8 * s + 4]])
+    if elem == "QUAD8":  # Elems/_quad.py QUAD8._dN
+        r, s = p
+        return np.array([
+            [-(r - 1) * (s - 1) / 4 - (s - 1) * (r + s + 1) / 4, -(r + 1) * (s - 1) / 4 - (s - 1) * (r - s - 1) / 4,
+             (r + 1) * (s + 1) / 4 + (s + 1) * (r + s - 1) / 4, (r - 1) * (s + 1) / 4 + (s + 1) * (r - s + 1) / 4,
+             (r - 1) * (s - 1) / 2 + (r + 1) * (s - 1) / 2, -(s - 1) * (s + 1) / 2,
+             -(r - 1) * (s + 1) / 2 - (r + 1) * (s + 1) / 2, (s - 1) * (s + 1) / 2],
+            [-(r - 1) * (s - 1) / 4 - (r - 1) * (r + s + 1) / 4, (r + 1) * (s - 1) / 4 - (r + 1) * (r - s - 1) / 4,
+             (r + 1) * (s + 1) / 4 + (r + 1) * (r + s - 1) / 4, -(r - 1) * (s + 1) / 4 + (r - 1) * (r - s + 1) / 4,
+             (r - 1) * (r + 1) / 2, -(r + 1) * (s - 1) / 2 - (r + 1) * (s + 1) / 2, -(r - 1) * (r + 1) / 2,
+             (r - 1) * (s - 1) / 2 + (r - 1) * (s + 1) / 2]])
+    if elem == "TETRA10":  # Elems/_tetra.py TETRA10._dN
+        r, s, t = p
+        a = 4 * r + 4 * s + 4 * t - 3
+        return np.array([
+            [a, 4 * r - 1, 0, 0, -8 * r - 4 * s - 4 * t + 4, 4 * s, -4 * s, -4 * t, 0, 4 * t],
+            [a, 0, 4 * s - 1, 0, -4 * r, 4 * r, -4 * r - 8 * s - 4 * t + 4, -4 * t, 4 * t, 0],
+            [a, 0, 0, 4 * t - 1, -4 * r, 0, -4 * s, -4 * r - 4 * s - 8 * t + 4, 4 * s, 4 * r]], dtype=float)
     raise NotImplementedError(elem)
 
 
-ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3, "TETRA4": 3}
+ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3, "TETRA4": 3, "SEG3": 1, "TRI6": 2,
+            "QUAD8": 2, "TETRA10": 3}
 
 
 def N_pg(elem, matrixType):

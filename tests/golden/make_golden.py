@@ -537,6 +537,23 @@ def _pf_solver_cases(R, out):
                    1.5e-3, out)
 
 
+def _quadratic_cases(R, out):
+    """TRI6 / QUAD8 (SEG3 edges) and TETRA10 (TRI6 faces): elastic cantilevers,
+    phase-field systems at a prescribed state and the post-processing
+    results."""
+    elastic_case(R, "el_tri6", gmesh.Mesh_Tri6_Rect(120.0, 13.0, 12, 3), 210000.0, 0.25, False, 1.0, -10.0, "y",
+                 out)
+    elastic_case(R, "el_quad8", gmesh.Mesh_Quad8_Rect(120.0, 13.0, 12, 3), 210000.0, 0.3, True, 13.0,
+                 -800 / 13**2, "y", out)
+    elastic_case(R, "el_tetra10", gmesh.Mesh_Tetra10_Box(60.0, 10.0, 10.0, 4, 2, 2), 210000.0, 0.3, False, 1.0,
+                 -1.0, "z", out)
+    pf_state_case(R, "pfsys_tri6_miehe_at2", gmesh.Mesh_Tri6_Rect(1.0, 1.0, 6, 6), "Miehe", "AT2", out)
+    pf_state_case(R, "pfsys_quad8_amor_at1", gmesh.Mesh_Quad8_Rect(1.0, 1.0, 5, 5), "Amor", "AT1", out)
+    pf_state_case(R, "pfsys_tetra10_miehe_at2", gmesh.Mesh_Tetra10_Box(1.0, 1.0, 0.5, 2, 2, 1), "Miehe", "AT2", out)
+    results_case(R, "res_quad8", gmesh.Mesh_Quad8_Rect(12.0, 3.0, 6, 2), 210000.0, 0.3, True, 13.0, out)
+    results_case(R, "res_tetra10", gmesh.Mesh_Tetra10_Box(6.0, 2.0, 2.0, 3, 1, 1), 210000.0, 0.3, False, 1.0, out)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
@@ -598,7 +615,7 @@ def _el_hexa8_hetero(R, out):
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
          "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases, "anisot": anisot_case,
-         "pf_solvers": _pf_solver_cases}
+         "pf_solvers": _pf_solver_cases, "quadratic": _quadratic_cases}
 
 
 if __name__ == "__main__":

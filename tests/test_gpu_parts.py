@@ -18,7 +18,8 @@ def meshes():
 
     return {"TRI3": gmesh.Mesh_Tri3_Rect(1.0, 1.0, 30, 30), "QUAD4": gmesh.Mesh_Quad4_Rect(12.0, 3.0, 60, 20),
             "QUAD9": gmesh.Mesh_Quad9_Rect(6.0, 2.0, 20, 8), "HEXA8": gmesh.Mesh_Hexa8_Box(4.0, 1.0, 1.0, 20, 6, 6),
-            "TETRA4": gmesh.Mesh_Tetra4_Box(3.0, 1.0, 1.0, 8, 4, 4)}
+            "TETRA4": gmesh.Mesh_Tetra4_Box(3.0, 1.0, 1.0, 8, 4, 4), "TRI6": gmesh.Mesh_Tri6_Rect(1.0, 1.0, 20, 20),
+            "QUAD8": gmesh.Mesh_Quad8_Rect(6.0, 2.0, 24, 8), "TETRA10": gmesh.Mesh_Tetra10_Box(2.0, 1.0, 1.0, 4, 2, 2)}
 
 
 def law(mode, dim, Ne, rng):
@@ -37,7 +38,7 @@ def law(mode, dim, Ne, rng):
     return np.concatenate([[lmbda, mu], f])
 
 
-@pytest.mark.parametrize("elem", ["TRI3", "QUAD4", "QUAD9", "HEXA8", "TETRA4"])
+@pytest.mark.parametrize("elem", ["TRI3", "QUAD4", "QUAD9", "HEXA8", "TETRA4", "TRI6", "QUAD8", "TETRA10"])
 @pytest.mark.parametrize("vt", ["f64", "f32"])
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
 def test_parts_match_atomic_kernel(elem, vt, mode):
@@ -76,7 +77,7 @@ def test_parts_match_atomic_kernel(elem, vt, mode):
     assert err.max() <= (1e-13 if vt == "f64" else 2e-5), err.max()
 
 
-@pytest.mark.parametrize("case", ["el_hexa8", "el_tetra4", "el_quad4_hetero"])
+@pytest.mark.parametrize("case", ["el_hexa8", "el_tetra4", "el_quad4_hetero", "el_tetra10", "el_quad8"])
 def test_parts_assembly_matches_reference(golden, case):
     """Elastic.Assembly with the row-owned schedule: K within 1e-12 of the
     reference's (row-scaled), as the atomic schedule."""

@@ -7,12 +7,13 @@ import pytest
 
 from oracle import fem
 
-ELASTIC = ["res_quad4", "res_quad4_hetero", "res_tri3", "res_quad9", "res_hexa8", "res_tetra4"]
+ELASTIC = ["res_quad4", "res_quad4_hetero", "res_tri3", "res_quad9", "res_hexa8", "res_tetra4", "res_quad8",
+           "res_tetra10"]
 PHASEFIELD = ["res_pf_tri3_miehe", "res_pf_quad4_amor", "res_pf_hexa8_miehe"]
 
 
 def elastic_C(g):
-    dim = 2 if str(g["elem"]) in ("TRI3", "QUAD4", "QUAD9") else 3
+    dim = fem.ELEM_DIM[str(g["elem"])]
     return fem.isotropic_C(g["E"], float(g["v"]), dim, bool(g["planeStress"])), dim
 
 

@@ -583,6 +583,8 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
     GFEA_ELASTIC_CASE(GFEA_TRI6)
     GFEA_ELASTIC_CASE(GFEA_QUAD8)
     GFEA_ELASTIC_CASE(GFEA_TETRA10)
+    GFEA_ELASTIC_CASE(GFEA_HEXA20)
+    GFEA_ELASTIC_CASE(GFEA_HEXA27)
     default: return GFEA_ERR_ARG;
   }
 #undef GFEA_ELASTIC_CASE
@@ -591,7 +593,7 @@ int dispatch_elastic(int elem, bool tune, const double* coord, const int32_t* co
 int elem_dim(int elem) {
   switch (elem) {
     case GFEA_SEG2: case GFEA_SEG3: return 1;
-    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: return 3;
+    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: case GFEA_HEXA20: case GFEA_HEXA27: return 3;
     case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: case GFEA_TRI6: case GFEA_QUAD8: return 2;
     default: return -1;
   }
@@ -665,6 +667,8 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_TRI6: return launch_mass<GFEA_TRI6, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_QUAD8: return launch_mass<GFEA_QUAD8, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_TETRA10: return launch_mass<GFEA_TETRA10, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA20: return launch_mass<GFEA_HEXA20, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA27: return launch_mass<GFEA_HEXA27, double, double>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   } else if (value_type == GFEA_F32) {
@@ -678,6 +682,8 @@ extern "C" int gfea_assemble_mass(int elem, const double* coord, const int32_t* 
       case GFEA_TRI6: return launch_mass<GFEA_TRI6, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_QUAD8: return launch_mass<GFEA_QUAD8, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       case GFEA_TETRA10: return launch_mass<GFEA_TETRA10, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA20: return launch_mass<GFEA_HEXA20, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
+      case GFEA_HEXA27: return launch_mass<GFEA_HEXA27, float, float>(coord, connect, n_elems, node_ptr, rank, dof_n, rho, factor, v, s);
       default: return GFEA_ERR_ARG;
     }
   }
@@ -719,6 +725,12 @@ extern "C" int gfea_surface_load(int belem, const double* coord, const int32_t* 
     case GFEA_TRI6:
       surface_load_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
       break;
+    case GFEA_QUAD8:
+      surface_load_kernel<GFEA_QUAD8><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
+    case GFEA_QUAD9:
+      surface_load_kernel<GFEA_QUAD9><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n, n_unknowns, uidx, uval, factor, b);
+      break;
     default:
       return GFEA_ERR_ARG;
   }
@@ -751,6 +763,14 @@ extern "C" int gfea_boundary_gauss_points(int belem, const double* coord, const 
     case GFEA_TRI6:
       *npg_host = RefTables<GFEA_TRI6, true>::nPg;
       if (n_belems) boundary_gauss_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_QUAD8:
+      *npg_host = RefTables<GFEA_QUAD8, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_QUAD8><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
+      break;
+    case GFEA_QUAD9:
+      *npg_host = RefTables<GFEA_QUAD9, true>::nPg;
+      if (n_belems) boundary_gauss_kernel<GFEA_QUAD9><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, xyz);
       break;
     default:
       return GFEA_ERR_ARG;
@@ -787,6 +807,14 @@ extern "C" int gfea_surface_load_field(int belem, const double* coord, const int
       break;
     case GFEA_TRI6:
       surface_load_field_kernel<GFEA_TRI6><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                           unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_QUAD8:
+      surface_load_field_kernel<GFEA_QUAD8><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
+                                                           unknown_idx, mode, values, factor, b);
+      break;
+    case GFEA_QUAD9:
+      surface_load_field_kernel<GFEA_QUAD9><<<blocks, 128, 0, s>>>(coord, bconnect, n_belems, node_mask, dof_n,
                                                            unknown_idx, mode, values, factor, b);
       break;
     default:

@@ -372,6 +372,70 @@ template <> struct Elem<GFEA_TETRA10> {
   }
 };
 
+// Quadratic hexahedra (EasyFEA/FEM/Elems/_hexa.py HEXA20, HEXA27): the
+// reference's node order, given by each node's local coordinates (corners,
+// then edge middles, then -- HEXA27 -- face centres and the centre); 27
+// Gauss points for both families (_gauss.py:216-261: a = sqrt(3/5), x
+// slowest, weights 5/9 and 8/9 per axis).  Shape functions: HEXA20 the
+// serendipity ones, corner (1+r ri)(1+s si)(1+t ti)(r ri+s si+t ti-2)/8 and
+// edge (1-r^2)(1+s si)(1+t ti)/4 (and permutations); HEXA27 the products of
+// the 1D quadratic Lagrange polynomials x(x-1)/2, 1-x^2, x(x+1)/2.
+static __device__ __constant__ const signed char kHexaLocal[27][3] = {
+    {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+    {0, -1, -1},  {-1, 0, -1}, {-1, -1, 0}, {1, 0, -1}, {1, -1, 0}, {0, 1, -1}, {1, 1, 0}, {-1, 1, 0},
+    {0, -1, 1},   {-1, 0, 1},  {1, 0, 1},   {0, 1, 1},  {0, 0, -1}, {0, -1, 0}, {-1, 0, 0}, {1, 0, 0},
+    {0, 1, 0},    {0, 0, 1},   {0, 0, 0}};
+
+__device__ inline void hexa27_gauss(int g, double* xi, double* w) {
+  const double a = sqrt(3.0 / 5.0), c1 = 5.0 / 9, c2 = 8.0 / 9;
+  const int i = g / 9, j = (g / 3) % 3, k = g % 3;
+  const double x[3] = {-a, 0.0, a};
+  xi[0] = x[i]; xi[1] = x[j]; xi[2] = x[k];
+  const int n0 = (i == 1) + (j == 1) + (k == 1);  // coordinates at the centre
+  *w = n0 == 0 ? c1 * c1 * c1 : (n0 == 1 ? c1 * c1 * c2 : (n0 == 2 ? c1 * c2 * c2 : c2 * c2 * c2));
+}
+
+// 1D quadratic Lagrange polynomial of the node at xa in {-1, 0, 1}, and its derivative
+__device__ inline double lag2(double x, int xa) { return xa == 0 ? 1 - x * x : x * (x + xa) / 2; }
+__device__ inline double dlag2(double x, int xa) { return xa == 0 ? -2 * x : x + xa * 0.5; }
+
+template <> struct Elem<GFEA_HEXA20> {
+  static constexpr int nPe = 20, dim = 3, nPg_rigi = 27, nPg_mass = 27;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { hexa27_gauss(g, xi, w); }
+  __device__ static double N(const double* p, int n) {
+    const double r = p[0], s = p[1], t = p[2];
+    const int ra = kHexaLocal[n][0], sa = kHexaLocal[n][1], ta = kHexaLocal[n][2];
+    if (n < 8) return (1 + r * ra) * (1 + s * sa) * (1 + t * ta) * (r * ra + s * sa + t * ta - 2) / 8;
+    if (ra == 0) return (1 - r * r) * (1 + s * sa) * (1 + t * ta) / 4;
+    if (sa == 0) return (1 + r * ra) * (1 - s * s) * (1 + t * ta) / 4;
+    return (1 + r * ra) * (1 + s * sa) * (1 - t * t) / 4;
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double x[3] = {p[0], p[1], p[2]};
+    const int c[3] = {kHexaLocal[n][0], kHexaLocal[n][1], kHexaLocal[n][2]};
+    const int e = (d + 1) % 3, f = (d + 2) % 3;  // the other two axes
+    if (n < 8)
+      return c[d] * (1 + x[e] * c[e]) * (1 + x[f] * c[f]) * (2 * x[d] * c[d] + x[e] * c[e] + x[f] * c[f] - 1) / 8;
+    if (c[d] == 0) return -2 * x[d] * (1 + x[e] * c[e]) * (1 + x[f] * c[f]) / 4;
+    // the zero coordinate is along e or f
+    const int z = c[e] == 0 ? e : f, o = c[e] == 0 ? f : e;
+    return c[d] * (1 - x[z] * x[z]) * (1 + x[o] * c[o]) / 4;
+  }
+};
+
+template <> struct Elem<GFEA_HEXA27> {
+  static constexpr int nPe = 27, dim = 3, nPg_rigi = 27, nPg_mass = 27;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { hexa27_gauss(g, xi, w); }
+  __device__ static double N(const double* p, int n) {
+    return lag2(p[0], kHexaLocal[n][0]) * lag2(p[1], kHexaLocal[n][1]) * lag2(p[2], kHexaLocal[n][2]);
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    double v = 1;
+    for (int k = 0; k < 3; ++k) v *= k == d ? dlag2(p[k], kHexaLocal[n][k]) : lag2(p[k], kHexaLocal[n][k]);
+    return v;
+  }
+};
+
 // Shared-memory reference tables of one element type and Gauss family.
 template <int ELEM, bool MASS>
 struct RefTables {

@@ -13,7 +13,7 @@
 namespace gfea {
 namespace {
 
-constexpr int kMaxNb = 96;       // neighbour capacity per node (HEXA8 27, QUAD9 25)
+constexpr int kMaxNb = 128;      // neighbour capacity per node (HEXA8 27, QUAD9 25, HEXA27 125)
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;

@@ -442,6 +442,8 @@ int dispatch_parts(int elem, const double* coord, const int32_t* connect, const 
     case GFEA_TRI6: return launch_parts<GFEA_TRI6, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     case GFEA_QUAD8: return launch_parts<GFEA_QUAD8, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     case GFEA_TETRA10: return launch_parts<GFEA_TETRA10, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
+    case GFEA_HEXA20: return launch_parts<GFEA_HEXA20, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
+    case GFEA_HEXA27: return launch_parts<GFEA_HEXA27, T>(coord, connect, node_ptr, rank, C, cpe, factor, A, n_parts, threads, vals, s);
     default: return GFEA_ERR_ARG;
   }
 }
@@ -477,6 +479,8 @@ extern "C" size_t gfea_part_smem_bytes(int elem, int value_type, int32_t max_par
     GFEA_PART_SMEM(GFEA_TRI6)
     GFEA_PART_SMEM(GFEA_QUAD8)
     GFEA_PART_SMEM(GFEA_TETRA10)
+    GFEA_PART_SMEM(GFEA_HEXA20)
+    GFEA_PART_SMEM(GFEA_HEXA27)
 #undef GFEA_PART_SMEM
     default: return 0;
   }

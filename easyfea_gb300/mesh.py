@@ -37,6 +37,8 @@ class ElemType(str, Enum):
     TRI6 = "TRI6"
     QUAD8 = "QUAD8"
     TETRA10 = "TETRA10"
+    HEXA20 = "HEXA20"
+    HEXA27 = "HEXA27"
 
 
 class MatrixType(str, Enum):
@@ -58,6 +60,8 @@ ELEM_INFO = {
     ElemType.QUAD8: (8, 2, 7),
     ElemType.TETRA10: (10, 3, 8),
     ElemType.SEG3: (3, 1, 9),
+    ElemType.HEXA20: (20, 3, 10),
+    ElemType.HEXA27: (27, 3, 11),
 }
 
 # Gauss points per (element, matrixType), as chosen by
@@ -84,6 +88,10 @@ NPG = {
     (ElemType.QUAD8, MatrixType.mass): 9,
     (ElemType.TETRA10, MatrixType.rigi): 4,
     (ElemType.TETRA10, MatrixType.mass): 4,
+    (ElemType.HEXA20, MatrixType.rigi): 27,
+    (ElemType.HEXA20, MatrixType.mass): 27,
+    (ElemType.HEXA27, MatrixType.rigi): 27,
+    (ElemType.HEXA27, MatrixType.mass): 27,
 }
 
 
@@ -441,6 +449,65 @@ def Mesh_Tetra10_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int)
     """Organised TETRA10 mesh (the TETRA4 mesh with mid-edge nodes) with TRI6 boundary faces."""
     return _quadratic(Mesh_Tetra4_Box(Lx, Ly, Lz, nx, ny, nz), ElemType.TETRA10,
                       [(0, 1), (1, 2), (2, 0), (0, 3), (2, 3), (1, 3)], ElemType.TRI6, [(0, 1), (1, 2), (2, 0)])
+
+
+# local coordinates of the HEXA27 nodes in the reference's order (corners,
+# edge middles, face centres, centre; EasyFEA/FEM/Elems/_hexa.py); HEXA20
+# takes the first 20
+_HEXA_LOCAL = np.array([
+    [-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1],
+    [0, -1, -1], [-1, 0, -1], [-1, -1, 0], [1, 0, -1], [1, -1, 0], [0, 1, -1], [1, 1, 0], [-1, 1, 0],
+    [0, -1, 1], [-1, 0, 1], [1, 0, 1], [0, 1, 1], [0, 0, -1], [0, -1, 0], [-1, 0, 0], [1, 0, 0],
+    [0, 1, 0], [0, 0, 1], [0, 0, 0]])
+
+
+def _hexa_quadratic_box(Lx, Ly, Lz, nx, ny, nz, nPe: int) -> Mesh:
+    """HEXA20 / HEXA27 box on the half-spacing node grid: element nodes at
+    their local coordinates, faces as QUAD8 / QUAD9 (corners around the face,
+    edge middles, centre), grid nodes no element uses dropped."""
+    NX, NY, NZ = 2 * nx, 2 * ny, 2 * nz
+    xs, ys, zs = np.linspace(0.0, Lx, NX + 1), np.linspace(0.0, Ly, NY + 1), np.linspace(0.0, Lz, NZ + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    coord = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    nid = lambda i, j, k: (k * (NY + 1) + j) * (NX + 1) + i  # noqa: E731
+    K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    I, J, K = 2 * I.ravel() + 1, 2 * J.ravel() + 1, 2 * K.ravel() + 1  # cell centres on the grid
+    loc = _HEXA_LOCAL[:nPe]
+    connect = np.stack([nid(I + a, J + b, K + c) for a, b, c in loc], axis=1)
+    # faces: on each side of the box, the face-local (u, v) grid of the cells there
+    ring = [(-1, -1), (1, -1), (1, 1), (-1, 1)]
+    mids = [(0, -1), (1, 0), (0, 1), (-1, 0)]
+    uv = ring + mids + ([(0, 0)] if nPe == 27 else [])
+    faces = []
+    for axis, side, n_cells in ((0, -1, None), (0, 1, None), (1, -1, None), (1, 1, None), (2, -1, None), (2, 1, None)):
+        sel = [(I, J, K)[axis] == (1 if side < 0 else (NX, NY, NZ)[axis] - 1)][0]
+        cols = []
+        for u, v in uv:
+            off = [0, 0, 0]
+            others = [a for a in range(3) if a != axis]
+            off[axis] = side
+            off[others[0]] = u
+            off[others[1]] = v
+            cols.append(nid(I[sel] + off[0], J[sel] + off[1], K[sel] + off[2]))
+        faces.append(np.stack(cols, axis=1))
+    faces = np.concatenate(faces)
+    used = np.unique(np.concatenate([connect.ravel(), faces.ravel()]))
+    new = -np.ones(len(coord), dtype=np.int64)
+    new[used] = np.arange(len(used))
+    belem = ElemType.QUAD9 if nPe == 27 else ElemType.QUAD8
+    elem = ElemType.HEXA27 if nPe == 27 else ElemType.HEXA20
+    c = coord[used]
+    return Mesh({belem: GroupElem(belem, new[faces], c), elem: GroupElem(elem, new[connect], c)})
+
+
+def Mesh_Hexa20_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised HEXA20 mesh of [0,Lx]x[0,Ly]x[0,Lz] with QUAD8 boundary faces."""
+    return _hexa_quadratic_box(Lx, Ly, Lz, nx, ny, nz, 20)
+
+
+def Mesh_Hexa27_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised HEXA27 mesh of [0,Lx]x[0,Ly]x[0,Lz] with QUAD9 boundary faces."""
+    return _hexa_quadratic_box(Lx, Ly, Lz, nx, ny, nz, 27)
 
 
 def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:

@@ -59,6 +59,8 @@ extern "C" {
 #define GFEA_QUAD8 7
 #define GFEA_TETRA10 8
 #define GFEA_SEG3 9
+#define GFEA_HEXA20 10
+#define GFEA_HEXA27 11
 
 /* value types */
 #define GFEA_F64 0

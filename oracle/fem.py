@@ -73,6 +73,16 @@ def gauss(elem: str, matrixType: str):
         return gauss("QUAD4" if matrixType == "rigi" else "QUAD9", matrixType)
     if elem == "TETRA10":  # 4 points for both (_gauss.py:470-472)
         return gauss("TETRA4", "mass")
+    if elem in ("HEXA20", "HEXA27"):  # 27 points for both (_gauss.py:216-261)
+        a = np.sqrt(3 / 5)
+        c1, c2 = 5 / 9, 8 / 9
+        x = [-a] * 9 + [0.0] * 9 + [a] * 9
+        y = [-a, -a, -a, 0.0, 0.0, 0.0, a, a, a] * 3
+        z = [-a, 0.0, a] * 9
+        c13, c23, c12, c22 = c1**3, c2**3, c1**2 * c2, c1 * c2**2
+        by_zeros = {0: c13, 1: c12, 2: c22, 3: c23}
+        w = [by_zeros[int(xi == 0) + int(yi == 0) + int(zi == 0)] for xi, yi, zi in zip(x, y, z)]
+        return np.array([x, y, z]).T, np.array(w)
     if elem == "TETRA4":  # _gauss.py:142-163 (rigi 1 point, mass 4)
         if matrixType == "rigi":
             return np.array([[1 / 4, 1 / 4, 1 / 4]]), np.array([1 / 6])
@@ -121,6 +131,8 @@ def shape_N(elem: str, p: np.ndarray) -> np.ndarray:
     if elem == "SEG3":  # Elems/_seg.py SEG3._N
         (r,) = p
         return np.array([r * (r - 1) / 2, r * (r + 1) / 2, -(r - 1) * (r + 1)])
+    if elem in ("HEXA20", "HEXA27"):
+        return _hexa_quadratic(elem, p)[0]
     if elem == "TRI6":  # Elems/_tri.py TRI6._N
         r, s = p
         return np.array([(r + s - 1) * (2 * r + 2 * s - 1), r * (2 * r - 1), s * (2 * s - 1), -4 * r * (r + s - 1),
@@ -190,6 +202,8 @@ def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
     if elem == "SEG3":  # Elems/_seg.py SEG3._dN
         (r,) = p
         return np.array([[r - 1 / 2, r + 1 / 2, -2 * r]])
+    if elem in ("HEXA20", "HEXA27"):
+        return _hexa_quadratic(elem, p)[1]
     if elem == "TRI6":  # Elems/_tri.py TRI6._dN
         r, s = p
         return np.array([[4 * r + 4 * s - 3, 4 * r - 1, 0.0, -8 * r - 4 * s + 4, 4 * s, -4 * s],
@@ -215,8 +229,53 @@ def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
     raise NotImplementedError(elem)
 
 
+# local coordinates of the HEXA27 nodes in the reference's order
+# (Elems/_hexa.py HEXA27.Get_Local_Coords); HEXA20 takes the first 20
+HEXA_LOCAL = np.array([
+    [-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1],
+    [0, -1, -1], [-1, 0, -1], [-1, -1, 0], [1, 0, -1], [1, -1, 0], [0, 1, -1], [1, 1, 0], [-1, 1, 0],
+    [0, -1, 1], [-1, 0, 1], [1, 0, 1], [0, 1, 1], [0, 0, -1], [0, -1, 0], [-1, 0, 0], [1, 0, 0],
+    [0, 1, 0], [0, 0, 1], [0, 0, 0]], dtype=float)
+
+
+def _hexa_quadratic(elem, p):
+    """N (nPe,) and dN (3, nPe) of HEXA20 (serendipity: corner
+    (1+r ri)(1+s si)(1+t ti)(r ri+s si+t ti-2)/8, edge (1-r^2)(1+s si)(1+t ti)/4
+    and permutations; Elems/_hexa.py HEXA20._N) or HEXA27 (products of the
+    quadratic Lagrange polynomials; HEXA27._N)."""
+    x = np.asarray(p, float)
+    if elem == "HEXA27":
+        def L(v, a):
+            return 1 - v * v if a == 0 else v * (v + a) / 2
+
+        def dL(v, a):
+            return -2 * v if a == 0 else v + a / 2
+        N = np.array([np.prod([L(x[k], c[k]) for k in range(3)]) for c in HEXA_LOCAL])
+        dN = np.array([[np.prod([dL(x[k], c[k]) if k == d else L(x[k], c[k]) for k in range(3)]) for c in HEXA_LOCAL]
+                       for d in range(3)])
+        return N, dN
+    N = np.zeros(20)
+    dN = np.zeros((3, 20))
+    for n, c in enumerate(HEXA_LOCAL[:20]):
+        f = [1 + x[k] * c[k] for k in range(3)]
+        if n < 8:
+            q = x @ c - 2
+            N[n] = f[0] * f[1] * f[2] * q / 8
+            for d in range(3):
+                e, g = (d + 1) % 3, (d + 2) % 3
+                dN[d, n] = c[d] * f[e] * f[g] * (2 * x[d] * c[d] + x[e] * c[e] + x[g] * c[g] - 1) / 8
+        else:
+            z = int(np.where(c == 0)[0][0])
+            f[z] = 1 - x[z] ** 2
+            N[n] = f[0] * f[1] * f[2] / 4
+            for d in range(3):
+                e, g = (d + 1) % 3, (d + 2) % 3
+                dN[d, n] = (-2 * x[d] if d == z else c[d]) * f[e] * f[g] / 4
+    return N, dN
+
+
 ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3, "TETRA4": 3, "SEG3": 1, "TRI6": 2,
-            "QUAD8": 2, "TETRA10": 3}
+            "QUAD8": 2, "TETRA10": 3, "HEXA20": 3, "HEXA27": 3}
 
 
 def N_pg(elem, matrixType):

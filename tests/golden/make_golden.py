@@ -538,7 +538,8 @@ def _pf_solver_cases(R, out):
 
 
 def _quadratic_cases(R, out):
-    """TRI6 / QUAD8 (SEG3 edges) and TETRA10 (TRI6 faces): elastic cantilevers,
+    """TRI6 / QUAD8 (SEG3 edges), TETRA10 (TRI6 faces), HEXA20 (QUAD8 faces) and
+    HEXA27 (QUAD9 faces): elastic cantilevers,
     phase-field systems at a prescribed state and the post-processing
     results."""
     elastic_case(R, "el_tri6", gmesh.Mesh_Tri6_Rect(120.0, 13.0, 12, 3), 210000.0, 0.25, False, 1.0, -10.0, "y",
@@ -550,6 +551,12 @@ def _quadratic_cases(R, out):
     pf_state_case(R, "pfsys_tri6_miehe_at2", gmesh.Mesh_Tri6_Rect(1.0, 1.0, 6, 6), "Miehe", "AT2", out)
     pf_state_case(R, "pfsys_quad8_amor_at1", gmesh.Mesh_Quad8_Rect(1.0, 1.0, 5, 5), "Amor", "AT1", out)
     pf_state_case(R, "pfsys_tetra10_miehe_at2", gmesh.Mesh_Tetra10_Box(1.0, 1.0, 0.5, 2, 2, 1), "Miehe", "AT2", out)
+    elastic_case(R, "el_hexa20", gmesh.Mesh_Hexa20_Box(60.0, 10.0, 10.0, 4, 2, 2), 210000.0, 0.3, False, 1.0, -1.0,
+                 "z", out)
+    elastic_case(R, "el_hexa27", gmesh.Mesh_Hexa27_Box(60.0, 10.0, 10.0, 3, 1, 1), 210000.0, 0.3, False, 1.0, -1.0,
+                 "z", out)
+    pf_state_case(R, "pfsys_hexa20_miehe_at2", gmesh.Mesh_Hexa20_Box(1.0, 1.0, 0.5, 2, 2, 1), "Miehe", "AT2", out)
+    results_case(R, "res_hexa27", gmesh.Mesh_Hexa27_Box(6.0, 2.0, 2.0, 2, 1, 1), 210000.0, 0.3, False, 1.0, out)
     results_case(R, "res_quad8", gmesh.Mesh_Quad8_Rect(12.0, 3.0, 6, 2), 210000.0, 0.3, True, 13.0, out)
     results_case(R, "res_tetra10", gmesh.Mesh_Tetra10_Box(6.0, 2.0, 2.0, 3, 1, 1), 210000.0, 0.3, False, 1.0, out)
 

@@ -19,7 +19,8 @@ def meshes():
     return {"TRI3": gmesh.Mesh_Tri3_Rect(1.0, 1.0, 30, 30), "QUAD4": gmesh.Mesh_Quad4_Rect(12.0, 3.0, 60, 20),
             "QUAD9": gmesh.Mesh_Quad9_Rect(6.0, 2.0, 20, 8), "HEXA8": gmesh.Mesh_Hexa8_Box(4.0, 1.0, 1.0, 20, 6, 6),
             "TETRA4": gmesh.Mesh_Tetra4_Box(3.0, 1.0, 1.0, 8, 4, 4), "TRI6": gmesh.Mesh_Tri6_Rect(1.0, 1.0, 20, 20),
-            "QUAD8": gmesh.Mesh_Quad8_Rect(6.0, 2.0, 24, 8), "TETRA10": gmesh.Mesh_Tetra10_Box(2.0, 1.0, 1.0, 4, 2, 2)}
+            "QUAD8": gmesh.Mesh_Quad8_Rect(6.0, 2.0, 24, 8), "TETRA10": gmesh.Mesh_Tetra10_Box(2.0, 1.0, 1.0, 4, 2, 2),
+            "HEXA20": gmesh.Mesh_Hexa20_Box(2.0, 1.0, 1.0, 6, 3, 3), "HEXA27": gmesh.Mesh_Hexa27_Box(2.0, 1.0, 1.0, 6, 3, 3)}
 
 
 def law(mode, dim, Ne, rng):
@@ -38,7 +39,8 @@ def law(mode, dim, Ne, rng):
     return np.concatenate([[lmbda, mu], f])
 
 
-@pytest.mark.parametrize("elem", ["TRI3", "QUAD4", "QUAD9", "HEXA8", "TETRA4", "TRI6", "QUAD8", "TETRA10"])
+@pytest.mark.parametrize("elem", ["TRI3", "QUAD4", "QUAD9", "HEXA8", "TETRA4", "TRI6", "QUAD8", "TETRA10", "HEXA20",
+                                  "HEXA27"])
 @pytest.mark.parametrize("vt", ["f64", "f32"])
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
 def test_parts_match_atomic_kernel(elem, vt, mode):

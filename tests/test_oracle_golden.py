@@ -8,7 +8,7 @@ from oracle import fem
 from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve, neumann
 
 ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26",
-           "el_tetra4", "el_tri6", "el_quad8", "el_tetra10"]
+           "el_tetra4", "el_tri6", "el_quad8", "el_tetra10", "el_hexa20", "el_hexa27"]
 
 
 def row_scaled_err(A, B):
@@ -173,7 +173,7 @@ def test_phasefield_oracle_convergence_options_match_reference(golden, opt):
 
 @pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2",
                                   "pfsys_tetra4_miehe_at2", "pfsys_tri6_miehe_at2", "pfsys_quad8_amor_at1",
-                                  "pfsys_tetra10_miehe_at2"])
+                                  "pfsys_tetra10_miehe_at2", "pfsys_hexa20_miehe_at2"])
 def test_phasefield_state_systems_match_reference(golden, case):
     g = golden(case)
     m = om(g)

@@ -39,8 +39,9 @@ Materials: isotropic elastic laws (homogeneous or with a per-element Young's
 modulus), homogeneous transversely isotropic and anisotropic laws and, for the
 phase field, a homogeneous material with the Bourdin / Amor / Miehe / He
 (isotropic) and AnisotStrain / AnisotStress splits, AT1 / AT2 and the
-History / HistoryDamage / BoundConstrain solvers; element groups of type SEG2, TRI3, QUAD4, QUAD9, HEXA8 and TETRA4.  Other
-models raise ``NotImplementedError`` at construction.
+History / HistoryDamage / BoundConstrain solvers; element groups of type
+SEG2, SEG3, TRI3, TRI6, QUAD4, QUAD8, QUAD9, HEXA8, HEXA20, HEXA27, TETRA4 and
+TETRA10.  Other models raise ``NotImplementedError`` at construction.
 
 EasyFEA must be importable (it imports gmsh at start-up).
 """

@@ -218,7 +218,11 @@ class _Simu:
                     continue
                 if callable(v):
                     npg = ctypes_int32()
-                    xyz = torch.empty((g.Ne, 8, 3), dtype=torch.float64, device=_dev())
+                    # the number of points first (no element), then the points
+                    _lib.check(L.gfea_boundary_gauss_points(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect),
+                                                            0, 0, __import__("ctypes").byref(npg), _lib.stream()),
+                               "gauss points")
+                    xyz = torch.empty((g.Ne, npg.value, 3), dtype=torch.float64, device=_dev())
                     _lib.check(L.gfea_boundary_gauss_points(g.code, _lib.ptr(self.dmesh.coord), _lib.ptr(g.connect),
                                                             g.Ne, _lib.ptr(xyz), __import__("ctypes").byref(npg),
                                                             _lib.stream()), "gauss points")

@@ -195,7 +195,8 @@ int gfea_surface_load(int belem, const double* coord, const int32_t* bconnect, i
                       double* b, void* stream);
 
 /* Coordinates of the mass Gauss points of boundary elements,
- * xyz[(e * nPg + g) * 3 + k] (n_belems * nPg * 3 doubles); *npg_host = nPg.
+ * xyz[(e * nPg + g) * 3 + k] (n_belems * nPg * 3 doubles); *npg_host = nPg
+ * (with n_belems = 0 only *npg_host is set: size xyz from it).
  * The points where _Simu.__Bc_evaluate evaluates a load given as a function
  * of position (EasyFEA/Simulations/_simu.py:2353-2385 with
  * Get_GaussCoordinates_e_pg, :2803-2811). */

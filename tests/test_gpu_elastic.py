@@ -137,3 +137,22 @@ def test_f32_element_path_matches_reference(golden, case):
     M32 = simu.K_device.to_scipy()
     M32.data = m32.double().cpu().numpy()
     assert row_scaled_err(M32, csr(g, "M", n)) <= 1e-6
+
+
+def test_function_load_on_nine_point_faces():
+    """A traction given as a function of position on QUAD9 faces (HEXA27, 9
+    mass Gauss points per face) and QUAD8 faces (HEXA20): the Gauss-point
+    buffer is sized from the face type; the load's resultant equals the
+    integral of the function over the loaded face."""
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    for m in (gmesh.Mesh_Hexa27_Box(2.0, 1.0, 1.0, 2, 2, 2), gmesh.Mesh_Hexa20_Box(2.0, 1.0, 1.0, 2, 2, 2)):
+        simu = Simulations.Elastic(m, Models.Elastic.Isotropic(3, E=1000.0, v=0.3, planeStress=False))
+        right = np.where(np.abs(m.coord[:, 0] - 2.0) < 1e-12)[0]
+        simu.add_surfLoad(right, [lambda x, y, z: 1.0 + y * z], ["z"])
+        b = simu._neumann_vec("elastic").cpu().numpy().reshape(-1, 3)
+        # integral over [0,1]^2 of 1 + y z = 1.25 (the 27-point rule is exact)
+        assert abs(b[:, 2].sum() - 1.25) <= 1e-12
+        assert np.abs(b[:, :2]).max() == 0.0

@@ -23,7 +23,8 @@ F64 = 0
 F32 = 1
 
 ELEM_CODE = {"SEG2": 0, "TRI3": 1, "QUAD4": 2, "QUAD9": 3, "HEXA8": 4, "TETRA4": 5, "TRI6": 6, "QUAD8": 7,
-             "TETRA10": 8, "SEG3": 9, "HEXA20": 10, "HEXA27": 11}
+             "TETRA10": 8, "SEG3": 9, "HEXA20": 10, "HEXA27": 11, "PRISM6": 12, "PRISM15": 13,
+             "PRISM18": 14, "TRI10": 15, "TRI15": 16, "SEG4": 17, "SEG5": 18}
 SPLIT_CODE = {"Bourdin": 0, "Amor": 1, "Miehe": 2, "Zhang": 3, "Stress": 4, "He": 5, "AnisotStrain": 6,
               "AnisotStrain_PM": 7, "AnisotStrain_MP": 8, "AnisotStrain_NoCross": 9, "AnisotStress": 10,
               "AnisotStress_PM": 11, "AnisotStress_MP": 12, "AnisotStress_NoCross": 13}

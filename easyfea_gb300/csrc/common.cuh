@@ -45,11 +45,18 @@ __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + 
 
 // ---------------------------------------------------------------------------
 // Element reference data.  Gauss tables follow EasyFEA/FEM/_gauss.py:364-480
-// and the shape functions EasyFEA/FEM/Elems/{_seg,_tri,_quad,_hexa,_tetra}.py; they
+// and the shape functions EasyFEA/FEM/Elems/{_seg,_tri,_quad,_hexa,_tetra,_prism}.py; they
 // are evaluated on the device into shared memory by each kernel's prologue.
 // ---------------------------------------------------------------------------
 
 template <int ELEM> struct Elem;
+
+// The higher-order elements whose launches compile in the *_ho.cu
+// translation units, and the dimension of every element code (-1: unknown).
+inline bool higher_order_elem(int elem) {
+  return elem == GFEA_TRI10 || elem == GFEA_TRI15 || elem == GFEA_PRISM6 || elem == GFEA_PRISM15 ||
+         elem == GFEA_PRISM18;
+}
 
 template <> struct Elem<GFEA_SEG2> {
   static constexpr int nPe = 2, dim = 1, nPg_rigi = 1, nPg_mass = 2;
@@ -433,6 +440,277 @@ template <> struct Elem<GFEA_HEXA27> {
     double v = 1;
     for (int k = 0; k < 3; ++k) v *= k == d ? dlag2(p[k], kHexaLocal[n][k]) : lag2(p[k], kHexaLocal[n][k]);
     return v;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Higher-order segments and triangles (EasyFEA/FEM/Elems/_seg.py SEG4, SEG5;
+// _tri.py TRI10, TRI15): the Lagrange interpolants of their nodes, written
+// from the nodes' positions rather than as expanded polynomials.
+//
+// Segment of order p: node n sits at x = -1 + 2 k/p, k = kSegK[p][n] (the end
+// nodes first, then the inner ones from the first end); with v = p (x + 1) / 2,
+// N = prod_{q != k} (v - q) / (k - q).
+// Triangle of order p: node n has barycentric indices (i0, i1, i2), i1 = p r,
+// i2 = p s, i0 = p - i1 - i2 (corners, then p - 1 nodes on each edge 01, 12,
+// 20 in that direction, then the inner nodes); with the barycentric
+// coordinates L0 = 1 - r - s, L1 = r, L2 = s,
+// N = phi_i0(p L0) phi_i1(p L1) phi_i2(p L2), phi_i(v) = prod_{q < i} (v - q) / (i - q).
+// ---------------------------------------------------------------------------
+static __device__ __constant__ const signed char kSegK[6][5] = {
+    {0}, {0}, {0}, {0, 3, 1, 2}, {0, 4, 1, 2, 3}, {0}};
+
+template <int P>
+__device__ inline double seg_lagrange(double x, int n) {
+  const double v = P * (x + 1) / 2;
+  const int k = kSegK[P][n];
+  double r = 1;
+#pragma unroll
+  for (int q = 0; q <= P; ++q)
+    if (q != k) r *= (v - q) / (k - q);
+  return r;
+}
+
+template <int P>
+__device__ inline double seg_lagrange_d(double x, int n) {
+  const double v = P * (x + 1) / 2;
+  const int k = kSegK[P][n];
+  double sum = 0;
+#pragma unroll
+  for (int j = 0; j <= P; ++j) {
+    if (j == k) continue;
+    double r = 1.0 / (k - j);
+#pragma unroll
+    for (int q = 0; q <= P; ++q)
+      if (q != k && q != j) r *= (v - q) / (k - q);
+    sum += r;
+  }
+  return sum * P / 2;  // dv/dx = p / 2
+}
+
+// phi_i(v) and its derivative
+__device__ inline double tri_phi(int i, double v) {
+  double r = 1;
+  for (int q = 0; q < i; ++q) r *= (v - q) / (i - q);
+  return r;
+}
+__device__ inline double tri_phi_d(int i, double v) {
+  double sum = 0;
+  for (int j = 0; j < i; ++j) {
+    double r = 1.0 / (i - j);
+    for (int q = 0; q < i; ++q)
+      if (q != j) r *= (v - q) / (i - q);
+    sum += r;
+  }
+  return sum;
+}
+
+// (i1, i2) of the TRI10 and TRI15 nodes in the reference's order
+static __device__ __constant__ const signed char kTri10I[10][2] = {
+    {0, 0}, {3, 0}, {0, 3}, {1, 0}, {2, 0}, {2, 1}, {1, 2}, {0, 2}, {0, 1}, {1, 1}};
+static __device__ __constant__ const signed char kTri15I[15][2] = {
+    {0, 0}, {4, 0}, {0, 4}, {1, 0}, {2, 0}, {3, 0}, {3, 1}, {2, 2}, {1, 3}, {0, 3}, {0, 2}, {0, 1},
+    {1, 1}, {2, 1}, {1, 2}};
+
+template <int P>
+__device__ inline double tri_lagrange(const double* p, int i1, int i2) {
+  const double L[3] = {1 - p[0] - p[1], p[0], p[1]};
+  const int ii[3] = {P - i1 - i2, i1, i2};
+  return tri_phi(ii[0], P * L[0]) * tri_phi(ii[1], P * L[1]) * tri_phi(ii[2], P * L[2]);
+}
+
+// d/dr (d = 0) or d/ds (d = 1): dL0 = -1, dL1 / dr = 1, dL2 / ds = 1
+template <int P>
+__device__ inline double tri_lagrange_d(const double* p, int d, int i1, int i2) {
+  const double L[3] = {1 - p[0] - p[1], p[0], p[1]};
+  const int ii[3] = {P - i1 - i2, i1, i2};
+  const double f[3] = {tri_phi(ii[0], P * L[0]), tri_phi(ii[1], P * L[1]), tri_phi(ii[2], P * L[2])};
+  const int b = d == 0 ? 1 : 2;  // the coordinate that grows with the derivative's variable
+  return P * (tri_phi_d(ii[b], P * L[b]) * f[0] - tri_phi_d(ii[0], P * L[0]) * f[b]) * f[3 - b];
+}
+
+// Gauss-Legendre rules of 2, 4 and 5 points (ascending abscissae, as
+// numpy.polynomial.legendre.leggauss, which EasyFEA/FEM/_gauss.py:395-420 calls)
+__device__ inline void legendre_gauss(int n, int g, double* x, double* w) {
+  if (n == 2) {
+    const double a = 1 / sqrt(3.0);
+    *x = g == 0 ? -a : a;
+    *w = 1.0;
+  } else if (n == 4) {
+    const double t = 2.0 / 7.0 * sqrt(6.0 / 5.0);
+    const double xo = sqrt(3.0 / 7.0 + t), xi = sqrt(3.0 / 7.0 - t);
+    const double wo = (18.0 - sqrt(30.0)) / 36.0, wi = (18.0 + sqrt(30.0)) / 36.0;
+    const double xs[4] = {-xo, -xi, xi, xo}, ws[4] = {wo, wi, wi, wo};
+    *x = xs[g];
+    *w = ws[g];
+  } else {  // 5
+    const double t = 2.0 * sqrt(10.0 / 7.0);
+    const double xo = sqrt(5.0 + t) / 3.0, xi = sqrt(5.0 - t) / 3.0;
+    const double wo = (322.0 - 13.0 * sqrt(70.0)) / 900.0, wi = (322.0 + 13.0 * sqrt(70.0)) / 900.0;
+    const double xs[5] = {-xo, -xi, 0.0, xi, xo}, ws[5] = {wo, wi, 128.0 / 225.0, wi, wo};
+    *x = xs[g];
+    *w = ws[g];
+  }
+}
+
+template <> struct Elem<GFEA_SEG4> {
+  static constexpr int nPe = 4, dim = 1, nPg_rigi = 2, nPg_mass = 4;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) { legendre_gauss(mass ? 4 : 2, g, xi, w); }
+  __device__ static double N(const double* p, int n) { return seg_lagrange<3>(p[0], n); }
+  __device__ static double dN(const double* p, int, int n) { return seg_lagrange_d<3>(p[0], n); }
+};
+
+template <> struct Elem<GFEA_SEG5> {
+  static constexpr int nPe = 5, dim = 1, nPg_rigi = 4, nPg_mass = 5;
+  __device__ static void gauss(bool mass, int g, double* xi, double* w) { legendre_gauss(mass ? 5 : 4, g, xi, w); }
+  __device__ static double N(const double* p, int n) { return seg_lagrange<4>(p[0], n); }
+  __device__ static double dN(const double* p, int, int n) { return seg_lagrange_d<4>(p[0], n); }
+};
+
+template <> struct Elem<GFEA_TRI10> {
+  static constexpr int nPe = 10, dim = 2, nPg_rigi = 6, nPg_mass = 6;  // _gauss.py: 6 points for both
+  __device__ static void gauss(bool, int g, double* xi, double* w) { Elem<GFEA_TRI6>::gauss(true, g, xi, w); }
+  __device__ static double N(const double* p, int n) { return tri_lagrange<3>(p, kTri10I[n][0], kTri10I[n][1]); }
+  __device__ static double dN(const double* p, int d, int n) {
+    return tri_lagrange_d<3>(p, d, kTri10I[n][0], kTri10I[n][1]);
+  }
+};
+
+template <> struct Elem<GFEA_TRI15> {
+  static constexpr int nPe = 15, dim = 2, nPg_rigi = 12, nPg_mass = 12;  // 12 points for both
+  __device__ static void gauss(bool, int g, double* xi, double* w) {
+    // the 12-point rule of degree 6 with the literals of EasyFEA/FEM/_gauss.py:92-104
+    const double a = 0.063089014491502, b = 0.249286745170910, c = 0.310352451033785, d = 0.053145049844816;
+    const double p1 = 0.025422453185103, p2 = 0.058393137863189, p3 = 0.041425537809187;
+    const double xs[12] = {a, 1 - 2 * a, a, b, 1 - 2 * b, b, c, d, 1 - c - d, 1 - c - d, c, d};
+    const double ys[12] = {a, a, 1 - 2 * a, b, b, 1 - 2 * b, d, c, c, d, 1 - c - d, 1 - c - d};
+    xi[0] = xs[g];
+    xi[1] = ys[g];
+    *w = g < 3 ? p1 : (g < 6 ? p2 : p3);
+  }
+  __device__ static double N(const double* p, int n) { return tri_lagrange<4>(p, kTri15I[n][0], kTri15I[n][1]); }
+  __device__ static double dN(const double* p, int d, int n) {
+    return tri_lagrange_d<4>(p, d, kTri15I[n][0], kTri15I[n][1]);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Prisms (EasyFEA/FEM/Elems/_prism.py PRISM6, PRISM15, PRISM18): a triangle
+// (r, s) times a segment t in [-1, 1].  Node n has local coordinates
+// (r, s, t) = (kPrismLocal[n][0] / 2, kPrismLocal[n][1] / 2, kPrismLocal[n][2])
+// in the reference's order: the corners of the t = -1 and t = 1 triangles,
+// the edge middles (01, 02, 03 vertical, 12, 14 vertical, 25 vertical, 34, 35,
+// 45), then -- PRISM18 -- the centres of the three quadrangular faces.
+//   PRISM6:  the triangle's L_a (a = the corner) times (1 + t tn) / 2.
+//   PRISM15 (serendipity): corner L_a (1 + t tn) (2 L_a + t tn - 2) / 2,
+//            triangle-edge middle 2 L_a L_b (1 + t tn), vertical-edge middle L_a (1 - t^2).
+//   PRISM18: the TRI6 function of (r, s) times the quadratic Lagrange
+//            polynomial of t (lag2).
+// Gauss points (_gauss.py:268-360; base triangle coordinates r, s, axis t):
+// 6 points (r, s) in {(1/2, 1/2), (0, 1/2), (1/2, 0)} at t = -+1/sqrt(3),
+// weight 1/6; 21 points: the 7-point triangle rule (closed-form
+// coordinates) at t = -sqrt(3/5), 0, sqrt(3/5) with weights 5/9, 8/9, 5/9.
+// ---------------------------------------------------------------------------
+static __device__ __constant__ const signed char kPrismLocal[18][3] = {
+    {0, 0, -1}, {2, 0, -1}, {0, 2, -1}, {0, 0, 1}, {2, 0, 1}, {0, 2, 1},
+    {1, 0, -1}, {0, 1, -1}, {0, 0, 0},  {1, 1, -1}, {2, 0, 0}, {0, 2, 0},
+    {1, 0, 1},  {0, 1, 1},  {1, 1, 1},  {1, 0, 0},  {0, 1, 0}, {1, 1, 0}};
+
+__device__ inline void prism_gauss(int npg, int g, double* xi, double* w) {
+  if (npg == 6) {
+    const double a = 1 / sqrt(3.0);
+    const double rs[3][2] = {{0.5, 0.5}, {0.0, 0.5}, {0.5, 0.0}};
+    xi[0] = rs[g % 3][0];
+    xi[1] = rs[g % 3][1];
+    xi[2] = g < 3 ? -a : a;
+    *w = 1.0 / 6;
+    return;
+  }
+  const double al = sqrt(3.0 / 5.0), c1 = 5.0 / 9, c2 = 8.0 / 9;
+  const double a = (6 + sqrt(15.0)) / 21, b = (6 - sqrt(15.0)) / 21;
+  const double cp = (155 + sqrt(15.0)) / 2400, cm = (155 - sqrt(15.0)) / 2400;
+  const int l = g / 7, k = g % 7;
+  const double r[7] = {1.0 / 3, a, 1 - 2 * a, a, b, 1 - 2 * b, b};
+  const double s[7] = {1.0 / 3, a, a, 1 - 2 * a, b, b, 1 - 2 * b};
+  const double wt[7] = {9.0 / 80, cp, cp, cp, cm, cm, cm};
+  xi[0] = r[k];
+  xi[1] = s[k];
+  xi[2] = l == 0 ? -al : (l == 1 ? 0.0 : al);
+  *w = (l == 1 ? c2 : c1) * wt[k];
+}
+
+// the corner a in {0, 1, 2} of the base triangle at doubled (r, s) = (2, 0) etc.
+__device__ inline int prism_corner(int r2, int s2) { return r2 == 2 ? 1 : (s2 == 2 ? 2 : 0); }
+// the corners (e0, e1) of the base-triangle edge whose middle is at doubled
+// (r, s) = (1, 0): 0-1, (0, 1): 0-2, (1, 1): 1-2
+__device__ inline void prism_edge(int r2, int s2, int* e0, int* e1) {
+  *e0 = r2 == 1 && s2 == 1 ? 1 : 0;
+  *e1 = s2 == 0 ? 1 : 2;
+}
+
+template <> struct Elem<GFEA_PRISM6> {
+  static constexpr int nPe = 6, dim = 3, nPg_rigi = 6, nPg_mass = 6;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { prism_gauss(6, g, xi, w); }
+  __device__ static double N(const double* p, int n) {
+    const double L[3] = {1 - p[0] - p[1], p[0], p[1]};
+    return L[n % 3] * (1 + p[2] * kPrismLocal[n][2]) / 2;
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double L[3] = {1 - p[0] - p[1], p[0], p[1]};
+    const int a = n % 3, tn = kPrismLocal[n][2];
+    if (d == 2) return L[a] * tn / 2;
+    const double dL = a == 0 ? -1.0 : (a == d + 1 ? 1.0 : 0.0);
+    return dL * (1 + p[2] * tn) / 2;
+  }
+};
+
+template <> struct Elem<GFEA_PRISM15> {
+  static constexpr int nPe = 15, dim = 3, nPg_rigi = 6, nPg_mass = 6;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { prism_gauss(6, g, xi, w); }
+  // dL_a / d(r or s)
+  __device__ static double dL(int a, int d) { return a == 0 ? -1.0 : (a == d + 1 ? 1.0 : 0.0); }
+  __device__ static double N(const double* p, int n) {
+    const double L[3] = {1 - p[0] - p[1], p[0], p[1]}, t = p[2];
+    const int r2 = kPrismLocal[n][0], s2 = kPrismLocal[n][1], tn = kPrismLocal[n][2];
+    if (n < 6) {
+      const int a = n % 3;
+      return L[a] * (1 + t * tn) * (2 * L[a] + t * tn - 2) / 2;
+    }
+    if (tn == 0) return L[prism_corner(r2, s2)] * (1 - t * t);
+    int e0, e1;
+    prism_edge(r2, s2, &e0, &e1);
+    return 2 * L[e0] * L[e1] * (1 + t * tn);
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const double L[3] = {1 - p[0] - p[1], p[0], p[1]}, t = p[2];
+    const int r2 = kPrismLocal[n][0], s2 = kPrismLocal[n][1], tn = kPrismLocal[n][2];
+    if (n < 6) {
+      const int a = n % 3;
+      const double ft = 1 + t * tn, q = 2 * L[a] + t * tn - 2;
+      if (d == 2) return L[a] * tn * (q + ft) / 2;
+      return dL(a, d) * ft * (q + 2 * L[a]) / 2;
+    }
+    if (tn == 0) {
+      const int a = prism_corner(r2, s2);
+      return d == 2 ? -2 * t * L[a] : dL(a, d) * (1 - t * t);
+    }
+    int e0, e1;
+    prism_edge(r2, s2, &e0, &e1);
+    if (d == 2) return 2 * L[e0] * L[e1] * tn;
+    return 2 * (dL(e0, d) * L[e1] + L[e0] * dL(e1, d)) * (1 + t * tn);
+  }
+};
+
+template <> struct Elem<GFEA_PRISM18> {
+  static constexpr int nPe = 18, dim = 3, nPg_rigi = 21, nPg_mass = 21;
+  __device__ static void gauss(bool, int g, double* xi, double* w) { prism_gauss(21, g, xi, w); }
+  __device__ static double N(const double* p, int n) {
+    return tri_lagrange<2>(p, kPrismLocal[n][0], kPrismLocal[n][1]) * lag2(p[2], kPrismLocal[n][2]);
+  }
+  __device__ static double dN(const double* p, int d, int n) {
+    const int i1 = kPrismLocal[n][0], i2 = kPrismLocal[n][1], tn = kPrismLocal[n][2];
+    if (d == 2) return tri_lagrange<2>(p, i1, i2) * dlag2(p[2], tn);
+    return tri_lagrange_d<2>(p, d, i1, i2) * lag2(p[2], tn);
   }
 };
 

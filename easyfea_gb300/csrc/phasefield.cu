@@ -1,5 +1,6 @@
 // Phase-field entry points and the 2D elements' launches (kernels in
-// phasefield.cuh, the 3D elements' launches in phasefield3d.cu).
+// phasefield.cuh, the 3D elements' launches in phasefield3d.cu, the
+// higher-order elements' in phasefield_ho.cu).
 
 #include "phasefield.cuh"
 
@@ -15,6 +16,8 @@ extern "C" int gfea_pf_damage(int elem, const double* coord, const int32_t* conn
   if (!coord || !connect || !node_ptr || !rank || !u || !H_new || !Kd_values || !Fd || n_elems < 0) return GFEA_ERR_ARG;
   if (n_elems == 0) return GFEA_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (higher_order_elem(elem))
+    return pf_damage_ho(elem, coord, connect, n_elems, node_ptr, rank, u, params_host, H_old, H_new, Kd_values, Fd, s);
   switch (elem) {
     case GFEA_TRI3: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_TRI3>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
     case GFEA_QUAD4: if (P.dim != 2) return GFEA_ERR_ARG; return launch_damage<GFEA_QUAD4>(coord, connect, n_elems, node_ptr, rank, u, P, H_old, H_new, Kd_values, Fd, s);
@@ -36,6 +39,8 @@ extern "C" int gfea_pf_elastic(int elem, const double* coord, const int32_t* con
   if (!coord || !connect || !node_ptr || !rank || !u || !d || !values || n_elems < 0) return GFEA_ERR_ARG;
   if (n_elems == 0) return GFEA_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (higher_order_elem(elem))
+    return pf_elastic_ho(elem, coord, connect, n_elems, node_ptr, rank, u, d, params_host, value_type, values, s);
   if (value_type == GFEA_F64) {
     auto* v = static_cast<double*>(values);
     switch (elem) {

@@ -282,6 +282,20 @@ int pf_damage_3d(int elem, const double* coord, const int32_t* connect, int64_t 
 int pf_elastic_3d(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
                   const uint8_t* rank, const double* u, const double* d, const gfea_pf_params* params,
                   int value_type, void* values, cudaStream_t s);
+// TRI10, TRI15 (through phasefield_ho2d.cu), PRISM6, PRISM15 and PRISM18 (phasefield_ho.cu)
+int pf_damage_ho(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                 const uint8_t* rank, const double* u, const gfea_pf_params* params, const double* H_old,
+                 double* H_new, double* Kd, double* Fd, cudaStream_t s);
+int pf_elastic_ho(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                  const uint8_t* rank, const double* u, const double* d, const gfea_pf_params* params,
+                  int value_type, void* values, cudaStream_t s);
+// TRI10 and TRI15 (phasefield_ho2d.cu)
+int pf_damage_ho2d(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                   const uint8_t* rank, const double* u, const gfea_pf_params* params, const double* H_old,
+                   double* H_new, double* Kd, double* Fd, cudaStream_t s);
+int pf_elastic_ho2d(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
+                    const uint8_t* rank, const double* u, const double* d, const gfea_pf_params* params,
+                    int value_type, void* values, cudaStream_t s);
 // HEXA20 and HEXA27 (phasefield_hexq.cu)
 int pf_damage_hexq(int elem, const double* coord, const int32_t* connect, int64_t Ne, const int32_t* node_ptr,
                    const uint8_t* rank, const double* u, const gfea_pf_params* params, const double* H_old,

@@ -1,5 +1,6 @@
 // Post-processing entry points and the 2D elements' launches; the kernels
-// are in results.cuh, the 3D elements' launches in results3d.cu.
+// are in results.cuh, the 3D elements' launches in results3d.cu and the
+// higher-order elements' in results_ho.cu.
 
 #include "results.cuh"
 
@@ -15,8 +16,10 @@ extern "C" int gfea_element_fields(int elem, const double* coord, const int32_t*
   const int st = fields_setup(f, &A, &P);
   int dim = 0;
   switch (elem) {
-    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: case GFEA_TRI6: case GFEA_QUAD8: dim = 2; break;
-    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: case GFEA_HEXA20: case GFEA_HEXA27: dim = 3; break;
+    case GFEA_TRI3: case GFEA_QUAD4: case GFEA_QUAD9: case GFEA_TRI6: case GFEA_QUAD8: case GFEA_TRI10:
+    case GFEA_TRI15: dim = 2; break;
+    case GFEA_HEXA8: case GFEA_TETRA4: case GFEA_TETRA10: case GFEA_HEXA20: case GFEA_HEXA27: case GFEA_PRISM6:
+    case GFEA_PRISM15: case GFEA_PRISM18: dim = 3; break;
     default: return GFEA_ERR_ARG;
   }
   if (A.pf) {
@@ -27,6 +30,7 @@ extern "C" int gfea_element_fields(int elem, const double* coord, const int32_t*
   if (n_elems == 0) return GFEA_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const bool mass = f->gauss == 1;
+  if (higher_order_elem(elem)) return fields_dispatch_ho(elem, mass, coord, connect, n_elems, u, f, s);
   switch (elem) {
     case GFEA_TRI3: return dispatch_fields<GFEA_TRI3>(mass, coord, connect, n_elems, u, A, P, s);
     case GFEA_QUAD4: return dispatch_fields<GFEA_QUAD4>(mass, coord, connect, n_elems, u, A, P, s);

@@ -320,6 +320,12 @@ inline int fields_setup(const gfea_fields* f, FieldArgs* A, PF* P) {
 // the 3D elements' launches, compiled in their own translation unit
 int fields_dispatch_3d(int elem, bool mass, const double* coord, const int32_t* connect, int64_t Ne,
                        const double* u, const gfea_fields* f, cudaStream_t s);
+// TRI10, TRI15 (through results_ho2d.cu), PRISM6, PRISM15 and PRISM18 (results_ho.cu)
+int fields_dispatch_ho(int elem, bool mass, const double* coord, const int32_t* connect, int64_t Ne,
+                       const double* u, const gfea_fields* f, cudaStream_t s);
+// TRI10 and TRI15 (results_ho2d.cu)
+int fields_dispatch_ho2d(int elem, bool mass, const double* coord, const int32_t* connect, int64_t Ne,
+                         const double* u, const gfea_fields* f, cudaStream_t s);
 // HEXA20 and HEXA27 (results_hexq.cu)
 int fields_dispatch_hexq(int elem, bool mass, const double* coord, const int32_t* connect, int64_t Ne,
                          const double* u, const gfea_fields* f, cudaStream_t s);

@@ -40,8 +40,8 @@ modulus), homogeneous transversely isotropic and anisotropic laws and, for the
 phase field, a homogeneous material with the Bourdin / Amor / Miehe / He
 (isotropic) and AnisotStrain / AnisotStress splits, AT1 / AT2 and the
 History / HistoryDamage / BoundConstrain solvers; element groups of type
-SEG2, SEG3, TRI3, TRI6, QUAD4, QUAD8, QUAD9, HEXA8, HEXA20, HEXA27, TETRA4 and
-TETRA10.  Other models raise ``NotImplementedError`` at construction.
+SEG2, SEG3, SEG4, SEG5, TRI3, TRI6, TRI10, TRI15, QUAD4, QUAD8, QUAD9, HEXA8,
+HEXA20, HEXA27, TETRA4, TETRA10, PRISM6, PRISM15 and PRISM18.  Other models raise ``NotImplementedError`` at construction.
 
 EasyFEA must be importable (it imports gmsh at start-up).
 """

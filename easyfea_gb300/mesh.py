@@ -39,6 +39,13 @@ class ElemType(str, Enum):
     TETRA10 = "TETRA10"
     HEXA20 = "HEXA20"
     HEXA27 = "HEXA27"
+    PRISM6 = "PRISM6"
+    PRISM15 = "PRISM15"
+    PRISM18 = "PRISM18"
+    TRI10 = "TRI10"
+    TRI15 = "TRI15"
+    SEG4 = "SEG4"
+    SEG5 = "SEG5"
 
 
 class MatrixType(str, Enum):
@@ -62,6 +69,13 @@ ELEM_INFO = {
     ElemType.SEG3: (3, 1, 9),
     ElemType.HEXA20: (20, 3, 10),
     ElemType.HEXA27: (27, 3, 11),
+    ElemType.PRISM6: (6, 3, 12),
+    ElemType.PRISM15: (15, 3, 13),
+    ElemType.PRISM18: (18, 3, 14),
+    ElemType.TRI10: (10, 2, 15),
+    ElemType.TRI15: (15, 2, 16),
+    ElemType.SEG4: (4, 1, 17),
+    ElemType.SEG5: (5, 1, 18),
 }
 
 # Gauss points per (element, matrixType), as chosen by
@@ -92,6 +106,20 @@ NPG = {
     (ElemType.HEXA20, MatrixType.mass): 27,
     (ElemType.HEXA27, MatrixType.rigi): 27,
     (ElemType.HEXA27, MatrixType.mass): 27,
+    (ElemType.PRISM6, MatrixType.rigi): 6,
+    (ElemType.PRISM6, MatrixType.mass): 6,
+    (ElemType.PRISM15, MatrixType.rigi): 6,
+    (ElemType.PRISM15, MatrixType.mass): 6,
+    (ElemType.PRISM18, MatrixType.rigi): 21,
+    (ElemType.PRISM18, MatrixType.mass): 21,
+    (ElemType.TRI10, MatrixType.rigi): 6,
+    (ElemType.TRI10, MatrixType.mass): 6,
+    (ElemType.TRI15, MatrixType.rigi): 12,
+    (ElemType.TRI15, MatrixType.mass): 12,
+    (ElemType.SEG4, MatrixType.rigi): 2,
+    (ElemType.SEG4, MatrixType.mass): 4,
+    (ElemType.SEG5, MatrixType.rigi): 4,
+    (ElemType.SEG5, MatrixType.mass): 5,
 }
 
 
@@ -510,6 +538,150 @@ def Mesh_Hexa27_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) 
     return _hexa_quadratic_box(Lx, Ly, Lz, nx, ny, nz, 27)
 
 
+# (i1, i2) = p (r, s) of the TRI10 / TRI15 nodes in the reference's order
+# (EasyFEA/FEM/Elems/_tri.py Get_Local_Coords: corners, p - 1 nodes along
+# each edge 01, 12, 20 in that direction, inner nodes)
+_TRI_LAGRANGE = {
+    3: [(0, 0), (3, 0), (0, 3), (1, 0), (2, 0), (2, 1), (1, 2), (0, 2), (0, 1), (1, 1)],
+    4: [(0, 0), (4, 0), (0, 4), (1, 0), (2, 0), (3, 0), (3, 1), (2, 2), (1, 3), (0, 3), (0, 2), (0, 1),
+        (1, 1), (2, 1), (1, 2)],
+}
+
+
+def _boundary_cells2d(nx: int, ny: int):
+    """The rectangle's boundary cell edges, counter-clockwise, as pairs of
+    coarse grid points ((i, j), (i', j'))."""
+    e = [((i, 0), (i + 1, 0)) for i in range(nx)]
+    e += [((nx, j), (nx, j + 1)) for j in range(ny)]
+    e += [((i, ny), (i - 1, ny)) for i in range(nx, 0, -1)]
+    e += [((0, j), (0, j - 1)) for j in range(ny, 0, -1)]
+    return e
+
+
+def _tri_lagrange_rect(L: float, h: float, nx: int, ny: int, p: int) -> Mesh:
+    """TRI10 (p = 3) / TRI15 (p = 4) rectangle: the cells of Mesh_Tri3_Rect
+    (split along their (i,j)-(i+1,j+1) diagonal) on a node grid of spacing
+    1/p of a cell, node id J*(p nx+1)+I; boundary edges SEG4 / SEG5 (the two
+    ends, then the inner nodes from the first end, counter-clockwise)."""
+    NX, NY = p * nx, p * ny
+    coord = _grid2d(L, h, NX, NY)
+    nid = lambda i, j: j * (NX + 1) + i  # noqa: E731
+    J, I = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    I, J = p * I.ravel(), p * J.ravel()
+    tris = []
+    for P0, P1, P2 in (((0, 0), (1, 0), (1, 1)), ((0, 0), (1, 1), (0, 1))):
+        cols = []
+        for i1, i2 in _TRI_LAGRANGE[p]:
+            dx = p * P0[0] + i1 * (P1[0] - P0[0]) + i2 * (P2[0] - P0[0])
+            dy = p * P0[1] + i1 * (P1[1] - P0[1]) + i2 * (P2[1] - P0[1])
+            cols.append(nid(I + dx, J + dy))
+        tris.append(np.stack(cols, axis=1))
+    connect = np.stack(tris, axis=1).reshape(-1, len(_TRI_LAGRANGE[p]))
+    segs = []
+    for (a, b) in _boundary_cells2d(nx, ny):
+        ia, ja, ib, jb = p * a[0], p * a[1], p * b[0], p * b[1]
+        di, dj = (ib - ia) // p, (jb - ja) // p
+        segs.append([nid(ia, ja), nid(ib, jb)] + [nid(ia + k * di, ja + k * dj) for k in range(1, p)])
+    belem = ElemType.SEG4 if p == 3 else ElemType.SEG5
+    elem = ElemType.TRI10 if p == 3 else ElemType.TRI15
+    return Mesh({belem: GroupElem(belem, np.asarray(segs, dtype=np.int64), coord),
+                 elem: GroupElem(elem, connect, coord)})
+
+
+def Mesh_Tri10_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised TRI10 mesh (cubic triangles) with SEG4 boundary edges."""
+    return _tri_lagrange_rect(L, h, nx, ny, 3)
+
+
+def Mesh_Tri15_Rect(L: float, h: float, nx: int, ny: int) -> Mesh:
+    """Organised TRI15 mesh (quartic triangles) with SEG5 boundary edges."""
+    return _tri_lagrange_rect(L, h, nx, ny, 4)
+
+
+# local coordinates (2 r, 2 s, t) of the PRISM18 nodes in the reference's order
+# (EasyFEA/FEM/Elems/_prism.py Get_Local_Coords: the corners of the t = -1
+# and t = 1 triangles, the edge middles, the quadrangular faces' centres);
+# PRISM6 takes the first 6, PRISM15 the first 15
+_PRISM_LOCAL = np.array([
+    [0, 0, -1], [2, 0, -1], [0, 2, -1], [0, 0, 1], [2, 0, 1], [0, 2, 1],
+    [1, 0, -1], [0, 1, -1], [0, 0, 0], [1, 1, -1], [2, 0, 0], [0, 2, 0],
+    [1, 0, 1], [0, 1, 1], [1, 1, 1], [1, 0, 0], [0, 1, 0], [1, 1, 0]])
+
+
+def _prism_box(Lx, Ly, Lz, nx, ny, nz, nPe: int) -> Mesh:
+    """Prisms of [0,Lx]x[0,Ly]x[0,Lz]: the triangles of Mesh_Tri3_Rect's
+    cells in x-y extruded over nz layers along z.  The quadratic prisms use
+    the half-spacing node grid (grid nodes no element uses are dropped).
+    Boundary faces: the triangles at z = 0 and z = Lz (TRI3 / TRI6: corners,
+    then the middles of edges 01, 12, 20) and the quadrangles of the four
+    sides (QUAD4 / QUAD8 / QUAD9: corners around the face, edge middles,
+    centre)."""
+    q = 1 if nPe == 6 else 2
+    NX, NY, NZ = q * nx, q * ny, q * nz
+    xs, ys, zs = np.linspace(0.0, Lx, NX + 1), np.linspace(0.0, Ly, NY + 1), np.linspace(0.0, Lz, NZ + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    coord = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    nid = lambda i, j, k: (k * (NY + 1) + j) * (NX + 1) + i  # noqa: E731
+    K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    K, J, I = K.ravel(), J.ravel(), I.ravel()
+    loc = _PRISM_LOCAL[:nPe]
+    prisms = []
+    for P0, P1, P2 in (((0, 0), (1, 0), (1, 1)), ((0, 0), (1, 1), (0, 1))):
+        cols = []
+        for r2, s2, t in loc:
+            # fine-grid offsets: q P0 + (q r) (P1 - P0) + (q s) (P2 - P0), layer q k + q (t + 1) / 2
+            di = q * P0[0] + (q * r2 // 2) * (P1[0] - P0[0]) + (q * s2 // 2) * (P2[0] - P0[0])
+            dj = q * P0[1] + (q * r2 // 2) * (P1[1] - P0[1]) + (q * s2 // 2) * (P2[1] - P0[1])
+            cols.append(nid(q * I + di, q * J + dj, q * K + q * (t + 1) // 2))
+        prisms.append(np.stack(cols, axis=1))
+    connect = np.stack(prisms, axis=1).reshape(-1, nPe)
+    # triangular faces: the bottom triangles of the first layer, the top ones of the last
+    tri_bot = [0, 1, 2] if q == 1 else [0, 1, 2, 6, 9, 7]
+    tri_top = [3, 4, 5] if q == 1 else [3, 4, 5, 12, 14, 13]
+    first = np.repeat(K == 0, 2)
+    last = np.repeat(K == nz - 1, 2)
+    tris = np.concatenate([connect[first][:, tri_bot], connect[last][:, tri_top]])
+    # quadrangular faces on the four sides, layer by layer
+    quads = []
+    for (a, b) in _boundary_cells2d(nx, ny):
+        for k in range(nz):
+            ia, ja, ib, jb = q * a[0], q * a[1], q * b[0], q * b[1]
+            k0, k1 = q * k, q * (k + 1)
+            row = [nid(ia, ja, k0), nid(ib, jb, k0), nid(ib, jb, k1), nid(ia, ja, k1)]
+            if q == 2:
+                im, jm, km = (ia + ib) // 2, (ja + jb) // 2, k0 + 1
+                row += [nid(im, jm, k0), nid(ib, jb, km), nid(im, jm, k1), nid(ia, ja, km)]
+                if nPe == 18:
+                    row.append(nid(im, jm, km))
+            quads.append(row)
+    quads = np.asarray(quads, dtype=np.int64)
+    used = np.unique(np.concatenate([connect.ravel(), tris.ravel(), quads.ravel()]))
+    new = -np.ones(len(coord), dtype=np.int64)
+    new[used] = np.arange(len(used))
+    c = coord[used]
+    elem = {6: ElemType.PRISM6, 15: ElemType.PRISM15, 18: ElemType.PRISM18}[nPe]
+    qelem = {6: ElemType.QUAD4, 15: ElemType.QUAD8, 18: ElemType.QUAD9}[nPe]
+    telem = ElemType.TRI3 if q == 1 else ElemType.TRI6
+    return Mesh({qelem: GroupElem(qelem, new[quads], c), telem: GroupElem(telem, new[tris], c),
+                 elem: GroupElem(elem, new[connect], c)})
+
+
+def Mesh_Prism6_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised PRISM6 mesh (triangles in x-y extruded along z) with QUAD4
+    side faces and TRI3 end faces."""
+    return _prism_box(Lx, Ly, Lz, nx, ny, nz, 6)
+
+
+def Mesh_Prism15_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised PRISM15 mesh with QUAD8 side faces and TRI6 end faces."""
+    return _prism_box(Lx, Ly, Lz, nx, ny, nz, 15)
+
+
+def Mesh_Prism18_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised PRISM18 mesh with QUAD9 side faces and TRI6 end faces."""
+    return _prism_box(Lx, Ly, Lz, nx, ny, nz, 18)
+
+
 def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
     elemType = ElemType(elemType)
     if elemType == ElemType.QUAD4:
@@ -522,4 +694,8 @@ def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
         return Mesh_Tri6_Rect(L, h, nx, ny)
     if elemType == ElemType.QUAD8:
         return Mesh_Quad8_Rect(L, h, nx, ny)
+    if elemType == ElemType.TRI10:
+        return Mesh_Tri10_Rect(L, h, nx, ny)
+    if elemType == ElemType.TRI15:
+        return Mesh_Tri15_Rect(L, h, nx, ny)
     raise NotImplementedError(elemType)

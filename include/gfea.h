@@ -48,7 +48,9 @@ extern "C" {
 #define GFEA_ERR_WORKSPACE 8    /* workspace too small                           */
 #define GFEA_ERR_TIMEOUT 9      /* a bounded device wait gave up (staged copies)  */
 
-/* element codes */
+/* element codes; each element's local node order is the reference's
+   (EasyFEA/FEM/Elems/_seg.py, _tri.py, _quad.py, _tetra.py, _hexa.py,
+   _prism.py Get_Local_Coords) */
 #define GFEA_SEG2 0
 #define GFEA_TRI3 1
 #define GFEA_QUAD4 2
@@ -61,6 +63,13 @@ extern "C" {
 #define GFEA_SEG3 9
 #define GFEA_HEXA20 10
 #define GFEA_HEXA27 11
+#define GFEA_PRISM6 12
+#define GFEA_PRISM15 13
+#define GFEA_PRISM18 14
+#define GFEA_TRI10 15
+#define GFEA_TRI15 16
+#define GFEA_SEG4 17
+#define GFEA_SEG5 18
 
 /* value types */
 #define GFEA_F64 0

@@ -89,6 +89,34 @@ def gauss(elem: str, matrixType: str):
         a = (5 - np.sqrt(5)) / 20
         b = (5 + 3 * np.sqrt(5)) / 20
         return np.array([[a, a, a, b], [a, a, b, a], [a, b, a, a]]).T, np.full(4, 1 / 24)
+    if elem in ("SEG4", "SEG5"):  # Gauss-Legendre: SEG4 rigi 2 / mass 4, SEG5 rigi 4 / mass 5 (_gauss.py:396-419)
+        n = {("SEG4", "rigi"): 2, ("SEG4", "mass"): 4, ("SEG5", "rigi"): 4, ("SEG5", "mass"): 5}[(elem, matrixType)]
+        x, w = np.polynomial.legendre.leggauss(n)
+        return x.reshape(-1, 1), w
+    if elem == "TRI10":  # 6 points for both (_gauss.py:440-442)
+        return gauss("TRI6", "mass")
+    if elem == "TRI15":  # 12 points for both (_gauss.py:92-104, :444-446)
+        a, b, c, d = 0.063089014491502, 0.249286745170910, 0.310352451033785, 0.053145049844816
+        p1, p2, p3 = 0.025422453185103, 0.058393137863189, 0.041425537809187
+        xi = [a, 1 - 2 * a, a, b, 1 - 2 * b, b, c, d, 1 - c - d, 1 - c - d, c, d]
+        eta = [a, a, 1 - 2 * a, b, b, 1 - 2 * b, d, c, c, d, 1 - c - d, 1 - c - d]
+        return np.array([xi, eta]).T, np.array([p1] * 3 + [p2] * 3 + [p3] * 6)
+    if elem in ("PRISM6", "PRISM15"):  # 6 points (_gauss.py:275-282; x <- yc, y <- zc, z <- xc)
+        a = 1 / np.sqrt(3)
+        r = [0.5, 0.0, 0.5] * 2
+        s_ = [0.5, 0.5, 0.0] * 2
+        t = [-a] * 3 + [a] * 3
+        return np.array([r, s_, t]).T, np.full(6, 1 / 6)
+    if elem == "PRISM18":  # 21 points (_gauss.py:293-350): 7-point triangle x 3-point Gauss-Legendre
+        al = np.sqrt(3 / 5)
+        a, b = (6 + np.sqrt(15)) / 21, (6 - np.sqrt(15)) / 21
+        cp, cm = (155 + np.sqrt(15)) / 2400, (155 - np.sqrt(15)) / 2400
+        r = [1 / 3, a, 1 - 2 * a, a, b, 1 - 2 * b, b] * 3
+        s_ = [1 / 3, a, a, 1 - 2 * a, b, b, 1 - 2 * b] * 3
+        t = [-al] * 7 + [0.0] * 7 + [al] * 7
+        wt = [9 / 80, cp, cp, cp, cm, cm, cm]
+        w = [5 / 9 * x for x in wt] + [8 / 9 * x for x in wt] + [5 / 9 * x for x in wt]
+        return np.array([r, s_, t]).T, np.array(w)
     raise NotImplementedError(elem)
 
 
@@ -133,6 +161,8 @@ def shape_N(elem: str, p: np.ndarray) -> np.ndarray:
         return np.array([r * (r - 1) / 2, r * (r + 1) / 2, -(r - 1) * (r + 1)])
     if elem in ("HEXA20", "HEXA27"):
         return _hexa_quadratic(elem, p)[0]
+    if elem in LOCAL_NODES:
+        return _interpolant(elem, p)[0]
     if elem == "TRI6":  # Elems/_tri.py TRI6._N
         r, s = p
         return np.array([(r + s - 1) * (2 * r + 2 * s - 1), r * (2 * r - 1), s * (2 * s - 1), -4 * r * (r + s - 1),
@@ -204,6 +234,8 @@ def shape_dN(elem: str, p: np.ndarray) -> np.ndarray:
         return np.array([[r - 1 / 2, r + 1 / 2, -2 * r]])
     if elem in ("HEXA20", "HEXA27"):
         return _hexa_quadratic(elem, p)[1]
+    if elem in LOCAL_NODES:
+        return _interpolant(elem, p)[1]
     if elem == "TRI6":  # Elems/_tri.py TRI6._dN
         r, s = p
         return np.array([[4 * r + 4 * s - 3, 4 * r - 1, 0.0, -8 * r - 4 * s + 4, 4 * s, -4 * s],
@@ -274,8 +306,72 @@ def _hexa_quadratic(elem, p):
     return N, dN
 
 
+# Local coordinates of the nodes of the higher-order segments, triangles and
+# prisms in the reference's order (EasyFEA/FEM/Elems/_seg.py, _tri.py,
+# _prism.py Get_Local_Coords)
+LOCAL_NODES = {
+    "SEG4": [[-1], [1], [-1 / 3], [1 / 3]],
+    "SEG5": [[-1], [1], [-1 / 2], [0], [1 / 2]],
+    "TRI10": [[0, 0], [1, 0], [0, 1], [1 / 3, 0], [2 / 3, 0], [2 / 3, 1 / 3], [1 / 3, 2 / 3], [0, 2 / 3],
+              [0, 1 / 3], [1 / 3, 1 / 3]],
+    "TRI15": [[0, 0], [1, 0], [0, 1], [1 / 4, 0], [1 / 2, 0], [3 / 4, 0], [3 / 4, 1 / 4], [1 / 2, 1 / 2],
+              [1 / 4, 3 / 4], [0, 3 / 4], [0, 1 / 2], [0, 1 / 4], [1 / 4, 1 / 4], [1 / 2, 1 / 4], [1 / 4, 1 / 2]],
+    "PRISM18": [[0, 0, -1], [1, 0, -1], [0, 1, -1], [0, 0, 1], [1, 0, 1], [0, 1, 1], [0.5, 0, -1], [0, 0.5, -1],
+                [0, 0, 0], [0.5, 0.5, -1], [1, 0, 0], [0, 1, 0], [0.5, 0, 1], [0, 0.5, 1], [0.5, 0.5, 1],
+                [0.5, 0, 0], [0, 0.5, 0], [0.5, 0.5, 0]],
+}
+LOCAL_NODES["PRISM6"] = LOCAL_NODES["PRISM18"][:6]
+LOCAL_NODES["PRISM15"] = LOCAL_NODES["PRISM18"][:15]
+
+
+def _monomials(elem):
+    """Exponent triples of the polynomial space each element interpolates in:
+    complete degree p in 1D and on the triangle; on the prisms the triangle's
+    degree-1 / degree-2 space times degree 1 / 2 in t, and for PRISM15 the
+    serendipity space P2(r, s) x P1(t) + {t^2, r t^2, s t^2}."""
+    p = {"SEG4": 3, "SEG5": 4, "TRI10": 3, "TRI15": 4}.get(elem)
+    if elem.startswith("SEG"):
+        return [(i, 0, 0) for i in range(p + 1)]
+    if elem.startswith("TRI"):
+        return [(i, j, 0) for i in range(p + 1) for j in range(p + 1 - i)]
+    tri1 = [(0, 0), (1, 0), (0, 1)]
+    tri2 = tri1 + [(2, 0), (1, 1), (0, 2)]
+    if elem == "PRISM6":
+        return [(i, j, k) for (i, j) in tri1 for k in (0, 1)]
+    if elem == "PRISM18":
+        return [(i, j, k) for (i, j) in tri2 for k in (0, 1, 2)]
+    return [(i, j, k) for (i, j) in tri2 for k in (0, 1)] + [(i, j, 2) for (i, j) in tri1]
+
+
+def _interpolant(elem, p):
+    """N (nPe,) and dN (dim, nPe) at p: the Lagrange interpolants of the
+    element's nodes in its polynomial space, N(x) = V^-T m(x) with V the
+    monomials m evaluated at the nodes."""
+    nodes = np.asarray(LOCAL_NODES[elem], float)
+    dim = nodes.shape[1]
+    mono = _monomials(elem)
+
+    def m(x, d=None):
+        x = np.concatenate([np.asarray(x, float), np.zeros(3 - dim)])
+        out = []
+        for e in mono:
+            if d is None:
+                out.append(np.prod([x[k] ** e[k] for k in range(3)]))
+            elif e[d] == 0:
+                out.append(0.0)
+            else:
+                out.append(e[d] * np.prod([x[k] ** (e[k] - (k == d)) for k in range(3)]))
+        return np.array(out)
+    V = np.array([m(x) for x in nodes])  # (nPe, nPe)
+    Vt_inv = np.linalg.inv(V).T
+    N = Vt_inv @ m(p)
+    dN = np.array([Vt_inv @ m(p, d) for d in range(dim)])
+    return N, dN
+
+
 ELEM_DIM = {"SEG2": 1, "TRI3": 2, "QUAD4": 2, "QUAD9": 2, "HEXA8": 3, "TETRA4": 3, "SEG3": 1, "TRI6": 2,
-            "QUAD8": 2, "TETRA10": 3, "HEXA20": 3, "HEXA27": 3}
+            "QUAD8": 2, "TETRA10": 3, "HEXA20": 3, "HEXA27": 3, "SEG4": 1, "SEG5": 1, "TRI10": 2, "TRI15": 2,
+            "PRISM6": 3, "PRISM15": 3, "PRISM18": 3}
 
 
 def N_pg(elem, matrixType):

@@ -56,10 +56,15 @@ def to_ref_mesh(R, m: gmesh.Mesh):
 
 
 def mesh_arrays(m: gmesh.Mesh):
+    """The main group and the boundary groups (belem/bconnect, and for the
+    prisms' second face type belem2/bconnect2)."""
     g = m.groupElem
-    b = m.Get_list_groupElem(m.dim - 1)[0]
-    return dict(elem=g.elemType.value, coord=m.coord, connect=g.connect,
-                belem=b.elemType.value, bconnect=b.connect)
+    bs = m.Get_list_groupElem(m.dim - 1)
+    d = dict(elem=g.elemType.value, coord=m.coord, connect=g.connect,
+             belem=bs[0].elemType.value, bconnect=bs[0].connect)
+    if len(bs) > 1:
+        d.update(belem2=bs[1].elemType.value, bconnect2=bs[1].connect)
+    return d
 
 
 def csr_parts(prefix, A):
@@ -69,9 +74,11 @@ def csr_parts(prefix, A):
             f"{prefix}_indptr": A.indptr.astype(np.int64)}
 
 
-def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out, law=None):
+def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out, law=None, load_axis=0):
     """``law``: None (isotropic E, v) or a dict of transversely isotropic
-    parameters (El, Et, Gl, vl, vt, axis_l, axis_t)."""
+    parameters (El, Et, Gl, vl, vt, axis_l, axis_t).  The body is clamped
+    at x = 0 and loaded on the face where coordinate ``load_axis`` is largest
+    (stored as ``right``)."""
     dim = m.dim
     rm = to_ref_mesh(R, m)
     if law is None:
@@ -82,7 +89,8 @@ def elastic_case(R, name, m, E, v, planeStress, thickness, loadval, loaddir, out
     simu.solver = R.SolverType.scipy
     L = m.coord[:, 0].max()
     left = rm.Nodes_Conditions(lambda x, y, z: x == 0)
-    right = rm.Nodes_Conditions(lambda x, y, z: x == L)
+    Lmax = m.coord[:, load_axis].max()
+    right = rm.Nodes_Conditions(lambda x, y, z: (x, y, z)[load_axis] == Lmax)
     unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
     simu.add_dirichlet(left, [0.0] * dim, unk)
     simu.add_surfLoad(right, [loadval], [loaddir])
@@ -186,7 +194,8 @@ def field_load_case(R, name, m, E, v, planeStress, thickness, out):
     simu.solver = R.SolverType.scipy
     L = m.coord[:, 0].max()
     left = rm.Nodes_Conditions(lambda x, y, z: x == 0)
-    right = rm.Nodes_Conditions(lambda x, y, z: x == L)
+    Lmax = m.coord[:, load_axis].max()
+    right = rm.Nodes_Conditions(lambda x, y, z: (x, y, z)[load_axis] == Lmax)
     unk = ["x", "y"] if dim == 2 else ["x", "y", "z"]
     simu.add_dirichlet(left, [0.0] * dim, unk)
     for nodes, vals, un in field_loads(dim, m.coord, right):
@@ -618,11 +627,40 @@ def _el_hexa8_hetero(R, out):
     elastic_case(R, "el_hexa8_hetero", mh, Eh, 0.3, False, 1.0, -1.0, "z", out)
 
 
+def _higher_order_cases(R, out):
+    """TRI10 (SEG4 edges), TRI15 (SEG5 edges) and the prisms PRISM6 (QUAD4 and
+    TRI3 faces), PRISM15 (QUAD8, TRI6) and PRISM18 (QUAD9, TRI6): elastic
+    cantilevers (the prisms loaded on an end face z = Lz, whose TRI faces
+    share the mesh with the QUAD side faces, or on x = L), phase-field
+    systems at a prescribed state and the post-processing results."""
+    elastic_case(R, "el_tri10", gmesh.Mesh_Tri10_Rect(120.0, 13.0, 8, 2), 210000.0, 0.25, True, 2.0, -10.0, "y",
+                 out)
+    elastic_case(R, "el_tri15", gmesh.Mesh_Tri15_Rect(120.0, 13.0, 6, 2), 210000.0, 0.3, False, 1.0, -10.0, "y",
+                 out)
+    elastic_case(R, "el_prism6", gmesh.Mesh_Prism6_Box(60.0, 10.0, 10.0, 6, 2, 2), 210000.0, 0.3, False, 1.0, -1.0,
+                 "z", out, load_axis=2)
+    elastic_case(R, "el_prism15", gmesh.Mesh_Prism15_Box(60.0, 10.0, 10.0, 4, 2, 2), 210000.0, 0.3, False, 1.0,
+                 -1.0, "z", out)
+    elastic_case(R, "el_prism18", gmesh.Mesh_Prism18_Box(60.0, 10.0, 10.0, 3, 1, 1), 210000.0, 0.3, False, 1.0,
+                 -1.0, "z", out, load_axis=2)
+    pf_state_case(R, "pfsys_tri10_miehe_at2", gmesh.Mesh_Tri10_Rect(1.0, 1.0, 4, 4), "Miehe", "AT2", out)
+    pf_state_case(R, "pfsys_tri15_amor_at1", gmesh.Mesh_Tri15_Rect(1.0, 1.0, 3, 3), "Amor", "AT1", out)
+    pf_state_case(R, "pfsys_prism6_miehe_at2", gmesh.Mesh_Prism6_Box(1.0, 1.0, 0.5, 3, 3, 2), "Miehe", "AT2", out)
+    pf_state_case(R, "pfsys_prism15_amor_at2", gmesh.Mesh_Prism15_Box(1.0, 1.0, 0.5, 2, 2, 1), "Amor", "AT2", out)
+    pf_state_case(R, "pfsys_prism18_miehe_at1", gmesh.Mesh_Prism18_Box(1.0, 1.0, 0.5, 2, 2, 1), "Miehe", "AT1",
+                  out)
+    results_case(R, "res_tri10", gmesh.Mesh_Tri10_Rect(12.0, 3.0, 6, 2), 210000.0, 0.3, True, 13.0, out)
+    results_case(R, "res_tri15", gmesh.Mesh_Tri15_Rect(12.0, 3.0, 4, 2), 210000.0, 0.3, False, 1.0, out)
+    results_case(R, "res_prism6", gmesh.Mesh_Prism6_Box(6.0, 2.0, 2.0, 3, 1, 2), 210000.0, 0.3, False, 1.0, out)
+    results_case(R, "res_prism15", gmesh.Mesh_Prism15_Box(6.0, 2.0, 2.0, 2, 1, 1), 210000.0, 0.3, False, 1.0, out)
+    results_case(R, "res_prism18", gmesh.Mesh_Prism18_Box(6.0, 2.0, 2.0, 2, 1, 1), 210000.0, 0.3, False, 1.0, out)
+
+
 # fixtures that can be regenerated alone (--only=name,...)
 CASES = {"el_hexa8_hetero": _el_hexa8_hetero, "pf_conv": _pf_conv_cases, "field_load": _field_load_cases,
          "split": split_case, "pf_splits": _pf_split_cases, "tetra4": _tetra4_cases,
          "pf_curve_tri3_200x200": pf_curve_case, "results": _results_cases, "anisot": anisot_case,
-         "pf_solvers": _pf_solver_cases, "quadratic": _quadratic_cases}
+         "pf_solvers": _pf_solver_cases, "quadratic": _quadratic_cases, "higher_order": _higher_order_cases}
 
 
 if __name__ == "__main__":

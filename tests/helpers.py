@@ -6,12 +6,20 @@ import scipy.sparse as sp
 from easyfea_gb300.mesh import ElemType, GroupElem, Mesh
 
 
+def boundary_groups(g):
+    """[(element type, connect)] of a fixture's boundary groups: belem /
+    bconnect, and belem2 / bconnect2 where the mesh has a second face type
+    (the prisms' quadrangles and triangles)."""
+    out = [(str(g["belem"]), g["bconnect"])]
+    if "belem2" in g:
+        out.append((str(g["belem2"]), g["bconnect2"]))
+    return out
+
+
 def mesh_from_golden(g) -> Mesh:
     coord = np.asarray(g["coord"], dtype=float)
-    groups = {
-        ElemType(str(g["belem"])): GroupElem(ElemType(str(g["belem"])), g["bconnect"], coord),
-        ElemType(str(g["elem"])): GroupElem(ElemType(str(g["elem"])), g["connect"], coord),
-    }
+    groups = {ElemType(e): GroupElem(ElemType(e), c, coord) for e, c in boundary_groups(g)}
+    groups[ElemType(str(g["elem"]))] = GroupElem(ElemType(str(g["elem"])), g["connect"], coord)
     return Mesh(groups)
 
 

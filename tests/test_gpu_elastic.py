@@ -8,7 +8,8 @@ from helpers import csr, mesh_from_golden, row_scaled_err, same_pattern
 pytestmark = pytest.mark.gpu
 
 CASES = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26",
-         "el_tetra4", "el_tri6", "el_quad8", "el_tetra10", "el_hexa20", "el_hexa27"]
+         "el_tetra4", "el_tri6", "el_quad8", "el_tetra10", "el_hexa20", "el_hexa27", "el_tri10", "el_tri15", "el_prism6",
+         "el_prism15", "el_prism18"]
 
 
 def run_case(g, precision="fp64", rtol=1e-12):

@@ -20,7 +20,10 @@ def meshes():
             "QUAD9": gmesh.Mesh_Quad9_Rect(6.0, 2.0, 20, 8), "HEXA8": gmesh.Mesh_Hexa8_Box(4.0, 1.0, 1.0, 20, 6, 6),
             "TETRA4": gmesh.Mesh_Tetra4_Box(3.0, 1.0, 1.0, 8, 4, 4), "TRI6": gmesh.Mesh_Tri6_Rect(1.0, 1.0, 20, 20),
             "QUAD8": gmesh.Mesh_Quad8_Rect(6.0, 2.0, 24, 8), "TETRA10": gmesh.Mesh_Tetra10_Box(2.0, 1.0, 1.0, 4, 2, 2),
-            "HEXA20": gmesh.Mesh_Hexa20_Box(2.0, 1.0, 1.0, 6, 3, 3), "HEXA27": gmesh.Mesh_Hexa27_Box(2.0, 1.0, 1.0, 6, 3, 3)}
+            "HEXA20": gmesh.Mesh_Hexa20_Box(2.0, 1.0, 1.0, 6, 3, 3), "HEXA27": gmesh.Mesh_Hexa27_Box(2.0, 1.0, 1.0, 6, 3, 3),
+            "TRI10": gmesh.Mesh_Tri10_Rect(1.0, 1.0, 12, 12), "TRI15": gmesh.Mesh_Tri15_Rect(1.0, 1.0, 10, 10),
+            "PRISM6": gmesh.Mesh_Prism6_Box(3.0, 1.0, 1.0, 12, 4, 4), "PRISM15": gmesh.Mesh_Prism15_Box(2.0, 1.0, 1.0, 6, 3, 3),
+            "PRISM18": gmesh.Mesh_Prism18_Box(2.0, 1.0, 1.0, 6, 3, 3)}
 
 
 def law(mode, dim, Ne, rng):
@@ -40,7 +43,7 @@ def law(mode, dim, Ne, rng):
 
 
 @pytest.mark.parametrize("elem", ["TRI3", "QUAD4", "QUAD9", "HEXA8", "TETRA4", "TRI6", "QUAD8", "TETRA10", "HEXA20",
-                                  "HEXA27"])
+                                  "HEXA27", "TRI10", "TRI15", "PRISM6", "PRISM15", "PRISM18"])
 @pytest.mark.parametrize("vt", ["f64", "f32"])
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
 def test_parts_match_atomic_kernel(elem, vt, mode):

@@ -23,7 +23,9 @@ def make_simu(g, planeStress=None):
 
 @pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2",
                                   "pfsys_tetra4_miehe_at2", "pfsys_tri6_miehe_at2", "pfsys_quad8_amor_at1",
-                                  "pfsys_tetra10_miehe_at2", "pfsys_hexa20_miehe_at2"])
+                                  "pfsys_tetra10_miehe_at2", "pfsys_hexa20_miehe_at2", "pfsys_tri10_miehe_at2",
+                                  "pfsys_tri15_amor_at1", "pfsys_prism6_miehe_at2", "pfsys_prism15_amor_at2",
+                                  "pfsys_prism18_miehe_at1"])
 def test_state_systems_match_reference(golden, case):
     g = golden(case)
     m, simu = make_simu(g, planeStress=False)

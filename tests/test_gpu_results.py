@@ -13,7 +13,7 @@ from oracle import fem
 pytestmark = pytest.mark.gpu
 
 ELASTIC = ["res_quad4", "res_quad4_hetero", "res_tri3", "res_quad9", "res_hexa8", "res_tetra4", "res_quad8",
-           "res_tetra10", "res_hexa27"]
+           "res_tetra10", "res_hexa27", "res_tri10", "res_tri15", "res_prism6", "res_prism15", "res_prism18"]
 PHASEFIELD = ["res_pf_tri3_miehe", "res_pf_quad4_amor", "res_pf_hexa8_miehe"]
 
 # element means of Gauss-point values and their node averages: FP64 with a

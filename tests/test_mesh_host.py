@@ -12,13 +12,20 @@ from oracle import fem
     (lambda: gmesh.Mesh_Tri3_Rect(1.0, 1.0, 8, 8), 1.0),
     (lambda: gmesh.Mesh_Quad9_Rect(3.0, 2.0, 4, 3), 6.0),
     (lambda: gmesh.Mesh_Hexa8_Box(3.0, 2.0, 1.0, 4, 3, 2), 6.0),
+    (lambda: gmesh.Mesh_Tri10_Rect(3.0, 2.0, 4, 3), 6.0),
+    (lambda: gmesh.Mesh_Tri15_Rect(3.0, 2.0, 4, 3), 6.0),
+    (lambda: gmesh.Mesh_Prism6_Box(3.0, 2.0, 1.0, 4, 3, 2), 6.0),
+    (lambda: gmesh.Mesh_Prism15_Box(3.0, 2.0, 1.0, 4, 3, 2), 6.0),
+    (lambda: gmesh.Mesh_Prism18_Box(3.0, 2.0, 1.0, 4, 3, 2), 6.0),
 ])
 def test_generators_positive_jacobian_and_measure(make, area):
     """Sum of wJ equals the domain measure (tests/FEM/mesh_test.py:135-149 of the reference)."""
     m = make()
     geo = fem.Geometry(m.elemType.value, m.coord, np.asarray(m.connect), "rigi")
     assert np.all(fem.det(geo.F) > 0), "elements must be positively oriented"
-    assert abs(geo.wJ.sum() - area) <= 1e-11 * area
+    # the reference's 6- and 12-point triangle rules have 15-digit literal
+    # weights (the 6 weights sum to 1/2 - 1.5e-11)
+    assert abs(geo.wJ.sum() - area) <= (1e-10 if m.elemType.value in ("TRI10", "TRI15") else 1e-11) * area
 
 
 def test_boundary_groups_cover_the_boundary():
@@ -29,6 +36,38 @@ def test_boundary_groups_cover_the_boundary():
     faces = h.Get_list_groupElem(2)[0]
     assert faces.Ne == 2 * (4 * 2 + 4 * 2 + 2 * 2)
     assert h.orphanNodes.size == 0
+
+
+@pytest.mark.parametrize("make", [gmesh.Mesh_Prism6_Box, gmesh.Mesh_Prism15_Box, gmesh.Mesh_Prism18_Box])
+def test_prism_faces_cover_the_box(make):
+    """The quadrangular side faces and the triangular end faces of a prism box
+    (two boundary groups) add up to its surface, each face once, and every
+    node belongs to an element."""
+    m = make(3.0, 2.0, 1.0, 4, 3, 2)
+    groups = m.Get_list_groupElem(2)
+    assert sorted(g.elemType.value[:4] for g in groups) == ["QUAD", "TRI3" if make is gmesh.Mesh_Prism6_Box else "TRI6"]
+    area = 0.0
+    for g in groups:
+        geo = fem.Geometry(g.elemType.value, m.coord, np.asarray(g.connect), "mass")
+        area += geo.wJ.sum()
+        assert len({tuple(sorted(r)) for r in g.connect}) == g.Ne
+    # TRI6 faces: the 6-point rule's literal weights (sum 1/2 - 1.5e-11)
+    assert abs(area - 2 * (3 * 2 + 3 * 1 + 2 * 1)) <= 1e-10 * area
+    assert m.orphanNodes.size == 0
+
+
+@pytest.mark.parametrize("make,p", [(gmesh.Mesh_Tri10_Rect, 3), (gmesh.Mesh_Tri15_Rect, 4)])
+def test_higher_order_triangle_edges(make, p):
+    """SEG4 / SEG5 boundary edges: the rectangle's perimeter, ends first and
+    the inner nodes evenly spaced from the first end."""
+    m = make(3.0, 2.0, 4, 3)
+    seg = m.Get_list_groupElem(1)[0]
+    x = m.coord[seg.connect]
+    assert seg.Ne == 2 * (4 + 3)
+    for k in range(1, p):
+        assert np.allclose(x[:, 1 + k], x[:, 0] + k / p * (x[:, 1] - x[:, 0]))
+    geo = fem.Geometry(seg.elemType.value, m.coord, np.asarray(seg.connect), "mass")
+    assert abs(geo.wJ.sum() - 10.0) <= 1e-12
 
 
 def test_assembly_e_layout():

@@ -8,7 +8,8 @@ from oracle import fem
 from oracle.simulate import OracleMesh, PhaseFieldOracle, elastic_solve, neumann
 
 ELASTIC = ["el_quad4", "el_tri3", "el_quad9", "el_hexa8", "el_quad4_hetero", "el_hexa8_hetero", "el_cantilever_240x26",
-           "el_tetra4", "el_tri6", "el_quad8", "el_tetra10", "el_hexa20", "el_hexa27"]
+           "el_tetra4", "el_tri6", "el_quad8", "el_tetra10", "el_hexa20", "el_hexa27", "el_tri10", "el_tri15",
+           "el_prism6", "el_prism15", "el_prism18"]
 
 
 def row_scaled_err(A, B):
@@ -25,7 +26,9 @@ def row_scaled_err(A, B):
 
 
 def om(g):
-    return OracleMesh(str(g["elem"]), g["coord"], g["connect"], [(str(g["belem"]), g["bconnect"])])
+    from helpers import boundary_groups
+
+    return OracleMesh(str(g["elem"]), g["coord"], g["connect"], boundary_groups(g))
 
 
 def csr(g, p, n):
@@ -173,7 +176,9 @@ def test_phasefield_oracle_convergence_options_match_reference(golden, opt):
 
 @pytest.mark.parametrize("case", ["pfsys_quad4_amor_at1", "pfsys_tri3_miehe_at1", "pfsys_hexa8_miehe_at2",
                                   "pfsys_tetra4_miehe_at2", "pfsys_tri6_miehe_at2", "pfsys_quad8_amor_at1",
-                                  "pfsys_tetra10_miehe_at2", "pfsys_hexa20_miehe_at2"])
+                                  "pfsys_tetra10_miehe_at2", "pfsys_hexa20_miehe_at2", "pfsys_tri10_miehe_at2",
+                                  "pfsys_tri15_amor_at1", "pfsys_prism6_miehe_at2", "pfsys_prism15_amor_at2",
+                                  "pfsys_prism18_miehe_at1"])
 def test_phasefield_state_systems_match_reference(golden, case):
     g = golden(case)
     m = om(g)

@@ -865,12 +865,19 @@ __global__ void __launch_bounds__(kThreads) dir_kernel(int64_t n, const T* __res
     p_new[i] = z[i] + beta * p_old[i];
 }
 
-// Ap = masked A p; partial p.Ap; the last block sets alpha.
-template <int D, int G, typename T, bool DIFF>
+// Ap = masked A p; partial p.Ap; the last block sets alpha.  DIR: the
+// search direction is formed on the fly, p = z + beta p_old (beta from the
+// scalar record), read for every neighbour from z and p_old and written for
+// the block's own rows into p_new -- the direction update of dir_kernel
+// fused into the SpMV ('p' is then p_old).
+template <int D, int G, typename T, bool DIFF, bool DIR = false>
 __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) apply_kernel(SysT<T> S, const T* __restrict__ p,
                                                                               T* __restrict__ Ap,
-                                                         double* partials, Scal* sc) {
+                                                         double* partials, Scal* sc,
+                                                         const T* __restrict__ z = nullptr,
+                                                         T* __restrict__ p_new = nullptr) {
   if (sc->done) return;
+  const T beta = DIR ? (T)sc->beta : (T)0;
   const int lane = threadIdx.x % G;
   const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
@@ -879,13 +886,15 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && D > 1) ? 8 : 6) a
   for (int64_t a0 = grp - (grp % (32 / G)); a0 < Nn; a0 += ngrp) {
     const int64_t a = a0 + (grp % (32 / G));
     const int64_t ac = a < Nn ? a : Nn - 1;
-    T av = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, [p](int64_t c) { return __ldg(p + c); });
+    auto pv = [p, z, beta](int64_t c) { return DIR ? __ldg(z + c) + beta * __ldg(p + c) : __ldg(p + c); };
+    T av = node_rows_t<D, G, T, T, false, DIFF>(ac, lane, S, pv);
     int r = -1;
 #pragma unroll
     for (int i = 0; i < D; ++i) if (lane == row_lane<D, G>(i)) r = i;
     if (a < Nn && r >= 0) {
       const int64_t dof = a * D + r;
-      const T pn = p[dof];
+      const T pn = DIR ? pv(dof) : p[dof];  // the value the neighbours' rows used
+      if (DIR) p_new[dof] = pn;
       if (S.known[dof]) av = 0;
       Ap[dof] = av;
       pap.add_prod(pn, av);
@@ -1560,9 +1569,11 @@ int launch_apply_staged(const SysT<T>& S, const StageGeom& g, const unsigned cha
 }
 
 // Masked SpMV with p.Ap and alpha: the staged kernel over the packed tiles
-// when the workspace holds them, else apply_kernel.
+// when the workspace holds them, else apply_kernel (with z given and no
+// packed tiles: the direction p_new = z + beta p formed inside it).
 template <typename T>
-int launch_apply(const gfea_system* s, int G, PcgWork& w, const T* p, cudaStream_t st) {
+int launch_apply(const gfea_system* s, int G, PcgWork& w, const T* p, cudaStream_t st, const T* z = nullptr,
+                 T* p_new = nullptr) {
   const SysT<T> S = sys_t<T>(s);
   const bool diff = sizeof(T) == 4 && s->translation_invariant;
   if (w.packed) {
@@ -1577,7 +1588,13 @@ int launch_apply(const gfea_system* s, int G, PcgWork& w, const T* p, cudaStream
     return e;
   }
   const int grid = grid_nodes(s->n_nodes, G);
-  if (diff) {
+  if (z && diff) {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true, true><<<grid, kThreads, 0, st>>>(
+                                    S, p, (T*)w.Ap, w.partials, w.sc, z, p_new)));
+  } else if (z) {
+    GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, false, true><<<grid, kThreads, 0, st>>>(
+                                    S, p, (T*)w.Ap, w.partials, w.sc, z, p_new)));
+  } else if (diff) {
     GFEA_DG_SWITCH(s->dof_n, G, (apply_kernel<DD, GG, T, true><<<grid, kThreads, 0, st>>>(S, p, (T*)w.Ap,
                                                                                          w.partials, w.sc)));
   } else {
@@ -1590,6 +1607,11 @@ int launch_apply(const gfea_system* s, int G, PcgWork& w, const T* p, cudaStream
 
 template <typename T>
 int launch_dir(const gfea_system* s, int G, PcgWork& w, const T* p_old, T* p_new, cudaStream_t st) {
+  if (!w.packed) {  // one kernel: the direction formed inside the SpMV
+    const int e = launch_apply<T>(s, G, w, p_old, st, (const T*)w.z, p_new);
+    if (e) return e;
+    return prof_mark(st, kTagApply);
+  }
   const int64_t N = s->n_nodes * s->dof_n;
   dir_kernel<T><<<grid_elems(N), kThreads, 0, st>>>(N, (const T*)w.z, p_old, p_new, w.sc);
   GFEA_LAUNCH_CHECK();
@@ -1901,11 +1923,12 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
   }
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(cs, &g);
-  // kernels per iteration: direction + SpMV, then update (block-Jacobi) or
+  // kernels per iteration: direction + SpMV (one kernel without packed
+  // tiles), then update (block-Jacobi) or
   // update/restrict + restriction sum (with restriction copies) + coarse
   // GEMV + finish (two-level); counted when the graph runs, not when it is
   // captured
-  w.gkernels = (long long)kGraphIters * (2 + (w.coarse ? (w.C.ncopies > 1 ? 4 : 3) : 1));
+  w.gkernels = (long long)kGraphIters * ((w.packed ? 2 : 1) + (w.coarse ? (w.C.ncopies > 1 ? 4 : 3) : 1));
   launch_counter().fetch_sub(w.gkernels);
   if (e || ce != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);
@@ -1924,12 +1947,17 @@ int capture_iterations(const gfea_system* s, int G, PcgWork& w, T* x, T* p0, T* 
 }
 
 // Runs PCG iterations until the device flags done, checking after chunks of
-// 'check' iterations (doubled after each chunk that did not finish when
-// 'grow' is set, so that few launches after convergence are wasted).  pa
+// 'check' iterations.  With 'grow' set, a chunk that did not finish is
+// followed by one sized from the iterated residual's decay since the start
+// of the call (rr0 at iters0): the iterations its log still needs to reach
+// the trigger at the mean rate so far, plus 15 % and two (doubling when the
+// residual has not decreased).  Iterations launched after the device set
+// 'done' are no-op kernels that still cost their launch, so sizing the chunk
+// to the expected remainder, rather than doubling it, keeps those few.  pa
 // holds the current search direction on entry and exit.
 template <typename T>
 int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow, Scal* host_sc, T*& pa,
-             T*& pb, int iters0, cudaStream_t st) {
+             T*& pb, int iters0, double rr0, cudaStream_t st) {
   // iteration j reads direction buf[j % 2] and writes buf[(j + 1) % 2]; launches
   // after the device set 'done' are no-ops, so the current direction follows
   // from the number of iterations actually performed
@@ -2000,7 +2028,20 @@ int pcg_loop(const gfea_system* s, int G, PcgWork& w, T* x, int check, bool grow
     }
     before = host_sc->iters;
     if (host_sc->done) break;
-    if (grow) check = check * 2 > cap ? cap : check * 2;
+    if (grow) {
+      int next = check * 2;
+      const int di = host_sc->iters - iters0;
+      if (di > 0 && rr0 > 0 && host_sc->rr > 0 && host_sc->tol2 > 0) {
+        const double lr = log(host_sc->rr);
+        const double rate = (lr - log(rr0)) / di;  // log-residual change per iteration
+        if (rate < 0 && isfinite(rate)) {
+          const double rem = (log(host_sc->tol2) - lr) / rate;
+          if (rem < 1e6) next = (int)ceil(1.15 * rem) + 2;
+        }
+      }
+      next = (next + kGraphIters - 1) / kGraphIters * kGraphIters;  // whole graph launches
+      check = next < kGraphIters ? kGraphIters : (next > cap ? cap : next);
+    }
   }
   const int performed = host_sc->iters - iters0;
   pa = buf[performed & 1];
@@ -2132,7 +2173,7 @@ int refine_solve(const gfea_system* s, const double* b, double* x, const gfea_pc
   int stall = 0;
   int iters0 = 0;
   for (int upd = 0;; ++upd) {
-    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, adaptive, &hs, pa, pb, iters0, st);
+    e = pcg_loop<T>(s, G, w, (T*)w.dx, check, adaptive, &hs, pa, pb, iters0, rr, st);
     if (adaptive) {
       const int cycle = hs.iters - iters0;
       check = cycle + 2 < 4 ? 4 : (cycle + 2 > 64 ? 64 : cycle + 2);

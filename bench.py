@@ -74,7 +74,8 @@ def parse():
     p.add_argument("--box", default=None,
                    help="nx,ny,nz of the HEXA8 box of the assembly and results workloads (default 400,40,40)")
     p.add_argument("--workload", default="stream",
-                   choices=["stream", "single", "batch", "batch_one_launch", "assembly", "phasefield", "results"],
+                   choices=["stream", "single", "batch", "batch_one_launch", "assembly", "phasefield", "results",
+                            "pf_solve"],
                    help="stream: the full benchmark; the others: only that measurement, printed as its own "
                         "JSON object (for profiling)")
     return p.parse_args()
@@ -396,6 +397,51 @@ def phasefield_measure(steps=8, window=(290, 320)):
     return out
 
 
+def pf_displacement_solve(reps=3):
+    """The notched plate's displacement system in its cracked state: the
+    200x200 TRI3 plate (AT2, Miehe) with the damage field of load step 300
+    of the reference's own load curve (tests/golden/pf_curve_tri3_200x200.npz,
+    used here as an input state), the top displaced by 300 x 1e-5, the
+    degraded stiffness assembled once and the system solved from zero in
+    mixed precision ``reps`` times (the first builds the coarse aggregation
+    and captures the iteration graphs).  A mid-size system whose PCG
+    iteration is bound by latency rather than bytes."""
+    import torch
+
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                             "pf_curve_tri3_200x200.npz"))
+    k = 300
+    m = gmesh.Mesh_Tri3_Rect(1.0, 1.0, 200, 200)
+    mat = Models.Elastic.Isotropic(2, E=210e3, v=0.3, planeStress=False)
+    simu = Simulations.PhaseField(m, Models.PhaseField(mat, "Miehe", "AT2", 2.7, 0.01))
+    simu.precision = "mixed"
+    simu._Set_solutions("damage", g["d"][list(g["d_steps"]).index(k)])
+    simu.add_dirichlet(g["notch"], [1.0], ["d"], problemType="damage")
+    simu.add_dirichlet(g["bottom"], [0.0, 0.0], ["x", "y"])
+    simu.add_dirichlet(g["top"], [0.0, k * float(g["dU"])], ["x", "y"])
+    simu._assemble_elastic()
+    Ku = simu._PhaseField__Ku
+    fu = simu._neumann_vec("elastic")
+    times, its = [], []
+    for _ in range(reps):
+        x0 = torch.zeros_like(fu)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        simu._solve_system(Ku, fu, "elastic", x0=x0)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        its.append(simu.last_solve.iterations)
+    best = int(np.argmin(times[1:])) + 1 if reps > 1 else 0
+    return {"workload": "notched TRI3 plate 200x200, displacement system at the damage of load step 300 "
+                        f"({fu.numel()} DOF), mixed precision, from zero",
+            "ms": 1e3 * times[best], "pcg_iterations": its[best], "reliable_updates": simu.last_solve.refinements,
+            "us_per_iteration": 1e6 * times[best] / max(its[best], 1), "rel_residual": simu.last_solve.rel_residual}
+
+
 def rate_sweep(server, sessions, rates=(10, 30, 100, 300, 1000, 2000), seconds=3.0, cap=300):
     """p50 / p99 latency and solves/s of the served stream at each Poisson
     arrival rate: about ``seconds`` of arrivals per rate (30 to ``cap``
@@ -690,6 +736,9 @@ def main():
         return
     if args.workload == "phasefield":
         print(json.dumps(phasefield_kernels()), flush=True)
+        return
+    if args.workload == "pf_solve":
+        print(json.dumps(pf_displacement_solve(reps=max(args.steps, 2))), flush=True)
         return
     if args.workload == "results":
         box = tuple(int(v) for v in args.box.split(",")) if args.box else None

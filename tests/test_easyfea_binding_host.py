@@ -35,11 +35,14 @@ def ref():
 
 
 def _mesh(R, g):
+    from helpers import boundary_groups
+
     coord = np.asarray(g["coord"], float)
-    return R.Mesh({getattr(R.ElemType, str(g["belem"])): R.GEF.Create(getattr(R.ElemType, str(g["belem"])),
-                                                                       g["bconnect"].astype(np.int64), coord.copy()),
-                   getattr(R.ElemType, str(g["elem"])): R.GEF.Create(getattr(R.ElemType, str(g["elem"])),
-                                                                      g["connect"].astype(np.int64), coord.copy())})
+    groups = {getattr(R.ElemType, e): R.GEF.Create(getattr(R.ElemType, e), np.asarray(c, np.int64), coord.copy())
+              for e, c in boundary_groups(g)}
+    groups[getattr(R.ElemType, str(g["elem"]))] = R.GEF.Create(getattr(R.ElemType, str(g["elem"])),
+                                                                g["connect"].astype(np.int64), coord.copy())
+    return R.Mesh(groups)
 
 
 def test_subclasses_and_mesh_conversion(ref, golden):
@@ -54,6 +57,24 @@ def test_subclasses_and_mesh_conversion(ref, golden):
     np.testing.assert_array_equal(m.groupElem.connect, mesh.groupElem.connect)
     simu = R.B.GpuElastic(mesh, R.Models.Elastic.Isotropic(2, E=210000.0, v=0.3, planeStress=True, thickness=13.0))
     assert simu.dim == 2 and simu.rho == 1.0
+
+
+@pytest.mark.parametrize("case,groups", [("el_prism15", {"QUAD8", "TRI6", "PRISM15"}),
+                                         ("el_prism6", {"QUAD4", "TRI3", "PRISM6"}),
+                                         ("el_tri15", {"SEG5", "TRI15"})])
+def test_higher_order_mesh_conversion(ref, golden, case, groups):
+    """EasyFEA meshes of the higher-order triangles and of the prisms (two
+    face groups) convert group by group, connectivity unchanged."""
+    R = ref
+    g = golden(case)
+    mesh = _mesh(R, g)
+    m = R.B.to_gpu_mesh(mesh)
+    assert {e.value for e in m.dict_groupElem} == groups
+    assert m.Nn == mesh.Nn and m.dim == mesh.dim
+    np.testing.assert_array_equal(m.groupElem.connect, mesh.groupElem.connect)
+    for gr in m.Get_list_groupElem(m.dim - 1):
+        ref_group = mesh.dict_groupElem[getattr(R.ElemType, gr.elemType.value)]
+        np.testing.assert_array_equal(gr.connect, ref_group.connect)
 
 
 def test_unsupported_models_rejected(ref, golden):

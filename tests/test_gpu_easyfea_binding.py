@@ -50,15 +50,17 @@ def ref():
 
 
 def ref_mesh(R, g):
+    from helpers import boundary_groups
+
     coord = np.asarray(g["coord"], dtype=float)
     groups = {}
-    for e, c in ((str(g["belem"]), g["bconnect"]), (str(g["elem"]), g["connect"])):
+    for e, c in boundary_groups(g) + [(str(g["elem"]), g["connect"])]:
         et = getattr(R.ElemType, e)
         groups[et] = R.GEF.Create(et, np.asarray(c, dtype=np.int64), coord.copy())
     return R.Mesh(groups)
 
 
-@pytest.mark.parametrize("case", ["el_cantilever_240x26", "el_quad4_hetero", "el_hexa8"])
+@pytest.mark.parametrize("case", ["el_cantilever_240x26", "el_quad4_hetero", "el_hexa8", "el_tri15", "el_prism15"])
 def test_gpu_elastic_inside_easyfea(ref, golden, case):
     """EasyFEA's Elastic.Solve() on the GPU subclass: u within 1e-8 of the
     reference's direct solve, K and M within 1e-12 (row-scaled) with the

@@ -11,6 +11,12 @@ node and element orderings of the reference's organised meshes:
   elements; SEG2 boundary groups on the four edges.
 * HEXA8 boxes: node id ``(k*(ny+1)+j)*(nx+1)+i``; local node order of
   ``EasyFEA/FEM/Elems/_hexa.py:14-60``; QUAD4 boundary faces on the six faces.
+* TETRA4 boxes (six tetrahedra per cell), the quadratic TRI6 / QUAD8 /
+  TETRA10 meshes (mid-edge nodes added to the linear ones), HEXA20 / HEXA27
+  and PRISM15 / PRISM18 boxes on the half-spacing node grid, PRISM6 boxes and
+  TRI10 / TRI15 rectangles; every element in the local node order of
+  ``EasyFEA/FEM/Elems``.  ``Mesh_Rect`` / ``Mesh_Box`` pick the generator of
+  an element type.
 
 Everything here is host-side numpy (set-up work done once per mesh); device
 copies are made by the simulations that use the mesh.
@@ -683,19 +689,20 @@ def Mesh_Prism18_Box(Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int)
 
 
 def Mesh_Rect(elemType: ElemType, L: float, h: float, nx: int, ny: int) -> Mesh:
-    elemType = ElemType(elemType)
-    if elemType == ElemType.QUAD4:
-        return Mesh_Quad4_Rect(L, h, nx, ny)
-    if elemType == ElemType.TRI3:
-        return Mesh_Tri3_Rect(L, h, nx, ny)
-    if elemType == ElemType.QUAD9:
-        return Mesh_Quad9_Rect(L, h, nx, ny)
-    if elemType == ElemType.TRI6:
-        return Mesh_Tri6_Rect(L, h, nx, ny)
-    if elemType == ElemType.QUAD8:
-        return Mesh_Quad8_Rect(L, h, nx, ny)
-    if elemType == ElemType.TRI10:
-        return Mesh_Tri10_Rect(L, h, nx, ny)
-    if elemType == ElemType.TRI15:
-        return Mesh_Tri15_Rect(L, h, nx, ny)
-    raise NotImplementedError(elemType)
+    """Organised mesh of [0,L]x[0,h] with nx x ny cells of any 2D element type."""
+    make = {ElemType.QUAD4: Mesh_Quad4_Rect, ElemType.TRI3: Mesh_Tri3_Rect, ElemType.QUAD9: Mesh_Quad9_Rect,
+            ElemType.TRI6: Mesh_Tri6_Rect, ElemType.QUAD8: Mesh_Quad8_Rect, ElemType.TRI10: Mesh_Tri10_Rect,
+            ElemType.TRI15: Mesh_Tri15_Rect}.get(ElemType(elemType))
+    if make is None:
+        raise NotImplementedError(elemType)
+    return make(L, h, nx, ny)
+
+
+def Mesh_Box(elemType: ElemType, Lx: float, Ly: float, Lz: float, nx: int, ny: int, nz: int) -> Mesh:
+    """Organised mesh of [0,Lx]x[0,Ly]x[0,Lz] with nx x ny x nz cells of any 3D element type."""
+    make = {ElemType.HEXA8: Mesh_Hexa8_Box, ElemType.HEXA20: Mesh_Hexa20_Box, ElemType.HEXA27: Mesh_Hexa27_Box,
+            ElemType.TETRA4: Mesh_Tetra4_Box, ElemType.TETRA10: Mesh_Tetra10_Box, ElemType.PRISM6: Mesh_Prism6_Box,
+            ElemType.PRISM15: Mesh_Prism15_Box, ElemType.PRISM18: Mesh_Prism18_Box}.get(ElemType(elemType))
+    if make is None:
+        raise NotImplementedError(elemType)
+    return make(Lx, Ly, Lz, nx, ny, nz)

@@ -70,6 +70,18 @@ def test_higher_order_triangle_edges(make, p):
     assert abs(geo.wJ.sum() - 10.0) <= 1e-12
 
 
+def test_rect_and_box_dispatch():
+    """Mesh_Rect / Mesh_Box give every 2D / 3D element type its generator."""
+    for et in ("TRI3", "TRI6", "TRI10", "TRI15", "QUAD4", "QUAD8", "QUAD9"):
+        m = gmesh.Mesh_Rect(et, 2.0, 1.0, 2, 2)
+        assert m.groupElem.elemType.value == et and m.dim == 2
+    for et in ("TETRA4", "TETRA10", "HEXA8", "HEXA20", "HEXA27", "PRISM6", "PRISM15", "PRISM18"):
+        m = gmesh.Mesh_Box(et, 2.0, 1.0, 1.0, 2, 1, 1)
+        assert m.groupElem.elemType.value == et and m.dim == 3
+    with pytest.raises(NotImplementedError):
+        gmesh.Mesh_Box("QUAD4", 1.0, 1.0, 1.0, 1, 1, 1)
+
+
 def test_assembly_e_layout():
     """Element DOF map node*dof_n + d (EasyFEA/FEM/_group_elem.py:346-380)."""
     m = gmesh.Mesh_Quad4_Rect(1.0, 1.0, 2, 2)

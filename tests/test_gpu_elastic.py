@@ -157,3 +157,38 @@ def test_function_load_on_nine_point_faces():
         # integral over [0,1]^2 of 1 + y z = 1.25 (the 27-point rule is exact)
         assert abs(b[:, 2].sum() - 1.25) <= 1e-12
         assert np.abs(b[:, :2]).max() == 0.0
+
+
+@pytest.mark.parametrize("make,dim", [("Mesh_Tri10_Rect", 2), ("Mesh_Tri15_Rect", 2), ("Mesh_Prism6_Box", 3),
+                                      ("Mesh_Prism18_Box", 3)])
+def test_function_load_on_higher_order_faces(make, dim):
+    """A traction given as a function of position on SEG4 / SEG5 edges (TRI10
+    / TRI15 rectangles, 4 / 5 mass points) and on the triangular end faces of
+    prism boxes (TRI3 / TRI6, beside the quadrangular side faces): the load's
+    resultant equals the integral of the function over the loaded edge or
+    face."""
+    from easyfea_gb300 import Models
+    from easyfea_gb300 import mesh as gmesh
+    from easyfea_gb300 import simulations as Simulations
+
+    if dim == 2:
+        m = getattr(gmesh, make)(2.0, 1.0, 3, 2)
+        simu = Simulations.Elastic(m, Models.Elastic.Isotropic(2, E=1000.0, v=0.3, planeStress=True, thickness=0.5))
+        right = np.where(np.abs(m.coord[:, 0] - 2.0) < 1e-12)[0]
+        simu.add_surfLoad(right, [lambda x, y, z: 1.0 + y * y], ["y"])
+        b = simu._neumann_vec("elastic").cpu().numpy().reshape(-1, 2)
+        # thickness x integral over [0, 1] of 1 + y^2 = 0.5 x 4/3 (both rules are exact)
+        assert abs(b[:, 1].sum() - 0.5 * 4.0 / 3.0) <= 1e-12
+        assert np.abs(b[:, 0]).max() == 0.0
+    else:
+        m = getattr(gmesh, make)(2.0, 1.0, 1.0, 2, 2, 2)
+        simu = Simulations.Elastic(m, Models.Elastic.Isotropic(3, E=1000.0, v=0.3, planeStress=False))
+        top = np.where(np.abs(m.coord[:, 2] - 1.0) < 1e-12)[0]
+        simu.add_surfLoad(top, [lambda x, y, z: 1.0 + x * y], ["x"])
+        b = simu._neumann_vec("elastic").cpu().numpy().reshape(-1, 3)
+        # integral over [0, 2] x [0, 1] of 1 + x y = 2 + 1 (the triangle rules are exact for degree 2;
+        # the 6-point rule of the TRI6 faces has 15-digit literal weights summing to 1/2 - 1.5e-11)
+        tol = 1e-12 if make == "Mesh_Prism6_Box" else 3e-10
+        assert abs(b[:, 0].sum() - 3.0) <= tol
+        assert np.abs(b[:, 1:]).max() == 0.0
+

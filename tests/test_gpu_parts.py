@@ -82,7 +82,8 @@ def test_parts_match_atomic_kernel(elem, vt, mode):
     assert err.max() <= (1e-13 if vt == "f64" else 2e-5), err.max()
 
 
-@pytest.mark.parametrize("case", ["el_hexa8", "el_tetra4", "el_quad4_hetero", "el_tetra10", "el_quad8"])
+@pytest.mark.parametrize("case", ["el_hexa8", "el_tetra4", "el_quad4_hetero", "el_tetra10", "el_quad8", "el_tri15",
+                                  "el_prism18"])
 def test_parts_assembly_matches_reference(golden, case):
     """Elastic.Assembly with the row-owned schedule: K within 1e-12 of the
     reference's (row-scaled), as the atomic schedule."""

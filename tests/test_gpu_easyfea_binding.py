@@ -174,7 +174,7 @@ def test_gpu_time_schemes_inside_easyfea(ref, golden, algo):
             assert np.abs(a - b).max() <= tol, (algo, step, name, np.abs(a - b).max(), tol)
 
 
-@pytest.mark.parametrize("case", ["res_quad4_hetero", "res_hexa8", "res_tetra4"])
+@pytest.mark.parametrize("case", ["res_quad4_hetero", "res_hexa8", "res_tetra4", "res_tri15", "res_prism15"])
 def test_gpu_results_inside_easyfea(ref, golden, case):
     """The reference's Result() on the GPU subclass: strain, stress, von Mises,
     energy and ZZ1 results from the device against the reference's own."""
